@@ -1,0 +1,374 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 FDTD engine.
+
+Workload: the 512x512x1024 Bloch cell (24-cell UPML in z, kx = 0.3*pi/dx, a
+200-cell layer with 200 seeded dielectric spheres, TF/SF Gaussian pulse,
+on-the-fly DFT at 300 frequencies on all six faces of the box, as the
+reference accumulates them in 3D), FP32 fields with FP64 incident field and
+FP64 DFT accumulation.  One bench step is one full time step of the hot path:
+E update, UPML-E, Bloch, H update, UPML-H, Bloch, TF/SF, DFT sample, plus the
+DFT block accumulation amortised over its K samples.
+
+Metric: Gcell/s = cells * steps / time.  `value` is device-timed (CUDA events
+on the engine's stream) with the state resident in HBM; `e2e` goes through the
+public API from host buffers (engine creation, material upload, the steps and
+the flux read back).  `roofline` is for the dominant kernel (the H update),
+algorithmic bytes per launch over its event-timed duration.
+
+--impl reference times the CPU restatement of the reference (the oracle; the
+Fortran reference has no compiler here) on the host cores, on a bounded
+column of the same workload, and scales its per-cell and per-DFT-point costs
+to the full workload.
+"""
+import argparse
+import glob
+import importlib
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "irisfdtd-academic_gb300"
+METRIC = "Gcell/s (E+H Yee step) & %HBM peak, FP32/batched vs FP64 plain, T/R err<=1e-4"
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """Host-side barrier and max-reduction across replicas (gloo; no data-path collective)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v):
+        if not self.dist:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+CLK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def start_clocks(device):
+    try:
+        f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        pr = subprocess.Popen(["nvidia-smi", f"--query-gpu={CLK_FIELDS}", "--format=csv,noheader,nounits",
+                               "-lms", "200", "-i", str(device)], stdout=f, stderr=subprocess.DEVNULL)
+        return pr, f.name
+    except Exception:
+        return None, None
+
+
+def stop_clocks(pr, path):
+    if pr is None:
+        return None
+    pr.terminate()
+    try:
+        pr.wait(timeout=5)
+    except Exception:
+        pr.kill()
+    sm, mx, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    try:
+        for line in open(path):
+            v = [x.strip() for x in line.split(",")]
+            if len(v) < 9:
+                continue
+            try:
+                sm.append(float(v[1]))
+                mx = float(v[2])
+            except ValueError:
+                continue
+            for n, x in zip(names, v[5:9]):
+                if x.lower() in ("active", "1"):
+                    reasons.add(n)
+        os.unlink(path)
+    except OSError:
+        pass
+    if not sm:
+        return None
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, workload):
+    """Per-launch DRAM bytes from a committed ncu summary, if one exists."""
+    for f in glob.glob(os.path.join(ROOT, "profiles", "*.json")):
+        try:
+            d = json.load(open(f))
+        except Exception:
+            continue
+        if d.get("kernel") == kernel and d.get("workload") == workload and "dram_bytes_per_launch" in d:
+            return float(d["dram_bytes_per_launch"]), os.path.relpath(f, ROOT)
+    return None, None
+
+
+def setup_workload(n, rank=0):
+    cfg = importlib.import_module(PKG + ".configs")
+    w = cfg.workload(n)
+    # replicas sweep the Bloch phase (independent k-points)
+    w.akx = w.akx + 0.01 * rank
+    t = time.perf_counter()
+    eps = cfg.material(w)
+    t_mat = time.perf_counter() - t
+    d = tempfile.mkdtemp(prefix="iris_bench_")
+    path = cfg.write_input(os.path.join(d, "inputFDTD.dat"), w)
+    return w, path, eps, t_mat
+
+
+def algorithmic_bytes(w, p, sc, sm):
+    """Per launch of the E and H updates: 9 complex values per cell (read own
+    field, read the other field, write own field, 3 components), the real
+    inverse permittivity per structure cell (E only), and the UPML auxiliary
+    read+write per PML cell (3 complex each way)."""
+    cells = w.nx * w.ny * w.nz
+    npml = w.nx * w.ny * (p.pmlzi + (p.nz - p.pmlzf + 1))
+    nstruct = w.nx * w.ny * (p.hf - p.hi + 1)
+    e = cells * 9 * sc + nstruct * sm + npml * 6 * sc
+    h = cells * 9 * sc + npml * 6 * sc
+    return e, h
+
+
+def run_engine(args, rank, world, local):
+    iris = importlib.import_module(PKG)
+    D = Dist(world)
+    w, path, eps, t_mat = setup_workload(args.workload, rank)
+    p, fw, _ = iris.setparam(path)
+    p.akx_re = w.akx
+    p.device = local
+    prec = iris.FP32 if args.precision == "fp32" else iris.FP64
+    cells = w.nx * w.ny * w.nz
+    K, W = args.steps, args.warmup
+
+    # --- end to end through the public API, host buffers in and out
+    D.barrier()
+    t0 = time.perf_counter()
+    eng = iris.Engine(p, fw, precision=prec, device=local)
+    eng.set_material(eps)
+    eng.step(1, K)
+    J = eng.flux(0)
+    t_e2e = time.perf_counter() - t0
+    t_e2e = D.max(t_e2e)
+    info = eng.info()
+    h2d = eps.size * 16 + fw.size * 8
+    d2h = J.size * 8
+
+    # --- device-timed steady state
+    it = K + 1
+    eng.step(it, W)
+    it += W
+    eng.sync()
+    D.barrier()
+    pr, cpath = start_clocks(local)
+    eng.timing_start(per_kernel=True)
+    eng.step(it, K)
+    reg_ms, kms, kn = eng.timing_read()
+    clocks = stop_clocks(pr, cpath)
+    it += K
+    reg_ms = D.max(reg_ms)
+    eng.close()
+
+    sc, sm = (8, 4) if prec == iris.FP32 else (16, 8)
+    eb, hb = algorithmic_bytes(w, p, sc, sm)
+    hbm, src = peaks()
+    t_e = kms["update_e"] / max(kn["update_e"], 1) * 1e-3
+    t_h = kms["update_h"] / max(kn["update_h"], 1) * 1e-3
+    dom, db, dt_ = ("update_h", hb, t_h) if t_h >= t_e else ("update_e", eb, t_e)
+    achieved = db / dt_ / 1e9
+    wl_name = f"{w.name} (configs[2])"
+    traffic, tsrc = ncu_traffic(dom, w.name + "_" + args.precision)
+    launches = kn["update_e"] + kn["update_h"] + kn["tfsf"] + kn["dft_gather"] + kn["flux"] + kn["dft_block"] * (
+        2 if prec == iris.FP32 else 1)
+    value = world * cells * K / (reg_ms * 1e-3) / 1e9
+    out = {
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": "Gcell/s",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": round(reg_ms / K, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c64 fields (fp32), fp64 incident field and DFT accumulation" if prec == iris.FP32 else "c128 (fp64)",
+        "data": "synthetic (seeded spheres, numpy PCG64 seed 0)",
+        "config": {
+            "workload": wl_name,
+            "grid": [w.nx, w.ny, w.nz], "upml": 24, "nof": w.nof, "dft_points": info["dft_points"],
+            "dft_block": info["dft_block"], "precision": args.precision,
+            "l2": "working set (fields %.1f GB, DFT accumulators %.1f GB) >> 129 MB L2; no flush needed" % (
+                2 * 3 * info["comp_elems"] * info["bytes_per_complex"] / 1e9,
+                info["dft_points"] * w.nof * 16 / 1e9),
+            "parallelism": f"replicas x{world} (independent Bloch cells, one per GPU)",
+        },
+        "e2e": {"value": round(world * cells * K / t_e2e / 1e9, 3), "unit": "Gcell/s",
+                "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(d2h / K, 1),
+                "what": "iris_create + iris_set_material (host eps) + %d steps + iris_flux to host" % K},
+        "gpu_launches": int(launches),
+        "kernels_ms_per_step": {k: round(v / K, 4) for k, v in kms.items()},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "peak_source": src,
+                     "traffic": traffic, "traffic_source": tsrc,
+                     "algorithmic_bytes_per_launch": db},
+        "stencil_gcells": round(cells / ((t_e + t_h)) / 1e9, 3),
+        "clocks": clocks,
+        "material_setup_s": round(t_mat, 2),
+    }
+    if rank == 0 and world == 1 and not args.no_fp64_compare and prec == iris.FP32:
+        out["fp64_plain"] = fp64_compare(iris, p, fw, eps, cells, local)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(w, info["dft_points"], args.cpu_sample_steps)
+    D.close()
+    return out
+
+
+def fp64_compare(iris, p, fw, eps, cells, local, K=8, W=2):
+    eng = iris.Engine(p, fw, precision=iris.FP64, device=local)
+    eng.set_material(eps)
+    eng.step(1, W)
+    eng.sync()
+    eng.timing_start(per_kernel=True)
+    eng.step(W + 1, K)
+    reg_ms, kms, kn = eng.timing_read()
+    eng.close()
+    st = (kms["update_e"] + kms["update_h"]) / K * 1e-3
+    return {"value": round(cells * K / (reg_ms * 1e-3) / 1e9, 3), "unit": "Gcell/s", "steps": K,
+            "stencil_gcells": round(cells / st / 1e9, 3),
+            "kernels_ms_per_step": {k: round(v / K, 3) for k, v in kms.items()},
+            "note": "same workload, FP64 fields and DFT (parity mode), per-step incl. DFT"}
+
+
+def cpu_sample(w, side, threads, steps, warm=1):
+    """Oracle on a side x side column of the workload (all z, same source, UPML
+    and DFT frequencies): seconds per cell-step (everything but the DFT) and
+    per DFT point-frequency-step."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import iris_oracle as O
+    cfg = importlib.import_module(PKG + ".configs")
+    ws = cfg.workload(3, nx=side, ny=side, box=(1, side, 1, side, w.box[4], w.box[5]))
+    ws.extra = dict(ws.extra, nspheres=4)
+    d = tempfile.mkdtemp(prefix="iris_cpu_")
+    path = cfg.write_input(os.path.join(d, "inputFDTD.dat"), ws)
+    op = O.setparam(path)
+    o = O.Oracle(op, ak=(complex(0.3 * math.pi * side), 0j, 0j), threads=threads)
+    o.set_eps_inv(cfg.spheres_material(ws))
+    o.run_timed(1, warm)
+    td, tr = o.run_timed(1 + warm, steps)
+    npts = o.total_points()
+    o.close()
+    return tr / (ws.cells * steps), td / (npts * op.nof * steps), ws
+
+
+def cpu_baseline(w, full_points, steps=12, side=24):
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    t_cell, t_pf, ws = cpu_sample(w, side, threads, steps)
+    wall = time.perf_counter() - t0
+    cells = w.nx * w.ny * w.nz
+    t_step = t_cell * cells + t_pf * full_points * w.nof
+    return {"value": round(cells / t_step / 1e9, 6), "unit": "Gcell/s", "cores": threads, "kind": "port",
+            "sample": (f"oracle (C++ FP64 restatement, OpenMP {threads} threads) on a {side}x{side}x{w.nz} column of "
+                       f"the workload for {steps} steps ({wall:.1f} s); per-cell ({t_cell * 1e9:.2f} ns) and per-DFT-"
+                       f"point-frequency ({t_pf * 1e9:.3f} ns) costs scaled to the full grid and its {full_points} "
+                       f"DFT points x {w.nof} frequencies")}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    cfg = importlib.import_module(PKG + ".configs")
+    w = cfg.workload(args.workload)
+    threads = os.cpu_count() or 1
+    # total DFT points of the full workload (x, y and z face pairs of the box)
+    b = w.box
+    nbx, nby, nbz = b[1] - b[0] + 1, b[3] - b[2] + 1, b[5] - b[4] + 1
+    full_points = 12 * (nby * nbz + nbx * nbz + nbx * nby)
+    cells = w.nx * w.ny * w.nz
+    # a column sized so that warmup + steps finish in about a minute
+    side = 16 if args.steps + args.warmup > 40 else 24
+    t_cell_w, t_pf_w, _ = cpu_sample(w, side, threads, max(1, args.warmup), warm=0)
+    t0 = time.perf_counter()
+    t_cell, t_pf, ws = cpu_sample(w, side, threads, args.steps, warm=0)
+    wall = time.perf_counter() - t0
+    t_step = t_cell * cells + t_pf * full_points * w.nof
+    v = cells / t_step / 1e9
+    sample = (f"oracle (C++ FP64 restatement of the Fortran path, OpenMP {threads} threads) on a {side}x{side}x{w.nz} "
+              f"column for {args.steps} steps ({wall:.1f} s), per-cell and per-DFT-point costs scaled to the "
+              f"{w.nx}x{w.ny}x{w.nz} grid with {full_points} DFT points x {w.nof} frequencies")
+    return {
+        "metric": METRIC, "impl": "reference", "value": round(v, 6), "unit": "Gcell/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)",
+        "data": "synthetic (seeded spheres)",
+        "config": {"workload": f"{w.name} (configs[2])", "grid": [w.nx, w.ny, w.nz], "nof": w.nof},
+        "cpu_baseline": {"value": round(v, 6), "unit": "Gcell/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(v, 6), "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=256)
+    ap.add_argument("--warmup", type=int, default=64)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", type=int, default=3)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-steps", type=int, default=12)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank, world, local = env_rank()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_engine(args, rank, world, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

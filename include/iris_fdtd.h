@@ -1,0 +1,245 @@
+/*
+ * iris_fdtd.h — C ABI of the GB300 FDTD time-stepping engine.
+ *
+ * A drop-in for the hot path of IrisFDTD-Academic (Fortran): the per-step
+ * operators that driver() calls (code/driver.f90:338-451) and the run set-up
+ * around them.  Every entry point below names the reference interface it
+ * replaces.  Arrays cross the boundary as plain host pointers in the
+ * reference's own layout; the engine owns all device memory.
+ *
+ * Conventions
+ *   - Every call returns IRIS_OK (0) or a negative IRIS_E* code; no call
+ *     aborts or exits (the reference's err() STOPs: code/files.f90:352-381).
+ *   - Host buffers are borrowed for the duration of the call only.
+ *   - One engine is driven by one host thread at a time; engines are
+ *     independent and each runs on its own CUDA stream.
+ *   - Time steps are numbered from 1 like the reference's `it`
+ *     (code/driver.f90:338).
+ *   - Field arrays in the reference layout are complex(8)
+ *     (3, 0:nx+1, 0:ny+1, 0:nz+1), component fastest, passed as two double
+ *     arrays (real parts, imaginary parts) of 3*(nx+2)*(ny+2)*(nz+2) values.
+ */
+#ifndef IRIS_FDTD_H
+#define IRIS_FDTD_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------- */
+#define IRIS_OK 0
+#define IRIS_EINVAL (-1)   /* bad argument or parameter combination          */
+#define IRIS_ENOMEM (-2)   /* device or host allocation failed               */
+#define IRIS_ECUDA (-3)    /* CUDA runtime error (message: iris_last_error)  */
+#define IRIS_EPARSE (-4)   /* inputFDTD.dat could not be read                */
+#define IRIS_EIO (-5)      /* output file could not be written               */
+#define IRIS_ENAN (-6)     /* non-finite value detected in the flux          */
+#define IRIS_ETIMEOUT (-7) /* a bounded device wait gave up                  */
+#define IRIS_ENODEV (-8)   /* no CUDA device                                 */
+
+/* ---- precision modes ------------------------------------------------ */
+/* FP64 fields and DFT, operations in the reference's order (parity mode). */
+#define IRIS_FP64 0
+/* FP32 fields; TF/SF incident field in FP64; DFT partial sums over a block
+ * of K samples in FP32 with FP64-exact twiddles, accumulated in FP64.     */
+#define IRIS_FP32 1
+
+/* ---- single operator groups (iris_apply) ----------------------------- */
+#define IRIS_OP_E 1    /* e_fdtd + UPML_Array_e + bc_{x,y,z}max_bloch      */
+#define IRIS_OP_H 2    /* h_fdtd + UPML_Array_h + bc_{x,y,z}min_bloch      */
+#define IRIS_OP_TFSF 3 /* tfsf_gauss/tfsf_plane_wave + tfsf_update_{2D,3D} */
+#define IRIS_OP_DFT 4  /* scattering_fourier for every box, arg = time idx */
+
+/* ---- field selectors (iris_get_field / iris_set_field) --------------- */
+#define IRIS_E 0
+#define IRIS_H 1
+
+/*
+ * Run parameters: the `module parameters` state after setparam()
+ * (code/parameters.f90:25-261, code/files.f90:39-344), in atomic units.
+ */
+typedef struct iris_params {
+  /* 'Mesh options' */
+  int i_pol;          /* 1: E//y, 2: E//x                                  */
+  int nx, ny, nz;     /* ixmax, iymax, izmax                               */
+  int pmlzi, pmlzf;   /* UPML slabs z in [1,pmlzi] and [pmlzf,nz]          */
+  int npml;           /* UPML grading exponent nPML (the reference fixes 2) */
+  int pml_taflove;    /* value read from the nPML line (unused)            */
+  double q_nm, Q;     /* cell size in nm, and in bohr                      */
+  double cfl, dt;     /* CFL number; time step in a.u.                     */
+  double wzpml;       /* UPML strength after the f_abohr/Q rescaling       */
+  /* 'Job options' */
+  int no_downloads;   /* output interval in steps: int(texit/no_downloads) */
+  int output_time_step;
+  int texit;          /* number of time steps                              */
+  double texit_fs;
+  int hi, hf;         /* structure z-range [hi, hf]                        */
+  int sdl_plane_on[3];
+  /* 'Dielectric constants' */
+  double eps1, eps3;  /* cover and substrate                               */
+  double eps_bbox_re, eps_bbox_im;
+  /* 'Fourier transformation options' */
+  int box1[6];        /* sxi, sxf, syi, syf, szi, szf                      */
+  int box2[6];        /* mxi, mxf, myi, myf, mzi, mzf                      */
+  int nof;            /* number of frequencies                             */
+  double dlamda, lno; /* wavelength step and first wavelength in nm        */
+  int to_fourier, sample_fourier;
+  /* 'Source options' */
+  int plane_wave;     /* 1: Gaussian pulse, 0: CW with ramps               */
+  int tfsf_zi, tfsf_zf; /* iz_min and iz_max (= tfsf_zi + 5)               */
+  int cosine;         /* 1: real-valued source                             */
+  double epump;       /* amplitude in a.u. (Epump and Eoxy)                */
+  double wlpump;      /* wavelength in nm                                  */
+  double pump_dt;     /* pulse duration in a.u.                            */
+  double def_pulse;
+  double gpump, zopump; /* pulse width (cells) and origin                  */
+  double tincr, tdecay; /* CW switch-on / switch-off times in a.u.         */
+  double gap;         /* GAP, never set by the reference (0)               */
+  double ratio_angle; /* 1: normal incidence                               */
+  /* 'Slit Array' */
+  int dh, dx, aix, afx;
+  /* constants as the reference evaluates them (code/physconst.f90:31-53) */
+  double pi, c0, eps0, mu0, f_abohr, uat, f_e, pmlalfa;
+  /* Bloch phases per period: complex akx, aky, akz (code/parameters.f90:85,
+   * never assigned by the reference, so 0 there)                          */
+  double akx_re, akx_im, aky_re, aky_im, akz_re, akz_im;
+  int system_model;   /* never assigned by the reference: 0                */
+  /* engine options (not part of the reference) */
+  int precision;      /* IRIS_FP64 or IRIS_FP32                            */
+  int dft_block;      /* samples buffered per DFT accumulation; 0: default */
+  int device;         /* CUDA device ordinal                               */
+} iris_params;
+
+typedef struct iris_engine iris_engine;
+
+/* Human-readable text of a status code / of the last error on this thread. */
+const char* iris_strerror(int status);
+const char* iris_last_error(void);
+
+/*
+ * Read inputFDTD.dat and fill *out; replaces setparam()
+ * (code/files.f90:39-344) with the reference's section scanning, list-
+ * directed reads, unit conversions and truncations.  fw receives the nof
+ * angular frequencies (code/files.f90:216-220) when fw_cap >= nof.
+ * desc (optional) receives the first line of the file (code/main.f90:111).
+ * single_literals: 1 evaluates unsuffixed literals as REAL(4), as standard
+ * Fortran does; 0 evaluates them in double.
+ */
+int iris_setparam(const char* input_path, int single_literals, iris_params* out,
+                  double* fw, int fw_cap, char* desc, int desc_cap);
+
+/* The constants of code/physconst.f90 into p (called by iris_setparam). */
+void iris_physconsts(iris_params* p, int single_literals);
+
+/* Angular frequencies fw(1:nof) from lno/dlamda, code/files.f90:216-220. */
+int iris_frequencies(const iris_params* p, double* fw, int fw_cap);
+
+/*
+ * Allocate and initialise one run: fields e,h = 0 (code/main.f90:166-170),
+ * the UPML slabs and set_sz() profiles (code/driver.f90:177-200,
+ * code/boundary_II.f90:224-276), the DFT sample tables and accumulators of
+ * both boxes (code/driver.f90:205-286, code/dataprocess.f90:793-903), the
+ * TF/SF scratch (code/driver.f90:310-331) and the material of
+ * set_emconstants() + slit() (code/mesh.f90:57-109).
+ */
+int iris_create(const iris_params* p, const double* fw, iris_engine** out);
+void iris_destroy(iris_engine* eng);
+
+/*
+ * Replace the inverse permittivity eps_inv(1,1,0:nx+1,0:ny+1,hi-1:hf+1)
+ * (code/mesh.f90:102-106), x fastest, as re/im arrays of
+ * (nx+2)*(ny+2)*(hf-hi+3) values (im may be NULL: real material).
+ * This is the hook the reference points users to for their own structures
+ * (modify slit(), code/mesh.f90:65-66).
+ */
+int iris_set_material(iris_engine* eng, const double* eps_inv_re, const double* eps_inv_im);
+
+/*
+ * Advance the fields by nsteps steps, it = it0 .. it0+nsteps-1: the body of
+ * the time loop, code/driver.f90:356-451, in the reference's order:
+ * E (all regions), UPML-E, Bloch max ghosts, H, UPML-H, Bloch min ghosts,
+ * TF/SF source, then the DFT sample of E and H when it >= to_fourier and
+ * mod(it, sample_fourier) == 0.  Asynchronous on the engine's stream.
+ */
+int iris_step(iris_engine* eng, int it0, int nsteps);
+
+/* Wait for the engine's stream; reports any deferred CUDA error. */
+int iris_sync(iris_engine* eng);
+
+/*
+ * Poynting flux per face of box 1 or 2 (box = 0 or 1), J[6][nof], face-
+ * major: the Jabs array of scattering_fourier_out
+ * (code/dataprocess.f90:243-277), eps0*Q/(2 dt) included.  Returns
+ * IRIS_ENAN if any value is not finite.
+ */
+int iris_flux(iris_engine* eng, int box, double* J);
+
+/*
+ * Append one output block to <box>_scatt1..6.dat and <box>_scatt.dat in
+ * dir, as scattering_fourier_out does (code/dataprocess.f90:279-299).
+ */
+int iris_write_scatt(const char* dir, int box, int it, int nof, const double* J);
+
+/* Field access in the reference layout (see top of file). */
+int iris_get_field(iris_engine* eng, int which, double* re, double* im);
+int iris_set_field(iris_engine* eng, int which, const double* re, const double* im);
+
+/*
+ * UPML auxiliaries d (which = 0) or b (which = 1) of slab 0 (z in
+ * [1,pmlzi]) or slab 1 (z in [pmlzf,nz]) in the reference layout
+ * (3,1:nx,1:ny,slab) (code/driver.f90:177-188), re/im arrays.
+ */
+int iris_get_pml(iris_engine* eng, int which, int slab, double* re, double* im);
+int iris_set_pml(iris_engine* eng, int which, int slab, const double* re, const double* im);
+
+/*
+ * DFT accumulator emg(j)%fdata(i_pts, iw) of box (0/1) and face pair
+ * j (1..3) in the reference order, i_pts fastest
+ * (code/dataprocess.f90:109-209); *npts receives the point count.
+ * Call with re == NULL to query npts only.
+ */
+int iris_get_fdata(iris_engine* eng, int box, int j, double* re, double* im, long* npts);
+
+/* Run one operator group (IRIS_OP_*) for parity checks; arg is `it` for
+ * IRIS_OP_TFSF and the DFT time index for IRIS_OP_DFT. */
+int iris_apply(iris_engine* eng, int op, int arg);
+
+/*
+ * Full drop-in run in directory dir: program IrisFDTD / main() / driver()
+ * (code/program.f90:25-61, code/main.f90:43-213, code/driver.f90:66-555):
+ * reads dir/inputFDTD.dat, writes log.dat and the <box>_scatt*.dat files
+ * every no_downloads steps and at the last step.  precision: IRIS_FP64 or
+ * IRIS_FP32.  The <<LOOP>> first line runs main() once per index.
+ */
+int iris_run_input(const char* dir, int precision);
+
+/* ---- engine instrumentation (no reference counterpart) --------------- */
+/* Kernel classes timed by iris_timing / iris_timing_read. */
+#define IRIS_KC_E 0      /* E update (e_fdtd + UPML-E + Bloch max)        */
+#define IRIS_KC_H 1      /* H update (h_fdtd + UPML-H + Bloch min)        */
+#define IRIS_KC_TFSF 2   /* TF/SF source                                  */
+#define IRIS_KC_GATHER 3 /* DFT face sample gather                        */
+#define IRIS_KC_DFT 4    /* DFT block accumulation (and its twiddles)     */
+#define IRIS_KC_FLUX 5   /* flux reduction                                */
+#define IRIS_NKC 6
+
+/*
+ * Start a timed region on the engine's stream: records a start event and,
+ * when enable != 0, a pair of CUDA events around every kernel launched
+ * until iris_timing_read.
+ */
+int iris_timing(iris_engine* eng, int enable);
+/* End the region: its device time, and per kernel class the summed device
+ * time (ms) and launch count (arrays of IRIS_NKC, either may be NULL). */
+int iris_timing_read(iris_engine* eng, double* region_ms, double* kernel_ms, long* launches);
+/* Sizes: info[0] DFT sample points, [1] DFT block length K, [2] bytes per
+ * stored complex value, [3] elements per field component, [4] complex
+ * material flag, [5] number of DFT boxes. */
+int iris_info(const iris_engine* eng, long* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IRIS_FDTD_H */

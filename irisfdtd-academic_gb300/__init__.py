@@ -1,0 +1,250 @@
+"""GB300-native FDTD engine with IrisFDTD-Academic's hot-path interface.
+
+Python host mirror of the reference's operator interface, over the C ABI in
+include/iris_fdtd.h (libiris_fdtd.so, CUDA kernels for sm_103a):
+
+=====================  =========================================================
+this module            reference (IrisFDTD-Academic, Fortran)
+=====================  =========================================================
+``setparam``           setparam(), code/files.f90:39-344
+``set_emconstants``    set_emconstants(), code/mesh.f90:75-109 (+ slit(), :57-69)
+``Engine``             main()/driver() state, code/main.f90:164-170, driver.f90:174-335
+``Engine.step``        the time-loop body, code/driver.f90:356-451
+``Engine.e_fdtd``      e_fdtd + UPML_Array_e + bc_*max_bloch (driver.f90:388-400)
+``Engine.h_fdtd``      h_fdtd + UPML_Array_h + bc_*min_bloch (driver.f90:405-415)
+``Engine.tfsf``        tfsf_gauss/tfsf_plane_wave + tfsf_update_* (driver.f90:420-442)
+``Engine.scattering_fourier``      scattering_fourier, code/dataprocess.f90:109-209
+``Engine.scattering_fourier_out``  flux of scattering_fourier_out, :213-277
+``run_input``          program IrisFDTD, code/program.f90:25-61
+``tr_normalise``       irisfdtd_scatt.py:40-42
+=====================  =========================================================
+
+Errors raise :class:`IrisError` carrying the C status code (the reference
+STOPs in err(), code/files.f90:352-381).  There is no CPU fallback: without
+the native library (or without a GPU) the engine entry points raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import native
+from .native import IrisError, IrisParams, build, check, lib
+
+FP64, FP32 = 0, 1
+E, H = 0, 1
+OP_E, OP_H, OP_TFSF, OP_DFT = 1, 2, 3, 4
+
+__all__ = [
+    "FP64", "FP32", "E", "H", "IrisError", "IrisParams", "Engine", "build", "lib", "setparam",
+    "set_emconstants", "run_input", "tr_normalise", "wavelength_axis", "frequencies", "physconsts",
+]
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def physconsts(single_literals: bool = True) -> IrisParams:
+    p = IrisParams()
+    lib().iris_physconsts(ctypes.byref(p), 1 if single_literals else 0)
+    return p
+
+
+def frequencies(p: IrisParams) -> np.ndarray:
+    fw = np.zeros(max(p.nof, 1))
+    check(lib().iris_frequencies(ctypes.byref(p), _dp(fw), len(fw)), "iris_frequencies")
+    return fw[: p.nof]
+
+
+def setparam(path: str, single_literals: bool = True):
+    """Read inputFDTD.dat: returns (params, fw, description)."""
+    L = lib()
+    p = IrisParams()
+    desc = ctypes.create_string_buffer(128)
+    check(L.iris_setparam(os.fsencode(path), 1 if single_literals else 0, ctypes.byref(p), None, 0, desc, 128),
+          "iris_setparam")
+    return p, frequencies(p), desc.value.decode("latin-1")
+
+
+def set_emconstants(p: IrisParams) -> np.ndarray:
+    """eps_inv over (hi-1:hf+1, 0:ny+1, 0:nx+1) as complex [z, y, x], with the
+    slit of slit() applied (code/mesh.f90:57-109)."""
+    nz = p.hf - p.hi + 3
+    eb = complex(p.eps_bbox_re, p.eps_bbox_im)
+    a = np.full((nz, p.ny + 2, p.nx + 2), 1.0 / eb, dtype=np.complex128)
+    a[0] = 1.0 / p.eps1
+    a[-1] = 1.0 / p.eps3
+    if p.afx >= p.aix:
+        a[1:-1, :, p.aix:p.afx + 1] = 1.0
+    return a
+
+
+class Engine:
+    """One run: device state of main()+driver() behind iris_create."""
+
+    def __init__(self, p: IrisParams, fw=None, precision: int | None = None, dft_block: int = 0, device: int = 0):
+        self.L = lib()
+        q = p.copy()
+        if precision is not None:
+            q.precision = precision
+        q.dft_block = dft_block
+        q.device = device
+        self.p = q
+        self.fw = np.ascontiguousarray(frequencies(q) if fw is None else np.asarray(fw, dtype=np.float64))
+        h = ctypes.c_void_p()
+        check(self.L.iris_create(ctypes.byref(self.p), _dp(self.fw), ctypes.byref(h)), "iris_create")
+        self.h = h
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.iris_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- shapes
+    @property
+    def field_shape(self):
+        p = self.p
+        return (p.nz + 2, p.ny + 2, p.nx + 2, 3)
+
+    def pml_shape(self, slab: int):
+        p = self.p
+        return ((p.pmlzi if slab == 0 else p.nz - p.pmlzf + 1), p.ny, p.nx, 3)
+
+    # -- material
+    def set_material(self, eps_inv: np.ndarray):
+        a = np.asarray(eps_inv, dtype=np.complex128)
+        p = self.p
+        want = (p.hf - p.hi + 3, p.ny + 2, p.nx + 2)
+        if a.shape != want:
+            raise ValueError(f"eps_inv shape {a.shape} != {want}")
+        re = np.ascontiguousarray(a.real)
+        im = np.ascontiguousarray(a.imag)
+        check(self.L.iris_set_material(self.h, _dp(re), _dp(im) if np.any(im) else None), "iris_set_material")
+
+    # -- stepping
+    def step(self, it0: int, n: int):
+        check(self.L.iris_step(self.h, it0, n), "iris_step")
+
+    def sync(self):
+        check(self.L.iris_sync(self.h), "iris_sync")
+
+    def e_fdtd(self):
+        check(self.L.iris_apply(self.h, OP_E, 0), "iris_apply(E)")
+
+    def h_fdtd(self):
+        check(self.L.iris_apply(self.h, OP_H, 0), "iris_apply(H)")
+
+    def tfsf(self, it: int):
+        check(self.L.iris_apply(self.h, OP_TFSF, it), "iris_apply(TFSF)")
+
+    def scattering_fourier(self, t: int):
+        check(self.L.iris_apply(self.h, OP_DFT, t), "iris_apply(DFT)")
+
+    def scattering_fourier_out(self, box: int = 0) -> np.ndarray:
+        return self.flux(box)
+
+    def flux(self, box: int = 0) -> np.ndarray:
+        J = np.zeros(6 * self.p.nof)
+        check(self.L.iris_flux(self.h, box, _dp(J)), "iris_flux")
+        return J.reshape(6, self.p.nof)
+
+    # -- state access in the reference layout
+    def get_field(self, which: int) -> np.ndarray:
+        n = int(np.prod(self.field_shape))
+        re, im = np.empty(n), np.empty(n)
+        check(self.L.iris_get_field(self.h, which, _dp(re), _dp(im)), "iris_get_field")
+        return (re + 1j * im).reshape(self.field_shape)
+
+    def set_field(self, which: int, f: np.ndarray):
+        a = np.asarray(f, dtype=np.complex128).reshape(-1)
+        re, im = np.ascontiguousarray(a.real), np.ascontiguousarray(a.imag)
+        check(self.L.iris_set_field(self.h, which, _dp(re), _dp(im)), "iris_set_field")
+
+    def get_pml(self, which: int, slab: int) -> np.ndarray:
+        n = int(np.prod(self.pml_shape(slab)))
+        re, im = np.empty(n), np.empty(n)
+        check(self.L.iris_get_pml(self.h, which, slab, _dp(re), _dp(im)), "iris_get_pml")
+        return (re + 1j * im).reshape(self.pml_shape(slab))
+
+    def set_pml(self, which: int, slab: int, v: np.ndarray):
+        a = np.asarray(v, dtype=np.complex128).reshape(-1)
+        re, im = np.ascontiguousarray(a.real), np.ascontiguousarray(a.imag)
+        check(self.L.iris_set_pml(self.h, which, slab, _dp(re), _dp(im)), "iris_set_pml")
+
+    # -- instrumentation
+    KERNELS = ("update_e", "update_h", "tfsf", "dft_gather", "dft_block", "flux")
+
+    def timing_start(self, per_kernel: bool = True):
+        check(self.L.iris_timing(self.h, 1 if per_kernel else 0), "iris_timing")
+
+    def timing_read(self):
+        """(region_ms, {kernel: ms}, {kernel: launches}) of the timed region."""
+        reg = ctypes.c_double(0)
+        ms = np.zeros(6)
+        n = (ctypes.c_long * 6)()
+        check(self.L.iris_timing_read(self.h, ctypes.byref(reg), _dp(ms), n), "iris_timing_read")
+        return reg.value, dict(zip(self.KERNELS, ms.tolist())), dict(zip(self.KERNELS, list(n)))
+
+    def info(self) -> dict:
+        a = (ctypes.c_long * 6)()
+        check(self.L.iris_info(self.h, a), "iris_info")
+        return dict(dft_points=a[0], dft_block=a[1], bytes_per_complex=a[2], comp_elems=a[3],
+                    complex_material=bool(a[4]), boxes=a[5])
+
+    def get_fdata(self, box: int, j: int) -> np.ndarray:
+        """emg(j)%fdata in the reference order as complex [iw, i_pts]."""
+        n = ctypes.c_long(0)
+        check(self.L.iris_get_fdata(self.h, box, j, None, None, ctypes.byref(n)), "iris_get_fdata")
+        npts = n.value
+        if npts == 0:
+            return np.zeros((self.p.nof, 0), dtype=np.complex128)
+        re, im = np.empty(npts * self.p.nof), np.empty(npts * self.p.nof)
+        check(self.L.iris_get_fdata(self.h, box, j, _dp(re), _dp(im), ctypes.byref(n)), "iris_get_fdata")
+        return (re + 1j * im).reshape(self.p.nof, npts)
+
+
+def run_input(directory: str, precision: int = FP64):
+    """The drop-in main program: reads directory/inputFDTD.dat, writes log.dat and
+    the <box>_scatt*.dat files there."""
+    check(lib().iris_run_input(os.fsencode(directory), precision), "iris_run_input")
+
+
+def tr_normalise(j5: np.ndarray, j6: np.ndarray):
+    """R = J5/(J5+J6), T = J6/(J5+J6) (irisfdtd_scatt.py:40-42), in FP64."""
+    j5 = np.asarray(j5, dtype=np.float64)
+    j6 = np.asarray(j6, dtype=np.float64)
+    tot = j5 + j6
+    return j5 / tot, j6 / tot
+
+
+def wavelength_axis(lno: float, dlamda: float, nof: int) -> np.ndarray:
+    """The plotting axis of IrisFDTD_scattering.py:111,143."""
+    return np.linspace(lno, lno + dlamda * nof, nof)
+
+
+def read_scatt(path: str, nof: int) -> np.ndarray:
+    """Blocks of a <box>_scatt<j>.dat file as [block, nof] (IrisFDTD_scattering.py:74-99)."""
+    vals = []
+    with open(path) as fh:
+        for line in fh:
+            v = line.split()
+            if v and v[0] != "#":
+                vals.append(float(v[0]))
+    a = np.asarray(vals)
+    return a.reshape(-1, nof)

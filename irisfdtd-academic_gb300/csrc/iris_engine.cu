@@ -1,0 +1,1407 @@
+// GB300 (sm_103a) FDTD engine: device state, kernels and the C ABI that
+// replaces the per-step operators of IrisFDTD-Academic's driver loop
+// (code/driver.f90:338-451).
+//
+// Data layout in HBM
+//   * E and H: three component arrays each, complex (double2 in FP64 mode,
+//     float2 in FP32 mode), x fastest, ghost planes 0 and n+1 on every axis,
+//     rows padded so that x = 1 starts on a 128-byte boundary.  Updated in
+//     place: the leapfrog update of a cell reads only its own old value, so
+//     the reference's cur/prev pointer swap (code/driver.f90:358-384) needs no
+//     second copy.
+//   * UPML auxiliaries D and B exist for the two z slabs only, also updated
+//     in place.
+//   * Structure inverse permittivity over z in [hi, hf] (real when the
+//     material is lossless, complex otherwise).
+//   * DFT: a ring of K sample slots [K][P] gathered from the box faces after
+//     each sampled step, accumulated into fdata [nof][P] (complex double)
+//     one block of samples at a time.
+//
+// Arithmetic: the FP64 mode uses __dmul_rn/__dadd_rn (never contracted to
+// FMA) so the stencil rounds exactly like the reference build; the FP32 mode
+// lets the compiler contract.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "iris_internal.h"
+
+namespace iris {
+namespace {
+
+// ---------------------------------------------------------------------------
+// device arithmetic
+
+template <typename T> struct V2;
+template <> struct V2<double> { using t = double2; };
+template <> struct V2<float> { using t = float2; };
+
+template <typename T> __device__ __forceinline__ T mul_(T a, T b);
+template <typename T> __device__ __forceinline__ T add_(T a, T b);
+template <typename T> __device__ __forceinline__ T sub_(T a, T b);
+template <> __device__ __forceinline__ double mul_<double>(double a, double b) { return __dmul_rn(a, b); }
+template <> __device__ __forceinline__ double add_<double>(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ double sub_<double>(double a, double b) { return __dsub_rn(a, b); }
+template <> __device__ __forceinline__ float mul_<float>(float a, float b) { return a * b; }
+template <> __device__ __forceinline__ float add_<float>(float a, float b) { return a + b; }
+template <> __device__ __forceinline__ float sub_<float>(float a, float b) { return a - b; }
+
+template <typename T> struct cx { T re, im; };
+
+template <typename T> __device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) { return {add_(a.re, b.re), add_(a.im, b.im)}; }
+template <typename T> __device__ __forceinline__ cx<T> csub(cx<T> a, cx<T> b) { return {sub_(a.re, b.re), sub_(a.im, b.im)}; }
+template <typename T> __device__ __forceinline__ cx<T> rmul(T r, cx<T> a) { return {mul_(r, a.re), mul_(r, a.im)}; }
+template <typename T> __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
+  return {sub_(mul_(a.re, b.re), mul_(a.im, b.im)), add_(mul_(a.re, b.im), mul_(a.im, b.re))};
+}
+template <typename T> __device__ __forceinline__ cx<T> ld(const typename V2<T>::t* p) {
+  typename V2<T>::t v = *p;
+  return {v.x, v.y};
+}
+template <typename T> __device__ __forceinline__ void st(typename V2<T>::t* p, cx<T> a) {
+  typename V2<T>::t v;
+  v.x = a.re;
+  v.y = a.im;
+  *p = v;
+}
+
+// ---------------------------------------------------------------------------
+// geometry of a ghost-padded field component
+
+struct Geo {
+  int nx, ny, nz;
+  long pitch, plane, comp;  // in elements
+  int xo;                   // storage index of x is x + xo
+  __host__ __device__ __forceinline__ long at(int x, int y, int z) const {
+    return (long)z * plane + (long)y * pitch + (long)(x + xo);
+  }
+};
+
+// UPML coefficient row (24 per PML z-plane), see make_coef()
+enum { CD_A = 0, CD_B = 3, CE_A = 6, CE_B = 9, C_FP = 12, C_FM = 15, CB_B = 18, CH_B = 21, NCOEF = 24 };
+
+template <typename T> struct FieldArgs {
+  typename V2<T>::t* e;  // component 0; components 1,2 at +comp, +2 comp
+  typename V2<T>::t* h;
+  Geo g;
+  typename V2<T>::t* pml_d[2];
+  typename V2<T>::t* pml_b[2];
+  long pcomp[2];
+  const T* coef;
+  int pmlzi, pmlzf, hi, hf;
+  const typename V2<T>::t* eps_c;  // complex structure material or null
+  const T* eps_r;                  // real structure material or null
+  T m1, m3, eps0sq, dtcq2;
+  cx<T> pxp, pyp, pzp, pxm, pym, pzm;  // Bloch phases exp(+-i ak)
+};
+
+// e_fdtd (code/fdtd.f90:57-153) + UPML_Array_e (code/boundary_II.f90:60-138)
+// + bc_{x,y,z}max_bloch (code/boundary.f90:193-216,257-284,321-348) for the
+// E ghosts.  Per z the reference's region order decides: the UPML slabs
+// overwrite whatever e_fdtd wrote there.
+template <typename T, bool CEPS>
+__global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
+  using V = typename V2<T>::t;
+  const Geo g = a.g;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (x > g.nx || y > g.ny || z > g.nz) return;
+  const long i = g.at(x, y, z);
+  const V* H1 = a.h;
+  const V* H2 = a.h + g.comp;
+  const V* H3 = a.h + 2 * g.comp;
+  V* E[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
+  const cx<T> h1 = ld<T>(H1 + i), h2 = ld<T>(H2 + i), h3 = ld<T>(H3 + i);
+  cx<T> c[3];
+  c[0] = cadd(csub(csub(h3, ld<T>(H3 + i - g.pitch)), h2), ld<T>(H2 + i - g.plane));
+  c[1] = cadd(csub(csub(h1, ld<T>(H1 + i - g.plane)), h3), ld<T>(H3 + i - 1));
+  c[2] = cadd(csub(csub(h2, ld<T>(H2 + i - 1)), h1), ld<T>(H1 + i - g.pitch));
+  cx<T> e[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) e[k] = ld<T>(E[k] + i);
+  if (z <= a.pmlzi || z >= a.pmlzf) {
+    const int slab = z <= a.pmlzi ? 0 : 1;
+    const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
+    const int row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
+    const T* cf = a.coef + NCOEF * row;
+    const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
+    V* D = a.pml_d[slab];
+    const long pc = a.pcomp[slab];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const cx<T> ck = rmul(a.eps0sq, c[k]);
+      const cx<T> dold = ld<T>(D + k * pc + pi);
+      const cx<T> dn = cadd(rmul(cf[CD_A + k], dold), rmul(cf[CD_B + k], ck));
+      st<T>(D + k * pc + pi, dn);
+      e[k] = cadd(rmul(cf[CE_A + k], e[k]), rmul(cf[CE_B + k], csub(rmul(cf[C_FP + k], dn), rmul(cf[C_FM + k], dold))));
+    }
+  } else if (z >= a.hi && z <= a.hf) {
+    const long ie = (long)(z - a.hi) * g.plane + (long)y * g.pitch + (long)(x + g.xo);
+    if (CEPS) {
+      const cx<T> ep = ld<T>(a.eps_c + ie);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) e[k] = cadd(e[k], cmul(ep, c[k]));
+    } else {
+      const T ep = a.eps_r[ie];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) e[k] = cadd(e[k], rmul(ep, c[k]));
+    }
+  } else {
+    const T m = z < a.hi ? a.m1 : a.m3;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) e[k] = cadd(e[k], rmul(m, c[k]));
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) st<T>(E[k] + i, e[k]);
+  if (x == 1) {
+    const long j = g.at(g.nx + 1, y, z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pxp, e[k]));
+  }
+  if (y == 1) {
+    const long j = g.at(x, g.ny + 1, z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pyp, e[k]));
+  }
+  if (z == 1) {
+    const long j = g.at(x, y, g.nz + 1);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pzp, e[k]));
+  }
+}
+
+// h_fdtd (code/fdtd.f90:157-248) + UPML_Array_h (code/boundary_II.f90:142-220)
+// + bc_{x,y,z}min_bloch (code/boundary.f90:163-187,224-251,288-315) for the
+// H ghosts and the E ghosts at 0.  The ghosts at nx+1/ny+1/nz+1 of H are
+// never read by any operator and are not maintained.
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_h(FieldArgs<T> a) {
+  using V = typename V2<T>::t;
+  const Geo g = a.g;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (x > g.nx || y > g.ny || z > g.nz) return;
+  const long i = g.at(x, y, z);
+  V* Ec[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
+  const V* E1 = Ec[0];
+  const V* E2 = Ec[1];
+  const V* E3 = Ec[2];
+  V* H[3] = {a.h, a.h + g.comp, a.h + 2 * g.comp};
+  cx<T> ev[3];
+  ev[0] = ld<T>(E1 + i);
+  ev[1] = ld<T>(E2 + i);
+  ev[2] = ld<T>(E3 + i);
+  cx<T> c[3];
+  c[0] = cadd(csub(csub(ld<T>(E3 + i + g.pitch), ev[2]), ld<T>(E2 + i + g.plane)), ev[1]);
+  c[1] = cadd(csub(csub(ld<T>(E1 + i + g.plane), ev[0]), ld<T>(E3 + i + 1)), ev[2]);
+  c[2] = cadd(csub(csub(ld<T>(E2 + i + 1), ev[1]), ld<T>(E1 + i + g.pitch)), ev[0]);
+  cx<T> h[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) h[k] = ld<T>(H[k] + i);
+  if (z <= a.pmlzi || z >= a.pmlzf) {
+    const int slab = z <= a.pmlzi ? 0 : 1;
+    const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
+    const int row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
+    const T* cf = a.coef + NCOEF * row;
+    const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
+    V* B = a.pml_b[slab];
+    const long pc = a.pcomp[slab];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const cx<T> bold = ld<T>(B + k * pc + pi);
+      const cx<T> bn = csub(rmul(cf[CD_A + k], bold), rmul(cf[CB_B + k], c[k]));
+      st<T>(B + k * pc + pi, bn);
+      h[k] = cadd(rmul(cf[CE_A + k], h[k]), rmul(cf[CH_B + k], csub(rmul(cf[C_FP + k], bn), rmul(cf[C_FM + k], bold))));
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) h[k] = csub(h[k], rmul(a.dtcq2, c[k]));
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) st<T>(H[k] + i, h[k]);
+  if (x == g.nx) {
+    const long j = g.at(0, y, z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      st<T>(Ec[k] + j, cmul(a.pxm, ev[k]));
+      st<T>(H[k] + j, cmul(a.pxm, h[k]));
+    }
+  }
+  if (y == g.ny) {
+    const long j = g.at(x, 0, z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      st<T>(Ec[k] + j, cmul(a.pym, ev[k]));
+      st<T>(H[k] + j, cmul(a.pym, h[k]));
+    }
+  }
+  if (z == g.nz) {
+    const long j = g.at(x, y, 0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      st<T>(Ec[k] + j, cmul(a.pzm, ev[k]));
+      st<T>(H[k] + j, cmul(a.pzm, h[k]));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// TF/SF source: tfsf_gauss (code/tfsf.f90:231-355) or tfsf_plane_wave
+// (code/tfsf.f90:359-517) evaluated in FP64 at the two planes the update
+// reads, then tfsf_update_3DArray (code/tfsf.f90:76-153) or
+// tfsf_update_2DArray (code/tfsf.f90:163-227) over the reference's ranges,
+// ghosts included.  The incident field is y-independent, so each thread
+// evaluates it once for its ix and walks a chunk of iy.
+
+struct SrcArgs {
+  int variant;  // 0 none, 1 update_3DArray, 2 update_2DArray
+  int i_pol, plane_wave, cosine;
+  int nx, ny, iz_min;
+  int ixo, izo_i;  // izo_i: the INTEGER izo of tfsf_plane_wave
+  double izo;      // the REAL izo of tfsf_gauss (zopump)
+  double Q, c0dt, ko, Dk, ux, uz;
+  double sign_kz;  // +1 source in the cover, -1 in the substrate
+  double sq_eps;   // sqrt(eps of the source medium)
+  double sqs;      // sqrt(eps)*sign_kz
+  double uzs;      // u_z*sign_kz
+  double amp;      // Epump*Q
+  double hcoef;    // Epump*Q*(dt*c0/Q)
+  double eps_in1, eps_src, dtcq2, s1, tincr, tdecay;
+};
+
+
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dq(double a, double b) { return __ddiv_rn(a, b); }
+
+// Incident field at (ix, iz), step it.  i_pol = 2: ta = tf1 (E_x), tb = tf5
+// (H_y, scaled by dt*c0/Q); i_pol = 1: ta = tf2 (E_y), tb = tf4 (H_x).  The
+// expressions keep the reference's association (code/tfsf.f90:306-347 and
+// :430-508), with exact shortcuts only where a factor is (1,0) or +-1.
+__device__ void incident(const SrcArgs& s, int ix, int iz, int it, cx<double>& ta, cx<double>& tb) {
+  double cs, sn, env;
+  const double t = dm(s.c0dt, (double)it);  // c0*dt*(it-ito), ito = 0
+  const bool gauss = s.plane_wave == 1;
+  if (gauss) {
+    const double A = da(dm(dm(s.Q, (double)(ix - s.ixo)), s.ux), dm(dm(s.Q, ds((double)iz, s.izo)), s.uz));
+    const double kzz = dm(s.ko, ds(dm(s.sqs, A), t));
+    const double arg = dq(ds(A, dq(t, s.sq_eps)), s.Dk);
+    env = exp(-dm(arg, arg));
+    sincos(kzz, &sn, &cs);
+  } else {
+    const double A = da(dm(dm(s.Q, (double)(ix - s.ixo)), s.ux), dm(dm(s.Q, (double)(iz - s.izo_i)), s.uz));
+    const double kzz = dm(s.ko, ds(A, dq(t, s.s1)));
+    const double d = dm(s.Q, fabs((double)(iz - s.izo_i)));
+    const double ton = dm(s.c0dt, ds((double)it, s.tincr));
+    const double toff = dm(s.c0dt, ds((double)it, s.tdecay));
+    if (ton <= d) env = exp(dq(-ds(d, ton), s.Dk));
+    else if (toff >= d) env = exp(dq(ds(d, toff), s.Dk));
+    else env = 1.0;
+    sincos(kzz, &sn, &cs);
+  }
+  const double sg = gauss ? s.sign_kz : 1.0;
+  // sign*(1,0)*exp(i kzz)*env  ->  (env*(sign*c), env*(sign*s))
+  const cx<double> w{dm(env, dm(sg, cs)), dm(env, dm(sg, sn))};
+  const cx<double> w1{dm(env, cs), dm(env, sn)};  // (1,0)*exp(i kzz)*env
+  if (s.i_pol == 2) {
+    const cx<double> ex{dm(s.uz, w.re), dm(s.uz, w.im)};
+    const cx<double> ez{-dm(s.ux, w1.re), -dm(s.ux, w1.im)};
+    cx<double> hy;
+    if (gauss) hy = {ds(dm(s.uzs, ex.re), dm(s.ux, ez.re)), ds(dm(s.uzs, ex.im), dm(s.ux, ez.im))};
+    else hy = {dm(s.s1, ds(dm(s.uz, ex.re), dm(s.ux, ez.re))), dm(s.s1, ds(dm(s.uz, ex.im), dm(s.ux, ez.im)))};
+    cx<double> exo = ex;
+    if (s.cosine == 1) {
+      exo.im = 0.0;
+      hy.im = 0.0;
+    }
+    ta = {dm(s.amp, exo.re), dm(s.amp, exo.im)};
+    tb = {dm(s.hcoef, hy.re), dm(s.hcoef, hy.im)};
+  } else if (s.i_pol == 1) {
+    const cx<double> hx{-dm(s.uz, w.re), -dm(s.uz, w.im)};
+    const cx<double> hz{dm(s.ux, w1.re), dm(s.ux, w1.im)};
+    cx<double> ey;
+    if (gauss) ey = {ds(dm(s.ux, hz.re), dm(s.uzs, hx.re)), ds(dm(s.ux, hz.im), dm(s.uzs, hx.im))};
+    else ey = {dm(s.s1, ds(dm(s.ux, hz.re), dm(s.uz, hx.re))), dm(s.s1, ds(dm(s.ux, hz.im), dm(s.uz, hx.im)))};
+    cx<double> hxo = hx;
+    if (s.cosine == 1) {
+      ey.im = 0.0;
+      hxo.im = 0.0;
+    }
+    ta = {dm(s.amp, ey.re), dm(s.amp, ey.im)};
+    tb = {dm(s.hcoef, hxo.re), dm(s.hcoef, hxo.im)};
+  } else {
+    ta = {0.0, 0.0};
+    tb = {0.0, 0.0};
+  }
+}
+
+// Add (sgn=+1) or subtract an FP64 correction to a stored field value.
+template <typename T> __device__ __forceinline__ void corr(typename V2<T>::t* p, cx<double> v, int sgn);
+template <> __device__ __forceinline__ void corr<double>(double2* p, cx<double> v, int sgn) {
+  double2 a = *p;
+  if (sgn > 0) { a.x = da(a.x, v.re); a.y = da(a.y, v.im); }
+  else { a.x = ds(a.x, v.re); a.y = ds(a.y, v.im); }
+  *p = a;
+}
+template <> __device__ __forceinline__ void corr<float>(float2* p, cx<double> v, int sgn) {
+  float2 a = *p;
+  if (sgn > 0) { a.x = (float)((double)a.x + v.re); a.y = (float)((double)a.y + v.im); }
+  else { a.x = (float)((double)a.x - v.re); a.y = (float)((double)a.y - v.im); }
+  *p = a;
+}
+
+constexpr int TFSF_YCH = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(64) k_tfsf(typename V2<T>::t* e, typename V2<T>::t* h, Geo g, SrcArgs s, int it) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ix > s.nx + 1) return;
+  const int y0 = blockIdx.y * TFSF_YCH;
+  const int y1 = min(y0 + TFSF_YCH - 1, s.ny + 1);
+  const int zm = s.iz_min;
+  cx<double> ta, tb, vE, vH;
+  typename V2<T>::t *pe, *ph;
+  int sE, sH, exE, exH, eyE, eyH;  // ix limit and iy limit per update
+  if (s.variant == 1) {
+    cx<double> a0, b0, a1, b1;
+    incident(s, ix, zm - 1, it, a0, b0);  // tfsf_data(:, ix, iy, iz_min-1)
+    incident(s, ix, zm, it, a1, b1);      // tfsf_data(:, ix, iy, iz_min)
+    vE = {dm(s.eps_in1, b0.re), dm(s.eps_in1, b0.im)};
+    vH = {dm(s.dtcq2, a1.re), dm(s.dtcq2, a1.im)};
+    if (s.i_pol == 2) {
+      // E_x(iz_min) += eps_in(1)*tf5(iz_min-1): ix in [0,nx], iy in [0,ny+1]
+      // H_y(iz_min-1) += dtcq2*tf1(iz_min):      ix in [0,nx], iy in [0,ny+1]
+      pe = e;
+      ph = h + g.comp;
+      sE = +1; sH = +1;
+      exE = s.nx; exH = s.nx; eyE = s.ny + 1; eyH = s.ny + 1;
+    } else {
+      // E_y(iz_min) -= eps_in(1)*tf4(iz_min-1): ix in [0,nx+1], iy in [0,ny]
+      // H_x(iz_min-1) -= dtcq2*tf2(iz_min):      ix in [0,nx+1], iy in [0,ny]
+      pe = e + g.comp;
+      ph = h;
+      sE = -1; sH = -1;
+      exE = s.nx + 1; exH = s.nx + 1; eyE = s.ny; eyH = s.ny;
+    }
+    for (int iy = y0; iy <= y1; ++iy) {
+      if (ix <= exE && iy <= eyE) corr<T>(pe + g.at(ix, iy, zm), vE, sE);
+      if (ix <= exH && iy <= eyH) corr<T>(ph + g.at(ix, iy, zm - 1), vH, sH);
+    }
+  } else if (s.variant == 2) {
+    // E_x(iz_min) += tf5(iz_min)/eps ; H_y(iz_min) += dtcq2*tf1(iz_min)
+    incident(s, ix, zm, it, ta, tb);
+    vE = {dq(tb.re, s.eps_src), dq(tb.im, s.eps_src)};
+    vH = {dm(s.dtcq2, ta.re), dm(s.dtcq2, ta.im)};
+    for (int iy = y0; iy <= y1; ++iy) {
+      corr<T>(e + g.at(ix, iy, zm), vE, +1);
+      corr<T>(h + g.comp + g.at(ix, iy, zm), vH, +1);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// On-the-fly DFT (code/dataprocess.f90:109-209)
+
+// One contiguous run of sample points: one component on one face of a box,
+// locations in the reference's order (code/dataprocess.f90:813-900).
+struct Seg {
+  long src;    // storage index of the first location
+  long su, sv; // storage strides of the two in-face axes
+  int nu, nv;  // extents (u fastest)
+  int field;   // 0..2 E components, 3..5 H components
+  int pad;
+  long p0;     // first sample index
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dft_gather(const typename V2<T>::t* __restrict__ e,
+                                                    const typename V2<T>::t* __restrict__ h, long comp,
+                                                    const Seg* __restrict__ segs, typename V2<T>::t* __restrict__ slot,
+                                                    int* tk, int islot, int t) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = t;
+  const Seg sg = segs[blockIdx.y];
+  const long L = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long n = (long)sg.nu * sg.nv;
+  if (L >= n) return;
+  const int u = (int)(L % sg.nu), v = (int)(L / sg.nu);
+  const typename V2<T>::t* src = sg.field < 3 ? e + sg.field * comp : h + (sg.field - 3) * comp;
+  slot[sg.p0 + L] = src[sg.src + (long)u * sg.su + (long)v * sg.sv];
+}
+
+// FP64 mode: fdata(p, iw) += dt*F_k(p)*exp(i*fw(iw)*t_k), k in order, one
+// rounding per reference operation (code/dataprocess.f90:143-147).
+constexpr int DFT64_WC = 8;
+__global__ void __launch_bounds__(128) k_dft_fp64(const double2* __restrict__ S, long P, int nk,
+                                                  const int* __restrict__ tk, const double* __restrict__ fw, int nof,
+                                                  double dt, double2* __restrict__ fd) {
+  extern __shared__ double2 W64[];  // [nk][WC]
+  const int w0 = blockIdx.y * DFT64_WC;
+  for (int t = threadIdx.x; t < nk * DFT64_WC; t += blockDim.x) {
+    const int k = t / DFT64_WC, j = t % DFT64_WC;
+    double2 v = make_double2(0.0, 0.0);
+    if (w0 + j < nof) {
+      double sn, cs;
+      sincos(dm(fw[w0 + j], (double)tk[k]), &sn, &cs);
+      v = make_double2(cs, sn);
+    }
+    W64[t] = v;
+  }
+  __syncthreads();
+  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const int nw = min(DFT64_WC, nof - w0);
+  cx<double> acc[DFT64_WC];
+#pragma unroll
+  for (int j = 0; j < DFT64_WC; ++j)
+    if (j < nw) acc[j] = ld<double>(fd + (long)(w0 + j) * P + p);
+  for (int k = 0; k < nk; ++k) {
+    const cx<double> a = rmul(dt, ld<double>(S + (long)k * P + p));
+#pragma unroll
+    for (int j = 0; j < DFT64_WC; ++j) {
+      const double2 w = W64[k * DFT64_WC + j];
+      acc[j] = cadd(acc[j], cmul(a, cx<double>{w.x, w.y}));
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < DFT64_WC; ++j)
+    if (j < nw) st<double>(fd + (long)(w0 + j) * P + p, acc[j]);
+}
+
+// FP32 mode twiddles: Wt[k][iw] = dt*exp(i*fw(iw)*t_k), phase formed in FP64
+// (it reaches ~1e4 rad), rounded to FP32 once.
+__global__ void k_twiddle(const int* __restrict__ tk, int nk, const double* __restrict__ fw, int nof, double dt,
+                          float2* __restrict__ Wt) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nk * nof) return;
+  const int k = t / nof, j = t % nof;
+  double sn, cs;
+  sincos(fw[j] * (double)tk[k], &sn, &cs);
+  Wt[t] = make_float2((float)(dt * cs), (float)(dt * sn));
+}
+
+// FP32 mode: partial[p][iw] = sum_k F_k(p)*Wt[k][iw] in FP32 registers over
+// the block, then one FP64 add into fdata.
+constexpr int DFT32_WC = 16;
+__global__ void __launch_bounds__(128) k_dft_fp32(const float2* __restrict__ S, long P, int nk,
+                                                  const float2* __restrict__ Wt, int nof, double2* __restrict__ fd) {
+  extern __shared__ float2 W32[];  // [nk][WC]
+  const int w0 = blockIdx.y * DFT32_WC;
+  for (int t = threadIdx.x; t < nk * DFT32_WC; t += blockDim.x) {
+    const int k = t / DFT32_WC, j = t % DFT32_WC;
+    W32[t] = (w0 + j < nof) ? Wt[(long)k * nof + w0 + j] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  float ar[DFT32_WC], ai[DFT32_WC];
+#pragma unroll
+  for (int j = 0; j < DFT32_WC; ++j) ar[j] = ai[j] = 0.f;
+  for (int k = 0; k < nk; ++k) {
+    const float2 s = S[(long)k * P + p];
+#pragma unroll
+    for (int j = 0; j < DFT32_WC; ++j) {
+      const float2 w = W32[k * DFT32_WC + j];
+      ar[j] = fmaf(s.x, w.x, fmaf(-s.y, w.y, ar[j]));
+      ai[j] = fmaf(s.x, w.y, fmaf(s.y, w.x, ai[j]));
+    }
+  }
+  const int nw = min(DFT32_WC, nof - w0);
+#pragma unroll
+  for (int j = 0; j < DFT32_WC; ++j)
+    if (j < nw) {
+      double2* q = fd + (long)(w0 + j) * P + p;
+      double2 f = *q;
+      f.x += (double)ar[j];
+      f.y += (double)ai[j];
+      *q = f;
+    }
+}
+
+// Poynting flux of one face, code/dataprocess.f90:246-277:
+// J = sign * sum Re(a*conj(b) - c*conj(d)) * eps0*Q/(2 dt).
+struct FluxFace {
+  long pa, pb, pc, pd;  // first sample index of the four components
+  long n;               // locations on the face
+  int sign, active;
+};
+
+__global__ void __launch_bounds__(256) k_flux(const double2* __restrict__ fd, long P, const FluxFace* __restrict__ faces,
+                                              int nof, double scale, double* __restrict__ J) {
+  __shared__ double red[256];
+  const int iw = blockIdx.x, f = blockIdx.y;
+  const FluxFace F = faces[f];
+  double s = 0.0;
+  if (F.active) {
+    const double2* row = fd + (long)iw * P;
+    for (long L = threadIdx.x; L < F.n; L += blockDim.x) {
+      const double2 a = row[F.pa + L], b = row[F.pb + L], c = row[F.pc + L], d = row[F.pd + L];
+      s += (a.x * b.x + a.y * b.y) - (c.x * d.x + c.y * d.y);
+    }
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) J[f * nof + iw] = scale * (F.sign > 0 ? red[0] : -red[0]);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+void clear_error() { g_last_error.clear(); }
+
+}  // namespace iris
+
+using namespace iris;
+
+#define CK(call)                                                                                      \
+  do {                                                                                                \
+    cudaError_t err_ = (call);                                                                        \
+    if (err_ != cudaSuccess)                                                                          \
+      return fail(err_ == cudaErrorMemoryAllocation ? IRIS_ENOMEM : IRIS_ECUDA,                      \
+                  std::string(#call) + ": " + cudaGetErrorString(err_));                              \
+  } while (0)
+
+
+namespace {
+
+struct FaceMap {
+  bool active = false;  // this face pair is accumulated by scattering_fourier
+  int nu = 0, nv = 0;
+  long nloc = 0;         // locations per face
+  long base[2][6] = {};  // first sample index per [side][component]
+};
+
+}  // namespace
+
+struct iris_engine {
+  iris_params p{};
+  std::vector<double> fw;
+  int prec = IRIS_FP64;
+  size_t esz = 16;  // bytes per stored complex value
+  int device = 0;
+  cudaStream_t st = nullptr;
+  Geo g{};
+  dim3 blk, grd;
+  void* e = nullptr;
+  void* h = nullptr;
+  void* pml_d[2] = {nullptr, nullptr};
+  void* pml_b[2] = {nullptr, nullptr};
+  long pcomp[2] = {0, 0};
+  int nbot = 0, ntop = 0;
+  void* coef = nullptr;
+  std::vector<double> coef_h;
+  void* eps = nullptr;
+  bool eps_complex = false;
+  double ph[6][2] = {};  // exp(+i akx), exp(+i aky), exp(+i akz), exp(-i akx), ...
+  SrcArgs src{};
+  dim3 tf_blk, tf_grd;
+  // DFT
+  int nboxes = 1;
+  FaceMap fm[2][3];
+  long P = 0;
+  int K = 0, nslot = 0;
+  std::vector<Seg> segs;
+  long max_seg = 0;
+  Seg* d_segs = nullptr;
+  void* S = nullptr;
+  int* d_tk = nullptr;
+  double* d_fw = nullptr;
+  double2* fd = nullptr;
+  float2* d_wt = nullptr;
+  FluxFace* d_faces = nullptr;
+  double* d_J = nullptr;
+  double* h_J = nullptr;
+  // timing: CUDA events on the engine stream, per kernel class
+  bool timing = false;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[IRIS_NKC];
+  size_t ev_used[IRIS_NKC] = {};
+};
+
+namespace {
+
+// Brackets one kernel launch with a pair of events when timing is on.
+struct KTimer {
+  iris_engine* E;
+  int k;
+  cudaEvent_t b = nullptr, e = nullptr;
+  KTimer(iris_engine* eng, int kind) : E(eng), k(kind) {
+    if (!E->timing) return;
+    auto& v = E->ev[k];
+    if (E->ev_used[k] == v.size()) {
+      cudaEvent_t x, y;
+      cudaEventCreate(&x);
+      cudaEventCreate(&y);
+      v.push_back({x, y});
+    }
+    b = v[E->ev_used[k]].first;
+    e = v[E->ev_used[k]].second;
+    ++E->ev_used[k];
+    cudaEventRecord(b, E->st);
+  }
+  ~KTimer() {
+    if (b) cudaEventRecord(e, E->st);
+  }
+};
+
+int p2ceil(int n) {
+  int v = 1;
+  while (v < n) v <<= 1;
+  return v;
+}
+
+// set_sz(), code/boundary_II.f90:224-276, and the per-plane UPML coefficient
+// rows.  Component -> profile permutation of code/boundary_II.f90:86-99:
+// D_k decays with profile pd[k]; E_k with profile pe[k].
+void make_coef(const iris_params& p, std::vector<double>& rows) {
+  const int nb = p.pmlzi, nt = p.nz - p.pmlzf + 1;
+  rows.assign((size_t)NCOEF * (nb + nt), 0.0);
+  const double dtq2 = (p.dt / p.Q) * (p.dt / p.Q);
+  static const int pd[3] = {1, 2, 0}, pe[3] = {2, 0, 1};
+  for (int slab = 0; slab < 2; ++slab) {
+    const int z0 = slab == 0 ? 1 : p.pmlzf, z1 = slab == 0 ? p.pmlzi : p.nz;
+    const double epsb = slab == 0 ? p.eps1 : p.eps3;
+    for (int z = z0; z <= z1; ++z) {
+      long ip = 1;
+      double den = 1.0;
+      double sg3, k3;
+      if (slab == 0) {
+        for (int k = 0; k < p.npml; ++k) { ip *= (long)(p.pmlzi - z); den *= (double)(p.pmlzi - 1); }
+        sg3 = std::sqrt(p.eps1) * p.wzpml * ((double)ip / den);
+        k3 = 1.0 + std::sqrt(p.eps1) * p.pmlalfa * ((double)ip / den);
+      } else {
+        for (int k = 0; k < p.npml; ++k) { ip *= (long)(z - p.pmlzf); den *= (double)(p.nz - p.pmlzf); }
+        sg3 = std::sqrt(p.eps3) * p.wzpml * (double)ip / den;
+        k3 = 1.0 + std::sqrt(p.eps3) * p.pmlalfa * (double)ip / den;
+      }
+      double fp[3], fm[3];
+      for (int c = 0; c < 3; ++c) {
+        const double sg = c == 2 ? sg3 : 0.0, kk = c == 2 ? k3 : 1.0;
+        fp[c] = 2 * p.eps0 * epsb * kk + p.dt * sg;
+        fm[c] = 2 * p.eps0 * epsb * kk - p.dt * sg;
+      }
+      const int row = slab == 0 ? z - 1 : nb + z - p.pmlzf;
+      double* r = rows.data() + (size_t)NCOEF * row;
+      for (int k = 0; k < 3; ++k) {
+        r[CD_A + k] = fm[pd[k]] / fp[pd[k]];
+        r[CD_B + k] = (2 * epsb) / fp[pd[k]];
+        r[CE_A + k] = fm[pe[k]] / fp[pe[k]];
+        r[CE_B + k] = 1 / (p.eps0 * epsb * fp[pe[k]]);
+        r[C_FP + k] = fp[k];
+        r[C_FM + k] = fm[k];
+        r[CB_B + k] = ((2 * epsb) / fp[pd[k]]) * dtq2;
+        r[CH_B + k] = 1 / (p.mu0 * fp[pe[k]]);
+      }
+    }
+  }
+}
+
+SrcArgs make_src(const iris_params& p) {
+  SrcArgs s{};
+  const bool two_d = !(p.ny != 1 && p.nx != 1);
+  if (!two_d) s.variant = 1;
+  else s.variant = p.i_pol == 2 ? 2 : (p.i_pol == 1 ? 1 : 0);
+  if (p.plane_wave != 0 && p.plane_wave != 1) s.variant = 0;  // tfsf_data stays zero
+  if (p.i_pol != 1 && p.i_pol != 2) s.variant = 0;
+  s.i_pol = p.i_pol;
+  s.plane_wave = p.plane_wave;
+  s.cosine = p.cosine;
+  s.nx = p.nx;
+  s.ny = p.ny;
+  s.iz_min = p.tfsf_zi;
+  s.ixo = p.pmlzi - 50;
+  s.izo = p.zopump;
+  s.izo_i = p.ratio_angle >= 0 ? (int)((double)p.pmlzi - 3.0 * p.gap) : (int)((double)p.nz + 3.0 * p.gap);
+  s.Q = p.Q;
+  s.c0dt = p.c0 * p.dt;
+  s.ko = 2 * p.pi / (p.wlpump * p.f_abohr);
+  s.Dk = p.plane_wave == 1 ? p.gpump * p.Q : p.gap * p.Q;
+  double eps_src, sign_kz;
+  if (p.tfsf_zi > p.hi) { eps_src = p.eps3; sign_kz = -1.0; }
+  else { eps_src = p.eps1; sign_kz = 1.0; }
+  s.sign_kz = sign_kz;
+  s.eps_src = eps_src;
+  s.sq_eps = std::sqrt(eps_src);
+  s.sqs = std::sqrt(eps_src) * sign_kz;
+  const double DELTA = p.ratio_angle * p.pi / 2.0;
+  s.ux = std::cos(DELTA);
+  s.uz = std::sin(DELTA);
+  s.uzs = s.uz * sign_kz;
+  s.amp = p.epump * p.Q;
+  s.hcoef = s.amp * (p.dt * p.c0 / p.Q);
+  s.eps_in1 = 1.0 / p.eps1;
+  const double dtc = p.dt * p.c0 / p.Q;
+  s.dtcq2 = (dtc * dtc) * 1.0;  // dtcq2*mu_inv
+  s.s1 = std::sqrt(p.eps1);
+  s.tincr = p.tincr;
+  s.tdecay = p.tdecay;
+  return s;
+}
+
+int validate(const iris_params& p) {
+  auto bad = [](const std::string& m) { return fail(IRIS_EINVAL, m); };
+  if (p.nx < 1 || p.ny < 1 || p.nz < 1) return bad("grid sizes must be >= 1");
+  if (p.pmlzi < 2) return bad("pmlzi must be >= 2 (set_sz divides by pmlzi-1)");
+  if (p.pmlzf > p.nz - 1) return bad("pmlzf must be <= nz-1 (set_sz divides by nz-pmlzf)");
+  if (p.pmlzf <= p.pmlzi) return bad("pmlzf must be > pmlzi");
+  if (p.hi < 1 || p.hf > p.nz || p.hf < p.hi - 1) return bad("structure range [hi,hf] must lie in [1,nz]");
+  if (p.tfsf_zi < 1 || p.tfsf_zi > p.nz) return bad("tfsf_zi must lie in [1,nz]");
+  if (p.nof < 1) return bad("nof must be >= 1");
+  if (p.sample_fourier < 1) return bad("sample_fourier must be >= 1");
+  if (p.npml < 0 || p.npml > 8) return bad("npml out of range");
+  if (p.system_model != 0) return bad("system_model must be 0");
+  if (p.Q <= 0 || p.dt <= 0) return bad("Q and dt must be > 0");
+  if (p.eps1 <= 0 || p.eps3 <= 0) return bad("eps1 and eps3 must be > 0");
+  const int* boxes[2] = {p.box1, p.box2};
+  const int n[3] = {p.nx, p.ny, p.nz};
+  for (int b = 0; b < 2; ++b)
+    for (int a = 0; a < 3; ++a) {
+      const int lo = boxes[b][2 * a], hi = boxes[b][2 * a + 1];
+      if (lo < 1 || hi > n[a] || lo > hi) return bad("DFT box planes must satisfy 1 <= lo <= hi <= n on every axis");
+    }
+  if (p.precision != IRIS_FP64 && p.precision != IRIS_FP32) return bad("precision must be IRIS_FP64 or IRIS_FP32");
+  return IRIS_OK;
+}
+
+template <typename T> FieldArgs<T> field_args(const iris_engine* E) {
+  using V = typename V2<T>::t;
+  const iris_params& p = E->p;
+  FieldArgs<T> a{};
+  a.e = (V*)E->e;
+  a.h = (V*)E->h;
+  a.g = E->g;
+  for (int s = 0; s < 2; ++s) {
+    a.pml_d[s] = (V*)E->pml_d[s];
+    a.pml_b[s] = (V*)E->pml_b[s];
+    a.pcomp[s] = E->pcomp[s];
+  }
+  a.coef = (const T*)E->coef;
+  a.pmlzi = p.pmlzi;
+  a.pmlzf = p.pmlzf;
+  a.hi = p.hi;
+  a.hf = p.hf;
+  a.eps_c = E->eps_complex ? (const V*)E->eps : nullptr;
+  a.eps_r = E->eps_complex ? nullptr : (const T*)E->eps;
+  a.m1 = (T)(1.0 / p.eps1);
+  a.m3 = (T)(1.0 / p.eps3);
+  a.eps0sq = (T)(p.eps0 * p.eps0);
+  const double dtc = p.dt * p.c0 / p.Q;
+  a.dtcq2 = (T)(dtc * dtc);
+  cx<T>* ph[6] = {&a.pxp, &a.pyp, &a.pzp, &a.pxm, &a.pym, &a.pzm};
+  for (int k = 0; k < 6; ++k) *ph[k] = cx<T>{(T)E->ph[k][0], (T)E->ph[k][1]};
+  return a;
+}
+
+template <typename T> void launch_e(iris_engine* E) {
+  KTimer tm(E, IRIS_KC_E);
+  FieldArgs<T> a = field_args<T>(E);
+  if (E->eps_complex) k_update_e<T, true><<<E->grd, E->blk, 0, E->st>>>(a);
+  else k_update_e<T, false><<<E->grd, E->blk, 0, E->st>>>(a);
+}
+template <typename T> void launch_h(iris_engine* E) {
+  KTimer tm(E, IRIS_KC_H);
+  k_update_h<T><<<E->grd, E->blk, 0, E->st>>>(field_args<T>(E));
+}
+template <typename T> void launch_tfsf(iris_engine* E, int it) {
+  if (E->src.variant == 0) return;
+  KTimer tm(E, IRIS_KC_TFSF);
+  using V = typename V2<T>::t;
+  k_tfsf<T><<<E->tf_grd, E->tf_blk, 0, E->st>>>((V*)E->e, (V*)E->h, E->g, E->src, it);
+}
+
+void dft_flush(iris_engine* E) {
+  if (E->nslot == 0) return;
+  KTimer tm(E, IRIS_KC_DFT);
+  const int nk = E->nslot;
+  const unsigned gx = (unsigned)((E->P + 127) / 128);
+  if (E->prec == IRIS_FP64) {
+    dim3 grid(gx, (E->p.nof + DFT64_WC - 1) / DFT64_WC);
+    k_dft_fp64<<<grid, 128, (size_t)nk * DFT64_WC * sizeof(double2), E->st>>>(
+        (const double2*)E->S, E->P, nk, E->d_tk, E->d_fw, E->p.nof, E->p.dt, E->fd);
+  } else {
+    const int nt = nk * E->p.nof;
+    k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
+    dim3 grid(gx, (E->p.nof + DFT32_WC - 1) / DFT32_WC);
+    k_dft_fp32<<<grid, 128, (size_t)nk * DFT32_WC * sizeof(float2), E->st>>>(
+        (const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, E->fd);
+  }
+  E->nslot = 0;
+}
+
+template <typename T> void dft_sample(iris_engine* E, int t) {
+  if (E->P == 0) return;
+  using V = typename V2<T>::t;
+  {
+  KTimer tm(E, IRIS_KC_GATHER);
+  V* slot = (V*)E->S + (long)E->nslot * E->P;
+  dim3 grid((unsigned)((E->max_seg + 255) / 256), (unsigned)E->segs.size());
+  k_dft_gather<T><<<grid, 256, 0, E->st>>>((const V*)E->e, (const V*)E->h, E->g.comp, E->d_segs, slot, E->d_tk,
+                                          E->nslot, t);
+  }
+  if (++E->nslot == E->K) dft_flush(E);
+}
+
+template <typename T> int step_t(iris_engine* E, int it0, int n) {
+  const iris_params& p = E->p;
+  for (int it = it0; it < it0 + n; ++it) {
+    launch_e<T>(E);
+    launch_h<T>(E);
+    launch_tfsf<T>(E, it);
+    if (it >= p.to_fourier && it % p.sample_fourier == 0) dft_sample<T>(E, it + 1 - p.to_fourier);
+  }
+  CK(cudaGetLastError());
+  return IRIS_OK;
+}
+
+// Reference material of set_emconstants() and slit() (code/mesh.f90:57-109)
+// over (0:nx+1, 0:ny+1, hi-1:hf+1), x fastest.
+void default_material(const iris_params& p, std::vector<double>& re, std::vector<double>& im) {
+  const long nxy = (long)(p.nx + 2) * (p.ny + 2);
+  const int nzs = p.hf - p.hi + 3;
+  re.assign(nxy * nzs, 0.0);
+  im.assign(nxy * nzs, 0.0);
+  // 1.0/eps_bbox as a complex division (Smith's algorithm)
+  double c = p.eps_bbox_re, d = p.eps_bbox_im, ir, ii;
+  if (std::fabs(c) >= std::fabs(d)) {
+    const double r = d / c, den = c + d * r;
+    ir = (1.0 + 0.0 * r) / den;
+    ii = (0.0 - 1.0 * r) / den;
+  } else {
+    const double r = c / d, den = c * r + d;
+    ir = (1.0 * r + 0.0) / den;
+    ii = (0.0 * r - 1.0) / den;
+  }
+  for (long i = 0; i < nxy * nzs; ++i) { re[i] = ir; im[i] = ii; }
+  for (long i = 0; i < nxy; ++i) {
+    re[i] = 1.0 / p.eps1; im[i] = 0.0;
+    re[(long)(nzs - 1) * nxy + i] = 1.0 / p.eps3; im[(long)(nzs - 1) * nxy + i] = 0.0;
+  }
+  for (int z = p.hi; z <= p.hf; ++z)
+    for (int y = 0; y <= p.ny + 1; ++y)
+      for (int x = p.aix; x <= p.afx; ++x) {
+        const long i = (long)(z - (p.hi - 1)) * nxy + (long)y * (p.nx + 2) + x;
+        re[i] = 1.0;
+        im[i] = 0.0;
+      }
+}
+
+int upload_material(iris_engine* E, const double* re, const double* im) {
+  const iris_params& p = E->p;
+  const Geo& g = E->g;
+  const int nzs = p.hf - p.hi + 1;  // planes stored: hi..hf
+  bool cplx = false;
+  const long nxy = (long)(p.nx + 2) * (p.ny + 2);
+  if (im)
+    for (long i = nxy; i < nxy * (nzs + 1); ++i)
+      if (im[i] != 0.0) { cplx = true; break; }
+  if (E->eps) { cudaFree(E->eps); E->eps = nullptr; }
+  if (nzs <= 0) { E->eps_complex = false; return IRIS_OK; }
+  const long n = (long)nzs * g.plane;
+  const size_t rsz = E->prec == IRIS_FP64 ? 8 : 4;
+  const size_t bytes = (size_t)n * rsz * (cplx ? 2 : 1);
+  std::vector<unsigned char> host(bytes, 0);
+  for (int zz = 0; zz < nzs; ++zz)
+    for (int y = 0; y <= p.ny + 1; ++y)
+      for (int x = 0; x <= p.nx + 1; ++x) {
+        const long src = (long)(zz + 1) * nxy + (long)y * (p.nx + 2) + x;
+        const long dst = (long)zz * g.plane + (long)y * g.pitch + (x + g.xo);
+        const double vr = re[src], vi = im ? im[src] : 0.0;
+        if (E->prec == IRIS_FP64) {
+          double* h = (double*)host.data();
+          if (cplx) { h[2 * dst] = vr; h[2 * dst + 1] = vi; }
+          else h[dst] = vr;
+        } else {
+          float* h = (float*)host.data();
+          if (cplx) { h[2 * dst] = (float)vr; h[2 * dst + 1] = (float)vi; }
+          else h[dst] = (float)vr;
+        }
+      }
+  CK(cudaMalloc(&E->eps, bytes));
+  CK(cudaMemcpy(E->eps, host.data(), bytes, cudaMemcpyHostToDevice));
+  E->eps_complex = cplx;
+  return IRIS_OK;
+}
+
+int build_dft(iris_engine* E) {
+  const iris_params& p = E->p;
+  bool single = true;
+  for (int i = 0; i < 6; ++i)
+    if (p.box1[i] != p.box2[i]) single = false;
+  E->nboxes = single ? 1 : 2;
+  bool on[3];
+  if (p.nx != 1 && p.ny != 1) on[0] = on[1] = on[2] = true;
+  else {
+    on[0] = (p.ny == 1 && p.nx != 1);
+    on[1] = (p.nx == 1 && p.ny != 1);
+    on[2] = true;
+  }
+  static const int comps[3][4] = {{1, 5, 2, 4}, {2, 3, 0, 5}, {0, 4, 1, 3}};  // (a,b,c,d) 0-based
+  std::vector<FluxFace> faces(12);
+  long P = 0;
+  E->segs.clear();
+  E->max_seg = 0;
+  for (int b = 0; b < E->nboxes; ++b) {
+    const int* bx = b == 0 ? p.box1 : p.box2;
+    const int bxi = bx[0], bxf = bx[1], byi = bx[2], byf = bx[3], bzi = bx[4], bzf = bx[5];
+    const int nbx = bxf + 1 - bxi, nby = byf + 1 - byi, nbz = bzf + 1 - bzi;
+    for (int j = 0; j < 3; ++j) {
+      FaceMap& F = E->fm[b][j];
+      F = FaceMap();
+      if (!on[j]) continue;
+      F.active = true;
+      for (int side = 0; side < 2; ++side) {
+        long src, su, sv;
+        int nu, nv;
+        if (j == 0) {
+          src = E->g.at(side ? bxf : bxi, byi, bzi); su = E->g.pitch; sv = E->g.plane; nu = nby; nv = nbz;
+        } else if (j == 1) {
+          src = E->g.at(bxi, side ? byf : byi, bzi); su = 1; sv = E->g.plane; nu = nbx; nv = nbz;
+        } else {
+          src = E->g.at(bxi, byi, side ? bzf : bzi); su = 1; sv = E->g.pitch; nu = nbx; nv = nby;
+        }
+        F.nu = nu;
+        F.nv = nv;
+        F.nloc = (long)nu * nv;
+        for (int ip = 0; ip < 6; ++ip) {
+          Seg s{};
+          s.src = src; s.su = su; s.sv = sv; s.nu = nu; s.nv = nv; s.field = ip; s.p0 = P;
+          E->segs.push_back(s);
+          F.base[side][ip] = P;
+          P += F.nloc;
+          E->max_seg = std::max(E->max_seg, F.nloc);
+        }
+        FluxFace& ff = faces[6 * b + 2 * j + side];
+        ff.pa = F.base[side][comps[j][0]];
+        ff.pb = F.base[side][comps[j][1]];
+        ff.pc = F.base[side][comps[j][2]];
+        ff.pd = F.base[side][comps[j][3]];
+        ff.n = F.nloc;
+        ff.sign = side == 0 ? -1 : +1;
+        ff.active = 1;
+      }
+    }
+  }
+  E->P = P;
+  // block length K: samples buffered before one accumulation pass
+  size_t freeb = 0, totb = 0;
+  CK(cudaMemGetInfo(&freeb, &totb));
+  const size_t fd_bytes = (size_t)P * p.nof * sizeof(double2);
+  if (fd_bytes > freeb) return fail(IRIS_ENOMEM, "DFT accumulators exceed free device memory");
+  // at most 256 slots: the block kernels stage K x 8 (FP64) or K x 16 (FP32)
+  // twiddles in 32 KB of shared memory
+  int K = std::min(256, p.dft_block > 0 ? p.dft_block : (E->prec == IRIS_FP64 ? 32 : 64));
+  const size_t slot_bytes = std::max<size_t>(1, (size_t)P * E->esz);
+  const size_t budget = (freeb - fd_bytes) / 4;
+  while (K > 1 && (size_t)K * slot_bytes > budget) K /= 2;
+  E->K = std::max(1, K);
+  E->nslot = 0;
+  CK(cudaMalloc(&E->fd, std::max<size_t>(fd_bytes, 16)));
+  CK(cudaMemsetAsync(E->fd, 0, std::max<size_t>(fd_bytes, 16), E->st));
+  CK(cudaMalloc(&E->S, (size_t)E->K * slot_bytes));
+  CK(cudaMalloc(&E->d_tk, sizeof(int) * E->K));
+  CK(cudaMalloc(&E->d_fw, sizeof(double) * p.nof));
+  CK(cudaMemcpy(E->d_fw, E->fw.data(), sizeof(double) * p.nof, cudaMemcpyHostToDevice));
+  if (E->prec == IRIS_FP32) CK(cudaMalloc(&E->d_wt, sizeof(float2) * (size_t)E->K * p.nof));
+  if (!E->segs.empty()) {
+    CK(cudaMalloc(&E->d_segs, sizeof(Seg) * E->segs.size()));
+    CK(cudaMemcpy(E->d_segs, E->segs.data(), sizeof(Seg) * E->segs.size(), cudaMemcpyHostToDevice));
+  }
+  CK(cudaMalloc(&E->d_faces, sizeof(FluxFace) * 12));
+  CK(cudaMemcpy(E->d_faces, faces.data(), sizeof(FluxFace) * 12, cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&E->d_J, sizeof(double) * 6 * p.nof));
+  CK(cudaMallocHost(&E->h_J, sizeof(double) * 6 * p.nof));
+  return IRIS_OK;
+}
+
+void free_engine(iris_engine* E) {
+  void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
+                  E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (E->h_J) cudaFreeHost(E->h_J);
+  for (int k = 0; k < IRIS_NKC; ++k)
+    for (auto& pr : E->ev[k]) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  if (E->t0) cudaEventDestroy(E->t0);
+  if (E->t1) cudaEventDestroy(E->t1);
+  if (E->st) cudaStreamDestroy(E->st);
+}
+
+}  // namespace
+
+long iris::engine_npts(const iris_engine* E, int box, int j) {
+  if (box < 0 || box >= E->nboxes || j < 1 || j > 3) return 0;
+  const FaceMap& F = E->fm[box][j - 1];
+  return F.active ? 12 * F.nloc : 0;
+}
+
+extern "C" {
+
+int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
+  clear_error();
+  if (!pin || !fw || !out) return fail(IRIS_EINVAL, "null argument");
+  *out = nullptr;
+  int rc = validate(*pin);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(IRIS_ENODEV, "no CUDA device");
+  if (pin->device < 0 || pin->device >= ndev) return fail(IRIS_EINVAL, "device ordinal out of range");
+  iris_engine* E = new iris_engine();
+  E->p = *pin;
+  const iris_params& p = E->p;
+  E->fw.assign(fw, fw + p.nof);
+  E->prec = p.precision;
+  E->esz = p.precision == IRIS_FP64 ? 16 : 8;
+  E->device = p.device;
+  auto bail = [&](int code) {
+    free_engine(E);
+    delete E;
+    return code;
+  };
+  if (cudaSetDevice(E->device) != cudaSuccess) return bail(fail(IRIS_ECUDA, "cudaSetDevice failed"));
+  if (cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(IRIS_ECUDA, "cudaStreamCreate failed"));
+  // geometry: x = 1 on a 128-byte boundary
+  Geo& g = E->g;
+  g.nx = p.nx;
+  g.ny = p.ny;
+  g.nz = p.nz;
+  const int align = (int)(128 / E->esz);
+  g.xo = align - 1;
+  g.pitch = ((long)(g.xo + p.nx + 2) + align - 1) / align * align;
+  g.plane = g.pitch * (p.ny + 2);
+  g.comp = (g.plane * (p.nz + 2) + align - 1) / align * align;
+  const size_t fbytes = (size_t)3 * g.comp * E->esz;
+  if (cudaMalloc(&E->e, fbytes) != cudaSuccess || cudaMalloc(&E->h, fbytes) != cudaSuccess)
+    return bail(fail(IRIS_ENOMEM, "field allocation failed"));
+  cudaMemsetAsync(E->e, 0, fbytes, E->st);
+  cudaMemsetAsync(E->h, 0, fbytes, E->st);
+  E->nbot = p.pmlzi;
+  E->ntop = p.nz - p.pmlzf + 1;
+  for (int s = 0; s < 2; ++s) {
+    E->pcomp[s] = (long)p.nx * p.ny * (s == 0 ? E->nbot : E->ntop);
+    const size_t b = (size_t)3 * E->pcomp[s] * E->esz;
+    if (cudaMalloc(&E->pml_d[s], b) != cudaSuccess || cudaMalloc(&E->pml_b[s], b) != cudaSuccess)
+      return bail(fail(IRIS_ENOMEM, "UPML allocation failed"));
+    cudaMemsetAsync(E->pml_d[s], 0, b, E->st);
+    cudaMemsetAsync(E->pml_b[s], 0, b, E->st);
+  }
+  make_coef(p, E->coef_h);
+  {
+    const size_t n = E->coef_h.size();
+    if (E->prec == IRIS_FP64) {
+      if (cudaMalloc(&E->coef, n * 8) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "coef allocation failed"));
+      cudaMemcpy(E->coef, E->coef_h.data(), n * 8, cudaMemcpyHostToDevice);
+    } else {
+      std::vector<float> f(n);
+      for (size_t i = 0; i < n; ++i) f[i] = (float)E->coef_h[i];
+      if (cudaMalloc(&E->coef, n * 4) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "coef allocation failed"));
+      cudaMemcpy(E->coef, f.data(), n * 4, cudaMemcpyHostToDevice);
+    }
+  }
+  // Bloch phases cdexp(+-ci*ak) (code/boundary.f90:175,205,237,270,301,334)
+  const double ak[3][2] = {{p.akx_re, p.akx_im}, {p.aky_re, p.aky_im}, {p.akz_re, p.akz_im}};
+  for (int a = 0; a < 3; ++a)
+    for (int sgn = 0; sgn < 2; ++sgn) {
+      const double s = sgn == 0 ? 1.0 : -1.0;
+      const double ar = -s * ak[a][1], ai = s * ak[a][0];  // (+-ci)*ak
+      const double m = std::exp(ar);
+      E->ph[3 * sgn + a][0] = m * std::cos(ai);
+      E->ph[3 * sgn + a][1] = m * std::sin(ai);
+    }
+  // launch shapes
+  const int bx = std::min(32, p2ceil(p.nx));
+  const int by = std::min(256 / bx, p2ceil(p.ny));
+  const int bz = std::min(256 / (bx * by), p2ceil(p.nz));
+  E->blk = dim3(bx, by, bz);
+  E->grd = dim3((p.nx + bx - 1) / bx, (p.ny + by - 1) / by, (p.nz + bz - 1) / bz);
+  E->src = make_src(p);
+  E->tf_blk = dim3(64);
+  E->tf_grd = dim3((p.nx + 2 + 63) / 64, (p.ny + 2 + TFSF_YCH - 1) / TFSF_YCH);
+  {
+    std::vector<double> re, im;
+    default_material(p, re, im);
+    rc = upload_material(E, re.data(), im.data());
+    if (rc) return bail(rc);
+  }
+  rc = build_dft(E);
+  if (rc) return bail(rc);
+  if (cudaStreamSynchronize(E->st) != cudaSuccess) return bail(fail(IRIS_ECUDA, "initialisation failed"));
+  *out = E;
+  return IRIS_OK;
+}
+
+void iris_destroy(iris_engine* E) {
+  if (!E) return;
+  cudaSetDevice(E->device);
+  cudaStreamSynchronize(E->st);
+  free_engine(E);
+  delete E;
+}
+
+int iris_set_material(iris_engine* E, const double* re, const double* im) {
+  clear_error();
+  if (!E || !re) return fail(IRIS_EINVAL, "null argument");
+  CK(cudaSetDevice(E->device));
+  CK(cudaStreamSynchronize(E->st));
+  return upload_material(E, re, im);
+}
+
+int iris_step(iris_engine* E, int it0, int nsteps) {
+  clear_error();
+  if (!E || nsteps < 0) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  return E->prec == IRIS_FP64 ? step_t<double>(E, it0, nsteps) : step_t<float>(E, it0, nsteps);
+}
+
+int iris_sync(iris_engine* E) {
+  if (!E) return fail(IRIS_EINVAL, "null engine");
+  CK(cudaSetDevice(E->device));
+  CK(cudaStreamSynchronize(E->st));
+  CK(cudaGetLastError());
+  return IRIS_OK;
+}
+
+int iris_flux(iris_engine* E, int box, double* J) {
+  clear_error();
+  if (!E || !J || box < 0 || box > 1) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  const iris_params& p = E->p;
+  if (box >= E->nboxes) box = 0;  // a single box: the second one is the same box
+  dft_flush(E);
+  const double scale = p.eps0 * p.Q / (2.0 * p.dt);
+  KTimer tm(E, IRIS_KC_FLUX);
+  k_flux<<<dim3(p.nof, 6), 256, 0, E->st>>>(E->fd, E->P, E->d_faces + 6 * box, p.nof, scale, E->d_J);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(E->h_J, E->d_J, sizeof(double) * 6 * p.nof, cudaMemcpyDeviceToHost, E->st));
+  CK(cudaStreamSynchronize(E->st));
+  bool finite = true;
+  for (int k = 0; k < 6 * p.nof; ++k) {
+    J[k] = E->h_J[k];
+    if (!std::isfinite(J[k])) finite = false;
+  }
+  if (!finite) return fail(IRIS_ENAN, "non-finite flux");
+  return IRIS_OK;
+}
+
+int iris_get_field(iris_engine* E, int which, double* re, double* im) {
+  clear_error();
+  if (!E || !re || !im || (which != IRIS_E && which != IRIS_H)) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  const Geo& g = E->g;
+  const size_t n = (size_t)3 * g.comp;
+  std::vector<unsigned char> buf(n * E->esz);
+  CK(cudaMemcpyAsync(buf.data(), which == IRIS_E ? E->e : E->h, n * E->esz, cudaMemcpyDeviceToHost, E->st));
+  CK(cudaStreamSynchronize(E->st));
+  for (int z = 0; z <= g.nz + 1; ++z)
+    for (int y = 0; y <= g.ny + 1; ++y)
+      for (int x = 0; x <= g.nx + 1; ++x)
+        for (int c = 0; c < 3; ++c) {
+          const long r = c + 3L * (x + (long)(g.nx + 2) * (y + (long)(g.ny + 2) * z));
+          const long s = c * g.comp + g.at(x, y, z);
+          if (E->prec == IRIS_FP64) {
+            re[r] = ((const double*)buf.data())[2 * s];
+            im[r] = ((const double*)buf.data())[2 * s + 1];
+          } else {
+            re[r] = ((const float*)buf.data())[2 * s];
+            im[r] = ((const float*)buf.data())[2 * s + 1];
+          }
+        }
+  return IRIS_OK;
+}
+
+int iris_set_field(iris_engine* E, int which, const double* re, const double* im) {
+  clear_error();
+  if (!E || !re || !im || (which != IRIS_E && which != IRIS_H)) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  const Geo& g = E->g;
+  const size_t n = (size_t)3 * g.comp;
+  std::vector<unsigned char> buf(n * E->esz, 0);
+  for (int z = 0; z <= g.nz + 1; ++z)
+    for (int y = 0; y <= g.ny + 1; ++y)
+      for (int x = 0; x <= g.nx + 1; ++x)
+        for (int c = 0; c < 3; ++c) {
+          const long r = c + 3L * (x + (long)(g.nx + 2) * (y + (long)(g.ny + 2) * z));
+          const long s = c * g.comp + g.at(x, y, z);
+          if (E->prec == IRIS_FP64) {
+            ((double*)buf.data())[2 * s] = re[r];
+            ((double*)buf.data())[2 * s + 1] = im[r];
+          } else {
+            ((float*)buf.data())[2 * s] = (float)re[r];
+            ((float*)buf.data())[2 * s + 1] = (float)im[r];
+          }
+        }
+  CK(cudaMemcpyAsync(which == IRIS_E ? E->e : E->h, buf.data(), n * E->esz, cudaMemcpyHostToDevice, E->st));
+  CK(cudaStreamSynchronize(E->st));
+  return IRIS_OK;
+}
+
+static int pml_io(iris_engine* E, int which, int slab, double* re, double* im, const double* cre, const double* cim) {
+  if (!E || (which != 0 && which != 1) || (slab != 0 && slab != 1)) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  const long pc = E->pcomp[slab];
+  const int nx = E->p.nx, ny = E->p.ny;
+  const long nzs = slab == 0 ? E->nbot : E->ntop;
+  void* dev = which == 0 ? E->pml_d[slab] : E->pml_b[slab];
+  std::vector<unsigned char> buf((size_t)3 * pc * E->esz);
+  if (re) {
+    CK(cudaMemcpyAsync(buf.data(), dev, buf.size(), cudaMemcpyDeviceToHost, E->st));
+    CK(cudaStreamSynchronize(E->st));
+  }
+  for (long zr = 0; zr < nzs; ++zr)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x)
+        for (int c = 0; c < 3; ++c) {
+          const long r = c + 3L * (x + (long)nx * (y + (long)ny * zr));
+          const long s = c * pc + (zr * ny + y) * (long)nx + x;
+          if (E->prec == IRIS_FP64) {
+            double* b = (double*)buf.data();
+            if (re) { re[r] = b[2 * s]; im[r] = b[2 * s + 1]; }
+            else { b[2 * s] = cre[r]; b[2 * s + 1] = cim[r]; }
+          } else {
+            float* b = (float*)buf.data();
+            if (re) { re[r] = b[2 * s]; im[r] = b[2 * s + 1]; }
+            else { b[2 * s] = (float)cre[r]; b[2 * s + 1] = (float)cim[r]; }
+          }
+        }
+  if (!re) {
+    CK(cudaMemcpyAsync(dev, buf.data(), buf.size(), cudaMemcpyHostToDevice, E->st));
+    CK(cudaStreamSynchronize(E->st));
+  }
+  return IRIS_OK;
+}
+
+int iris_get_pml(iris_engine* E, int which, int slab, double* re, double* im) {
+  clear_error();
+  if (!re || !im) return fail(IRIS_EINVAL, "null buffer");
+  return pml_io(E, which, slab, re, im, nullptr, nullptr);
+}
+
+int iris_set_pml(iris_engine* E, int which, int slab, const double* re, const double* im) {
+  clear_error();
+  if (!re || !im) return fail(IRIS_EINVAL, "null buffer");
+  return pml_io(E, which, slab, nullptr, nullptr, re, im);
+}
+
+int iris_get_fdata(iris_engine* E, int box, int j, double* re, double* im, long* npts) {
+  clear_error();
+  if (!E || box < 0 || box > 1 || j < 1 || j > 3) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  if (box >= E->nboxes) box = 0;
+  const FaceMap& F = E->fm[box][j - 1];
+  const long n = F.active ? 12 * F.nloc : 0;
+  if (npts) *npts = n;
+  if (!re || n == 0) return IRIS_OK;
+  if (!im) return fail(IRIS_EINVAL, "null buffer");
+  dft_flush(E);
+  const int nof = E->p.nof;
+  std::vector<double2> row((size_t)E->P);
+  for (int iw = 0; iw < nof; ++iw) {
+    CK(cudaMemcpyAsync(row.data(), E->fd + (size_t)iw * E->P, sizeof(double2) * E->P, cudaMemcpyDeviceToHost, E->st));
+    CK(cudaStreamSynchronize(E->st));
+    for (int side = 0; side < 2; ++side)
+      for (int ip = 0; ip < 6; ++ip)
+        for (long L = 0; L < F.nloc; ++L) {
+          const long q = side * 6 * F.nloc + ip + 6 * L;
+          const double2 v = row[F.base[side][ip] + L];
+          re[(size_t)iw * n + q] = v.x;
+          im[(size_t)iw * n + q] = v.y;
+        }
+  }
+  return IRIS_OK;
+}
+
+int iris_timing(iris_engine* E, int enable) {
+  clear_error();
+  if (!E) return fail(IRIS_EINVAL, "null engine");
+  CK(cudaSetDevice(E->device));
+  if (!E->t0) {
+    CK(cudaEventCreate(&E->t0));
+    CK(cudaEventCreate(&E->t1));
+  }
+  for (int k = 0; k < IRIS_NKC; ++k) E->ev_used[k] = 0;
+  E->timing = enable != 0;
+  CK(cudaEventRecord(E->t0, E->st));
+  return IRIS_OK;
+}
+
+int iris_timing_read(iris_engine* E, double* region_ms, double* kernel_ms, long* launches) {
+  clear_error();
+  if (!E || !E->t0) return fail(IRIS_EINVAL, "timing was not started");
+  CK(cudaSetDevice(E->device));
+  CK(cudaEventRecord(E->t1, E->st));
+  CK(cudaEventSynchronize(E->t1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, E->t0, E->t1));
+  if (region_ms) *region_ms = ms;
+  for (int k = 0; k < IRIS_NKC; ++k) {
+    double tot = 0.0;
+    for (size_t i = 0; i < E->ev_used[k]; ++i) {
+      float x = 0.f;
+      CK(cudaEventElapsedTime(&x, E->ev[k][i].first, E->ev[k][i].second));
+      tot += x;
+    }
+    if (kernel_ms) kernel_ms[k] = tot;
+    if (launches) launches[k] = (long)E->ev_used[k];
+  }
+  E->timing = false;
+  return IRIS_OK;
+}
+
+int iris_info(const iris_engine* E, long* info) {
+  if (!E || !info) return fail(IRIS_EINVAL, "bad argument");
+  info[0] = E->P;
+  info[1] = E->K;
+  info[2] = (long)E->esz;
+  info[3] = E->g.comp;
+  info[4] = E->eps_complex ? 1 : 0;
+  info[5] = E->nboxes;
+  return IRIS_OK;
+}
+
+int iris_apply(iris_engine* E, int op, int arg) {
+  clear_error();
+  if (!E) return fail(IRIS_EINVAL, "null engine");
+  CK(cudaSetDevice(E->device));
+  const bool d = E->prec == IRIS_FP64;
+  switch (op) {
+    case IRIS_OP_E: d ? launch_e<double>(E) : launch_e<float>(E); break;
+    case IRIS_OP_H: d ? launch_h<double>(E) : launch_h<float>(E); break;
+    case IRIS_OP_TFSF: d ? launch_tfsf<double>(E, arg) : launch_tfsf<float>(E, arg); break;
+    case IRIS_OP_DFT:
+      dft_flush(E);
+      d ? dft_sample<double>(E, arg) : dft_sample<float>(E, arg);
+      dft_flush(E);
+      break;
+    default: return fail(IRIS_EINVAL, "unknown operator");
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(E->st));
+  return IRIS_OK;
+}
+
+}  // extern "C"
+
+extern "C" const char* iris_last_error(void) { return iris::g_last_error.c_str(); }

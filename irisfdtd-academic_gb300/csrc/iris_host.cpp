@@ -1,0 +1,429 @@
+// Host side of the GB300 FDTD engine: the inputFDTD.dat reader (setparam),
+// the physical constants, the output writers and the drop-in main program
+// (program IrisFDTD -> main -> driver) on top of the C ABI.
+#include <cerrno>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "iris_internal.h"
+
+using iris::fail;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Fortran list-directed input: a read of n items takes the leading values of
+// the next record, continuing on following records until n values are found;
+// the rest of the last record is skipped.  Values are separated by blanks,
+// tabs or commas; '/' ends the read; quoted strings and parenthesised
+// complex constants are single values.
+
+struct Tok {
+  enum Kind { WORD, STR, CPLX, SLASH } kind;
+  std::string text;
+};
+
+class ListReader {
+ public:
+  explicit ListReader(std::vector<std::string> lines) : lines_(std::move(lines)) {}
+  void rewind() { pos_ = 0; }
+  bool eof() const { return pos_ >= lines_.size(); }
+  // false at end of file
+  bool read(size_t n, std::vector<Tok>& out) {
+    out.clear();
+    while (out.size() < n) {
+      if (eof()) return false;
+      std::vector<Tok> t = split(lines_[pos_++]);
+      for (const Tok& k : t) {
+        if (k.kind == Tok::SLASH) {
+          while (out.size() < n) out.push_back(Tok{Tok::WORD, ""});
+          return true;
+        }
+        out.push_back(k);
+        if (out.size() == n) break;
+      }
+    }
+    return true;
+  }
+
+ private:
+  static std::vector<Tok> split(const std::string& s) {
+    std::vector<Tok> out;
+    size_t i = 0, n = s.size();
+    auto sep = [](char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\n' || c == ','; };
+    while (i < n) {
+      const char c = s[i];
+      if (sep(c)) { ++i; continue; }
+      if (c == '/') { out.push_back({Tok::SLASH, "/"}); break; }
+      if (c == '\'' || c == '"') {
+        size_t j = s.find(c, i + 1);
+        if (j == std::string::npos) j = n;
+        out.push_back({Tok::STR, s.substr(i + 1, j - i - 1)});
+        i = j + 1;
+        continue;
+      }
+      if (c == '(') {
+        size_t j = s.find(')', i);
+        if (j == std::string::npos) j = n;
+        out.push_back({Tok::CPLX, s.substr(i + 1, j - i - 1)});
+        i = j + 1;
+        continue;
+      }
+      size_t j = i;
+      while (j < n && !sep(s[j]) && s[j] != '/') ++j;
+      out.push_back({Tok::WORD, s.substr(i, j - i)});
+      i = j;
+    }
+    return out;
+  }
+  std::vector<std::string> lines_;
+  size_t pos_ = 0;
+};
+
+bool to_int(const Tok& t, int& v) {
+  if (t.kind != Tok::WORD || t.text.empty()) return false;
+  char* end = nullptr;
+  errno = 0;
+  long x = std::strtol(t.text.c_str(), &end, 10);
+  if (errno || *end != '\0') return false;
+  v = (int)x;
+  return true;
+}
+
+bool to_real_str(std::string s, double& v) {
+  for (char& c : s)
+    if (c == 'd' || c == 'D') c = 'e';
+  if (s.empty()) return false;
+  char* end = nullptr;
+  errno = 0;
+  v = std::strtod(s.c_str(), &end);
+  return !errno && *end == '\0';
+}
+
+bool to_real(const Tok& t, double& v) { return t.kind == Tok::WORD && to_real_str(t.text, v); }
+
+bool to_complex(const Tok& t, double& re, double& im) {
+  if (t.kind == Tok::CPLX) {
+    size_t k = t.text.find(',');
+    if (k == std::string::npos) return false;
+    std::string a = t.text.substr(0, k), b = t.text.substr(k + 1);
+    auto trim = [](std::string x) {
+      size_t i = x.find_first_not_of(" \t"), j = x.find_last_not_of(" \t");
+      return i == std::string::npos ? std::string() : x.substr(i, j - i + 1);
+    };
+    return to_real_str(trim(a), re) && to_real_str(trim(b), im);
+  }
+  im = 0.0;
+  return to_real(t, re);
+}
+
+// struct_limit, code/files.f90:385-409
+void struct_limit(int N, int a, int& ai, int& af) {
+  if (a % 2 == 0) {
+    if (N % 2 == 0) { ai = N / 2 - (a / 2 - 1); af = N / 2 + (a / 2); }
+    else { ai = (N + 1) / 2 - a / 2; af = (N + 1) / 2 + a / 2 - 1; }
+  } else {
+    if (N % 2 == 0) { ai = N / 2 - ((a + 1) / 2 - 1); af = N / 2 + ((a - 1) / 2); }
+    else { ai = (N + 1) / 2 - (a - 1) / 2; af = (N + 1) / 2 + (a - 1) / 2; }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* iris_strerror(int status) {
+  switch (status) {
+    case IRIS_OK: return "success";
+    case IRIS_EINVAL: return "invalid argument";
+    case IRIS_ENOMEM: return "out of memory";
+    case IRIS_ECUDA: return "CUDA error";
+    case IRIS_EPARSE: return "invalid input file";
+    case IRIS_EIO: return "I/O error";
+    case IRIS_ENAN: return "non-finite value";
+    case IRIS_ETIMEOUT: return "device wait timed out";
+    case IRIS_ENODEV: return "no CUDA device";
+    default: return "unknown error";
+  }
+}
+
+// code/physconst.f90:31-53.  Unsuffixed literals are default REAL: rounded to
+// single precision first, then widened.
+void iris_physconsts(iris_params* p, int single_literals) {
+  if (single_literals) {
+    p->pi = (double)(float)3.14159265358979323846;
+    p->c0 = (double)137.0360f;
+    p->f_abohr = (double)((float)10 / 0.529177249f);
+    p->uat = (double)24.188843265E-3f;
+    p->f_e = (double)514.2208281e9f;
+    p->pmlalfa = (double)1.8f;
+  } else {
+    p->pi = 3.14159265358979323846;
+    p->c0 = 137.0360;
+    p->f_abohr = 10 / 0.529177249;
+    p->uat = 24.188843265E-3;
+    p->f_e = 514.2208281e9;
+    p->pmlalfa = 1.8;
+  }
+  p->eps0 = 1.0 / (4.0 * p->pi);
+  p->mu0 = 1.0 / (p->eps0 * (p->c0 * p->c0));
+}
+
+int iris_frequencies(const iris_params* p, double* fw, int fw_cap) {
+  if (!p || !fw || fw_cap < p->nof) return fail(IRIS_EINVAL, "fw buffer too small");
+  double lno_aux = p->lno;
+  for (int i = 0; i < p->nof; ++i) {
+    fw[i] = 2.0 * p->pi * p->c0 * p->dt / (p->f_abohr * lno_aux);
+    lno_aux = lno_aux + p->dlamda;
+  }
+  return IRIS_OK;
+}
+
+int iris_setparam(const char* path, int single_literals, iris_params* out, double* fw, int fw_cap, char* desc,
+                  int desc_cap) {
+  iris::clear_error();
+  if (!path || !out) return fail(IRIS_EINVAL, "null argument");
+  std::ifstream in(path);
+  if (!in) return fail(IRIS_EPARSE, std::string("cannot open ") + path);
+  std::vector<std::string> lines;
+  for (std::string l; std::getline(in, l);) lines.push_back(l);
+  if (desc && desc_cap > 0) {
+    std::string d = lines.empty() ? "" : lines[0].substr(0, 100);
+    std::snprintf(desc, desc_cap, "%s", d.c_str());
+  }
+  iris_params p;
+  std::memset(&p, 0, sizeof(p));
+  iris_physconsts(&p, single_literals);
+  ListReader R(lines);
+  std::vector<Tok> t;
+  auto perr = [](const std::string& m) { return fail(IRIS_EPARSE, "invalid input file: " + m); };
+  // seek a quoted section header by reading the first value of each record
+  auto seek = [&](const char* header, bool guarded) {
+    R.rewind();
+    while (true) {
+      if (guarded && R.eof()) return false;
+      if (!R.read(1, t)) return false;
+      if (t[0].text == header) return true;
+    }
+  };
+  auto rd_int = [&](int& v) { return R.read(1, t) && to_int(t[0], v); };
+  auto rd_real = [&](double& v) { return R.read(1, t) && to_real(t[0], v); };
+
+  // 'Mesh options', code/files.f90:48-115
+  if (!seek("Mesh options", false)) return perr("no 'Mesh options'");
+  if (!rd_int(p.i_pol) || p.i_pol < 1 || p.i_pol > 4) return perr("i_pol");
+  if (!rd_real(p.q_nm) || p.q_nm <= 0) return perr("q");
+  if (!rd_int(p.nx) || p.nx < 1) return perr("ixmax");
+  if (!rd_int(p.ny) || p.ny < 1) return perr("iymax");
+  if (!rd_int(p.nz) || p.nz < 1) return perr("izmax");
+  p.Q = p.f_abohr * p.q_nm;
+  if (!rd_real(p.cfl) || p.cfl <= 0) return perr("CFL");
+  p.dt = p.cfl / (p.c0 * std::sqrt(3.0 / (p.Q * p.Q)));
+  if (!(p.dt > 0)) return perr("dt");
+  if (!rd_real(p.wzpml) || p.wzpml < 0) return perr("wzPML");
+  p.wzpml = p.f_abohr * (p.wzpml / p.Q);
+  if (!rd_int(p.pml_taflove)) return perr("nPML line");
+  p.npml = 2;
+  if (!rd_int(p.pmlzi)) return perr("pmlzi");
+  if (!rd_int(p.pmlzf)) return perr("pmlzf");
+
+  // 'Job options', code/files.f90:118-154
+  if (!seek("Job options", false)) return perr("no 'Job options'");
+  int ndl = 0;
+  if (!R.read(2, t) || !to_int(t[0], ndl) || !to_int(t[1], p.output_time_step)) return perr("no_downloads");
+  if (!rd_real(p.texit_fs)) return perr("itmax");
+  p.texit = (int)(p.texit_fs / (p.dt * p.uat));
+  if (ndl == 0) return perr("no_downloads = 0");
+  p.no_downloads = p.texit / ndl;
+  if (!rd_int(p.hi)) return perr("hi");
+  if (!R.read(3, t) || !to_int(t[0], p.sdl_plane_on[0]) || !to_int(t[1], p.sdl_plane_on[1]) ||
+      !to_int(t[2], p.sdl_plane_on[2]))
+    return perr("SDL planes");
+
+  // 'Dielectric constants', code/files.f90:156-170
+  if (!seek("Dielectric constants", false)) return perr("no 'Dielectric constants'");
+  if (!rd_real(p.eps1)) return perr("eps cover");
+  if (!R.read(1, t) || !to_complex(t[0], p.eps_bbox_re, p.eps_bbox_im)) return perr("eps_bbox");
+  if (!rd_real(p.eps3)) return perr("eps substrate");
+
+  // 'Fourier transformation options', code/files.f90:173-253
+  if (!seek("Fourier transformation options", true)) return perr("no 'Fourier transformation options'");
+  for (int k = 0; k < 6; ++k)
+    if (!R.read(2, t) || !to_int(t[0], p.box1[k]) || !to_int(t[1], p.box2[k])) return perr("DFT box");
+  if (!rd_int(p.nof) || p.nof < 1) return perr("nof");
+  if (!rd_real(p.dlamda)) return perr("dlambda");
+  if (!rd_real(p.lno)) return perr("lno");
+  if (!R.read(2, t) || !to_int(t[0], p.to_fourier) || !to_int(t[1], p.sample_fourier)) return perr("to_Fourier");
+
+  // 'Source options', code/files.f90:256-289
+  if (!seek("Source options", true)) return perr("no 'Source options'");
+  if (!rd_int(p.plane_wave)) return perr("plane_wave");
+  if (!R.read(2, t) || !to_real(t[0], p.tincr) || !to_real(t[1], p.tdecay)) return perr("tincr/tdecay");
+  if (!R.read(4, t) || !to_real(t[0], p.epump) || !to_real(t[1], p.wlpump) || !to_real(t[2], p.pump_dt) ||
+      !to_real(t[3], p.def_pulse))
+    return perr("Epump line");
+  if (!rd_int(p.tfsf_zi)) return perr("tfsf_zi");
+  p.tfsf_zf = p.tfsf_zi + 5;
+  if (!rd_int(p.cosine)) return perr("cosine");
+  p.ratio_angle = 1.0;
+  p.tincr = p.tincr / p.uat;
+  p.tdecay = p.tdecay / p.uat;
+  p.epump = p.epump / (p.f_e * (single_literals ? (double)1e-5f : 1e-5));
+  p.pump_dt = p.pump_dt / p.uat;
+  p.gpump = p.c0 * p.pump_dt / (2.0 * p.Q * std::sqrt(p.eps1 * p.def_pulse));
+  p.zopump = -(std::sqrt(p.def_pulse) * p.gpump) - p.tfsf_zi;
+  p.gap = 0.0;
+
+  // 'Slit Array', code/files.f90:322-342
+  if (!seek("Slit Array", false)) return perr("no 'Slit Array'");
+  if (!rd_int(p.dh)) return perr("Dh");
+  p.hf = (p.hi + p.dh) - 1;
+  if (!rd_int(p.dx)) return perr("dx");
+  struct_limit(p.nx, p.dx, p.aix, p.afx);
+
+  p.precision = IRIS_FP64;
+  p.dft_block = 0;
+  p.device = 0;
+  *out = p;
+  if (fw) {
+    if (fw_cap < p.nof) return fail(IRIS_EINVAL, "fw buffer too small");
+    iris_frequencies(&p, fw, fw_cap);
+  }
+  return IRIS_OK;
+}
+
+int iris_write_scatt(const char* dir, int box, int it, int nof, const double* J) {
+  if (!dir || !J || nof < 1) return fail(IRIS_EINVAL, "bad argument");
+  const std::string base = std::string(dir) + "/" + std::to_string(box + 1) + "_scatt";
+  for (int j = 0; j < 6; ++j) {
+    FILE* f = std::fopen((base + std::to_string(j + 1) + ".dat").c_str(), "a");
+    if (!f) return fail(IRIS_EIO, "cannot open " + base + std::to_string(j + 1) + ".dat");
+    std::fprintf(f, " #  %10d\n", it);
+    for (int iw = 0; iw < nof; ++iw) std::fprintf(f, "  %24.16E\n", J[j * nof + iw]);
+    std::fclose(f);
+  }
+  FILE* f = std::fopen((base + ".dat").c_str(), "a");
+  if (!f) return fail(IRIS_EIO, "cannot open " + base + ".dat");
+  std::fprintf(f, " #  %10d\n", it);
+  for (int iw = 0; iw < nof; ++iw) {
+    const double s = J[0 * nof + iw] + J[1 * nof + iw] + J[2 * nof + iw] + J[3 * nof + iw] + J[4 * nof + iw] +
+                     J[5 * nof + iw];
+    std::fprintf(f, "  %24.16E\n", s);
+  }
+  std::fclose(f);
+  return IRIS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// spectra_lossless_dielectric, code/common.f90:104-131
+void write_film_spectrum(const std::string& dir, const iris_params& p) {
+  FILE* f = std::fopen((dir + "/dielectric_layer_spectra.dat").c_str(), "w");
+  if (!f) return;
+  const std::complex<double> nII = std::sqrt(std::complex<double>(p.eps_bbox_re, p.eps_bbox_im));
+  const std::complex<double> nIII = std::sqrt(std::complex<double>(p.eps3, 0.0));
+  const std::complex<double> ci(0.0, 1.0);
+  for (int iw = 1; iw <= p.nof; ++iw) {
+    const double lp = p.lno + p.dlamda * (iw - 1.0);
+    const double del = (2 * p.pi * nII * (double)p.dh * p.Q / (lp * p.f_abohr)).real();
+    const double c = std::cos(del), s = std::sin(del);
+    std::complex<double> cn = (c + ci * (nIII / nII) * s - nIII * c - ci * nII * s);
+    cn = cn / (c + ci * (nIII / nII) * s + nIII * c + ci * nII * s);
+    const double R = std::abs(std::conj(cn) * cn);
+    std::fprintf(f, "  %24.16E  %24.16E  %24.16E\n", lp, R, 1.0 - R);
+  }
+  std::fclose(f);
+}
+
+// main() + driver(), code/main.f90:43-213 and code/driver.f90:66-555
+int run_main(const std::string& dir, int precision) {
+  iris_params p;
+  char desc[128] = {0};
+  int rc = iris_setparam((dir + "/inputFDTD.dat").c_str(), 1, &p, nullptr, 0, desc, sizeof(desc));
+  if (rc) return rc;
+  p.precision = precision;
+  std::vector<double> fw(p.nof);
+  iris_frequencies(&p, fw.data(), p.nof);
+  FILE* log = std::fopen((dir + "/log.dat").c_str(), "w");
+  if (!log) return fail(IRIS_EIO, "cannot write log.dat");
+  std::fprintf(log, " Description     : %s\n", desc);
+  std::fprintf(log, "# q(nm)=%15.5f q(u.a)=%15.5f\n", p.q_nm, p.Q);
+  std::fprintf(log, "# ixmax=%d iymax=%d izmax=%d\n", p.nx, p.ny, p.nz);
+  std::fprintf(log, "# CFL =%15.5f\n", p.cfl);
+  std::fprintf(log, "# dt(fs)=%15.8f\n", p.dt * p.uat);
+  std::fprintf(log, "# Iteration max. number = %d Simulation time = %15.5f (fs)\n", p.texit, p.uat * p.dt * p.texit);
+  std::fprintf(log, "# pmlzi=%d pmlzf=%d hi=%d hf=%d aix=%d afx=%d\n", p.pmlzi, p.pmlzf, p.hi, p.hf, p.aix, p.afx);
+  std::fprintf(log, "# precision=%s\n", precision == IRIS_FP64 ? "fp64" : "fp32");
+  write_film_spectrum(dir, p);
+  iris_engine* eng = nullptr;
+  rc = iris_create(&p, fw.data(), &eng);
+  if (rc) { std::fclose(log); return rc; }
+  bool single = true;
+  for (int i = 0; i < 6; ++i)
+    if (p.box1[i] != p.box2[i]) single = false;
+  std::vector<double> J(6 * (size_t)p.nof);
+  int nos = 1;
+  // step in chunks that end at output steps
+  int it = 1;
+  while (it <= p.texit && rc == IRIS_OK) {
+    int next = p.texit;
+    if (p.to_fourier + p.no_downloads * nos >= it && p.to_fourier + p.no_downloads * nos < next)
+      next = p.to_fourier + p.no_downloads * nos;
+    if (next < it) next = it;
+    rc = iris_step(eng, it, next - it + 1);
+    if (rc) break;
+    it = next;
+    if (it >= p.to_fourier && (it == p.to_fourier + p.no_downloads * nos || it == p.texit)) {
+      rc = iris_flux(eng, 0, J.data());
+      if (rc == IRIS_OK || rc == IRIS_ENAN) rc = iris_write_scatt(dir.c_str(), 0, it, p.nof, J.data()) ? IRIS_EIO : rc;
+      if (!single && rc == IRIS_OK) {
+        rc = iris_flux(eng, 1, J.data());
+        if (rc == IRIS_OK) rc = iris_write_scatt(dir.c_str(), 1, it, p.nof, J.data());
+      }
+      ++nos;
+    }
+    ++it;
+  }
+  if (rc == IRIS_OK) rc = iris_sync(eng);
+  std::fprintf(log, " ...done! status=%d\n", rc);
+  std::fclose(log);
+  iris_destroy(eng);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" int iris_run_input(const char* dir, int precision) {
+  iris::clear_error();
+  if (!dir) return fail(IRIS_EINVAL, "null directory");
+  const std::string d(dir);
+  std::ifstream in(d + "/inputFDTD.dat");
+  if (!in) return fail(IRIS_EPARSE, "cannot open " + d + "/inputFDTD.dat");
+  std::string first;
+  std::getline(in, first);
+  if (first.rfind("<<LOOP>>", 0) != 0) return run_main(d, precision);
+  // program.f90:40-57: io_main, if_main, delta_x, delta_y, delta_z
+  std::vector<std::string> rest;
+  for (std::string l; std::getline(in, l);) rest.push_back(l);
+  ListReader R(rest);
+  std::vector<Tok> t;
+  int io = 0, ifm = 0;
+  if (!R.read(1, t) || !to_int(t[0], io) || !R.read(1, t) || !to_int(t[0], ifm))
+    return fail(IRIS_EPARSE, "invalid <<LOOP>> header");
+  int rc = IRIS_OK;
+  if (io != ifm) {
+    for (int i = io; i <= ifm && rc == IRIS_OK; ++i) rc = run_main(d, precision);
+  } else {
+    rc = run_main(d, precision);
+  }
+  return rc;
+}

@@ -1,0 +1,65 @@
+"""The C-ABI library builds, loads and exports every entry point of
+include/iris_fdtd.h; without a GPU the engine refuses loudly."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "iris_fdtd.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(iris_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_exports_match_header(iris):
+    L = iris.lib()
+    names = header_functions()
+    assert len(names) >= 18
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(iris.native.EXPORTS)
+
+
+def test_strerror(iris):
+    L = iris.lib()
+    assert L.iris_strerror(0) == b"success"
+    assert L.iris_strerror(-4) == b"invalid input file"
+
+
+def test_struct_layout_matches_header(iris):
+    # the ctypes mirror and the C struct agree field by field: round-trip through the C parser
+    p, fw, _ = iris.setparam(golden("example_2.inputFDTD.dat"))
+    assert (p.nx, p.ny, p.nz, p.nof, p.aix, p.afx) == (100, 1, 400, 500, 41, 60)
+    assert p.tfsf_zf == 110 and p.precision == 0 and p.device == 0
+
+
+def test_no_gpu_means_error_not_fallback(iris):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    p, fw, _ = iris.setparam(golden("example_1.inputFDTD.dat"))
+    with pytest.raises(iris.IrisError) as e:
+        iris.Engine(p, fw)
+    assert e.value.code in (-8, -3)
+
+
+def test_invalid_parameters_rejected(iris):
+    p, fw, _ = iris.setparam(golden("example_1.inputFDTD.dat"))
+    q = p.copy()
+    q.pmlzi = 1  # set_sz would divide by zero
+    with pytest.raises(iris.IrisError) as e:
+        iris.Engine(q, fw)
+    assert e.value.code == -1
+    q = p.copy()
+    q.box1[5] = q.nz + 1
+    with pytest.raises(iris.IrisError) as e:
+        iris.Engine(q, fw)
+    assert e.value.code == -1
