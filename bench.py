@@ -142,9 +142,11 @@ def ncu_traffic(kernel, workload):
     return None, None
 
 
-def setup_workload(n, rank=0):
+def setup_workload(n, rank=0, grid=None, nof=None):
     cfg = importlib.import_module(PKG + ".configs")
     w = cfg.workload(n)
+    if grid:
+        w = cfg.resized(w, *grid, nof=nof)
     # replicas sweep the Bloch phase (independent k-points)
     w.akx = w.akx + 0.01 * rank
     t = time.perf_counter()
@@ -171,7 +173,7 @@ def algorithmic_bytes(w, p, sc, sm):
 def run_engine(args, rank, world, local):
     iris = importlib.import_module(PKG)
     D = Dist(world)
-    w, path, eps, t_mat = setup_workload(args.workload, rank)
+    w, path, eps, t_mat = setup_workload(args.workload, rank, args.grid, args.nof)
     p, fw, _ = iris.setparam(path)
     p.akx_re = w.akx
     p.device = local
@@ -214,7 +216,7 @@ def run_engine(args, rank, world, local):
     t_h = kms["update_h"] / max(kn["update_h"], 1) * 1e-3
     dom, db, dt_ = ("update_h", hb, t_h) if t_h >= t_e else ("update_e", eb, t_e)
     achieved = db / dt_ / 1e9
-    wl_name = f"{w.name} (configs[2])"
+    wl_name = f"{w.name} (configs[2])" if not args.grid else w.name
     traffic, tsrc = ncu_traffic(dom, w.name + "_" + args.precision)
     launches = kn["update_e"] + kn["update_h"] + kn["tfsf"] + kn["dft_gather"] + kn["flux"] + kn["dft_block"] * (
         2 if prec == iris.FP32 else 1)
@@ -358,6 +360,9 @@ def main():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
+    ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
+                    help="run the workload resized to this grid (profiling cases)")
+    ap.add_argument("--nof", type=int, default=None, help="number of DFT frequencies with --grid")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -155,6 +155,20 @@ def workload(n: int, **over) -> Workload:
     return w
 
 
+def resized(w: Workload, nx: int, ny: int, nz: int, nof: int | None = None) -> Workload:
+    """The same workload on another grid: UPML thickness, TF/SF plane and DFT
+    planes keep their distance to the z ends, the structure layer keeps its
+    relative position and thickness (used for small profiling cases)."""
+    f = nz / w.nz
+    hi = max(w.tfsf_zi + 8, int(round(w.hi * f)))
+    dh = max(1, int(round(w.dh * f)))
+    box = (1, nx, 1, ny, w.box[4], nz - (w.nz - w.box[5]))
+    out = Workload(f"{w.name}_as_{nx}x{ny}x{nz}", nx, ny, nz, w.pmlzi, nz - (w.nz - w.pmlzf), hi, dh, w.eps_bbox, 0,
+                   w.tfsf_zi, box, nof or w.nof, w.nsteps, w.eps1, w.eps3, 0.3 * math.pi * nx if w.akx else 0.0,
+                   w.aky, w.structure, dict(w.extra))
+    return out
+
+
 def batch_cells(ncells: int = 256, seed: int = 0, nsteps: int = 6000, nof: int = 128):
     """Batched form: ncells independent Bloch cells of uneven size, cell i
     seeded with seed+i: nx, ny ~ U{32..160}, nz ~ U{256..768}, UPML 16,

@@ -442,9 +442,11 @@ __global__ void __launch_bounds__(256) k_dft_gather(const typename V2<T>::t* __r
 constexpr int DFT64_WC = 8;
 __global__ void __launch_bounds__(128) k_dft_fp64(const double2* __restrict__ S, long P, int nk,
                                                   const int* __restrict__ tk, const double* __restrict__ fw, int nof,
-                                                  double dt, double2* __restrict__ fd) {
+                                                  int nwc, double dt, double2* __restrict__ fd) {
   extern __shared__ double2 W64[];  // [nk][WC]
-  const int w0 = blockIdx.y * DFT64_WC;
+  // 1-D grid, frequency chunks fastest: the chunks of one point block share its samples in L2
+  const int w0 = (blockIdx.x % nwc) * DFT64_WC;
+  const long pblk = blockIdx.x / nwc;
   for (int t = threadIdx.x; t < nk * DFT64_WC; t += blockDim.x) {
     const int k = t / DFT64_WC, j = t % DFT64_WC;
     double2 v = make_double2(0.0, 0.0);
@@ -456,7 +458,7 @@ __global__ void __launch_bounds__(128) k_dft_fp64(const double2* __restrict__ S,
     W64[t] = v;
   }
   __syncthreads();
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long p = pblk * blockDim.x + threadIdx.x;
   if (p >= P) return;
   const int nw = min(DFT64_WC, nof - w0);
   cx<double> acc[DFT64_WC];
@@ -489,41 +491,80 @@ __global__ void k_twiddle(const int* __restrict__ tk, int nk, const double* __re
 }
 
 // FP32 mode: partial[p][iw] = sum_k F_k(p)*Wt[k][iw] in FP32 registers over
-// the block, then one FP64 add into fdata.
-constexpr int DFT32_WC = 16;
-__global__ void __launch_bounds__(128) k_dft_fp32(const float2* __restrict__ S, long P, int nk,
-                                                  const float2* __restrict__ Wt, int nof, double2* __restrict__ fd) {
-  extern __shared__ float2 W32[];  // [nk][WC]
-  const int w0 = blockIdx.y * DFT32_WC;
-  for (int t = threadIdx.x; t < nk * DFT32_WC; t += blockDim.x) {
-    const int k = t / DFT32_WC, j = t % DFT32_WC;
-    W32[t] = (w0 + j < nof) ? Wt[(long)k * nof + w0 + j] : make_float2(0.f, 0.f);
-  }
-  __syncthreads();
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  float ar[DFT32_WC], ai[DFT32_WC];
+// the block of nk samples, then one FP64 add per (p, iw) into fdata.
+// CTA tile: 128 points x 64 frequencies, 256 threads; lane l owns points
+// l + 32 i (i < 4), warp w owns frequencies 8 w + j (j < 8), so each thread
+// keeps a 4 x 8 complex register tile and every k costs 8 shared loads for
+// 128 FMAs.  Samples and twiddles are staged through shared memory 32 k at a
+// time.  The 1-D grid runs the frequency chunks of one point tile back to
+// back so the tile's samples are read from HBM once and from L2 after that.
+constexpr int DFT_TP = 128, DFT_TW = 64, DFT_KC = 32;
+__global__ void __launch_bounds__(256) k_dft_fp32(const float2* __restrict__ S, long P, int nk,
+                                                  const float2* __restrict__ Wt, int nof, int nwc,
+                                                  double2* __restrict__ fd) {
+  __shared__ float2 Ss[DFT_KC][DFT_TP];
+  __shared__ float4 Ws[DFT_KC][DFT_TW / 2];
+  const int wc = blockIdx.x % nwc;
+  const long p0 = (long)(blockIdx.x / nwc) * DFT_TP;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float ar[4][8], ai[4][8];
 #pragma unroll
-  for (int j = 0; j < DFT32_WC; ++j) ar[j] = ai[j] = 0.f;
-  for (int k = 0; k < nk; ++k) {
-    const float2 s = S[(long)k * P + p];
+  for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < DFT32_WC; ++j) {
-      const float2 w = W32[k * DFT32_WC + j];
-      ar[j] = fmaf(s.x, w.x, fmaf(-s.y, w.y, ar[j]));
-      ai[j] = fmaf(s.x, w.y, fmaf(s.y, w.x, ai[j]));
+    for (int j = 0; j < 8; ++j) ar[i][j] = ai[i][j] = 0.f;
+  for (int kc = 0; kc < nk; kc += DFT_KC) {
+    const int kn = min(DFT_KC, nk - kc);
+    for (int t = threadIdx.x; t < kn * DFT_TP; t += blockDim.x) {
+      const int k = t / DFT_TP, q = t % DFT_TP;
+      const long p = p0 + q;
+      Ss[k][q] = p < P ? S[(long)(kc + k) * P + p] : make_float2(0.f, 0.f);
     }
-  }
-  const int nw = min(DFT32_WC, nof - w0);
+    for (int t = threadIdx.x; t < kn * (DFT_TW / 2); t += blockDim.x) {
+      const int k = t / (DFT_TW / 2), j2 = t % (DFT_TW / 2);
+      const int w = wc * DFT_TW + 2 * j2;
+      const float2 a = w < nof ? Wt[(long)(kc + k) * nof + w] : make_float2(0.f, 0.f);
+      const float2 b = w + 1 < nof ? Wt[(long)(kc + k) * nof + w + 1] : make_float2(0.f, 0.f);
+      Ws[k][j2] = make_float4(a.x, a.y, b.x, b.y);
+    }
+    __syncthreads();
+    for (int k = 0; k < kn; ++k) {
+      float2 sv[4];
 #pragma unroll
-  for (int j = 0; j < DFT32_WC; ++j)
-    if (j < nw) {
-      double2* q = fd + (long)(w0 + j) * P + p;
+      for (int i = 0; i < 4; ++i) sv[i] = Ss[k][lane + 32 * i];
+      float wr[8], wi[8];
+#pragma unroll
+      for (int j2 = 0; j2 < 4; ++j2) {
+        const float4 w = Ws[k][warp * 4 + j2];
+        wr[2 * j2] = w.x;
+        wi[2 * j2] = w.y;
+        wr[2 * j2 + 1] = w.z;
+        wi[2 * j2 + 1] = w.w;
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          ar[i][j] = fmaf(sv[i].x, wr[j], fmaf(-sv[i].y, wi[j], ar[i][j]));
+          ai[i][j] = fmaf(sv[i].x, wi[j], fmaf(sv[i].y, wr[j], ai[i][j]));
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const long p = p0 + lane + 32 * i;
+    if (p >= P) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int w = wc * DFT_TW + warp * 8 + j;
+      if (w >= nof) continue;
+      double2* q = fd + (long)w * P + p;
       double2 f = *q;
-      f.x += (double)ar[j];
-      f.y += (double)ai[j];
+      f.x += (double)ar[i][j];
+      f.y += (double)ai[i][j];
       *q = f;
     }
+  }
 }
 
 // Poynting flux of one face, code/dataprocess.f90:246-277:
@@ -833,17 +874,18 @@ void dft_flush(iris_engine* E) {
   if (E->nslot == 0) return;
   KTimer tm(E, IRIS_KC_DFT);
   const int nk = E->nslot;
-  const unsigned gx = (unsigned)((E->P + 127) / 128);
   if (E->prec == IRIS_FP64) {
-    dim3 grid(gx, (E->p.nof + DFT64_WC - 1) / DFT64_WC);
-    k_dft_fp64<<<grid, 128, (size_t)nk * DFT64_WC * sizeof(double2), E->st>>>(
-        (const double2*)E->S, E->P, nk, E->d_tk, E->d_fw, E->p.nof, E->p.dt, E->fd);
+    const int nwc = (E->p.nof + DFT64_WC - 1) / DFT64_WC;
+    const long nblk = (E->P + 127) / 128;
+    k_dft_fp64<<<(unsigned)(nblk * nwc), 128, (size_t)nk * DFT64_WC * sizeof(double2), E->st>>>(
+        (const double2*)E->S, E->P, nk, E->d_tk, E->d_fw, E->p.nof, nwc, E->p.dt, E->fd);
   } else {
     const int nt = nk * E->p.nof;
     k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
-    dim3 grid(gx, (E->p.nof + DFT32_WC - 1) / DFT32_WC);
-    k_dft_fp32<<<grid, 128, (size_t)nk * DFT32_WC * sizeof(float2), E->st>>>(
-        (const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, E->fd);
+    const int nwc = (E->p.nof + DFT_TW - 1) / DFT_TW;
+    const long nblk = (E->P + DFT_TP - 1) / DFT_TP;
+    k_dft_fp32<<<(unsigned)(nblk * nwc), 256, 0, E->st>>>((const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, nwc,
+                                                        E->fd);
   }
   E->nslot = 0;
 }
@@ -1007,9 +1049,9 @@ int build_dft(iris_engine* E) {
   CK(cudaMemGetInfo(&freeb, &totb));
   const size_t fd_bytes = (size_t)P * p.nof * sizeof(double2);
   if (fd_bytes > freeb) return fail(IRIS_ENOMEM, "DFT accumulators exceed free device memory");
-  // at most 256 slots: the block kernels stage K x 8 (FP64) or K x 16 (FP32)
-  // twiddles in 32 KB of shared memory
-  int K = std::min(256, p.dft_block > 0 ? p.dft_block : (E->prec == IRIS_FP64 ? 32 : 64));
+  // at most 256 slots (the FP64 block kernel stages K x 8 twiddles in 32 KB of
+  // shared memory); FP32 defaults to 256 so the FP64 epilogue is amortised
+  int K = std::min(256, p.dft_block > 0 ? p.dft_block : (E->prec == IRIS_FP64 ? 32 : 256));
   const size_t slot_bytes = std::max<size_t>(1, (size_t)P * E->esz);
   const size_t budget = (freeb - fd_bytes) / 4;
   while (K > 1 && (size_t)K * slot_bytes > budget) K /= 2;

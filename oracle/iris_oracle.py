@@ -545,18 +545,19 @@ class Oracle:
         return J.reshape(6, self.p.nof)
 
     def fdata(self, box: int, j: int) -> np.ndarray:
-        """emg(j)%fdata(i_pts, iw) as complex [iw, i_pts]."""
-        n = int(self.L.orc_fdata_len(self.h, box, j))
+        """emg(j)%fdata(i_pts, iw) of face pair j = 1..3 as complex [iw, i_pts]."""
+        n = int(self.L.orc_fdata_len(self.h, box, j - 1))
         re = np.empty(n)
         im = np.empty(n)
-        self.L.orc_get_fdata(self.h, box, j, _dp(re), _dp(im))
+        self.L.orc_get_fdata(self.h, box, j - 1, _dp(re), _dp(im))
         npts = n // self.p.nof
         return (re + 1j * im).reshape(self.p.nof, npts)
 
     def pto(self, box: int, j: int) -> np.ndarray:
-        n = int(self.L.orc_fdata_len(self.h, box, j)) // self.p.nof
+        """spts(j)%pto(i_pts, 1:4) of face pair j = 1..3."""
+        n = int(self.L.orc_fdata_len(self.h, box, j - 1)) // self.p.nof
         out = np.empty(4 * n, dtype=np.int32)
-        self.L.orc_get_pto(self.h, box, j, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        self.L.orc_get_pto(self.h, box, j - 1, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
         return out.reshape(n, 4)
 
     def tfsf_data(self) -> np.ndarray:

@@ -172,13 +172,11 @@ def test_op_dft(iris, oracle, tmp_path, dims):
         eng.scattering_fourier(t)
     for j in (1, 2, 3):
         fg = eng.get_fdata(0, j)
-        on = (j == 1 and nx != 1 and (ny != 1 or nx != 1)) or (j == 2 and ny != 1) or j == 3
+        # face pairs scattering_fourier accumulates (code/dataprocess.f90:138-205)
         if nx != 1 and ny != 1:
             on = True
-        elif j == 1:
-            on = ny == 1 and nx != 1
-        elif j == 2:
-            on = nx == 1 and ny != 1
+        else:
+            on = {1: ny == 1 and nx != 1, 2: nx == 1 and ny != 1, 3: True}[j]
         if not on:
             assert fg.shape[1] == 0
             continue
