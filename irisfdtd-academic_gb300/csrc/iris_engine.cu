@@ -492,14 +492,15 @@ __global__ void k_twiddle(const int* __restrict__ tk, int nk, const double* __re
 
 // FP32 mode: partial[p][iw] = sum_k F_k(p)*Wt[k][iw] in FP32 registers over
 // the block of nk samples, then one FP64 add per (p, iw) into fdata.
-// CTA tile: 128 points x 64 frequencies, 256 threads; lane l owns points
-// l + 32 i (i < 4), warp w owns frequencies 8 w + j (j < 8), so each thread
-// keeps a 4 x 8 complex register tile and every k costs 8 shared loads for
-// 128 FMAs.  Samples and twiddles are staged through shared memory 32 k at a
-// time.  The 1-D grid runs the frequency chunks of one point tile back to
-// back so the tile's samples are read from HBM once and from L2 after that.
-constexpr int DFT_TP = 128, DFT_TW = 64, DFT_KC = 32;
-__global__ void __launch_bounds__(256) k_dft_fp32(const float2* __restrict__ S, long P, int nk,
+// CTA tile: 128 points x 32 frequencies, 128 threads (three CTAs per SM, so one
+// CTA's staging overlaps the others' FMAs).  Lane l owns points l + 32 i
+// (i < 4), warp w owns frequencies 8 w + j (j < 8), so each thread keeps a
+// 4 x 8 complex register tile and every k costs 8 shared loads for 128 FMAs.
+// Samples and twiddles are staged through shared memory 32 k at a time.  The
+// 1-D grid runs the frequency chunks of one point tile back to back so the
+// tile's samples are read from HBM once and from L2 after that.
+constexpr int DFT_TP = 128, DFT_TW = 32, DFT_KC = 32, DFT_THREADS = 128;
+__global__ void __launch_bounds__(DFT_THREADS) k_dft_fp32(const float2* __restrict__ S, long P, int nk,
                                                   const float2* __restrict__ Wt, int nof, int nwc,
                                                   double2* __restrict__ fd) {
   __shared__ float2 Ss[DFT_KC][DFT_TP];
@@ -884,7 +885,7 @@ void dft_flush(iris_engine* E) {
     k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
     const int nwc = (E->p.nof + DFT_TW - 1) / DFT_TW;
     const long nblk = (E->P + DFT_TP - 1) / DFT_TP;
-    k_dft_fp32<<<(unsigned)(nblk * nwc), 256, 0, E->st>>>((const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, nwc,
+    k_dft_fp32<<<(unsigned)(nblk * nwc), DFT_THREADS, 0, E->st>>>((const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, nwc,
                                                         E->fd);
   }
   E->nslot = 0;
@@ -1176,7 +1177,7 @@ int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
   // launch shapes
   const int bx = std::min(32, p2ceil(p.nx));
   const int by = std::min(256 / bx, p2ceil(p.ny));
-  const int bz = std::min(256 / (bx * by), p2ceil(p.nz));
+  const int bz = std::min(std::min(256 / (bx * by), p2ceil(p.nz)), 64);  // blockDim.z <= 64
   E->blk = dim3(bx, by, bz);
   E->grd = dim3((p.nx + bx - 1) / bx, (p.ny + by - 1) / by, (p.nz + bz - 1) / bz);
   E->src = make_src(p);
