@@ -216,6 +216,15 @@ def assert_spectra(Jg, Jo, tol=TOL):
         assert np.max(np.abs(Rg - Ro)) <= tol
 
 
+def field_err(a, b, op):
+    """Interior field error relative to the incident amplitude Epump*Q (after a
+    long run the pulse has left and the fields sit at the roundoff floor, where
+    a norm relative to the fields themselves says nothing)."""
+    amp = op.epump * op.Q
+    ia, ib = interior(a, op), interior(b, op)
+    return float(np.max(np.abs(ia - ib)) / max(amp, np.max(np.abs(ib))))
+
+
 def full_run(iris, oracle, op, nsteps=None, ak=(0j, 0j, 0j), eps=None, precision=0):
     if nsteps is not None:
         op.texit = nsteps
@@ -237,9 +246,9 @@ def test_example1_full_length(iris, oracle):
     assert Jg.shape == (51, 6, 500)
     assert_spectra(Jg, Jo)
     Eg, Eo = eng.get_field(iris.E), o.get_field(o.E_CUR)
-    assert rel_err(interior(Eg, op), interior(Eo, op)) <= TOL
+    assert field_err(Eg, Eo, op) <= TOL
     Hg, Ho = eng.get_field(iris.H), o.get_field(o.H_CUR)
-    assert rel_err(interior(Hg, op), interior(Ho, op)) <= TOL
+    assert field_err(Hg, Ho, op) <= TOL
 
 
 def test_example2_slit(iris, oracle):
@@ -247,7 +256,7 @@ def test_example2_slit(iris, oracle):
     op.texit = 6000
     o, eng, Jo, Jg = full_run(iris, oracle, op)
     assert_spectra(Jg, Jo)
-    assert rel_err(interior(eng.get_field(iris.E), op), interior(o.get_field(o.E_CUR), op)) <= TOL
+    assert field_err(eng.get_field(iris.E), o.get_field(o.E_CUR), op) <= TOL
 
 
 def test_workload1_slab(iris, oracle, tmp_path):
@@ -262,7 +271,7 @@ def test_workload2_slit_reduced(iris, oracle, tmp_path):
     op = oracle.setparam(cfg.write_input(str(tmp_path / "w2.dat"), w, no_downloads=2))
     o, eng, Jo, Jg = full_run(iris, oracle, op, nsteps=400, eps=cfg.slit_material(w))
     assert_spectra(Jg, Jo)
-    assert rel_err(interior(eng.get_field(iris.H), op), interior(o.get_field(o.H_CUR), op)) <= TOL
+    assert field_err(eng.get_field(iris.H), o.get_field(o.H_CUR), op) <= TOL
 
 
 def test_bloch_cell_spheres_reduced(iris, oracle, tmp_path):
@@ -274,7 +283,7 @@ def test_bloch_cell_spheres_reduced(iris, oracle, tmp_path):
     ak = (complex(w.akx), 0j, 0j)
     o, eng, Jo, Jg = full_run(iris, oracle, op, ak=ak, eps=cfg.spheres_material(w, seed=7))
     assert_spectra(Jg, Jo)
-    assert rel_err(interior(eng.get_field(iris.E), op), interior(o.get_field(o.E_CUR), op)) <= TOL
+    assert field_err(eng.get_field(iris.E), o.get_field(o.E_CUR), op) <= TOL
 
 
 def test_fp32_mode_tr_error(iris, oracle):
