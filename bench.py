@@ -184,7 +184,7 @@ def run_engine(args, rank, world, local):
     # --- end to end through the public API, host buffers in and out
     D.barrier()
     t0 = time.perf_counter()
-    eng = iris.Engine(p, fw, precision=prec, device=local)
+    eng = iris.Engine(p, fw, precision=prec, dft_block=args.dft_block, device=local)
     eng.set_material(eps)
     eng.step(1, K)
     J = eng.flux(0)
@@ -363,6 +363,7 @@ def main():
     ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="run the workload resized to this grid (profiling cases)")
     ap.add_argument("--nof", type=int, default=None, help="number of DFT frequencies with --grid")
+    ap.add_argument("--dft-block", type=int, default=0, help="DFT samples per accumulation block (0: engine default)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
