@@ -239,6 +239,40 @@ int iris_timing_read(iris_engine* eng, double* region_ms, double* kernel_ms, lon
  * material flag, [5] number of DFT boxes. */
 int iris_info(const iris_engine* eng, long* info);
 
+/* ---- allocation-free DFT block ---------------------------------------- */
+/*
+ * This entry point has no counterpart in the reference.  It exists for
+ * callers that cannot call cudaMalloc while they run: a host code whose
+ * device memory is owned by a pooling allocator (a framework's caching
+ * allocator, a buffer pool registered once for communication) or a
+ * deployment that forbids device allocation after start-up.  Such a caller
+ * cannot create an engine (iris_create allocates), but can still run the
+ * engine's FP32 DFT block accumulation on buffers it already owns.
+ *
+ * It adds nk samples to caller-owned accumulators, on the caller's stream:
+ *   fdata[iw][p] += sum_k samples[k][p] * dt * exp(i*fw[iw]*(t0 + k*t_step))
+ * with the partial sum over the block in FP32 and one FP64 add per
+ * (p, iw), exactly like the engine's FP32 mode.  All pointers are device
+ * pointers owned by the caller: samples [nk][npts] complex float (re, im
+ * interleaved), fw [nof] double, fdata [nof][npts] complex double.
+ * stream is a cudaStream_t (NULL: the legacy default stream).
+ *
+ * It allocates nothing.  The twiddle table it needs lives in a fixed device
+ * array of IRIS_NOALLOC_MAX_TWIDDLES complex floats (512 KiB) that every
+ * GPU which loads the library holds until the process exits; calls with
+ * nk*nof above that are rejected with IRIS_EINVAL (split the block).  The
+ * first call on each device looks up that array's device address (a
+ * one-time set-up per device, made with the caller's current device); make
+ * that first call before any stream capture.  Every call reuses the same
+ * array and overwrites the entries it uses, so nothing needs clearing, but
+ * calls whose kernels overlap on the GPU (different streams, no ordering)
+ * race on it.  Returns before the kernels finish; errors of the launches
+ * are reported, errors of their execution surface at the next sync.
+ */
+#define IRIS_NOALLOC_MAX_TWIDDLES 65536
+int iris_dft_block_noalloc(const void* samples, int nk, long npts, int t0, int t_step,
+                           const double* fw, int nof, double dt, void* fdata, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,6 +28,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "iris_internal.h"
@@ -480,13 +481,15 @@ __global__ void __launch_bounds__(128) k_dft_fp64(const double2* __restrict__ S,
 
 // FP32 mode twiddles: Wt[k][iw] = dt*exp(i*fw(iw)*t_k), phase formed in FP64
 // (it reaches ~1e4 rad), rounded to FP32 once.
-__global__ void k_twiddle(const int* __restrict__ tk, int nk, const double* __restrict__ fw, int nof, double dt,
-                          float2* __restrict__ Wt) {
+// Time index of sample k: tk[k], or t0 + k*tstep when tk is null.
+__global__ void k_twiddle(const int* __restrict__ tk, int t0, int tstep, int nk, const double* __restrict__ fw,
+                          int nof, double dt, float2* __restrict__ Wt) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nk * nof) return;
   const int k = t / nof, j = t % nof;
+  const int tt = tk ? tk[k] : t0 + k * tstep;
   double sn, cs;
-  sincos(fw[j] * (double)tk[k], &sn, &cs);
+  sincos(fw[j] * (double)tt, &sn, &cs);
   Wt[t] = make_float2((float)(dt * cs), (float)(dt * sn));
 }
 
@@ -882,7 +885,7 @@ void dft_flush(iris_engine* E) {
         (const double2*)E->S, E->P, nk, E->d_tk, E->d_fw, E->p.nof, nwc, E->p.dt, E->fd);
   } else {
     const int nt = nk * E->p.nof;
-    k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
+    k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
     const int nwc = (E->p.nof + DFT_TW - 1) / DFT_TW;
     const long nblk = (E->P + DFT_TP - 1) / DFT_TP;
     k_dft_fp32<<<(unsigned)(nblk * nwc), DFT_THREADS, 0, E->st>>>((const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, nwc,
@@ -1448,3 +1451,58 @@ int iris_apply(iris_engine* E, int op, int arg) {
 }  // extern "C"
 
 extern "C" const char* iris_last_error(void) { return iris::g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------
+// Allocation-free DFT block accumulation.
+//
+// The twiddle table that k_dft_fp32 reads lives in this fixed device array
+// instead of memory the engine allocates: IRIS_NOALLOC_MAX_TWIDDLES float2
+// values (512 KiB), present on every GPU that loads the library until the
+// process exits.  Host code cannot use the symbol itself as a device pointer,
+// so the first call on each device looks its address up with
+// cudaGetSymbolAddress (with that device current) and caches it.  All calls
+// share the array: each call overwrites the nk*nof entries it uses, so nothing
+// has to be cleared, and two calls whose kernels overlap on the GPU race on it.
+static __device__ __align__(256) float2 g_noalloc_twiddles[IRIS_NOALLOC_MAX_TWIDDLES];
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoallocMaxDevices] = {};
+}  // namespace
+
+extern "C" int iris_dft_block_noalloc(const void* samples, int nk, long npts, int t0, int t_step, const double* fw,
+                                      int nof, double dt, void* fdata, void* stream) {
+  clear_error();
+  if (!samples || !fw || !fdata) return fail(IRIS_EINVAL, "iris_dft_block_noalloc: null device pointer");
+  if (nk < 1 || npts < 1 || nof < 1) return fail(IRIS_EINVAL, "iris_dft_block_noalloc: nk, npts and nof must be >= 1");
+  if ((long)nk * nof > IRIS_NOALLOC_MAX_TWIDDLES)
+    return fail(IRIS_EINVAL, "iris_dft_block_noalloc: nk*nof = " + std::to_string((long)nk * nof) +
+                                 " exceeds the static scratch of " + std::to_string(IRIS_NOALLOC_MAX_TWIDDLES) +
+                                 " twiddles; split the block");
+  const int nwc = (nof + DFT_TW - 1) / DFT_TW;
+  const long nblk = (npts + DFT_TP - 1) / DFT_TP;
+  if (nblk * nwc > 0x7fffffffL) return fail(IRIS_EINVAL, "iris_dft_block_noalloc: npts too large for one launch");
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoallocMaxDevices) return fail(IRIS_EINVAL, "iris_dft_block_noalloc: device ordinal >= 64");
+  void* wt = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* a = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_twiddles);
+      if (e != cudaSuccess)
+        return fail(IRIS_ECUDA, std::string("iris_dft_block_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      g_noalloc_addr[dev] = a;
+    }
+    wt = g_noalloc_addr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nt = nk * nof;
+  k_twiddle<<<(nt + 255) / 256, 256, 0, st>>>(nullptr, t0, t_step, nk, fw, nof, dt, (float2*)wt);
+  k_dft_fp32<<<(unsigned)(nblk * nwc), DFT_THREADS, 0, st>>>((const float2*)samples, npts, nk, (const float2*)wt, nof,
+                                                           nwc, (double2*)fdata);
+  CK(cudaGetLastError());
+  return IRIS_OK;
+}

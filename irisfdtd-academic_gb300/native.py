@@ -99,6 +99,7 @@ EXPORTS = [
     "iris_create", "iris_destroy", "iris_set_material", "iris_step", "iris_sync", "iris_flux",
     "iris_write_scatt", "iris_get_field", "iris_set_field", "iris_get_pml", "iris_set_pml",
     "iris_get_fdata", "iris_apply", "iris_run_input", "iris_timing", "iris_timing_read", "iris_info",
+    "iris_dft_block_noalloc",
 ]
 
 _lib = None
@@ -140,6 +141,7 @@ def lib():
     L.iris_timing.argtypes = [vp, ip]
     L.iris_timing_read.argtypes = [vp, dp, dp, ctypes.POINTER(ctypes.c_long)]
     L.iris_info.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
+    L.iris_dft_block_noalloc.argtypes = [vp, ip, ctypes.c_long, ip, ip, vp, ip, ctypes.c_double, vp, vp]
     _lib = L
     return L
 
