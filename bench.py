@@ -184,7 +184,7 @@ def run_engine(args, rank, world, local):
     # --- end to end through the public API, host buffers in and out
     D.barrier()
     t0 = time.perf_counter()
-    eng = iris.Engine(p, fw, precision=prec, dft_block=args.dft_block, device=local)
+    eng = iris.Engine(p, fw, precision=prec, dft_block=args.dft_block, device=local, stencil=args.stencil)
     eng.set_material(eps)
     eng.step(1, K)
     J = eng.flux(0)
@@ -212,14 +212,26 @@ def run_engine(args, rank, world, local):
     sc, sm = (8, 4) if prec == iris.FP32 else (16, 8)
     eb, hb = algorithmic_bytes(w, p, sc, sm)
     hbm, src = peaks()
-    t_e = kms["update_e"] / max(kn["update_e"], 1) * 1e-3
-    t_h = kms["update_h"] / max(kn["update_h"], 1) * 1e-3
-    dom, db, dt_ = ("update_h", hb, t_h) if t_h >= t_e else ("update_e", eb, t_e)
+    fused = kn["fused_eh"] > 0
+    if fused:
+        # one launch does the whole E+H step: the algorithmic bytes of both passes
+        t_f = kms["fused_eh"] / kn["fused_eh"] * 1e-3
+        dom, db, dt_ = "fused_eh", eb + hb, t_f
+        t_e = t_h = t_f / 2
+        # what one fused pass must move at least: read E,H and write E,H (12 complex per
+        # cell), eps_inv in the structure, D read+write and B read+write in the PML
+        npml = w.nx * w.ny * (p.pmlzi + (p.nz - p.pmlzf + 1))
+        min_bytes = cells * 12 * sc + w.nx * w.ny * (p.hf - p.hi + 1) * sm + npml * 12 * sc
+    else:
+        t_e = kms["update_e"] / max(kn["update_e"], 1) * 1e-3
+        t_h = kms["update_h"] / max(kn["update_h"], 1) * 1e-3
+        dom, db, dt_ = ("update_h", hb, t_h) if t_h >= t_e else ("update_e", eb, t_e)
+        min_bytes = db
     achieved = db / dt_ / 1e9
     wl_name = f"{w.name} (configs[2])" if not args.grid else w.name
     traffic, tsrc = ncu_traffic(dom, w.name + "_" + args.precision)
-    launches = kn["update_e"] + kn["update_h"] + kn["tfsf"] + kn["dft_gather"] + kn["flux"] + kn["dft_block"] * (
-        2 if prec == iris.FP32 else 1)
+    launches = kn["update_e"] + kn["update_h"] + kn["tfsf"] + kn["dft_gather"] + kn["flux"] + kn["fused_eh"] + \
+        kn["dft_block"] * (2 if prec == iris.FP32 else 1)
     value = world * cells * K / (reg_ms * 1e-3) / 1e9
     out = {
         "metric": METRIC,
@@ -251,7 +263,9 @@ def run_engine(args, rank, world, local):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "peak_source": src,
                      "traffic": traffic, "traffic_source": tsrc,
-                     "algorithmic_bytes_per_launch": db},
+                     "algorithmic_bytes_per_launch": db,
+                     "min_bytes_per_launch": min_bytes,
+                     "frac_of_min_bytes": round(min_bytes / dt_ / 1e9 / hbm, 4)},
         "stencil_gcells": round(cells / ((t_e + t_h)) / 1e9, 3),
         "clocks": clocks,
         "material_setup_s": round(t_mat, 2),
@@ -364,6 +378,8 @@ def main():
                     help="run the workload resized to this grid (profiling cases)")
     ap.add_argument("--nof", type=int, default=None, help="number of DFT frequencies with --grid")
     ap.add_argument("--dft-block", type=int, default=0, help="DFT samples per accumulation block (0: engine default)")
+    ap.add_argument("--stencil", type=int, default=0, choices=[0, 1, 2],
+                    help="0: engine default (fused in fp32), 1: split E and H passes, 2: fused E+H pass")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

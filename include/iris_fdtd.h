@@ -110,7 +110,17 @@ typedef struct iris_params {
   int precision;      /* IRIS_FP64 or IRIS_FP32                            */
   int dft_block;      /* samples buffered per DFT accumulation; 0: default */
   int device;         /* CUDA device ordinal                               */
+  int stencil;        /* IRIS_STENCIL_*: how E and H are stepped           */
 } iris_params;
+
+/* ---- stencil variants (iris_params.stencil) -------------------------- */
+/* default: the split passes (the faster variant on GB300 at present)      */
+#define IRIS_STENCIL_DEFAULT 0
+/* separate in-place E and H passes (18 complex values per cell per step)  */
+#define IRIS_STENCIL_SPLIT 1
+/* one fused E+H pass over double-buffered fields (12 values per cell);
+ * IRIS_FP32 only                                                          */
+#define IRIS_STENCIL_FUSED 2
 
 typedef struct iris_engine iris_engine;
 
@@ -223,7 +233,8 @@ int iris_run_input(const char* dir, int precision);
 #define IRIS_KC_GATHER 3 /* DFT face sample gather                        */
 #define IRIS_KC_DFT 4    /* DFT block accumulation (and its twiddles)     */
 #define IRIS_KC_FLUX 5   /* flux reduction                                */
-#define IRIS_NKC 6
+#define IRIS_KC_FUSED 6  /* fused E+H pass (TF/SF and DFT samples inside) */
+#define IRIS_NKC 7
 
 /*
  * Start a timed region on the engine's stream: records a start event and,

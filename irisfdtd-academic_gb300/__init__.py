@@ -34,6 +34,7 @@ from . import native
 from .native import IrisError, IrisParams, build, check, lib
 
 FP64, FP32 = 0, 1
+STENCIL_DEFAULT, STENCIL_SPLIT, STENCIL_FUSED = 0, 1, 2
 E, H = 0, 1
 OP_E, OP_H, OP_TFSF, OP_DFT = 1, 2, 3, 4
 
@@ -85,12 +86,14 @@ def set_emconstants(p: IrisParams) -> np.ndarray:
 class Engine:
     """One run: device state of main()+driver() behind iris_create."""
 
-    def __init__(self, p: IrisParams, fw=None, precision: int | None = None, dft_block: int = 0, device: int = 0):
+    def __init__(self, p: IrisParams, fw=None, precision: int | None = None, dft_block: int = 0, device: int = 0,
+                 stencil: int = 0):
         self.L = lib()
         q = p.copy()
         if precision is not None:
             q.precision = precision
         q.dft_block = dft_block
+        q.stencil = stencil
         q.device = device
         self.p = q
         self.fw = np.ascontiguousarray(frequencies(q) if fw is None else np.asarray(fw, dtype=np.float64))
@@ -188,7 +191,7 @@ class Engine:
         check(self.L.iris_set_pml(self.h, which, slab, _dp(re), _dp(im)), "iris_set_pml")
 
     # -- instrumentation
-    KERNELS = ("update_e", "update_h", "tfsf", "dft_gather", "dft_block", "flux")
+    KERNELS = ("update_e", "update_h", "tfsf", "dft_gather", "dft_block", "flux", "fused_eh")
 
     def timing_start(self, per_kernel: bool = True):
         check(self.L.iris_timing(self.h, 1 if per_kernel else 0), "iris_timing")
@@ -196,8 +199,8 @@ class Engine:
     def timing_read(self):
         """(region_ms, {kernel: ms}, {kernel: launches}) of the timed region."""
         reg = ctypes.c_double(0)
-        ms = np.zeros(6)
-        n = (ctypes.c_long * 6)()
+        ms = np.zeros(len(self.KERNELS))
+        n = (ctypes.c_long * len(self.KERNELS))()
         check(self.L.iris_timing_read(self.h, ctypes.byref(reg), _dp(ms), n), "iris_timing_read")
         return reg.value, dict(zip(self.KERNELS, ms.tolist())), dict(zip(self.KERNELS, list(n)))
 

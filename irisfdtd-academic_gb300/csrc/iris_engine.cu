@@ -102,45 +102,44 @@ template <typename T> struct FieldArgs {
   cx<T> pxp, pyp, pzp, pxm, pym, pzm;  // Bloch phases exp(+-i ak)
 };
 
-// e_fdtd (code/fdtd.f90:57-153) + UPML_Array_e (code/boundary_II.f90:60-138)
-// + bc_{x,y,z}max_bloch (code/boundary.f90:193-216,257-284,321-348) for the
-// E ghosts.  Per z the reference's region order decides: the UPML slabs
-// overwrite whatever e_fdtd wrote there.
-template <typename T, bool CEPS>
-__global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
+// New E of interior cell (x, y, z) from the old E and H: e_fdtd
+// (code/fdtd.f90:57-153) and UPML_Array_e (code/boundary_II.f90:60-138).
+// Per z the reference's region order decides: the UPML slabs overwrite
+// whatever e_fdtd wrote there.  The UPML auxiliary is read from a.pml_d and,
+// when dnew is given, its new value written there (dnew == a.pml_d updates in
+// place).
+// The E update of one cell given its own old H (h), the old H one plane
+// below (hzm, components 1 and 2) and its old E (e, replaced by the new E);
+// the x-1 and y-1 neighbours are loaded here.  MASK selects the components
+// computed (bit k: E_{k+1}); loads only the others need are never issued.
+template <typename T, bool CEPS, int MASK = 7>
+__device__ __forceinline__ void e_update(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
+                                         const cx<T> h[3], const cx<T> hzm[3], cx<T> e[3]) {
   using V = typename V2<T>::t;
-  const Geo g = a.g;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
-  if (x > g.nx || y > g.ny || z > g.nz) return;
+  const Geo& g = a.g;
   const long i = g.at(x, y, z);
   const V* H1 = a.h;
   const V* H2 = a.h + g.comp;
   const V* H3 = a.h + 2 * g.comp;
-  V* E[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
-  const cx<T> h1 = ld<T>(H1 + i), h2 = ld<T>(H2 + i), h3 = ld<T>(H3 + i);
   cx<T> c[3];
-  c[0] = cadd(csub(csub(h3, ld<T>(H3 + i - g.pitch)), h2), ld<T>(H2 + i - g.plane));
-  c[1] = cadd(csub(csub(h1, ld<T>(H1 + i - g.plane)), h3), ld<T>(H3 + i - 1));
-  c[2] = cadd(csub(csub(h2, ld<T>(H2 + i - 1)), h1), ld<T>(H1 + i - g.pitch));
-  cx<T> e[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) e[k] = ld<T>(E[k] + i);
+  if (MASK & 1) c[0] = cadd(csub(csub(h[2], ld<T>(H3 + i - g.pitch)), h[1]), hzm[1]);
+  if (MASK & 2) c[1] = cadd(csub(csub(h[0], hzm[0]), h[2]), ld<T>(H3 + i - 1));
+  if (MASK & 4) c[2] = cadd(csub(csub(h[1], ld<T>(H2 + i - 1)), h[0]), ld<T>(H1 + i - g.pitch));
   if (z <= a.pmlzi || z >= a.pmlzf) {
     const int slab = z <= a.pmlzi ? 0 : 1;
     const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
     const int row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
     const T* cf = a.coef + NCOEF * row;
     const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
-    V* D = a.pml_d[slab];
+    const V* D = a.pml_d[slab];
     const long pc = a.pcomp[slab];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
+      if (!(MASK & (1 << k))) continue;
       const cx<T> ck = rmul(a.eps0sq, c[k]);
       const cx<T> dold = ld<T>(D + k * pc + pi);
       const cx<T> dn = cadd(rmul(cf[CD_A + k], dold), rmul(cf[CD_B + k], ck));
-      st<T>(D + k * pc + pi, dn);
+      if (dnew) st<T>(dnew[slab] + k * pc + pi, dn);
       e[k] = cadd(rmul(cf[CE_A + k], e[k]), rmul(cf[CE_B + k], csub(rmul(cf[C_FP + k], dn), rmul(cf[C_FM + k], dold))));
     }
   } else if (z >= a.hi && z <= a.hf) {
@@ -148,65 +147,55 @@ __global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
     if (CEPS) {
       const cx<T> ep = ld<T>(a.eps_c + ie);
 #pragma unroll
-      for (int k = 0; k < 3; ++k) e[k] = cadd(e[k], cmul(ep, c[k]));
+      for (int k = 0; k < 3; ++k)
+        if (MASK & (1 << k)) e[k] = cadd(e[k], cmul(ep, c[k]));
     } else {
       const T ep = a.eps_r[ie];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) e[k] = cadd(e[k], rmul(ep, c[k]));
+      for (int k = 0; k < 3; ++k)
+        if (MASK & (1 << k)) e[k] = cadd(e[k], rmul(ep, c[k]));
     }
   } else {
     const T m = z < a.hi ? a.m1 : a.m3;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) e[k] = cadd(e[k], rmul(m, c[k]));
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) st<T>(E[k] + i, e[k]);
-  if (x == 1) {
-    const long j = g.at(g.nx + 1, y, z);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pxp, e[k]));
-  }
-  if (y == 1) {
-    const long j = g.at(x, g.ny + 1, z);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pyp, e[k]));
-  }
-  if (z == 1) {
-    const long j = g.at(x, y, g.nz + 1);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pzp, e[k]));
+    for (int k = 0; k < 3; ++k)
+      if (MASK & (1 << k)) e[k] = cadd(e[k], rmul(m, c[k]));
   }
 }
 
-// h_fdtd (code/fdtd.f90:157-248) + UPML_Array_h (code/boundary_II.f90:142-220)
-// + bc_{x,y,z}min_bloch (code/boundary.f90:163-187,224-251,288-315) for the
-// H ghosts and the E ghosts at 0.  The ghosts at nx+1/ny+1/nz+1 of H are
-// never read by any operator and are not maintained.
-template <typename T>
-__global__ void __launch_bounds__(256) k_update_h(FieldArgs<T> a) {
-  using V = typename V2<T>::t;
-  const Geo g = a.g;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
-  if (x > g.nx || y > g.ny || z > g.nz) return;
+// New E of interior cell (x, y, z) from the old E and H in memory: e_fdtd
+// (code/fdtd.f90:57-153) and UPML_Array_e (code/boundary_II.f90:60-138).
+template <typename T, bool CEPS, int MASK = 7>
+__device__ __forceinline__ void e_cell(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
+                                       cx<T> e[3]) {
+  const Geo& g = a.g;
   const long i = g.at(x, y, z);
-  V* Ec[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
-  const V* E1 = Ec[0];
-  const V* E2 = Ec[1];
-  const V* E3 = Ec[2];
-  V* H[3] = {a.h, a.h + g.comp, a.h + 2 * g.comp};
-  cx<T> ev[3];
-  ev[0] = ld<T>(E1 + i);
-  ev[1] = ld<T>(E2 + i);
-  ev[2] = ld<T>(E3 + i);
-  cx<T> c[3];
-  c[0] = cadd(csub(csub(ld<T>(E3 + i + g.pitch), ev[2]), ld<T>(E2 + i + g.plane)), ev[1]);
-  c[1] = cadd(csub(csub(ld<T>(E1 + i + g.plane), ev[0]), ld<T>(E3 + i + 1)), ev[2]);
-  c[2] = cadd(csub(csub(ld<T>(E2 + i + 1), ev[1]), ld<T>(E1 + i + g.pitch)), ev[0]);
-  cx<T> h[3];
+  cx<T> h[3], hzm[3];
+  // own H: c1 uses H3, H2; c2 uses H1, H3; c3 uses H2, H1
+  if (MASK & 6) h[0] = ld<T>(a.h + i);
+  if (MASK & 5) h[1] = ld<T>(a.h + g.comp + i);
+  if (MASK & 3) h[2] = ld<T>(a.h + 2 * g.comp + i);
+  if (MASK & 2) hzm[0] = ld<T>(a.h + i - g.plane);
+  if (MASK & 1) hzm[1] = ld<T>(a.h + g.comp + i - g.plane);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) h[k] = ld<T>(H[k] + i);
+  for (int k = 0; k < 3; ++k)
+    if (MASK & (1 << k)) e[k] = ld<T>(a.e + k * g.comp + i);
+  e_update<T, CEPS, MASK>(a, dnew, x, y, z, h, hzm, e);
+}
+
+// New H of interior cell (x, y, z): h_fdtd (code/fdtd.f90:157-248) and
+// UPML_Array_h (code/boundary_II.f90:142-220), from the new E of the cell (ev)
+// and of its +x, +y, +z neighbours (xp: components 2,3; yp: 1,3; zp: 1,2),
+// the old H read from a.h, the UPML auxiliary B updated in place.
+template <typename T>
+__device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, int z, const cx<T> ev[3],
+                                         const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3]) {
+  using V = typename V2<T>::t;
+  const Geo& g = a.g;
+  cx<T> c[3];
+  c[0] = cadd(csub(csub(yp[2], ev[2]), zp[1]), ev[1]);
+  c[1] = cadd(csub(csub(zp[0], ev[0]), xp[2]), ev[2]);
+  c[2] = cadd(csub(csub(xp[1], ev[1]), yp[0]), ev[0]);
   if (z <= a.pmlzi || z >= a.pmlzf) {
     const int slab = z <= a.pmlzi ? 0 : 1;
     const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
@@ -226,6 +215,76 @@ __global__ void __launch_bounds__(256) k_update_h(FieldArgs<T> a) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) h[k] = csub(h[k], rmul(a.dtcq2, c[k]));
   }
+}
+
+// h_update with the old H of the cell loaded from a.h.
+template <typename T>
+__device__ __forceinline__ void h_cell(const FieldArgs<T>& a, int x, int y, int z, const cx<T> ev[3],
+                                       const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3]) {
+  const long i = a.g.at(x, y, z);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) h[k] = ld<T>(a.h + k * a.g.comp + i);
+  h_update<T>(a, x, y, z, ev, xp, yp, zp, h);
+}
+
+// Split E pass: e_cell in place + bc_{x,y,z}max_bloch
+// (code/boundary.f90:193-216,257-284,321-348) for the E ghosts.
+template <typename T, bool CEPS>
+__global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
+  using V = typename V2<T>::t;
+  const Geo g = a.g;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (x > g.nx || y > g.ny || z > g.nz) return;
+  const long i = g.at(x, y, z);
+  V* E[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
+  cx<T> e[3];
+  e_cell<T, CEPS>(a, a.pml_d, x, y, z, e);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) st<T>(E[k] + i, e[k]);
+  if (x == 1) {
+    const long j = g.at(g.nx + 1, y, z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pxp, e[k]));
+  }
+  if (y == 1) {
+    const long j = g.at(x, g.ny + 1, z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pyp, e[k]));
+  }
+  if (z == 1) {
+    const long j = g.at(x, y, g.nz + 1);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pzp, e[k]));
+  }
+}
+
+// Split H pass: h_cell in place + bc_{x,y,z}min_bloch
+// (code/boundary.f90:163-187,224-251,288-315) for the H ghosts and the E
+// ghosts at 0.  The ghosts at nx+1/ny+1/nz+1 of H are never read by any
+// operator and are not maintained.
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_h(FieldArgs<T> a) {
+  using V = typename V2<T>::t;
+  const Geo g = a.g;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (x > g.nx || y > g.ny || z > g.nz) return;
+  const long i = g.at(x, y, z);
+  V* Ec[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
+  V* H[3] = {a.h, a.h + g.comp, a.h + 2 * g.comp};
+  cx<T> ev[3], xp[3], yp[3], zp[3], h[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ev[k] = ld<T>(Ec[k] + i);
+  xp[1] = ld<T>(Ec[1] + i + 1);
+  xp[2] = ld<T>(Ec[2] + i + 1);
+  yp[0] = ld<T>(Ec[0] + i + g.pitch);
+  yp[2] = ld<T>(Ec[2] + i + g.pitch);
+  zp[0] = ld<T>(Ec[0] + i + g.plane);
+  zp[1] = ld<T>(Ec[1] + i + g.plane);
+  h_cell<T>(a, x, y, z, ev, xp, yp, zp, h);
 #pragma unroll
   for (int k = 0; k < 3; ++k) st<T>(H[k] + i, h[k]);
   if (x == g.nx) {
@@ -601,6 +660,272 @@ __global__ void __launch_bounds__(256) k_flux(const double2* __restrict__ fd, lo
   if (threadIdx.x == 0) J[f * nof + iw] = scale * (F.sign > 0 ? red[0] : -red[0]);
 }
 
+// ---------------------------------------------------------------------------
+// Fused E+H step (FP32 mode).
+//
+// One pass per time step over double-buffered fields: E_new and H_new from
+// E_old and H_old, so each field value is read once and written once per step
+// (12 complex values per cell instead of the 18 of separate E and H passes).
+// A CTA owns an FX x FY column tile and marches z over a chunk of planes.  At
+// plane z it first computes E_new(z+1) for its cells and for the one-cell
+// high halo (x = x0+FX column, y = y0+FY row) that H_new needs, exchanging
+// them through shared memory, then H_new(z).  Halo values are recomputed from
+// the old fields, never read from another CTA's output, so CTAs never wait on
+// each other; this is why E, H and the UPML auxiliary D are double buffered
+// here (B is only ever touched by its owner and stays in place).  The
+// reference's Bloch ghost planes of E become index mapping with a phase:
+// E_new at x = nx+1 is exp(i akx) E_new(1), and likewise for y and z.  TF/SF
+// corrections (FP64 values per x, from k_incident) are added as each plane is
+// written, H's ghosts at x = 0, y = 0, z = 0 (the only ghosts any operator
+// reads) are written with the reference's Bloch copy plus their own TF/SF
+// correction, and DFT face samples are stored straight from registers.
+
+struct FusedSrc {
+  int zE, zH;  // planes of the E and H corrections (-1: none)
+  int cE, cH;  // corrected components
+  int sE, sH;  // +1 add, -1 subtract
+};
+
+struct FusedFace {  // one face pair of one box, as accumulated by scattering_fourier
+  int active;
+  int lo[3], hi[3];  // box bounds in x, y, z
+  int nu;            // extent of the fast in-face axis
+  long base[2][6];   // first sample index per [side][component]
+};
+
+template <typename T> struct FusedArgs {
+  FieldArgs<T> f;  // the old state: f.e, f.h, f.pml_d (D old), f.pml_b (B, in place)
+  typename V2<T>::t* e_new;
+  typename V2<T>::t* h_new;
+  typename V2<T>::t* d_new[2];
+  const double2* inc;  // [2][nx+2]: E and H corrections per ix, FP64
+  FusedSrc src;
+  typename V2<T>::t* slot;  // DFT sample slot of this step, or null
+  int* tk;
+  int islot, t;
+  int nboxes;
+  FusedFace faces[2][3];
+  int zchunk;  // planes per CTA
+};
+
+constexpr int FX = 32, FY = 8;
+
+__device__ __forceinline__ void corr_f(cx<float>& v, double2 c, int sgn) {
+  if (sgn > 0) { v.re = (float)((double)v.re + c.x); v.im = (float)((double)v.im + c.y); }
+  else { v.re = (float)((double)v.re - c.x); v.im = (float)((double)v.im - c.y); }
+}
+
+// Store the six samples of cell (x, y, z) for every face (pair) it lies on.
+__device__ __forceinline__ void dft_store(const FusedArgs<float>& a, int x, int y, int z, const cx<float> e[3],
+                                          const cx<float> h[3]) {
+  for (int b = 0; b < a.nboxes; ++b)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const FusedFace& F = a.faces[b][j];
+      if (!F.active) continue;
+      // normal axis j; in-face axes u (fast) and v: x faces (y, z), y faces (x, z), z faces (x, y)
+      const int cn = j == 0 ? x : (j == 1 ? y : z);
+      const int cu = j == 0 ? y : x, cv = j == 2 ? y : z;
+      const int lu = j == 0 ? F.lo[1] : F.lo[0], hu = j == 0 ? F.hi[1] : F.hi[0];
+      const int lv = j == 2 ? F.lo[1] : F.lo[2], hv = j == 2 ? F.hi[1] : F.hi[2];
+      const int ln = j == 0 ? F.lo[0] : (j == 1 ? F.lo[1] : F.lo[2]);
+      const int hn = j == 0 ? F.hi[0] : (j == 1 ? F.hi[1] : F.hi[2]);
+      if (cu < lu || cu > hu || cv < lv || cv > hv) continue;
+      const long L = (long)(cu - lu) + (long)F.nu * (cv - lv);
+      for (int side = 0; side < 2; ++side) {
+        if (cn != (side ? hn : ln)) continue;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          st<float>(a.slot + F.base[side][k] + L, e[k]);
+          st<float>(a.slot + F.base[side][k + 3] + L, h[k]);
+        }
+      }
+    }
+}
+
+// Per-thread asynchronous global -> shared copies (8 bytes, cached in L1).
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Bloch image: multiply the listed components by the phase when wrapped.
+template <int MASK>
+__device__ __forceinline__ void image(bool wrapped, cx<float> ph, cx<float> v[3]) {
+  if (!wrapped) return;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (MASK & (1 << k)) v[k] = cmul(ph, v[k]);
+}
+
+// One thread per (x, y) column of a FX x FY tile, marching z over the CTA's
+// chunk with no shared memory and no barriers: at plane z the thread computes
+// E_new(z+1) of its cell and the two components H_new needs at its +x
+// neighbour (E2, E3) and +y neighbour (E1, E3), recomputing those from the old
+// fields itself (their loads hit L1/L2: the neighbour thread loads the same
+// values), then H_new(z).  DRAM traffic stays at one read and one write of E
+// and H per cell.  Neighbours past nx or ny are the Bloch images of x = 1 or
+// y = 1; the plane past nz is the image of z = 1.
+template <bool CEPS>
+__global__ void __launch_bounds__(FX* FY) k_fused(FusedArgs<float> a) {
+  using T = float;
+  const Geo g = a.f.g;
+  const int x = blockIdx.x * FX + threadIdx.x + 1;
+  const int y = blockIdx.y * FY + threadIdx.y + 1;
+  if (a.slot && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    a.tk[a.islot] = a.t;
+  if (x > g.nx || y > g.ny) return;
+  const int z0 = blockIdx.z * a.zchunk + 1;
+  const int z1 = min(z0 + a.zchunk - 1, g.nz);
+  const bool wx = x == g.nx, wy = y == g.ny;
+  const int xs = wx ? 1 : x + 1, ys = wy ? 1 : y + 1;
+  // The cell's own old H and E of plane p are copied asynchronously into
+  // stage slot p % 3 two planes before they are used; each thread waits only
+  // for its own copies, so no barrier is involved.
+  __shared__ float2 stg[3][6][FY][FX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int pmax = min(z1 + 1, g.nz);
+  auto stage = [&](int pz) {
+    if (pz <= pmax) {
+      const long ip = g.at(x, y, pz);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        cp_async8(&stg[pz % 3][c][ty][tx], a.f.h + c * g.comp + ip);
+        cp_async8(&stg[pz % 3][3 + c][ty][tx], a.f.e + c * g.comp + ip);
+      }
+    }
+    cp_commit();
+  };
+  auto staged = [&](int pz, int c) {
+    const float2 q = stg[pz % 3][c][ty][tx];
+    return cx<T>{q.x, q.y};
+  };
+  cx<T> ecur[3], xcur[3], ycur[3], enxt[3], xnxt[3], ynxt[3];
+  stage(z0);
+  stage(z0 + 1);
+  cp_wait<1>();
+  {
+    cx<T> hh[3], hzm[3];
+    const long im = g.at(x, y, z0 - 1);
+    hzm[0] = ld<T>(a.f.h + im);
+    hzm[1] = ld<T>(a.f.h + g.comp + im);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      hh[c] = staged(z0, c);
+      ecur[c] = staged(z0, 3 + c);
+    }
+    e_update<T, CEPS, 7>(a.f, a.d_new, x, y, z0, hh, hzm, ecur);
+  }
+  e_cell<T, CEPS, 6>(a.f, nullptr, xs, y, z0, xcur);
+  image<6>(wx, a.f.pxp, xcur);
+  e_cell<T, CEPS, 5>(a.f, nullptr, x, ys, z0, ycur);
+  image<5>(wy, a.f.pyp, ycur);
+  const double2* incE = a.inc;
+  const double2* incH = a.inc + (g.nx + 2);
+  for (int z = z0; z <= z1; ++z) {
+    const int zn = z + 1;
+    stage(z + 2);
+    cp_wait<1>();  // plane z+1 has landed
+    if (zn <= g.nz) {
+      cx<T> hh[3], hzm[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        hh[c] = staged(zn, c);
+        enxt[c] = staged(zn, 3 + c);
+      }
+      hzm[0] = staged(z, 0);
+      hzm[1] = staged(z, 1);
+      e_update<T, CEPS, 7>(a.f, zn <= z1 ? a.d_new : nullptr, x, y, zn, hh, hzm, enxt);
+      if (z < z1) {
+        e_cell<T, CEPS, 6>(a.f, nullptr, xs, y, zn, xnxt);
+        image<6>(wx, a.f.pxp, xnxt);
+        e_cell<T, CEPS, 5>(a.f, nullptr, x, ys, zn, ynxt);
+        image<5>(wy, a.f.pyp, ynxt);
+      }
+    } else {
+      e_cell<T, CEPS, 7>(a.f, nullptr, x, y, 1, enxt);
+      image<7>(true, a.f.pzp, enxt);
+    }
+    cx<T> h[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) h[c] = staged(z, c);
+    h_update<T>(a.f, x, y, z, ecur, xcur, ycur, enxt, h);
+    const long i = g.at(x, y, z);
+    const bool onH = z == a.src.zH, onE = z == a.src.zE;
+    // H ghosts read by the next step: the Bloch copy, then their own TF/SF correction
+    if (wx) {
+      const long j = g.at(0, y, z);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        cx<T> v = cmul(a.f.pxm, h[k]);
+        if (onH && k == a.src.cH) corr_f(v, incH[0], a.src.sH);
+        st<T>(a.h_new + k * g.comp + j, v);
+      }
+    }
+    if (wy) {
+      const long j = g.at(x, 0, z);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        cx<T> v = cmul(a.f.pym, h[k]);
+        if (onH && k == a.src.cH) corr_f(v, incH[x], a.src.sH);
+        st<T>(a.h_new + k * g.comp + j, v);
+      }
+    }
+    if (z == g.nz) {
+      const long j = g.at(x, y, 0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        cx<T> v = cmul(a.f.pzm, h[k]);
+        if (a.src.zH == 0 && k == a.src.cH) corr_f(v, incH[x], a.src.sH);
+        st<T>(a.h_new + k * g.comp + j, v);
+      }
+    }
+    cx<T> e[3] = {ecur[0], ecur[1], ecur[2]};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {  // static indices keep h and e in registers
+      if (onH && k == a.src.cH) corr_f(h[k], incH[x], a.src.sH);
+      if (onE && k == a.src.cE) corr_f(e[k], incE[x], a.src.sE);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      st<T>(a.h_new + k * g.comp + i, h[k]);
+      st<T>(a.e_new + k * g.comp + i, e[k]);
+    }
+    if (a.slot) dft_store(a, x, y, z, e, h);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      ecur[k] = enxt[k];
+      xcur[k] = xnxt[k];
+      ycur[k] = ynxt[k];
+    }
+  }
+}
+
+// The FP64 TF/SF correction values of one step per ix in [0, nx+1]: inc[ix]
+// for E, inc[nx+2+ix] for H (the values k_tfsf adds, see there).
+__global__ void k_incident(SrcArgs s, int it, double2* inc) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ix > s.nx + 1) return;
+  cx<double> a0, b0, a1, b1, vE, vH;
+  const int zm = s.iz_min;
+  if (s.variant == 1) {
+    incident(s, ix, zm - 1, it, a0, b0);
+    incident(s, ix, zm, it, a1, b1);
+    vE = {dm(s.eps_in1, b0.re), dm(s.eps_in1, b0.im)};
+    vH = {dm(s.dtcq2, a1.re), dm(s.dtcq2, a1.im)};
+  } else {
+    incident(s, ix, zm, it, a1, b1);
+    vE = {dq(b1.re, s.eps_src), dq(b1.im, s.eps_src)};
+    vH = {dm(s.dtcq2, a1.re), dm(s.dtcq2, a1.im)};
+  }
+  inc[ix] = make_double2(vE.re, vE.im);
+  inc[s.nx + 2 + ix] = make_double2(vH.re, vH.im);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -676,6 +1001,14 @@ struct iris_engine {
   FluxFace* d_faces = nullptr;
   double* d_J = nullptr;
   double* h_J = nullptr;
+  // fused E+H stepping (FP32): second field buffers and D, per-step TF/SF table
+  bool fused = false;
+  void* e2 = nullptr;
+  void* h2 = nullptr;
+  void* pml_d2[2] = {nullptr, nullptr};
+  double2* d_inc = nullptr;
+  int zchunk = 0;
+  dim3 fblk, fgrd;
   // timing: CUDA events on the engine stream, per kernel class
   bool timing = false;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -825,6 +1158,8 @@ int validate(const iris_params& p) {
       if (lo < 1 || hi > n[a] || lo > hi) return bad("DFT box planes must satisfy 1 <= lo <= hi <= n on every axis");
     }
   if (p.precision != IRIS_FP64 && p.precision != IRIS_FP32) return bad("precision must be IRIS_FP64 or IRIS_FP32");
+  if (p.stencil < IRIS_STENCIL_DEFAULT || p.stencil > IRIS_STENCIL_FUSED) return bad("unknown stencil variant");
+  if (p.stencil == IRIS_STENCIL_FUSED && p.precision != IRIS_FP32) return bad("the fused stencil is FP32 only");
   return IRIS_OK;
 }
 
@@ -905,6 +1240,78 @@ template <typename T> void dft_sample(iris_engine* E, int t) {
                                           E->nslot, t);
   }
   if (++E->nslot == E->K) dft_flush(E);
+}
+
+FusedArgs<float> fused_args(const iris_engine* E) {
+  const iris_params& p = E->p;
+  FusedArgs<float> a{};
+  a.f = field_args<float>(E);
+  a.e_new = (float2*)E->e2;
+  a.h_new = (float2*)E->h2;
+  for (int s = 0; s < 2; ++s) a.d_new[s] = (float2*)E->pml_d2[s];
+  a.inc = E->d_inc;
+  const SrcArgs& s = E->src;
+  a.src.zE = a.src.zH = -1;
+  if (s.variant == 1) {
+    a.src.zE = s.iz_min;
+    a.src.zH = s.iz_min - 1;
+    const bool ex = s.i_pol == 2;
+    a.src.cE = ex ? 0 : 1;
+    a.src.cH = ex ? 1 : 0;
+    a.src.sE = a.src.sH = ex ? +1 : -1;
+  } else if (s.variant == 2) {
+    a.src.zE = a.src.zH = s.iz_min;
+    a.src.cE = 0;
+    a.src.cH = 1;
+    a.src.sE = a.src.sH = +1;
+  }
+  a.nboxes = E->nboxes;
+  for (int b = 0; b < E->nboxes; ++b) {
+    const int* bx = b == 0 ? p.box1 : p.box2;
+    for (int j = 0; j < 3; ++j) {
+      const FaceMap& F = E->fm[b][j];
+      FusedFace& f = a.faces[b][j];
+      f.active = F.active ? 1 : 0;
+      for (int d = 0; d < 3; ++d) {
+        f.lo[d] = bx[2 * d];
+        f.hi[d] = bx[2 * d + 1];
+      }
+      f.nu = F.nu;
+      for (int side = 0; side < 2; ++side)
+        for (int c = 0; c < 6; ++c) f.base[side][c] = F.base[side][c];
+    }
+  }
+  a.zchunk = E->zchunk;
+  return a;
+}
+
+int step_fused(iris_engine* E, int it0, int n) {
+  const iris_params& p = E->p;
+  for (int it = it0; it < it0 + n; ++it) {
+    if (E->src.variant != 0) {
+      KTimer tm(E, IRIS_KC_TFSF);
+      k_incident<<<(p.nx + 2 + 127) / 128, 128, 0, E->st>>>(E->src, it, E->d_inc);
+    }
+    FusedArgs<float> a = fused_args(E);
+    const bool sampled = E->P > 0 && it >= p.to_fourier && it % p.sample_fourier == 0;
+    if (sampled) {
+      a.slot = (float2*)E->S + (long)E->nslot * E->P;
+      a.tk = E->d_tk;
+      a.islot = E->nslot;
+      a.t = it + 1 - p.to_fourier;
+    }
+    {
+      KTimer tm(E, IRIS_KC_FUSED);
+      if (E->eps_complex) k_fused<true><<<E->fgrd, E->fblk, 0, E->st>>>(a);
+      else k_fused<false><<<E->fgrd, E->fblk, 0, E->st>>>(a);
+    }
+    std::swap(E->e, E->e2);
+    std::swap(E->h, E->h2);
+    for (int s = 0; s < 2; ++s) std::swap(E->pml_d[s], E->pml_d2[s]);
+    if (sampled && ++E->nslot == E->K) dft_flush(E);
+  }
+  CK(cudaGetLastError());
+  return IRIS_OK;
 }
 
 template <typename T> int step_t(iris_engine* E, int it0, int n) {
@@ -1081,7 +1488,8 @@ int build_dft(iris_engine* E) {
 
 void free_engine(iris_engine* E) {
   void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
-                  E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J};
+                  E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J, E->e2, E->h2, E->pml_d2[0],
+                  E->pml_d2[1], E->d_inc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (E->h_J) cudaFreeHost(E->h_J);
@@ -1186,6 +1594,31 @@ int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
   E->src = make_src(p);
   E->tf_blk = dim3(64);
   E->tf_grd = dim3((p.nx + 2 + 63) / 64, (p.ny + 2 + TFSF_YCH - 1) / TFSF_YCH);
+  // fused E+H pass: FP32 only
+  // fused on request only: it moves fewer bytes but issues ~1.6x the
+  // instructions of the split passes and measures slower on GB300 for now
+  E->fused = E->prec == IRIS_FP32 && p.stencil == IRIS_STENCIL_FUSED;
+  if (E->fused) {
+    if (cudaMalloc(&E->e2, fbytes) != cudaSuccess || cudaMalloc(&E->h2, fbytes) != cudaSuccess)
+      return bail(fail(IRIS_ENOMEM, "second field buffers: allocation failed"));
+    cudaMemsetAsync(E->e2, 0, fbytes, E->st);
+    cudaMemsetAsync(E->h2, 0, fbytes, E->st);
+    for (int s = 0; s < 2; ++s) {
+      const size_t b = (size_t)3 * E->pcomp[s] * E->esz;
+      if (cudaMalloc(&E->pml_d2[s], b) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "UPML allocation failed"));
+      cudaMemsetAsync(E->pml_d2[s], 0, b, E->st);
+    }
+    if (cudaMalloc(&E->d_inc, sizeof(double2) * 2 * (p.nx + 2)) != cudaSuccess)
+      return bail(fail(IRIS_ENOMEM, "TF/SF table allocation failed"));
+    cudaMemsetAsync(E->d_inc, 0, sizeof(double2) * 2 * (p.nx + 2), E->st);
+    // z chunks: enough CTAs for many waves over 152 SMs, at least 8 planes each
+    const long tiles = (long)((p.nx + FX - 1) / FX) * ((p.ny + FY - 1) / FY);
+    long nch = std::max(1L, (8L * 152 * 4 + tiles - 1) / tiles);
+    nch = std::min<long>(nch, std::max(1, p.nz / 8));
+    E->zchunk = (int)((p.nz + nch - 1) / nch);
+    E->fblk = dim3(FX, FY, 1);
+    E->fgrd = dim3((p.nx + FX - 1) / FX, (p.ny + FY - 1) / FY, (p.nz + E->zchunk - 1) / E->zchunk);
+  }
   {
     std::vector<double> re, im;
     default_material(p, re, im);
@@ -1219,6 +1652,7 @@ int iris_step(iris_engine* E, int it0, int nsteps) {
   clear_error();
   if (!E || nsteps < 0) return fail(IRIS_EINVAL, "bad argument");
   CK(cudaSetDevice(E->device));
+  if (E->fused) return step_fused(E, it0, nsteps);
   return E->prec == IRIS_FP64 ? step_t<double>(E, it0, nsteps) : step_t<float>(E, it0, nsteps);
 }
 

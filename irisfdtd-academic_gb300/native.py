@@ -85,7 +85,7 @@ class IrisParams(ctypes.Structure):
         ("pi", _D), ("c0", _D), ("eps0", _D), ("mu0", _D), ("f_abohr", _D), ("uat", _D), ("f_e", _D),
         ("pmlalfa", _D),
         ("akx_re", _D), ("akx_im", _D), ("aky_re", _D), ("aky_im", _D), ("akz_re", _D), ("akz_im", _D),
-        ("system_model", _I), ("precision", _I), ("dft_block", _I), ("device", _I),
+        ("system_model", _I), ("precision", _I), ("dft_block", _I), ("device", _I), ("stencil", _I),
     ]
 
     def copy(self) -> "IrisParams":

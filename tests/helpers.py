@@ -15,6 +15,9 @@ def rel_err(a, b):
     """Norm-wise relative error max|a-b| / max|b|."""
     a = np.asarray(a)
     b = np.asarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    if b.size == 0:
+        return 0.0
     den = np.max(np.abs(b))
     if den == 0:
         return float(np.max(np.abs(a)))

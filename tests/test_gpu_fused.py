@@ -1,0 +1,116 @@
+"""The fused FP32 E+H pass (IRIS_STENCIL_FUSED) against the split FP32 passes
+and against the FP64 oracle.
+
+The fused pass computes every cell with the same per-cell arithmetic as the
+split passes but reorders the work (one z-marching pass over double buffers,
+halo cells recomputed, Bloch ghosts as index images, TF/SF and DFT samples
+applied in-kernel).  Tolerances: 1e-5 norm-wise relative against the split
+FP32 run (only FP32 rounding differs), 1e-4 against the FP64 oracle, and the
+reference-order DFT accumulators of every face pair within 1e-5 of the split
+run.
+"""
+import importlib
+import os
+
+import numpy as np
+import pytest
+
+from helpers import engine_params_from_oracle, interior, output_steps, rel_err, run_engine_blocks
+
+pytestmark = pytest.mark.gpu
+cfg = importlib.import_module("irisfdtd-academic_gb300.configs")
+THREADS = max(1, min(16, os.cpu_count() or 1))
+
+# name, (nx, ny, nz, pmlzi, pmlzf, hi, dh, eps_bbox, tfsf_zi, box), i_pol, ak, material, steps
+CASES = [
+    ("3d_partial_tiles_pol2", (37, 21, 64, 8, 57, 24, 14, 2.25, 12, (1, 37, 1, 21, 9, 54)), 2,
+     (0.4 + 0j, -0.2 + 0j, 0j), "spheres", 160),
+    ("3d_pol1_complex_eps", (33, 9, 48, 6, 43, 18, 10, 4.0, 10, (2, 30, 1, 9, 7, 40)), 1,
+     (0j, 0.3 + 0j, 0j), "complex", 140),
+    ("2d_xz_slit", (40, 1, 80, 10, 71, 30, 12, 9.0, 16, (1, 40, 1, 1, 12, 66)), 2, (0j, 0j, 0j), "slit", 200),
+    ("1d_slab", (1, 1, 120, 12, 109, 50, 20, 9.0, 20, (1, 1, 1, 1, 15, 100)), 2, (0j, 0j, 0j), "slab", 300),
+]
+
+
+def make_case(oracle, tmp_path, spec, i_pol):
+    nx, ny, nz, pmlzi, pmlzf, hi, dh, eps, zi, box = spec
+    w = cfg.Workload("fused", nx, ny, nz, pmlzi, pmlzf, hi, dh, eps, 8 if nx >= 16 else 0, zi, box, 11, 50,
+                     structure="spheres", extra=dict(nspheres=6, rmin=2, rmax=5, emin=1.5, emax=6.0))
+    op = oracle.setparam(cfg.write_input(str(tmp_path / "in.dat"), w, i_pol=i_pol, no_downloads=3))
+    return w, op
+
+
+def material(w, op, kind, rng):
+    if kind == "spheres":
+        return cfg.spheres_material(w, seed=3)
+    if kind == "complex":
+        shp = (op.hf - op.hi + 3, op.ny + 2, op.nx + 2)
+        return 1.0 / rng.uniform(1, 5, shp) + 1j * rng.uniform(-0.05, 0.05, shp)
+    if kind == "slit":
+        return cfg.slit_material(w)
+    return None
+
+
+def run(iris, op, stencil, ak, eps, precision=1):
+    eng = iris.Engine(engine_params_from_oracle(iris, op, precision=precision, ak=ak), op.fw, stencil=stencil)
+    if eps is not None:
+        eng.set_material(eps)
+    J = run_engine_blocks(eng, op, output_steps(op))
+    return eng, J
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_fused_against_split_and_oracle(iris, oracle, tmp_path, case):
+    name, spec, i_pol, ak, kind, steps = case
+    w, op = make_case(oracle, tmp_path, spec, i_pol)
+    op.texit = steps
+    eps = material(w, op, kind, np.random.default_rng(5))
+    es, Js = run(iris, op, 1, ak, eps)
+    ef, Jf = run(iris, op, 2, ak, eps)
+    assert ef.info()["dft_points"] == es.info()["dft_points"]
+    for which in (iris.E, iris.H):
+        fs, ff = interior(es.get_field(which), op), interior(ef.get_field(which), op)
+        assert rel_err(ff, fs) <= 1e-5, which
+    assert rel_err(Jf, Js) <= 1e-5
+    for j in (1, 2, 3):
+        assert rel_err(ef.get_fdata(0, j), es.get_fdata(0, j)) <= 1e-5, j
+    # against the FP64 oracle
+    o = oracle.Oracle(op, ak=ak, threads=THREADS)
+    if eps is not None:
+        o.set_eps_inv(eps)
+    Jo, _ = o.run(1, op.texit, max_out=len(output_steps(op)))
+    assert rel_err(Jf, Jo) <= 1e-4
+    assert rel_err(interior(ef.get_field(iris.E), op), interior(o.get_field(o.E_CUR), op)) <= 1e-4
+
+
+def test_fused_two_boxes(iris, oracle, tmp_path):
+    w, op = make_case(oracle, tmp_path, (20, 12, 56, 7, 50, 22, 12, 2.25, 10, (1, 20, 1, 12, 8, 48)), 2)
+    op.box2 = (3, 17, 2, 10, 12, 40)
+    op.texit = 120
+    es, Js = run(iris, op, 1, (0j, 0j, 0j), None)
+    ef, Jf = run(iris, op, 2, (0j, 0j, 0j), None)
+    assert rel_err(ef.flux(1), es.flux(1)) <= 1e-5
+    for j in (1, 2, 3):
+        assert rel_err(ef.get_fdata(1, j), es.get_fdata(1, j)) <= 1e-5
+
+
+def test_fused_rejected_in_fp64(iris, oracle, tmp_path):
+    w, op = make_case(oracle, tmp_path, (8, 6, 40, 6, 35, 15, 10, 4.0, 10, (1, 8, 1, 6, 8, 32)), 2)
+    with pytest.raises(iris.IrisError) as e:
+        iris.Engine(engine_params_from_oracle(iris, op, precision=0), op.fw, stencil=2)
+    assert e.value.code == -1
+
+
+def test_stencil_selection(iris, oracle, tmp_path):
+    """The per-kernel timers show which pass ran: split by default, fused on request."""
+    w, op = make_case(oracle, tmp_path, (16, 8, 40, 6, 35, 15, 10, 4.0, 10, (1, 16, 1, 8, 8, 32)), 2)
+    for stencil, fused in ((0, False), (1, False), (2, True)):
+        eng = iris.Engine(engine_params_from_oracle(iris, op, precision=1), op.fw, stencil=stencil)
+        eng.timing_start()
+        eng.step(1, 5)
+        _, ms, n = eng.timing_read()
+        if fused:
+            assert n["fused_eh"] == 5 and n["update_e"] == 0 and n["update_h"] == 0
+        else:
+            assert n["fused_eh"] == 0 and n["update_e"] == 5 and n["update_h"] == 5
+        eng.close()
