@@ -278,6 +278,110 @@ def run_engine(args, rank, world, local):
     return out
 
 
+def run_batch(args, rank, world, local):
+    """configs[3]: 256 independent Bloch cells of uneven size (seed+i per cell),
+    FP32 fields, FP64 DFT at 128 frequencies on the reflection and transmission
+    planes, all cells stepped by one launch per operator."""
+    iris = importlib.import_module(PKG)
+    cfg = importlib.import_module(PKG + ".configs")
+    D = Dist(world)
+    ncells = args.cells
+    ws = cfg.batch_cells(ncells, seed=1000 * rank, nof=128)
+    d = tempfile.mkdtemp(prefix="iris_batch_")
+    params, mats = [], []
+    t = time.perf_counter()
+    for i, w in enumerate(ws):
+        p, fw, _ = iris.setparam(cfg.write_input(os.path.join(d, f"c{i}.dat"), w))
+        p.device = local
+        params.append(p)
+        mats.append(cfg.binary_pattern_material(w))
+    t_mat = time.perf_counter() - t
+    cells = sum(w.cells for w in ws)
+    K, W = args.steps, args.warmup
+    D.barrier()
+    t0 = time.perf_counter()
+    b = iris.Batch(params, fw, precision=iris.FP32, dft_faces=iris.DFT_Z, device=local)
+    for i, m in enumerate(mats):
+        b.set_material(i, m)
+    tile, tune_ms = b.tune(reps=2)
+    b.step(1, K)
+    J = [b.flux(i) for i in range(ncells)]
+    t_e2e = D.max(time.perf_counter() - t0)
+    info = b.info()
+    b.step(K + 1, W)
+    D.barrier()
+    pr, cpath = start_clocks(local)
+    b.timing_start(per_kernel=True)
+    b.step(K + W + 1, K)
+    reg_ms, kms, kn = b.timing_read()
+    clocks = stop_clocks(pr, cpath)
+    reg_ms = D.max(reg_ms)
+    b.close()
+    hbm, src = peaks()
+    # algorithmic bytes of one E and one H pass over every cell (as for one engine)
+    eb = hb = 0
+    for w, p in zip(ws, params):
+        e, h = algorithmic_bytes(w, p, 8, 4)
+        eb += e
+        hb += h
+    t_e = kms["update_e"] / kn["update_e"] * 1e-3
+    t_h = kms["update_h"] / kn["update_h"] * 1e-3
+    dom, db, dt_ = ("update_h", hb, t_h) if t_h >= t_e else ("update_e", eb, t_e)
+    achieved = db / dt_ / 1e9
+    launches = sum(kn[k] for k in ("update_e", "update_h", "tfsf", "dft_gather", "flux")) + 2 * kn["dft_block"]
+    value = world * cells * K / (reg_ms * 1e-3) / 1e9
+    h2d = sum(m.size * 16 for m in mats)
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": round(reg_ms / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 fields (fp32), fp64 incident field and DFT accumulation",
+        "data": "synthetic (seeded binary eps patterns, numpy PCG64 seed+i per cell)",
+        "config": {"workload": f"batch of {ncells} uneven Bloch cells (configs[3])", "grid_cells": cells,
+                   "nof": 128, "dft_points": info["dft_points"], "dft_block": info["dft_block"],
+                   "dft_faces": "z planes (reflection, transmission)", "tile": list(tile),
+                   "tune_ms_per_eh_pass": {"x".join(map(str, k)): round(v, 3) for k, v in tune_ms.items()},
+                   "l2": "working set >> 129 MB L2; no flush needed",
+                   "parallelism": f"replicas x{world} (independent batches, one per GPU)"},
+        "e2e": {"value": round(world * cells * K / t_e2e / 1e9, 3), "unit": "Gcell/s",
+                "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(sum(j.size for j in J) * 8 / K, 1),
+                "what": "iris_batch_create + set_material x%d (host eps) + tune + %d steps + flux of every cell" % (
+                    ncells, K)},
+        "gpu_launches": int(launches),
+        "kernels_ms_per_step": {k: round(v / K, 4) for k, v in kms.items()},
+        "roofline": {"kernel": "batch_" + dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
+                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_source": src, "traffic": None,
+                     "algorithmic_bytes_per_launch": db},
+        "stencil_gcells": round(cells / (t_e + t_h) / 1e9, 3),
+        "clocks": clocks, "material_setup_s": round(t_mat, 2),
+    }
+    if rank == 0 and world == 1 and args.loop_sample:
+        out["loop_plain"] = loop_plain(iris, ws, params, mats, fw, local, args.loop_sample, steps=16)
+    D.close()
+    return out
+
+
+def loop_plain(iris, ws, params, mats, fw, local, nsample, steps):
+    """The same cells stepped one after another, each on its own engine (the plain
+    solver in a loop), on a sample of the batch: aggregate Gcell/s."""
+    tot_cells, tot_ms = 0, 0.0
+    idx = list(range(0, len(ws), max(1, len(ws) // nsample)))[:nsample]
+    for i in idx:
+        q = params[i].copy()
+        q.dft_faces = iris.DFT_Z
+        e = iris.Engine(q, fw, precision=iris.FP32, device=local)
+        e.set_material(mats[i])
+        e.step(1, 3)
+        e.sync()
+        e.timing_start(per_kernel=False)
+        e.step(4, steps)
+        reg, _, _ = e.timing_read()
+        e.close()
+        tot_cells += ws[i].cells * steps
+        tot_ms += reg
+    return {"value": round(tot_cells / (tot_ms * 1e-3) / 1e9, 3), "unit": "Gcell/s", "cells_sampled": len(idx),
+            "steps": steps, "note": "each sampled cell on its own engine, device time summed"}
+
+
 def fp64_compare(iris, p, fw, eps, cells, local, K=8, W=2):
     eng = iris.Engine(p, fw, precision=iris.FP64, device=local)
     eng.set_material(eps)
@@ -379,13 +483,18 @@ def main():
     ap.add_argument("--nof", type=int, default=None, help="number of DFT frequencies with --grid")
     ap.add_argument("--dft-block", type=int, default=0, help="DFT samples per accumulation block (0: engine default)")
     ap.add_argument("--stencil", type=int, default=0, choices=[0, 1, 2],
-                    help="0: engine default (fused in fp32), 1: split E and H passes, 2: fused E+H pass")
+                    help="0: engine default (split), 1: split E and H passes, 2: fused E+H pass (fp32)")
+    ap.add_argument("--cells", type=int, default=256, help="cells in the batch (workload 4)")
+    ap.add_argument("--loop-sample", type=int, default=16,
+                    help="workload 4: cells of the batch also stepped one by one on plain engines (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     rank, world, local = env_rank()
     if args.impl == "reference":
         out = run_reference(args, rank, world)
+    elif args.workload == 4:
+        out = run_batch(args, rank, world, local)
     else:
         out = run_engine(args, rank, world, local)
     if rank == 0 and out is not None:

@@ -111,7 +111,14 @@ typedef struct iris_params {
   int dft_block;      /* samples buffered per DFT accumulation; 0: default */
   int device;         /* CUDA device ordinal                               */
   int stencil;        /* IRIS_STENCIL_*: how E and H are stepped           */
+  int dft_faces;      /* IRIS_DFT_ALL or IRIS_DFT_Z                        */
 } iris_params;
+
+/* ---- DFT faces (iris_params.dft_faces) -------------------------------- */
+/* every face pair scattering_fourier accumulates (the reference)          */
+#define IRIS_DFT_ALL 0
+/* only the two z planes (reflection and transmission, all T/R needs)      */
+#define IRIS_DFT_Z 1
 
 /* ---- stencil variants (iris_params.stencil) -------------------------- */
 /* default: the split passes (the faster variant on GB300 at present)      */
@@ -249,6 +256,42 @@ int iris_timing_read(iris_engine* eng, double* region_ms, double* kernel_ms, lon
  * stored complex value, [3] elements per field component, [4] complex
  * material flag, [5] number of DFT boxes. */
 int iris_info(const iris_engine* eng, long* info);
+
+/* ---- batched form ------------------------------------------------------ */
+/*
+ * Many independent Bloch cells (or k-points of one cell) stepped together;
+ * no counterpart in the reference beyond its <<LOOP>> mode, which re-runs
+ * main() per index (code/program.f90:36-57).  Each cell has its own grid,
+ * UPML, structure, source plane, DFT box and Bloch phases; all cells share
+ * the precision, Q, dt, the frequency list, the DFT sampling and the device.
+ * One launch per operator covers every cell: persistent kernels walk a work
+ * list of (cell, tile) items.  dft_faces: IRIS_DFT_ALL or IRIS_DFT_Z.
+ */
+typedef struct iris_batch iris_batch;
+int iris_batch_create(int ncells, const iris_params* params, const double* fw, int dft_faces, iris_batch** out);
+void iris_batch_destroy(iris_batch* b);
+/* iris_set_material for one cell of the batch. */
+int iris_batch_set_material(iris_batch* b, int cell, const double* eps_inv_re, const double* eps_inv_im);
+/* iris_step for every cell: steps it0 .. it0+nsteps-1. */
+int iris_batch_step(iris_batch* b, int it0, int nsteps);
+/* iris_flux (box 1) of one cell. */
+int iris_batch_flux(iris_batch* b, int cell, double* J);
+/* iris_get_field of one cell. */
+int iris_batch_get_field(iris_batch* b, int cell, int which, double* re, double* im);
+/*
+ * Tile-shape autotuner: times every candidate tile of the E/H work list
+ * (reps E+H passes each) on this batch and keeps the fastest; ms[i]
+ * (optional, 5 entries) receives the time per E+H pass of candidate i.  Call
+ * before the first step (the passes run on the zero initial state).
+ */
+int iris_batch_tune(iris_batch* b, int reps, int* best, double* ms);
+/* Force a candidate tile (0..4: 32x8x1, 32x4x2, 64x4x1, 16x16x1, 32x2x4). */
+int iris_batch_set_tile(iris_batch* b, int tile);
+int iris_batch_timing(iris_batch* b, int enable);
+int iris_batch_timing_read(iris_batch* b, double* region_ms, double* kernel_ms, long* launches);
+/* info[0] cells, [1] total grid cells, [2] DFT points, [3] DFT block K,
+ * [4] tile index, [5] work items per pass. */
+int iris_batch_info(const iris_batch* b, long* info);
 
 /* ---- allocation-free DFT block ---------------------------------------- */
 /*

@@ -222,6 +222,91 @@ class Engine:
         return (re + 1j * im).reshape(self.p.nof, npts)
 
 
+DFT_ALL, DFT_Z = 0, 1
+TILES = ((32, 8, 1), (32, 4, 2), (64, 4, 1), (16, 16, 1), (32, 2, 4))
+
+
+class Batch:
+    """Many independent cells stepped together (iris_batch_*): each cell its own
+    grid, structure, source and Bloch phases; shared precision, dt, frequencies."""
+
+    def __init__(self, params, fw, precision: int | None = None, dft_faces: int = DFT_Z, device: int = 0,
+                 dft_block: int = 0):
+        self.L = lib()
+        arr = (IrisParams * len(params))()
+        for i, p in enumerate(params):
+            q = p.copy()
+            if precision is not None:
+                q.precision = precision
+            q.device = device
+            q.dft_block = dft_block
+            arr[i] = q
+        self.params = arr
+        self.n = len(params)
+        self.fw = np.ascontiguousarray(np.asarray(fw, dtype=np.float64))
+        h = ctypes.c_void_p()
+        check(self.L.iris_batch_create(self.n, arr, _dp(self.fw), dft_faces, ctypes.byref(h)), "iris_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.iris_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_material(self, cell: int, eps_inv: np.ndarray):
+        a = np.asarray(eps_inv, dtype=np.complex128)
+        re, im = np.ascontiguousarray(a.real), np.ascontiguousarray(a.imag)
+        check(self.L.iris_batch_set_material(self.h, cell, _dp(re), _dp(im) if np.any(im) else None),
+              "iris_batch_set_material")
+
+    def step(self, it0: int, n: int):
+        check(self.L.iris_batch_step(self.h, it0, n), "iris_batch_step")
+
+    def flux(self, cell: int) -> np.ndarray:
+        J = np.zeros(6 * self.params[cell].nof)
+        check(self.L.iris_batch_flux(self.h, cell, _dp(J)), "iris_batch_flux")
+        return J.reshape(6, -1)
+
+    def get_field(self, cell: int, which: int) -> np.ndarray:
+        p = self.params[cell]
+        shape = (p.nz + 2, p.ny + 2, p.nx + 2, 3)
+        n = int(np.prod(shape))
+        re, im = np.empty(n), np.empty(n)
+        check(self.L.iris_batch_get_field(self.h, cell, which, _dp(re), _dp(im)), "iris_batch_get_field")
+        return (re + 1j * im).reshape(shape)
+
+    def tune(self, reps: int = 3):
+        """Autotune the E/H tile shape on this batch (before the first step)."""
+        best = ctypes.c_int(0)
+        ms = np.zeros(len(TILES))
+        check(self.L.iris_batch_tune(self.h, reps, ctypes.byref(best), _dp(ms)), "iris_batch_tune")
+        return TILES[best.value], dict(zip(TILES, ms.tolist()))
+
+    def set_tile(self, tile_index: int):
+        check(self.L.iris_batch_set_tile(self.h, tile_index), "iris_batch_set_tile")
+
+    def timing_start(self, per_kernel: bool = True):
+        check(self.L.iris_batch_timing(self.h, 1 if per_kernel else 0), "iris_batch_timing")
+
+    def timing_read(self):
+        reg = ctypes.c_double(0)
+        ms = np.zeros(len(Engine.KERNELS))
+        n = (ctypes.c_long * len(Engine.KERNELS))()
+        check(self.L.iris_batch_timing_read(self.h, ctypes.byref(reg), _dp(ms), n), "iris_batch_timing_read")
+        return reg.value, dict(zip(Engine.KERNELS, ms.tolist())), dict(zip(Engine.KERNELS, list(n)))
+
+    def info(self) -> dict:
+        a = (ctypes.c_long * 6)()
+        check(self.L.iris_batch_info(self.h, a), "iris_batch_info")
+        return dict(cells=a[0], grid_cells=a[1], dft_points=a[2], dft_block=a[3], tile=TILES[a[4]], items=a[5])
+
+
 def run_input(directory: str, precision: int = FP64):
     """The drop-in main program: reads directory/inputFDTD.dat, writes log.dat and
     the <box>_scatt*.dat files there."""

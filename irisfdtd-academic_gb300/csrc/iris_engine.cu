@@ -227,16 +227,12 @@ __device__ __forceinline__ void h_cell(const FieldArgs<T>& a, int x, int y, int 
   h_update<T>(a, x, y, z, ev, xp, yp, zp, h);
 }
 
-// Split E pass: e_cell in place + bc_{x,y,z}max_bloch
+// Split E pass of one cell: e_cell in place + bc_{x,y,z}max_bloch
 // (code/boundary.f90:193-216,257-284,321-348) for the E ghosts.
 template <typename T, bool CEPS>
-__global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
+__device__ __forceinline__ void e_split_cell(const FieldArgs<T>& a, int x, int y, int z) {
   using V = typename V2<T>::t;
-  const Geo g = a.g;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
-  if (x > g.nx || y > g.ny || z > g.nz) return;
+  const Geo& g = a.g;
   const long i = g.at(x, y, z);
   V* E[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
   cx<T> e[3];
@@ -260,18 +256,23 @@ __global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
   }
 }
 
-// Split H pass: h_cell in place + bc_{x,y,z}min_bloch
+template <typename T, bool CEPS>
+__global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (x > a.g.nx || y > a.g.ny || z > a.g.nz) return;
+  e_split_cell<T, CEPS>(a, x, y, z);
+}
+
+// Split H pass of one cell: h_cell in place + bc_{x,y,z}min_bloch
 // (code/boundary.f90:163-187,224-251,288-315) for the H ghosts and the E
 // ghosts at 0.  The ghosts at nx+1/ny+1/nz+1 of H are never read by any
 // operator and are not maintained.
 template <typename T>
-__global__ void __launch_bounds__(256) k_update_h(FieldArgs<T> a) {
+__device__ __forceinline__ void h_split_cell(const FieldArgs<T>& a, int x, int y, int z) {
   using V = typename V2<T>::t;
-  const Geo g = a.g;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
-  if (x > g.nx || y > g.ny || z > g.nz) return;
+  const Geo& g = a.g;
   const long i = g.at(x, y, z);
   V* Ec[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
   V* H[3] = {a.h, a.h + g.comp, a.h + 2 * g.comp};
@@ -311,6 +312,15 @@ __global__ void __launch_bounds__(256) k_update_h(FieldArgs<T> a) {
       st<T>(H[k] + j, cmul(a.pzm, h[k]));
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_h(FieldArgs<T> a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (x > a.g.nx || y > a.g.ny || z > a.g.nz) return;
+  h_split_cell<T>(a, x, y, z);
 }
 
 // ---------------------------------------------------------------------------
@@ -421,12 +431,10 @@ template <> __device__ __forceinline__ void corr<float>(float2* p, cx<double> v,
 
 constexpr int TFSF_YCH = 16;
 
+// Incident field at ix and the corrections of the rows iy in [y0, y1].
 template <typename T>
-__global__ void __launch_bounds__(64) k_tfsf(typename V2<T>::t* e, typename V2<T>::t* h, Geo g, SrcArgs s, int it) {
-  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ix > s.nx + 1) return;
-  const int y0 = blockIdx.y * TFSF_YCH;
-  const int y1 = min(y0 + TFSF_YCH - 1, s.ny + 1);
+__device__ __forceinline__ void tfsf_column(typename V2<T>::t* e, typename V2<T>::t* h, const Geo& g,
+                                            const SrcArgs& s, int it, int ix, int y0, int y1) {
   const int zm = s.iz_min;
   cx<double> ta, tb, vE, vH;
   typename V2<T>::t *pe, *ph;
@@ -466,6 +474,14 @@ __global__ void __launch_bounds__(64) k_tfsf(typename V2<T>::t* e, typename V2<T
       corr<T>(h + g.comp + g.at(ix, iy, zm), vH, +1);
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(64) k_tfsf(typename V2<T>::t* e, typename V2<T>::t* h, Geo g, SrcArgs s, int it) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ix > s.nx + 1) return;
+  const int y0 = blockIdx.y * TFSF_YCH;
+  tfsf_column<T>(e, h, g, s, it, ix, y0, min(y0 + TFSF_YCH - 1, s.ny + 1));
 }
 
 // ---------------------------------------------------------------------------
@@ -1001,6 +1017,10 @@ struct iris_engine {
   FluxFace* d_faces = nullptr;
   double* d_J = nullptr;
   double* h_J = nullptr;
+  // batch member: no DFT buffers of its own; z-plane DFT only on request
+  bool member = false;
+  bool dft_z_only = false;
+  std::vector<FluxFace> host_faces;
   // fused E+H stepping (FP32): second field buffers and D, per-step TF/SF table
   bool fused = false;
   void* e2 = nullptr;
@@ -1160,6 +1180,7 @@ int validate(const iris_params& p) {
   if (p.precision != IRIS_FP64 && p.precision != IRIS_FP32) return bad("precision must be IRIS_FP64 or IRIS_FP32");
   if (p.stencil < IRIS_STENCIL_DEFAULT || p.stencil > IRIS_STENCIL_FUSED) return bad("unknown stencil variant");
   if (p.stencil == IRIS_STENCIL_FUSED && p.precision != IRIS_FP32) return bad("the fused stencil is FP32 only");
+  if (p.dft_faces != IRIS_DFT_ALL && p.dft_faces != IRIS_DFT_Z) return bad("dft_faces must be IRIS_DFT_ALL or IRIS_DFT_Z");
   return IRIS_OK;
 }
 
@@ -1395,6 +1416,8 @@ int upload_material(iris_engine* E, const double* re, const double* im) {
   return IRIS_OK;
 }
 
+int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces);
+
 int build_dft(iris_engine* E) {
   const iris_params& p = E->p;
   bool single = true;
@@ -1408,6 +1431,7 @@ int build_dft(iris_engine* E) {
     on[1] = (p.nx == 1 && p.ny != 1);
     on[2] = true;
   }
+  if (E->dft_z_only) on[0] = on[1] = false;
   static const int comps[3][4] = {{1, 5, 2, 4}, {2, 3, 0, 5}, {0, 4, 1, 3}};  // (a,b,c,d) 0-based
   std::vector<FluxFace> faces(12);
   long P = 0;
@@ -1455,6 +1479,16 @@ int build_dft(iris_engine* E) {
     }
   }
   E->P = P;
+  E->host_faces = faces;
+  if (E->member) return IRIS_OK;  // a batch member: the batch owns the DFT buffers
+  return alloc_dft(E, faces.data(), 12);
+}
+
+// DFT buffers for E->P sample points: accumulators, the K-slot sample ring,
+// twiddles, the flux faces (nfaces FluxFace) and the flux output.
+int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
+  const iris_params& p = E->p;
+  const long P = E->P;
   // block length K: samples buffered before one accumulation pass
   size_t freeb = 0, totb = 0;
   CK(cudaMemGetInfo(&freeb, &totb));
@@ -1479,8 +1513,8 @@ int build_dft(iris_engine* E) {
     CK(cudaMalloc(&E->d_segs, sizeof(Seg) * E->segs.size()));
     CK(cudaMemcpy(E->d_segs, E->segs.data(), sizeof(Seg) * E->segs.size(), cudaMemcpyHostToDevice));
   }
-  CK(cudaMalloc(&E->d_faces, sizeof(FluxFace) * 12));
-  CK(cudaMemcpy(E->d_faces, faces.data(), sizeof(FluxFace) * 12, cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&E->d_faces, sizeof(FluxFace) * nfaces));
+  CK(cudaMemcpy(E->d_faces, faces, sizeof(FluxFace) * nfaces, cudaMemcpyHostToDevice));
   CK(cudaMalloc(&E->d_J, sizeof(double) * 6 * p.nof));
   CK(cudaMallocHost(&E->h_J, sizeof(double) * 6 * p.nof));
   return IRIS_OK;
@@ -1513,7 +1547,15 @@ long iris::engine_npts(const iris_engine* E, int box, int j) {
 
 extern "C" {
 
+static int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out);
+
 int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
+  return create_engine(pin, fw, false, false, out);
+}
+
+}  // extern "C"
+
+static int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out) {
   clear_error();
   if (!pin || !fw || !out) return fail(IRIS_EINVAL, "null argument");
   *out = nullptr;
@@ -1524,6 +1566,8 @@ int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
   if (pin->device < 0 || pin->device >= ndev) return fail(IRIS_EINVAL, "device ordinal out of range");
   iris_engine* E = new iris_engine();
   E->p = *pin;
+  E->member = member;
+  E->dft_z_only = z_only || pin->dft_faces == IRIS_DFT_Z;
   const iris_params& p = E->p;
   E->fw.assign(fw, fw + p.nof);
   E->prec = p.precision;
@@ -1631,6 +1675,8 @@ int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
   *out = E;
   return IRIS_OK;
 }
+
+extern "C" {
 
 void iris_destroy(iris_engine* E) {
   if (!E) return;
@@ -1940,3 +1986,468 @@ extern "C" int iris_dft_block_noalloc(const void* samples, int nk, long npts, in
   CK(cudaGetLastError());
   return IRIS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batched form: many independent Bloch cells (or k-points) stepped together.
+//
+// Each cell is a member engine (its own fields, UPML, material, source and
+// DFT point layout, but no DFT buffers).  One launch per operator covers
+// every cell: a persistent kernel walks a work list of (cell, tile) items in
+// cell, z, y, x order, so the CTAs running together touch neighbouring tiles
+// of one cell and the neighbour loads hit L2.  The DFT samples of all cells go
+// to one shared ring and one accumulator array (all cells share dt and the
+// frequency list) and are accumulated by the single-engine block kernel.  The
+// tile shape is picked by iris_batch_tune, which times the candidates on the
+// batch itself.
+
+namespace iris {
+namespace {
+
+struct BItem {
+  int cell, x0, y0, z0;  // tile origin (1-based)
+};
+struct TItem {
+  int cell, ix0, iy0, pad;
+};
+struct BSeg {
+  Seg s;
+  int cell, pad;
+};
+
+constexpr int NTILES = 5;
+constexpr int TILES[NTILES][3] = {{32, 8, 1}, {32, 4, 2}, {64, 4, 1}, {16, 16, 1}, {32, 2, 4}};
+
+// Copies the cell's arguments into shared memory when the item's cell changes.
+template <typename A>
+__device__ __forceinline__ void cell_args(const A* args, int cell, A& sa, int& scell, int tid) {
+  if (cell != scell) {
+    __syncthreads();
+    if (tid == 0) {
+      sa = args[cell];
+      scell = cell;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX* TY* TZ) k_batch_e(const FieldArgs<T>* __restrict__ args,
+                                                        const BItem* __restrict__ items, long nitems) {
+  __shared__ FieldArgs<T> sa;
+  __shared__ int scell;
+  const int tid = (threadIdx.z * TY + threadIdx.y) * TX + threadIdx.x;
+  if (tid == 0) scell = -1;
+  __syncthreads();
+  for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
+    const BItem b = items[k];
+    cell_args(args, b.cell, sa, scell, tid);
+    const int x = b.x0 + threadIdx.x, y = b.y0 + threadIdx.y, z = b.z0 + threadIdx.z;
+    if (x <= sa.g.nx && y <= sa.g.ny && z <= sa.g.nz) {
+      if (sa.eps_c) e_split_cell<T, true>(sa, x, y, z);
+      else e_split_cell<T, false>(sa, x, y, z);
+    }
+  }
+}
+
+template <typename T, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX* TY* TZ) k_batch_h(const FieldArgs<T>* __restrict__ args,
+                                                        const BItem* __restrict__ items, long nitems) {
+  __shared__ FieldArgs<T> sa;
+  __shared__ int scell;
+  const int tid = (threadIdx.z * TY + threadIdx.y) * TX + threadIdx.x;
+  if (tid == 0) scell = -1;
+  __syncthreads();
+  for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
+    const BItem b = items[k];
+    cell_args(args, b.cell, sa, scell, tid);
+    const int x = b.x0 + threadIdx.x, y = b.y0 + threadIdx.y, z = b.z0 + threadIdx.z;
+    if (x <= sa.g.nx && y <= sa.g.ny && z <= sa.g.nz) h_split_cell<T>(sa, x, y, z);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(64) k_batch_tfsf(const FieldArgs<T>* __restrict__ args,
+                                                   const SrcArgs* __restrict__ srcs, const TItem* __restrict__ items,
+                                                   long nitems, int it) {
+  for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
+    const TItem b = items[k];
+    const FieldArgs<T>& a = args[b.cell];
+    const SrcArgs& s = srcs[b.cell];
+    const int ix = b.ix0 + threadIdx.x;
+    if (s.variant == 0 || ix > s.nx + 1) continue;
+    tfsf_column<T>(a.e, a.h, a.g, s, it, ix, b.iy0, min(b.iy0 + TFSF_YCH - 1, s.ny + 1));
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_batch_gather(const FieldArgs<T>* __restrict__ args,
+                                                      const BSeg* __restrict__ segs,
+                                                      typename V2<T>::t* __restrict__ slot, int* tk, int islot,
+                                                      int t) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = t;
+  const BSeg b = segs[blockIdx.y];
+  const long L = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= (long)b.s.nu * b.s.nv) return;
+  const FieldArgs<T>& a = args[b.cell];
+  const int u = (int)(L % b.s.nu), v = (int)(L / b.s.nu);
+  const typename V2<T>::t* src = b.s.field < 3 ? a.e + b.s.field * a.g.comp : a.h + (b.s.field - 3) * a.g.comp;
+  slot[b.s.p0 + L] = src[b.s.src + (long)u * b.s.su + (long)v * b.s.sv];
+}
+
+}  // namespace
+}  // namespace iris
+
+struct iris_batch {
+  int n = 0;
+  int prec = IRIS_FP64;
+  int device = 0;
+  iris_engine* master = nullptr;  // stream, timing and the shared DFT buffers
+  std::vector<iris_engine*> cells;
+  std::vector<long> pbase;
+  void* d_args = nullptr;  // FieldArgs<T>[n]
+  SrcArgs* d_src = nullptr;
+  BItem* d_items = nullptr;
+  long nitems = 0;
+  int tile = 0;  // index into TILES
+  int grid_e = 0, grid_h = 0;
+  TItem* d_titems = nullptr;
+  long ntitems = 0;
+  BSeg* d_bsegs = nullptr;
+  int nbsegs = 0;
+  long max_seg = 0;
+  long steps_taken = 0;
+};
+
+namespace {
+
+int batch_upload_args(iris_batch* B) {
+  const size_t sz = B->prec == IRIS_FP64 ? sizeof(FieldArgs<double>) : sizeof(FieldArgs<float>);
+  std::vector<unsigned char> h(sz * B->n);
+  for (int c = 0; c < B->n; ++c) {
+    if (B->prec == IRIS_FP64) {
+      FieldArgs<double> a = field_args<double>(B->cells[c]);
+      std::memcpy(h.data() + sz * c, &a, sz);
+    } else {
+      FieldArgs<float> a = field_args<float>(B->cells[c]);
+      std::memcpy(h.data() + sz * c, &a, sz);
+    }
+  }
+  if (!B->d_args) CK(cudaMalloc(&B->d_args, h.size()));
+  CK(cudaMemcpy(B->d_args, h.data(), h.size(), cudaMemcpyHostToDevice));
+  return IRIS_OK;
+}
+
+int batch_build_items(iris_batch* B, int tile) {
+  const int TX = TILES[tile][0], TY = TILES[tile][1], TZ = TILES[tile][2];
+  std::vector<BItem> items;
+  for (int c = 0; c < B->n; ++c) {
+    const iris_params& p = B->cells[c]->p;
+    for (int z = 1; z <= p.nz; z += TZ)
+      for (int y = 1; y <= p.ny; y += TY)
+        for (int x = 1; x <= p.nx; x += TX) items.push_back(BItem{c, x, y, z});
+  }
+  if (B->d_items) cudaFree(B->d_items);
+  B->d_items = nullptr;
+  CK(cudaMalloc(&B->d_items, sizeof(BItem) * items.size()));
+  CK(cudaMemcpy(B->d_items, items.data(), sizeof(BItem) * items.size(), cudaMemcpyHostToDevice));
+  B->nitems = (long)items.size();
+  B->tile = tile;
+  return IRIS_OK;
+}
+
+template <typename T, int TX, int TY, int TZ> int persistent_grid(const void* kern) {
+  int nsm = 0, per = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TX * TY * TZ, 0);
+  return std::max(1, nsm * std::max(1, per));
+}
+
+template <typename T, int TX, int TY, int TZ> void launch_batch_eh(iris_batch* B, bool e) {
+  iris_engine* M = B->master;
+  const dim3 blk(TX, TY, TZ);
+  const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
+  if (e) {
+    static int grid = 0;
+    if (!grid) grid = persistent_grid<T, TX, TY, TZ>((const void*)k_batch_e<T, TX, TY, TZ>);
+    const long g = std::min<long>(grid, B->nitems);
+    KTimer tm(M, IRIS_KC_E);
+    k_batch_e<T, TX, TY, TZ><<<(unsigned)g, blk, 0, M->st>>>(args, B->d_items, B->nitems);
+  } else {
+    static int grid = 0;
+    if (!grid) grid = persistent_grid<T, TX, TY, TZ>((const void*)k_batch_h<T, TX, TY, TZ>);
+    const long g = std::min<long>(grid, B->nitems);
+    KTimer tm(M, IRIS_KC_H);
+    k_batch_h<T, TX, TY, TZ><<<(unsigned)g, blk, 0, M->st>>>(args, B->d_items, B->nitems);
+  }
+}
+
+template <typename T> void batch_eh(iris_batch* B, bool e) {
+  switch (B->tile) {
+    case 0: launch_batch_eh<T, 32, 8, 1>(B, e); break;
+    case 1: launch_batch_eh<T, 32, 4, 2>(B, e); break;
+    case 2: launch_batch_eh<T, 64, 4, 1>(B, e); break;
+    case 3: launch_batch_eh<T, 16, 16, 1>(B, e); break;
+    default: launch_batch_eh<T, 32, 2, 4>(B, e); break;
+  }
+}
+
+template <typename T> int batch_step_t(iris_batch* B, int it0, int n) {
+  iris_engine* M = B->master;
+  const iris_params& p = M->p;
+  using V = typename V2<T>::t;
+  const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
+  for (int it = it0; it < it0 + n; ++it) {
+    batch_eh<T>(B, true);
+    batch_eh<T>(B, false);
+    if (B->ntitems) {
+      KTimer tm(M, IRIS_KC_TFSF);
+      const long g = std::min<long>(B->ntitems, 152L * 16);
+      k_batch_tfsf<T><<<(unsigned)g, 64, 0, M->st>>>(args, B->d_src, B->d_titems, B->ntitems, it);
+    }
+    if (M->P > 0 && it >= p.to_fourier && it % p.sample_fourier == 0) {
+      {
+        KTimer tm(M, IRIS_KC_GATHER);
+        V* slot = (V*)M->S + (long)M->nslot * M->P;
+        dim3 grid((unsigned)((B->max_seg + 255) / 256), (unsigned)B->nbsegs);
+        k_batch_gather<T><<<grid, 256, 0, M->st>>>(args, B->d_bsegs, slot, M->d_tk, M->nslot, it + 1 - p.to_fourier);
+      }
+      if (++M->nslot == M->K) dft_flush(M);
+    }
+  }
+  B->steps_taken += n;
+  CK(cudaGetLastError());
+  return IRIS_OK;
+}
+
+void batch_free(iris_batch* B) {
+  for (iris_engine* E : B->cells)
+    if (E) iris_destroy(E);
+  void* ptrs[] = {B->d_args, B->d_src, B->d_items, B->d_titems, B->d_bsegs};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (B->master) {
+    free_engine(B->master);
+    delete B->master;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int iris_batch_create(int ncells, const iris_params* params, const double* fw, int dft_faces, iris_batch** out) {
+  clear_error();
+  if (ncells < 1 || !params || !fw || !out) return fail(IRIS_EINVAL, "bad argument");
+  *out = nullptr;
+  const iris_params& p0 = params[0];
+  for (int c = 1; c < ncells; ++c) {
+    const iris_params& q = params[c];
+    if (q.precision != p0.precision || q.nof != p0.nof || q.dt != p0.dt || q.to_fourier != p0.to_fourier ||
+        q.sample_fourier != p0.sample_fourier || q.device != p0.device || q.Q != p0.Q)
+      return fail(IRIS_EINVAL, "batch cells must share precision, dt, Q, nof, DFT sampling and device");
+  }
+  if (p0.stencil == IRIS_STENCIL_FUSED) return fail(IRIS_EINVAL, "the batch steps with the split passes");
+  iris_batch* B = new iris_batch();
+  B->n = ncells;
+  B->prec = p0.precision;
+  B->device = p0.device;
+  auto bail = [&](int code) {
+    batch_free(B);
+    delete B;
+    return code;
+  };
+  B->cells.assign(ncells, nullptr);
+  long P = 0;
+  std::vector<BSeg> bsegs;
+  std::vector<FluxFace> faces(6 * (size_t)ncells);
+  std::vector<SrcArgs> srcs(ncells);
+  std::vector<TItem> titems;
+  for (int c = 0; c < ncells; ++c) {
+    iris_params q = params[c];
+    q.stencil = IRIS_STENCIL_SPLIT;
+    int rc = create_engine(&q, fw, true, dft_faces == IRIS_DFT_Z, &B->cells[c]);
+    if (rc) return bail(rc);
+    iris_engine* E = B->cells[c];
+    B->pbase.push_back(P);
+    for (const Seg& s : E->segs) {
+      BSeg b{};
+      b.s = s;
+      b.s.p0 += P;
+      b.cell = c;
+      bsegs.push_back(b);
+      B->max_seg = std::max(B->max_seg, (long)s.nu * s.nv);
+    }
+    for (int f = 0; f < 6; ++f) {
+      FluxFace ff = E->host_faces[f];
+      if (ff.active) {
+        ff.pa += P;
+        ff.pb += P;
+        ff.pc += P;
+        ff.pd += P;
+      }
+      faces[6 * c + f] = ff;
+    }
+    srcs[c] = E->src;
+    if (E->src.variant != 0)
+      for (int iy = 0; iy <= q.ny + 1; iy += TFSF_YCH)
+        for (int ix = 0; ix <= q.nx + 1; ix += 64) titems.push_back(TItem{c, ix, iy, 0});
+    P += E->P;
+  }
+  // the shell: one stream, the timers and the shared DFT buffers
+  iris_engine* M = new iris_engine();
+  B->master = M;
+  M->p = params[0];
+  M->fw.assign(fw, fw + p0.nof);
+  M->prec = p0.precision;
+  M->esz = p0.precision == IRIS_FP64 ? 16 : 8;
+  M->device = p0.device;
+  M->P = P;
+  if (cudaSetDevice(M->device) != cudaSuccess) return bail(fail(IRIS_ECUDA, "cudaSetDevice failed"));
+  if (cudaStreamCreateWithFlags(&M->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(IRIS_ECUDA, "cudaStreamCreate failed"));
+  int rc = alloc_dft(M, faces.data(), (int)faces.size());
+  if (rc) return bail(rc);
+  if (cudaMalloc(&B->d_bsegs, sizeof(BSeg) * std::max<size_t>(1, bsegs.size())) != cudaSuccess ||
+      cudaMalloc(&B->d_src, sizeof(SrcArgs) * ncells) != cudaSuccess ||
+      cudaMalloc(&B->d_titems, sizeof(TItem) * std::max<size_t>(1, titems.size())) != cudaSuccess)
+    return bail(fail(IRIS_ENOMEM, "batch tables: allocation failed"));
+  cudaMemcpy(B->d_bsegs, bsegs.data(), sizeof(BSeg) * bsegs.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(B->d_src, srcs.data(), sizeof(SrcArgs) * ncells, cudaMemcpyHostToDevice);
+  cudaMemcpy(B->d_titems, titems.data(), sizeof(TItem) * titems.size(), cudaMemcpyHostToDevice);
+  B->nbsegs = (int)bsegs.size();
+  B->ntitems = (long)titems.size();
+  rc = batch_upload_args(B);
+  if (rc) return bail(rc);
+  rc = batch_build_items(B, 0);
+  if (rc) return bail(rc);
+  if (cudaStreamSynchronize(M->st) != cudaSuccess) return bail(fail(IRIS_ECUDA, "batch initialisation failed"));
+  *out = B;
+  return IRIS_OK;
+}
+
+void iris_batch_destroy(iris_batch* B) {
+  if (!B) return;
+  cudaSetDevice(B->device);
+  if (B->master && B->master->st) cudaStreamSynchronize(B->master->st);
+  batch_free(B);
+  delete B;
+}
+
+int iris_batch_set_material(iris_batch* B, int cell, const double* re, const double* im) {
+  clear_error();
+  if (!B || cell < 0 || cell >= B->n) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(B->device));
+  CK(cudaStreamSynchronize(B->master->st));
+  int rc = iris_set_material(B->cells[cell], re, im);
+  if (rc) return rc;
+  return batch_upload_args(B);  // the material pointer may have changed
+}
+
+int iris_batch_step(iris_batch* B, int it0, int nsteps) {
+  clear_error();
+  if (!B || nsteps < 0) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(B->device));
+  return B->prec == IRIS_FP64 ? batch_step_t<double>(B, it0, nsteps) : batch_step_t<float>(B, it0, nsteps);
+}
+
+int iris_batch_flux(iris_batch* B, int cell, double* J) {
+  clear_error();
+  if (!B || !J || cell < 0 || cell >= B->n) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(B->device));
+  iris_engine* M = B->master;
+  const iris_params& p = M->p;
+  dft_flush(M);
+  const double scale = p.eps0 * p.Q / (2.0 * p.dt);
+  k_flux<<<dim3(p.nof, 6), 256, 0, M->st>>>(M->fd, M->P, M->d_faces + 6 * cell, p.nof, scale, M->d_J);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(M->h_J, M->d_J, sizeof(double) * 6 * p.nof, cudaMemcpyDeviceToHost, M->st));
+  CK(cudaStreamSynchronize(M->st));
+  bool finite = true;
+  for (int k = 0; k < 6 * p.nof; ++k) {
+    J[k] = M->h_J[k];
+    if (!std::isfinite(J[k])) finite = false;
+  }
+  return finite ? IRIS_OK : fail(IRIS_ENAN, "non-finite flux");
+}
+
+int iris_batch_get_field(iris_batch* B, int cell, int which, double* re, double* im) {
+  clear_error();
+  if (!B || cell < 0 || cell >= B->n) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(B->device));
+  CK(cudaStreamSynchronize(B->master->st));
+  return iris_get_field(B->cells[cell], which, re, im);
+}
+
+int iris_batch_set_tile(iris_batch* B, int tile) {
+  clear_error();
+  if (!B || tile < 0 || tile >= NTILES) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(B->device));
+  CK(cudaStreamSynchronize(B->master->st));
+  return batch_build_items(B, tile);
+}
+
+int iris_batch_tune(iris_batch* B, int reps, int* best, double* ms) {
+  clear_error();
+  if (!B || reps < 1) return fail(IRIS_EINVAL, "bad argument");
+  if (B->steps_taken) return fail(IRIS_EINVAL, "tune before the first step (it runs E and H passes on the state)");
+  CK(cudaSetDevice(B->device));
+  iris_engine* M = B->master;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  int arg = 0;
+  double bestms = 1e30;
+  for (int t = 0; t < NTILES; ++t) {
+    int rc = batch_build_items(B, t);
+    if (rc) return rc;
+    // fields are still zero, so E and H passes leave the state unchanged
+    for (int r = 0; r < 2; ++r) {
+      B->prec == IRIS_FP64 ? batch_eh<double>(B, true) : batch_eh<float>(B, true);
+      B->prec == IRIS_FP64 ? batch_eh<double>(B, false) : batch_eh<float>(B, false);
+    }
+    CK(cudaEventRecord(a, M->st));
+    for (int r = 0; r < reps; ++r) {
+      B->prec == IRIS_FP64 ? batch_eh<double>(B, true) : batch_eh<float>(B, true);
+      B->prec == IRIS_FP64 ? batch_eh<double>(B, false) : batch_eh<float>(B, false);
+    }
+    CK(cudaEventRecord(b, M->st));
+    CK(cudaEventSynchronize(b));
+    float x = 0;
+    CK(cudaEventElapsedTime(&x, a, b));
+    if (ms) ms[t] = x / reps;
+    if (x < bestms) {
+      bestms = x;
+      arg = t;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (best) *best = arg;
+  return batch_build_items(B, arg);
+}
+
+int iris_batch_timing(iris_batch* B, int enable) {
+  if (!B) return fail(IRIS_EINVAL, "null batch");
+  return iris_timing(B->master, enable);
+}
+
+int iris_batch_timing_read(iris_batch* B, double* region_ms, double* kernel_ms, long* launches) {
+  if (!B) return fail(IRIS_EINVAL, "null batch");
+  return iris_timing_read(B->master, region_ms, kernel_ms, launches);
+}
+
+int iris_batch_info(const iris_batch* B, long* info) {
+  if (!B || !info) return fail(IRIS_EINVAL, "bad argument");
+  long cells = 0;
+  for (const iris_engine* E : B->cells) cells += (long)E->p.nx * E->p.ny * E->p.nz;
+  info[0] = B->n;
+  info[1] = cells;
+  info[2] = B->master->P;
+  info[3] = B->master->K;
+  info[4] = B->tile;
+  info[5] = B->nitems;
+  return IRIS_OK;
+}
+
+}  // extern "C"

@@ -86,6 +86,7 @@ class IrisParams(ctypes.Structure):
         ("pmlalfa", _D),
         ("akx_re", _D), ("akx_im", _D), ("aky_re", _D), ("aky_im", _D), ("akz_re", _D), ("akz_im", _D),
         ("system_model", _I), ("precision", _I), ("dft_block", _I), ("device", _I), ("stencil", _I),
+        ("dft_faces", _I),
     ]
 
     def copy(self) -> "IrisParams":
@@ -99,7 +100,9 @@ EXPORTS = [
     "iris_create", "iris_destroy", "iris_set_material", "iris_step", "iris_sync", "iris_flux",
     "iris_write_scatt", "iris_get_field", "iris_set_field", "iris_get_pml", "iris_set_pml",
     "iris_get_fdata", "iris_apply", "iris_run_input", "iris_timing", "iris_timing_read", "iris_info",
-    "iris_dft_block_noalloc",
+    "iris_dft_block_noalloc", "iris_batch_create", "iris_batch_destroy", "iris_batch_set_material",
+    "iris_batch_step", "iris_batch_flux", "iris_batch_get_field", "iris_batch_tune", "iris_batch_set_tile",
+    "iris_batch_timing", "iris_batch_timing_read", "iris_batch_info",
 ]
 
 _lib = None
@@ -142,6 +145,19 @@ def lib():
     L.iris_timing_read.argtypes = [vp, dp, dp, ctypes.POINTER(ctypes.c_long)]
     L.iris_info.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
     L.iris_dft_block_noalloc.argtypes = [vp, ip, ctypes.c_long, ip, ip, vp, ip, ctypes.c_double, vp, vp]
+    lp = ctypes.POINTER(ctypes.c_long)
+    L.iris_batch_create.argtypes = [ip, P, dp, ip, ctypes.POINTER(vp)]
+    L.iris_batch_destroy.argtypes = [vp]
+    L.iris_batch_destroy.restype = None
+    L.iris_batch_set_material.argtypes = [vp, ip, dp, dp]
+    L.iris_batch_step.argtypes = [vp, ip, ip]
+    L.iris_batch_flux.argtypes = [vp, ip, dp]
+    L.iris_batch_get_field.argtypes = [vp, ip, ip, dp, dp]
+    L.iris_batch_tune.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int), dp]
+    L.iris_batch_set_tile.argtypes = [vp, ip]
+    L.iris_batch_timing.argtypes = [vp, ip]
+    L.iris_batch_timing_read.argtypes = [vp, dp, dp, lp]
+    L.iris_batch_info.argtypes = [vp, lp]
     _lib = L
     return L
 

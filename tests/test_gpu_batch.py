@@ -1,0 +1,99 @@
+"""The batched form (iris_batch_*): every cell of an uneven batch against the
+same cell stepped on its own engine and against the FP64 oracle.
+
+The batch runs the same per-cell arithmetic as a single engine (the same
+device functions, one launch per operator over all cells), so FP64 cells
+agree with their single-engine runs to the last bit (asserted <= 1e-15) and
+with the oracle within 1e-12; FP32 cells within 1e-6 of FP32 single runs.
+"""
+import importlib
+import os
+
+import numpy as np
+import pytest
+
+from helpers import engine_params_from_oracle, interior, output_steps, rel_err, run_engine_blocks
+
+pytestmark = pytest.mark.gpu
+cfg = importlib.import_module("irisfdtd-academic_gb300.configs")
+THREADS = max(1, min(16, os.cpu_count() or 1))
+
+# nx, ny, nz, pmlzi, pmlzf, hi, dh, tfsf_zi, box, akx, structure
+CELLS = [
+    (12, 7, 60, 8, 53, 24, 10, 14, (1, 12, 1, 7, 10, 50), 0.3, "pattern"),
+    (33, 9, 48, 6, 43, 18, 8, 10, (1, 33, 1, 9, 8, 40), 0.0, "pattern"),
+    (5, 17, 72, 8, 65, 30, 12, 14, (1, 5, 1, 17, 11, 62), -0.7, "pattern"),
+    (40, 1, 64, 8, 57, 26, 10, 14, (1, 40, 1, 1, 10, 54), 0.0, "slab"),
+    (1, 1, 90, 10, 81, 40, 15, 16, (1, 1, 1, 1, 12, 78), 0.0, "slab"),
+]
+STEPS = 150
+
+
+def make_cells(oracle, tmp_path):
+    out = []
+    for i, (nx, ny, nz, pi, pf, hi, dh, zi, box, akx, kind) in enumerate(CELLS):
+        w = cfg.Workload(f"c{i}", nx, ny, nz, pi, pf, hi, dh, 4.0 if kind == "slab" else 1.0, 0, zi, box, 9, STEPS,
+                         structure=kind, extra=dict(seed=100 + i, fill=0.5))
+        op = oracle.setparam(cfg.write_input(str(tmp_path / f"c{i}.dat"), w, no_downloads=3))
+        eps = cfg.binary_pattern_material(w) if kind == "pattern" else cfg.slit_material(w)
+        out.append((w, op, (complex(akx), 0j, 0j), eps))
+    return out
+
+
+def batch_and_singles(iris, cells, precision, tune=False):
+    params = [engine_params_from_oracle(iris, op, precision=precision, ak=ak) for _, op, ak, _ in cells]
+    b = iris.Batch(params, cells[0][1].fw, dft_faces=iris.DFT_Z)
+    for c, (_, _, _, eps) in enumerate(cells):
+        b.set_material(c, eps)
+    if tune:
+        tile, ms = b.tune(reps=2)
+        assert tile in iris.TILES and len(ms) == len(iris.TILES)
+    its = output_steps(cells[0][1])
+    it = 1
+    for t in its:
+        b.step(it, t - it + 1)
+        it = t + 1
+    singles = []
+    for (_, op, ak, eps), p in zip(cells, params):
+        q = p.copy()
+        q.dft_faces = iris.DFT_Z
+        e = iris.Engine(q, op.fw)
+        e.set_material(eps)
+        J = run_engine_blocks(e, op, its)
+        singles.append((e, J[-1]))
+    return b, singles
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-15), (1, 1e-6)])
+def test_batch_matches_single_engines(iris, oracle, tmp_path, precision, tol):
+    cells = make_cells(oracle, tmp_path)
+    b, singles = batch_and_singles(iris, cells, precision)
+    assert b.info()["cells"] == len(CELLS)
+    for c, (e, Js) in enumerate(singles):
+        Jb = b.flux(c)
+        assert rel_err(Jb, Js) <= tol, c
+        assert np.all(Jb[:4] == 0)  # only the z planes are accumulated
+        for which in (iris.E, iris.H):
+            fb = interior(b.get_field(c, which), cells[c][1])
+            fs = interior(e.get_field(which), cells[c][1])
+            assert rel_err(fb, fs) <= tol, (c, which)
+
+
+def test_batch_against_oracle(iris, oracle, tmp_path):
+    cells = make_cells(oracle, tmp_path)
+    b, _ = batch_and_singles(iris, cells, 0, tune=True)
+    for c, (w, op, ak, eps) in enumerate(cells):
+        o = oracle.Oracle(op, ak=ak, threads=THREADS)
+        o.set_eps_inv(eps)
+        o.run(1, op.texit)
+        Jo = o.flux(0)
+        assert rel_err(b.flux(c)[4:], Jo[4:]) <= 1e-12, c
+
+
+def test_batch_rejects_mixed_timesteps(iris, oracle, tmp_path):
+    cells = make_cells(oracle, tmp_path)[:2]
+    params = [engine_params_from_oracle(iris, op) for _, op, _, _ in cells]
+    params[1].dt *= 1.01
+    with pytest.raises(iris.IrisError) as e:
+        iris.Batch(params, cells[0][1].fw)
+    assert e.value.code == -1
