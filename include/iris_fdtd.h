@@ -293,6 +293,54 @@ int iris_batch_timing_read(iris_batch* b, double* region_ms, double* kernel_ms, 
  * [4] tile index, [5] work items per pass. */
 int iris_batch_info(const iris_batch* b, long* info);
 
+/* ---- adjoint (gradient) form ------------------------------------------- */
+/*
+ * dL/d(eps_inv) over a design region of the structure layer for the
+ * objective
+ *     L = sum_w  w5[w] * J5(w) + w6[w] * J6(w)
+ * where J5 and J6 are the reflection and transmission fluxes of box 1
+ * (the scattering_fourier_out numbers, code/dataprocess.f90:246-277).  No
+ * counterpart in the reference: it differentiates the time loop that
+ * code/driver.f90:338-451 runs.
+ *
+ * The gradient is the exact discrete adjoint of the engine's update: the
+ * transposed E/H/UPML step run backwards in time with the conjugate-
+ * transposed DFT as its source, accumulated against the forward curl of H
+ * over the design cells.  Forward states are checkpointed every
+ * checkpoint_every steps and each segment is recomputed from its checkpoint
+ * during the backward sweep.
+ *
+ * design: {x0, x1, y0, y1, z0, z1}, 1-based and inclusive, inside
+ * [1,nx] x [1,ny] x [hi,hf].  weights: [2][nof] (w5 then w6), or NULL for
+ * w5 = 0, w6 = 1.  The material must be real; the z planes of box 1 must lie
+ * outside the UPML slabs (pmlzi < szi, szf < pmlzf).  Only box 1's z faces
+ * are accumulated.
+ */
+typedef struct iris_adjoint iris_adjoint;
+int iris_adjoint_create(const iris_params* p, const double* fw, const int design[6], int checkpoint_every,
+                        const double* weights, iris_adjoint** out);
+void iris_adjoint_destroy(iris_adjoint* a);
+/* Whole structure material, as iris_set_material (imaginary part zero). */
+int iris_adjoint_set_material(iris_adjoint* a, const double* eps_inv_re, const double* eps_inv_im);
+/* eps_inv of the design cells, [z][y][x] with x fastest. */
+int iris_adjoint_set_design(iris_adjoint* a, const double* eps_inv);
+/* Forward solve from zero fields over steps 1..nsteps, saving checkpoints;
+ * L receives the objective, J (optional, [6][nof]) the box-1 fluxes. */
+int iris_adjoint_forward(iris_adjoint* a, int nsteps, double* L, double* J);
+/* Backward sweep for the last forward: grad[z][y][x] = dL/d eps_inv. */
+int iris_adjoint_backward(iris_adjoint* a, double* grad);
+/* The forward engine (which = 0) or the engine holding the adjoint state
+ * (which = 1: E, H, D, B read and written with iris_get/set_field and
+ * iris_get/set_pml).  Borrowed: owned by the adjoint object. */
+int iris_adjoint_engine(iris_adjoint* a, int which, iris_engine** eng);
+/* nsteps steps of the homogeneous adjoint recursion (no sources, no
+ * gradient) applied to the adjoint state, for a step at time index it: the
+ * conjugate transpose of nsteps source-free forward steps. */
+int iris_adjoint_apply(iris_adjoint* a, int nsteps);
+/* Device time (ms) of the last forward, of the last backward's recompute
+ * and of its adjoint sweep; ms[3]. */
+int iris_adjoint_timing(const iris_adjoint* a, double* ms);
+
 /* ---- allocation-free DFT block ---------------------------------------- */
 /*
  * This entry point has no counterpart in the reference.  It exists for

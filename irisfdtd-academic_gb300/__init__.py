@@ -101,8 +101,18 @@ class Engine:
         check(self.L.iris_create(ctypes.byref(self.p), _dp(self.fw), ctypes.byref(h)), "iris_create")
         self.h = h
 
+    @classmethod
+    def _view(cls, handle, p: IrisParams, fw, owner) -> "Engine":
+        """A borrowed engine handle (owned and destroyed by owner)."""
+        e = cls.__new__(cls)
+        e.L, e.p, e.fw, e.h, e._owner = lib(), p, fw, handle, owner
+        return e
+
     # -- lifetime
     def close(self):
+        if getattr(self, "_owner", None) is not None:
+            self.h = None
+            return
         if getattr(self, "h", None):
             self.L.iris_destroy(self.h)
             self.h = None
@@ -305,6 +315,9 @@ class Batch:
         a = (ctypes.c_long * 6)()
         check(self.L.iris_batch_info(self.h, a), "iris_batch_info")
         return dict(cells=a[0], grid_cells=a[1], dft_points=a[2], dft_block=a[3], tile=TILES[a[4]], items=a[5])
+
+
+from .adjoint import Adjoint, design_objective  # noqa: E402
 
 
 def run_input(directory: str, precision: int = FP64):

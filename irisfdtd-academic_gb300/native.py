@@ -103,6 +103,9 @@ EXPORTS = [
     "iris_dft_block_noalloc", "iris_batch_create", "iris_batch_destroy", "iris_batch_set_material",
     "iris_batch_step", "iris_batch_flux", "iris_batch_get_field", "iris_batch_tune", "iris_batch_set_tile",
     "iris_batch_timing", "iris_batch_timing_read", "iris_batch_info",
+    "iris_adjoint_create", "iris_adjoint_destroy", "iris_adjoint_set_material", "iris_adjoint_set_design",
+    "iris_adjoint_forward", "iris_adjoint_backward", "iris_adjoint_engine", "iris_adjoint_apply",
+    "iris_adjoint_timing",
 ]
 
 _lib = None
@@ -158,6 +161,16 @@ def lib():
     L.iris_batch_timing.argtypes = [vp, ip]
     L.iris_batch_timing_read.argtypes = [vp, dp, dp, lp]
     L.iris_batch_info.argtypes = [vp, lp]
+    L.iris_adjoint_create.argtypes = [P, dp, ctypes.POINTER(ctypes.c_int), ip, dp, ctypes.POINTER(vp)]
+    L.iris_adjoint_destroy.argtypes = [vp]
+    L.iris_adjoint_destroy.restype = None
+    L.iris_adjoint_set_material.argtypes = [vp, dp, dp]
+    L.iris_adjoint_set_design.argtypes = [vp, dp]
+    L.iris_adjoint_forward.argtypes = [vp, ip, dp, dp]
+    L.iris_adjoint_backward.argtypes = [vp, dp]
+    L.iris_adjoint_engine.argtypes = [vp, ip, ctypes.POINTER(vp)]
+    L.iris_adjoint_apply.argtypes = [vp, ip]
+    L.iris_adjoint_timing.argtypes = [vp, dp]
     _lib = L
     return L
 
