@@ -32,6 +32,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 PKG = "irisfdtd-academic_gb300"
@@ -360,6 +362,109 @@ def run_batch(args, rank, world, local):
     return out
 
 
+def run_adjoint(args, rank, world, local):
+    """configs[4]: dL/d eps over a 128x128x32 design region (eps ~U[1,12],
+    seed 0) of a 160x160x512 cell, L = sum over 64 frequencies of J6, FP32
+    forward and adjoint, checkpoints every 256 steps.  Reports the gradient
+    throughput, its cost against the forward solve, and its error against
+    the FP64 adjoint and against central differences of the FP64 forward."""
+    iris = importlib.import_module(PKG)
+    cfg = importlib.import_module(PKG + ".configs")
+    D = Dist(world)
+    w = cfg.workload(5)
+    ex = w.extra
+    design = (ex["x0"], ex["x1"], ex["y0"], ex["y1"], w.hi, w.hi + w.dh - 1)
+    t = time.perf_counter()
+    eps_inv = cfg.design_region_material(w, seed=rank).real
+    t_mat = time.perf_counter() - t
+    path = cfg.write_input(os.path.join(tempfile.mkdtemp(prefix="iris_adj_"), "inputFDTD.dat"), w)
+    p, fw, _ = iris.setparam(path)
+    p.device = local
+    N = args.adjoint_steps or w.nsteps
+    cells = w.nx * w.ny * w.nz
+    eta = eps_inv[1:-1, design[2]:design[3] + 1, design[0]:design[1] + 1].copy()
+
+    def solve(precision, warm):
+        adj = iris.Adjoint(p, fw, design, checkpoint_every=256, precision=precision, device=local)
+        adj.set_material(eps_inv)
+        if warm:
+            adj.forward(8)
+            adj.backward()
+        t0 = time.perf_counter()
+        L, _ = adj.forward(N)
+        g = adj.backward()
+        wall = time.perf_counter() - t0
+        return adj, L, g, adj.timing(), wall
+
+    D.barrier()
+    pr, cpath = start_clocks(local)
+    adj32, L32, g32, tm32, wall32 = solve(iris.FP32, True)
+    clocks = stop_clocks(pr, cpath)
+    fwd_ms = D.max(tm32["forward_ms"])
+    bwd_ms = D.max(tm32["recompute_ms"] + tm32["adjoint_ms"])
+    out = {
+        "metric": METRIC, "value": round(world * cells * N / ((fwd_ms + bwd_ms) * 1e-3) / 1e9, 3),
+        "unit": "Gcell/s", "n_gpus": world, "steps": N, "warmup": 8,
+        "ms_per_step": round((fwd_ms + bwd_ms) / N, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 fields and adjoint (fp32), fp64 DFT and gradient accumulation",
+        "data": "synthetic (design eps ~U[1,12], numpy PCG64 seed = rank)",
+        "config": {"workload": f"{w.name} gradient (configs[4])", "grid": [w.nx, w.ny, w.nz],
+                   "design_region": list(design), "nof": w.nof, "checkpoint_every": 256,
+                   "objective": "sum_w J6(w)",
+                   "l2": "fields 2 x %.2f GB >> 129 MB L2" % (cells * 24 / 1e9),
+                   "parallelism": f"replicas x{world} (independent designs, one per GPU)"},
+        "value_is": "grid cell-updates of the forward solve / device time of forward + backward",
+        "forward_gcells": round(cells * N / (fwd_ms * 1e-3) / 1e9, 3),
+        "forward_ms": round(fwd_ms, 1), "recompute_ms": round(tm32["recompute_ms"], 1),
+        "adjoint_ms": round(tm32["adjoint_ms"], 1),
+        "gradient_cost_vs_forward": round(bwd_ms / fwd_ms, 3),
+        "e2e": {"value": round(world * cells * N / wall32 / 1e9, 3), "unit": "Gcell/s",
+                "h2d_bytes_per_step": round(eps_inv.size * 16 / N, 1),
+                "d2h_bytes_per_step": round(g32.size * 8 / N, 1),
+                "what": "forward (%d steps, checkpoints) + backward through the C ABI, gradient to host" % N},
+        "clocks": clocks, "material_setup_s": round(t_mat, 2),
+    }
+    hbm, src = peaks()
+    eb, hb = algorithmic_bytes(w, p, 8, 4)
+    fwd_bw = (eb + hb) * N / (fwd_ms * 1e-3) / 1e9
+    out["roofline"] = {"kernel": "forward step (update_e + update_h + tfsf + dft)", "bound": "hbm",
+                       "achieved": round(fwd_bw, 1), "peak": hbm, "unit": "GB/s", "frac": round(fwd_bw / hbm, 4),
+                       "peak_source": src, "traffic": None}
+    if rank == 0 and world == 1 and not args.no_fp64_compare:
+        adj64, L64, g64, tm64, _ = solve(iris.FP64, False)
+        g32e, g64e = -g32 * eta ** 2, -g64 * eta ** 2
+        check = {"L_rel_err_fp32": abs(L32 - L64) / abs(L64),
+                 "grad_rel_err_fp32_vs_fp64": float(np.max(np.abs(g32e - g64e)) / np.max(np.abs(g64e))),
+                 "fp64_forward_ms": round(tm64["forward_ms"], 1),
+                 "fp64_backward_ms": round(tm64["recompute_ms"] + tm64["adjoint_ms"], 1)}
+        if args.fd_voxels:
+            r = np.random.default_rng(0)
+            eps = 1.0 / eta
+            fd, ad32, ad64 = [], [], []
+            h = 1e-3
+            for q in r.choice(eta.size, args.fd_voxels, replace=False):
+                idx = np.unravel_index(q, eta.shape)
+                v = []
+                for sgn in (1, -1):
+                    e2 = eps.copy()
+                    e2[idx] += sgn * h
+                    adj64.set_design(1.0 / e2)
+                    v.append(adj64.forward(N)[0])
+                fd.append((v[0] - v[1]) / (2 * h))
+                ad32.append(g32e[idx])
+                ad64.append(g64e[idx])
+            fd, ad32, ad64 = map(np.asarray, (fd, ad32, ad64))
+            check["fd_voxels"] = int(args.fd_voxels)
+            check["fd_h"] = h
+            check["grad_rel_err_fp32_vs_fd"] = float(np.max(np.abs(ad32 - fd)) / np.max(np.abs(fd)))
+            check["grad_rel_err_fp64_vs_fd"] = float(np.max(np.abs(ad64 - fd)) / np.max(np.abs(fd)))
+        out["gradient_check"] = check
+        adj64.close()
+    adj32.close()
+    D.close()
+    return out
+
+
 def loop_plain(iris, ws, params, mats, fw, local, nsample, steps):
     """The same cells stepped one after another, each on its own engine (the plain
     solver in a loop), on a sample of the batch: aggregate Gcell/s."""
@@ -485,6 +590,9 @@ def main():
     ap.add_argument("--stencil", type=int, default=0, choices=[0, 1, 2],
                     help="0: engine default (split), 1: split E and H passes, 2: fused E+H pass (fp32)")
     ap.add_argument("--cells", type=int, default=256, help="cells in the batch (workload 4)")
+    ap.add_argument("--adjoint-steps", type=int, default=0, help="workload 5: forward steps (0: the workload's 6000)")
+    ap.add_argument("--fd-voxels", type=int, default=4,
+                    help="workload 5: voxels checked against central differences of the FP64 forward")
     ap.add_argument("--loop-sample", type=int, default=16,
                     help="workload 4: cells of the batch also stepped one by one on plain engines (0: skip)")
     args = ap.parse_args()
@@ -495,6 +603,8 @@ def main():
         out = run_reference(args, rank, world)
     elif args.workload == 4:
         out = run_batch(args, rank, world, local)
+    elif args.workload == 5:
+        out = run_adjoint(args, rank, world, local)
     else:
         out = run_engine(args, rank, world, local)
     if rank == 0 and out is not None:
