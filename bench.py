@@ -587,8 +587,8 @@ def main():
                     help="run the workload resized to this grid (profiling cases)")
     ap.add_argument("--nof", type=int, default=None, help="number of DFT frequencies with --grid")
     ap.add_argument("--dft-block", type=int, default=0, help="DFT samples per accumulation block (0: engine default)")
-    ap.add_argument("--stencil", type=int, default=0, choices=[0, 1, 2],
-                    help="0: engine default (split), 1: split E and H passes, 2: fused E+H pass (fp32)")
+    ap.add_argument("--stencil", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="0: engine default, 1: split E and H passes, 2: fused E+H pass (fp32), 3: streamed split passes (fp32)")
     ap.add_argument("--cells", type=int, default=256, help="cells in the batch (workload 4)")
     ap.add_argument("--adjoint-steps", type=int, default=0, help="workload 5: forward steps (0: the workload's 6000)")
     ap.add_argument("--fd-voxels", type=int, default=4,

@@ -128,6 +128,10 @@ typedef struct iris_params {
 /* one fused E+H pass over double-buffered fields (12 values per cell);
  * IRIS_FP32 only                                                          */
 #define IRIS_STENCIL_FUSED 2
+/* the split passes with each plane staged in shared memory by bulk (TMA)
+ * copies, z-marching tiles; IRIS_FP32 with a real material (a complex
+ * material steps with the split passes)                                   */
+#define IRIS_STENCIL_STREAM 3
 
 typedef struct iris_engine iris_engine;
 

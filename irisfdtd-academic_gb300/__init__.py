@@ -34,7 +34,7 @@ from . import native
 from .native import IrisError, IrisParams, build, check, lib
 
 FP64, FP32 = 0, 1
-STENCIL_DEFAULT, STENCIL_SPLIT, STENCIL_FUSED = 0, 1, 2
+STENCIL_DEFAULT, STENCIL_SPLIT, STENCIL_FUSED, STENCIL_STREAM = 0, 1, 2, 3
 E, H = 0, 1
 OP_E, OP_H, OP_TFSF, OP_DFT = 1, 2, 3, 4
 

@@ -27,8 +27,9 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
-#include <string>
 #include <mutex>
+#include <string>
+#include <type_traits>
 #include <vector>
 
 #include "iris_internal.h"
@@ -102,29 +103,20 @@ template <typename T> struct FieldArgs {
   cx<T> pxp, pyp, pzp, pxm, pym, pzm;  // Bloch phases exp(+-i ak)
 };
 
-// New E of interior cell (x, y, z) from the old E and H: e_fdtd
+// New E of interior cell (x, y, z) from the curl of the old H (c) and the
+// old E (e, replaced): the material and UPML part of e_fdtd
 // (code/fdtd.f90:57-153) and UPML_Array_e (code/boundary_II.f90:60-138).
 // Per z the reference's region order decides: the UPML slabs overwrite
 // whatever e_fdtd wrote there.  The UPML auxiliary is read from a.pml_d and,
 // when dnew is given, its new value written there (dnew == a.pml_d updates in
-// place).
-// The E update of one cell given its own old H (h), the old H one plane
-// below (hzm, components 1 and 2) and its old E (e, replaced by the new E);
-// the x-1 and y-1 neighbours are loaded here.  MASK selects the components
-// computed (bit k: E_{k+1}); loads only the others need are never issued.
-template <typename T, bool CEPS, int MASK = 7>
-__device__ __forceinline__ void e_update(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
-                                         const cx<T> h[3], const cx<T> hzm[3], cx<T> e[3]) {
+// place).  With EPV the caller supplies the real structure eps_inv of the
+// cell (ep) instead of it being read from a.eps_r.  MASK selects the
+// components computed (bit k: E_{k+1}).
+template <typename T, bool CEPS, int MASK = 7, bool EPV = false>
+__device__ __forceinline__ void e_apply(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
+                                        const cx<T> c[3], cx<T> e[3], T ep = T(0)) {
   using V = typename V2<T>::t;
   const Geo& g = a.g;
-  const long i = g.at(x, y, z);
-  const V* H1 = a.h;
-  const V* H2 = a.h + g.comp;
-  const V* H3 = a.h + 2 * g.comp;
-  cx<T> c[3];
-  if (MASK & 1) c[0] = cadd(csub(csub(h[2], ld<T>(H3 + i - g.pitch)), h[1]), hzm[1]);
-  if (MASK & 2) c[1] = cadd(csub(csub(h[0], hzm[0]), h[2]), ld<T>(H3 + i - 1));
-  if (MASK & 4) c[2] = cadd(csub(csub(h[1], ld<T>(H2 + i - 1)), h[0]), ld<T>(H1 + i - g.pitch));
   if (z <= a.pmlzi || z >= a.pmlzf) {
     const int slab = z <= a.pmlzi ? 0 : 1;
     const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
@@ -145,15 +137,15 @@ __device__ __forceinline__ void e_update(const FieldArgs<T>& a, typename V2<T>::
   } else if (z >= a.hi && z <= a.hf) {
     const long ie = (long)(z - a.hi) * g.plane + (long)y * g.pitch + (long)(x + g.xo);
     if (CEPS) {
-      const cx<T> ep = ld<T>(a.eps_c + ie);
+      const cx<T> epc = ld<T>(a.eps_c + ie);
 #pragma unroll
       for (int k = 0; k < 3; ++k)
-        if (MASK & (1 << k)) e[k] = cadd(e[k], cmul(ep, c[k]));
+        if (MASK & (1 << k)) e[k] = cadd(e[k], cmul(epc, c[k]));
     } else {
-      const T ep = a.eps_r[ie];
+      const T epr = EPV ? ep : a.eps_r[ie];
 #pragma unroll
       for (int k = 0; k < 3; ++k)
-        if (MASK & (1 << k)) e[k] = cadd(e[k], rmul(ep, c[k]));
+        if (MASK & (1 << k)) e[k] = cadd(e[k], rmul(epr, c[k]));
     }
   } else {
     const T m = z < a.hi ? a.m1 : a.m3;
@@ -161,6 +153,26 @@ __device__ __forceinline__ void e_update(const FieldArgs<T>& a, typename V2<T>::
     for (int k = 0; k < 3; ++k)
       if (MASK & (1 << k)) e[k] = cadd(e[k], rmul(m, c[k]));
   }
+}
+
+// The E update of one cell given its own old H (h), the old H one plane
+// below (hzm, components 1 and 2) and its old E (e, replaced by the new E);
+// the x-1 and y-1 neighbours are loaded here.  MASK selects the components
+// computed (bit k: E_{k+1}); loads only the others need are never issued.
+template <typename T, bool CEPS, int MASK = 7>
+__device__ __forceinline__ void e_update(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
+                                         const cx<T> h[3], const cx<T> hzm[3], cx<T> e[3]) {
+  using V = typename V2<T>::t;
+  const Geo& g = a.g;
+  const long i = g.at(x, y, z);
+  const V* H1 = a.h;
+  const V* H2 = a.h + g.comp;
+  const V* H3 = a.h + 2 * g.comp;
+  cx<T> c[3];
+  if (MASK & 1) c[0] = cadd(csub(csub(h[2], ld<T>(H3 + i - g.pitch)), h[1]), hzm[1]);
+  if (MASK & 2) c[1] = cadd(csub(csub(h[0], hzm[0]), h[2]), ld<T>(H3 + i - 1));
+  if (MASK & 4) c[2] = cadd(csub(csub(h[1], ld<T>(H2 + i - 1)), h[0]), ld<T>(H1 + i - g.pitch));
+  e_apply<T, CEPS, MASK>(a, dnew, x, y, z, c, e);
 }
 
 // New E of interior cell (x, y, z) from the old E and H in memory: e_fdtd
@@ -321,6 +333,321 @@ __global__ void __launch_bounds__(256) k_update_h(FieldArgs<T> a) {
   const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
   if (x > a.g.nx || y > a.g.ny || z > a.g.nz) return;
   h_split_cell<T>(a, x, y, z);
+}
+
+// ---------------------------------------------------------------------------
+// Streamed split passes (FP32, real material).
+//
+// A CTA owns an SX x SY column tile of one cell and marches z over a chunk of
+// up to SZC planes.  Each plane a pass reads is staged in shared memory by
+// 1-D bulk copies (cp.async.bulk: the TMA engine, issued by one warp, one
+// copy per row and component) into a ring of SNST stage buffers, each with an
+// mbarrier that completes when its bytes have landed; the next two planes
+// are in flight while one is computed.  Rows are copied from 16-byte aligned
+// starts (x = 1 sits on a 128-byte boundary, SX is a multiple of 4) and
+// trimmed to the cells the tile needs, so DRAM traffic stays at the
+// algorithmic bytes.  The arithmetic is that of the split passes.
+
+constexpr int SX = 32, SY = 8, SNST = 4, SZC = 32;
+
+struct StageE {                 // E pass, plane z
+  float2 h[3][SY + 1][SX + 2];  // H rows y0-1 .. y0+SY-1, cells x0-2 .. x0+SX-1
+  float2 e[3][SY][SX];          // E rows y0 .. y0+SY-1, cells x0 .. x0+SX-1
+  float eps[SY][SX];            // structure eps_inv (planes hi..hf)
+};
+struct StageH {                 // H pass, plane z
+  float2 e[3][SY + 1][SX + 2];  // E rows y0 .. y0+SY, cells x0 .. x0+SX+1
+  float2 h[3][SY][SX];          // H rows y0 .. y0+SY-1, cells x0 .. x0+SX-1
+};
+static_assert(sizeof(StageE) % 16 == 0 && sizeof(StageH) % 16 == 0, "stage buffers keep 16-byte alignment");
+constexpr size_t STREAM_SMEM_E = SNST * sizeof(StageE);
+constexpr size_t STREAM_SMEM_H = SNST * sizeof(StageH);
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for phase parity of bar for at most about limit clock cycles;
+// false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, long long limit) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > limit) return false;
+  return true;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+constexpr long long STREAM_WAIT_CYCLES = 1LL << 31;  // about a second
+
+// Issue (warp 0) the bulk copies of plane z into stage S of the E pass:
+// full: H (3 components, rows y0-1 .. y0+nye-1), E (3 components, own rows)
+// and, on structure planes, eps_inv; otherwise H components 1, 2 of the own
+// rows (the plane below the chunk).
+__device__ __forceinline__ void stream_issue_e(const FieldArgs<float>& a, StageE* S, uint64_t* bar, int x0, int y0,
+                                               int z, bool full) {
+  const Geo& g = a.g;
+  const int lane = threadIdx.x;
+  const int nxe = min(SX, g.nx - x0 + 1), nye = min(SY, g.ny - y0 + 1);
+  const unsigned bh = (unsigned)((nxe + 3) & ~1) * 8u;  // cells x0-2 .. x0+nxe-1
+  const unsigned be = (unsigned)((nxe + 1) & ~1) * 8u;  // cells x0 .. x0+nxe-1
+  const unsigned bp = (unsigned)((nxe + 3) & ~3) * 4u;
+  const bool ep = full && z >= a.hi && z <= a.hf;
+  const int nh = full ? 3 * (nye + 1) : 2 * nye, ne = full ? 3 * nye : 0, np = ep ? nye : 0;
+  if (lane == 0) mbar_expect_tx(bar, nh * bh + ne * be + np * bp);
+  __syncwarp();
+  fence_proxy_async();
+  for (int q = lane; q < nh + ne + np; q += 32) {
+    if (q < nh) {
+      const int k = full ? q / (nye + 1) : q / nye;
+      const int r = full ? q % (nye + 1) : 1 + q % nye;
+      bulk_g2s(&S->h[k][r][0], a.h + k * g.comp + g.at(x0 - 2, y0 - 1 + r, z), bh, bar);
+    } else if (q < nh + ne) {
+      const int k = (q - nh) / nye, r = (q - nh) % nye;
+      bulk_g2s(&S->e[k][r][0], a.e + k * g.comp + g.at(x0, y0 + r, z), be, bar);
+    } else {
+      const int r = q - nh - ne;
+      bulk_g2s(&S->eps[r][0], a.eps_r + (long)(z - a.hi) * g.plane + g.at(x0, y0 + r, 0), bp, bar);
+    }
+  }
+}
+
+// Issue (warp 0) the bulk copies of plane z into stage S of the H pass:
+// full: E (3 components, rows y0 .. y0+nye, cells x0 .. x0+nxe) and H (own
+// rows and cells); otherwise E components 1, 2 of the own rows and cells
+// (the plane above the chunk).
+__device__ __forceinline__ void stream_issue_h(const FieldArgs<float>& a, StageH* S, uint64_t* bar, int x0, int y0,
+                                               int z, bool full) {
+  const Geo& g = a.g;
+  const int lane = threadIdx.x;
+  const int nxe = min(SX, g.nx - x0 + 1), nye = min(SY, g.ny - y0 + 1);
+  const unsigned bx = (unsigned)((nxe + 2) & ~1) * 8u;  // cells x0 .. x0+nxe
+  const unsigned bo = (unsigned)((nxe + 1) & ~1) * 8u;  // cells x0 .. x0+nxe-1
+  const int ne = full ? 3 * (nye + 1) : 2 * nye, nh = full ? 3 * nye : 0;
+  if (lane == 0) mbar_expect_tx(bar, full ? ne * bx + nh * bo : ne * bo);
+  __syncwarp();
+  fence_proxy_async();
+  for (int q = lane; q < ne + nh; q += 32) {
+    if (q < ne) {
+      const int k = full ? q / (nye + 1) : q / nye;
+      const int r = full ? q % (nye + 1) : q % nye;
+      bulk_g2s(&S->e[k][r][0], a.e + k * g.comp + g.at(x0, y0 + r, z), full ? bx : bo, bar);
+    } else {
+      const int k = (q - ne) / nye, r = (q - ne) % nye;
+      bulk_g2s(&S->h[k][r][0], a.h + k * g.comp + g.at(x0, y0 + r, z), bo, bar);
+    }
+  }
+}
+
+// Bounded wait for every stage still being filled (after a failed wait).
+__device__ __forceinline__ void stream_drain(uint64_t* bar, unsigned par, unsigned pend) {
+  for (int s = 0; s < SNST; ++s)
+    if (pend & (1u << s)) mbar_wait(bar + s, (par >> s) & 1u, STREAM_WAIT_CYCLES >> 4);
+}
+
+// The E pass over planes zs .. min(zs+SZC-1, nz) of the tile at (x0, y0).
+// par: expected phase parity per stage, block-uniform, carried across tiles.
+// Returns false when a stage never completed (*err is then set).
+__device__ bool stream_tile_e(const FieldArgs<float>& a, int x0, int y0, int zs, StageE* S, uint64_t* bar,
+                              unsigned& par, int* err) {
+  const Geo& g = a.g;
+  const int ze = min(zs + SZC - 1, g.nz);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x = x0 + tx, y = y0 + ty;
+  const bool own = x <= g.nx && y <= g.ny;
+  const bool w0 = ty == 0;
+  unsigned pend = 0;
+  // ring slot of plane p: (p - zs + 1) % SNST
+  if (w0) {
+    stream_issue_e(a, S + 0, bar + 0, x0, y0, zs - 1, false);
+    stream_issue_e(a, S + 1, bar + 1, x0, y0, zs, true);
+    if (zs + 1 <= ze) stream_issue_e(a, S + 2, bar + 2, x0, y0, zs + 1, true);
+  }
+  pend = zs + 1 <= ze ? 7u : 3u;
+  bool bad = false;
+  for (int z = zs; z <= ze; ++z) {
+    const int j = z - zs;
+    if (z + 2 <= ze) {
+      if (w0) stream_issue_e(a, S + (j + 3) % SNST, bar + (j + 3) % SNST, x0, y0, z + 2, true);
+      pend |= 1u << ((j + 3) % SNST);
+    }
+    if (j == 0) {
+      bad |= !mbar_wait(bar, par & 1u, STREAM_WAIT_CYCLES);
+      par ^= 1u;
+      pend &= ~1u;
+    }
+    const int c = (j + 1) % SNST, pv = j % SNST;
+    bad |= !mbar_wait(bar + c, (par >> c) & 1u, STREAM_WAIT_CYCLES);
+    par ^= 1u << c;
+    pend &= ~(1u << c);
+    if (own) {
+      const StageE& C = S[c];
+      const StageE& P = S[pv];
+      const float2 a0 = C.h[0][ty + 1][tx + 2], a1 = C.h[1][ty + 1][tx + 2], a2 = C.h[2][ty + 1][tx + 2];
+      const cx<float> h0{a0.x, a0.y}, h1{a1.x, a1.y}, h2{a2.x, a2.y};
+      auto f = [](float2 v) { return cx<float>{v.x, v.y}; };
+      cx<float> cu[3], e[3];
+      cu[0] = cadd(csub(csub(h2, f(C.h[2][ty][tx + 2])), h1), f(P.h[1][ty + 1][tx + 2]));
+      cu[1] = cadd(csub(csub(h0, f(P.h[0][ty + 1][tx + 2])), h2), f(C.h[2][ty + 1][tx + 1]));
+      cu[2] = cadd(csub(csub(h1, f(C.h[1][ty + 1][tx + 1])), h0), f(C.h[0][ty][tx + 2]));
+#pragma unroll
+      for (int k = 0; k < 3; ++k) e[k] = f(C.e[k][ty][tx]);
+      e_apply<float, false, 7, true>(a, a.pml_d, x, y, z, cu, e, C.eps[ty][tx]);
+      const long i = g.at(x, y, z);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) st<float>(a.e + k * g.comp + i, e[k]);
+      if (x == 1) {
+        const long q = g.at(g.nx + 1, y, z);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) st<float>(a.e + k * g.comp + q, cmul(a.pxp, e[k]));
+      }
+      if (y == 1) {
+        const long q = g.at(x, g.ny + 1, z);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) st<float>(a.e + k * g.comp + q, cmul(a.pyp, e[k]));
+      }
+      if (z == 1) {
+        const long q = g.at(x, y, g.nz + 1);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) st<float>(a.e + k * g.comp + q, cmul(a.pzp, e[k]));
+      }
+    }
+    if (__syncthreads_or(bad)) {
+      if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(err, 1);
+      stream_drain(bar, par, pend);
+      return false;
+    }
+  }
+  return true;
+}
+
+// The H pass over planes zs .. min(zs+SZC-1, nz) of the tile at (x0, y0).
+__device__ bool stream_tile_h(const FieldArgs<float>& a, int x0, int y0, int zs, StageH* S, uint64_t* bar,
+                              unsigned& par, int* err) {
+  const Geo& g = a.g;
+  const int ze = min(zs + SZC - 1, g.nz);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x = x0 + tx, y = y0 + ty;
+  const bool own = x <= g.nx && y <= g.ny;
+  const bool w0 = ty == 0;
+  // ring slot of plane p: (p - zs) % SNST; plane ze+1 is partial
+  unsigned pend = 0;
+  for (int p = zs; p <= min(zs + 2, ze + 1); ++p) {
+    if (w0) stream_issue_h(a, S + (p - zs), bar + (p - zs), x0, y0, p, p <= ze);
+    pend |= 1u << (p - zs);
+  }
+  bool bad = false;
+  for (int z = zs; z <= ze; ++z) {
+    const int j = z - zs;
+    if (z + 3 <= ze + 1) {
+      if (w0) stream_issue_h(a, S + (j + 3) % SNST, bar + (j + 3) % SNST, x0, y0, z + 3, z + 3 <= ze);
+      pend |= 1u << ((j + 3) % SNST);
+    }
+    if (j == 0) {
+      bad |= !mbar_wait(bar, par & 1u, STREAM_WAIT_CYCLES);
+      par ^= 1u;
+      pend &= ~1u;
+    }
+    const int c = j % SNST, n = (j + 1) % SNST;
+    bad |= !mbar_wait(bar + n, (par >> n) & 1u, STREAM_WAIT_CYCLES);
+    par ^= 1u << n;
+    pend &= ~(1u << n);
+    if (own) {
+      const StageH& C = S[c];
+      const StageH& N = S[n];
+      auto f = [](float2 v) { return cx<float>{v.x, v.y}; };
+      cx<float> ev[3], xp[3], yp[3], zp[3], h[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        ev[k] = f(C.e[k][ty][tx]);
+        h[k] = f(C.h[k][ty][tx]);
+      }
+      xp[1] = f(C.e[1][ty][tx + 1]);
+      xp[2] = f(C.e[2][ty][tx + 1]);
+      yp[0] = f(C.e[0][ty + 1][tx]);
+      yp[2] = f(C.e[2][ty + 1][tx]);
+      zp[0] = f(N.e[0][ty][tx]);
+      zp[1] = f(N.e[1][ty][tx]);
+      h_update<float>(a, x, y, z, ev, xp, yp, zp, h);
+      const long i = g.at(x, y, z);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) st<float>(a.h + k * g.comp + i, h[k]);
+      if (x == g.nx) {
+        const long q = g.at(0, y, z);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          st<float>(a.e + k * g.comp + q, cmul(a.pxm, ev[k]));
+          st<float>(a.h + k * g.comp + q, cmul(a.pxm, h[k]));
+        }
+      }
+      if (y == g.ny) {
+        const long q = g.at(x, 0, z);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          st<float>(a.e + k * g.comp + q, cmul(a.pym, ev[k]));
+          st<float>(a.h + k * g.comp + q, cmul(a.pym, h[k]));
+        }
+      }
+      if (z == g.nz) {
+        const long q = g.at(x, y, 0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          st<float>(a.e + k * g.comp + q, cmul(a.pzm, ev[k]));
+          st<float>(a.h + k * g.comp + q, cmul(a.pzm, h[k]));
+        }
+      }
+    }
+    if (__syncthreads_or(bad)) {
+      if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(err, 2);
+      stream_drain(bar, par, pend);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void stream_init(uint64_t* bar) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    for (int s = 0; s < SNST; ++s) mbar_init(bar + s, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+// One engine: grid (ceil(nx/SX), ceil(ny/SY), ceil(nz/SZC)), block (SX, SY).
+__global__ void __launch_bounds__(SX* SY) k_stream_e(FieldArgs<float> a, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint64_t bar[SNST];
+  stream_init(bar);
+  unsigned par = 0;
+  stream_tile_e(a, 1 + blockIdx.x * SX, 1 + blockIdx.y * SY, 1 + blockIdx.z * SZC, (StageE*)smem, bar, par, err);
+}
+
+__global__ void __launch_bounds__(SX* SY) k_stream_h(FieldArgs<float> a, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint64_t bar[SNST];
+  stream_init(bar);
+  unsigned par = 0;
+  stream_tile_h(a, 1 + blockIdx.x * SX, 1 + blockIdx.y * SY, 1 + blockIdx.z * SZC, (StageH*)smem, bar, par, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1029,6 +1356,10 @@ struct iris_engine {
   double2* d_inc = nullptr;
   int zchunk = 0;
   dim3 fblk, fgrd;
+  // streamed split passes (FP32, real material); d_err: a kernel's give-up record
+  bool stream = false;
+  dim3 sgrd;
+  int* d_err = nullptr;
   // timing: CUDA events on the engine stream, per kernel class
   bool timing = false;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -1178,8 +1509,9 @@ int validate(const iris_params& p) {
       if (lo < 1 || hi > n[a] || lo > hi) return bad("DFT box planes must satisfy 1 <= lo <= hi <= n on every axis");
     }
   if (p.precision != IRIS_FP64 && p.precision != IRIS_FP32) return bad("precision must be IRIS_FP64 or IRIS_FP32");
-  if (p.stencil < IRIS_STENCIL_DEFAULT || p.stencil > IRIS_STENCIL_FUSED) return bad("unknown stencil variant");
+  if (p.stencil < IRIS_STENCIL_DEFAULT || p.stencil > IRIS_STENCIL_STREAM) return bad("unknown stencil variant");
   if (p.stencil == IRIS_STENCIL_FUSED && p.precision != IRIS_FP32) return bad("the fused stencil is FP32 only");
+  if (p.stencil == IRIS_STENCIL_STREAM && p.precision != IRIS_FP32) return bad("the streamed stencil is FP32 only");
   if (p.dft_faces != IRIS_DFT_ALL && p.dft_faces != IRIS_DFT_Z) return bad("dft_faces must be IRIS_DFT_ALL or IRIS_DFT_Z");
   return IRIS_OK;
 }
@@ -1216,11 +1548,23 @@ template <typename T> FieldArgs<T> field_args(const iris_engine* E) {
 template <typename T> void launch_e(iris_engine* E) {
   KTimer tm(E, IRIS_KC_E);
   FieldArgs<T> a = field_args<T>(E);
+  if constexpr (std::is_same<T, float>::value) {
+    if (E->stream && !E->eps_complex) {
+      k_stream_e<<<E->sgrd, dim3(SX, SY), STREAM_SMEM_E, E->st>>>(a, E->d_err);
+      return;
+    }
+  }
   if (E->eps_complex) k_update_e<T, true><<<E->grd, E->blk, 0, E->st>>>(a);
   else k_update_e<T, false><<<E->grd, E->blk, 0, E->st>>>(a);
 }
 template <typename T> void launch_h(iris_engine* E) {
   KTimer tm(E, IRIS_KC_H);
+  if constexpr (std::is_same<T, float>::value) {
+    if (E->stream && !E->eps_complex) {
+      k_stream_h<<<E->sgrd, dim3(SX, SY), STREAM_SMEM_H, E->st>>>(field_args<float>(E), E->d_err);
+      return;
+    }
+  }
   k_update_h<T><<<E->grd, E->blk, 0, E->st>>>(field_args<T>(E));
 }
 template <typename T> void launch_tfsf(iris_engine* E, int it) {
@@ -1523,7 +1867,7 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
 void free_engine(iris_engine* E) {
   void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
                   E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J, E->e2, E->h2, E->pml_d2[0],
-                  E->pml_d2[1], E->d_inc};
+                  E->pml_d2[1], E->d_inc, E->d_err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (E->h_J) cudaFreeHost(E->h_J);
@@ -1663,6 +2007,17 @@ static int create_engine(const iris_params* pin, const double* fw, bool member, 
     E->fblk = dim3(FX, FY, 1);
     E->fgrd = dim3((p.nx + FX - 1) / FX, (p.ny + FY - 1) / FY, (p.nz + E->zchunk - 1) / E->zchunk);
   }
+  if (cudaMalloc(&E->d_err, sizeof(int)) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "allocation failed"));
+  cudaMemsetAsync(E->d_err, 0, sizeof(int), E->st);
+  E->stream = E->prec == IRIS_FP32 && p.stencil == IRIS_STENCIL_STREAM;
+  if (E->stream) {
+    if (cudaFuncSetAttribute(k_stream_e, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STREAM_SMEM_E) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_stream_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STREAM_SMEM_H) !=
+            cudaSuccess)
+      return bail(fail(IRIS_ECUDA, "streamed stencil: shared memory opt-in failed"));
+    E->sgrd = dim3((p.nx + SX - 1) / SX, (p.ny + SY - 1) / SY, (p.nz + SZC - 1) / SZC);
+  }
   {
     std::vector<double> re, im;
     default_material(p, re, im);
@@ -1673,6 +2028,18 @@ static int create_engine(const iris_params* pin, const double* fw, bool member, 
   if (rc) return bail(rc);
   if (cudaStreamSynchronize(E->st) != cudaSuccess) return bail(fail(IRIS_ECUDA, "initialisation failed"));
   *out = E;
+  return IRIS_OK;
+}
+
+// Status of the engine's bounded device waits: IRIS_ETIMEOUT once a kernel
+// gave up on one (the stream is synchronised first).
+static int stream_status(iris_engine* E) {
+  if (!E->d_err) return IRIS_OK;
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, E->d_err, sizeof(int), cudaMemcpyDeviceToHost, E->st));
+  CK(cudaStreamSynchronize(E->st));
+  if (h) return fail(IRIS_ETIMEOUT, std::string("a streamed ") + (h == 1 ? "E" : "H") +
+                                        " pass gave up waiting for its staged plane");
   return IRIS_OK;
 }
 
@@ -1707,7 +2074,7 @@ int iris_sync(iris_engine* E) {
   CK(cudaSetDevice(E->device));
   CK(cudaStreamSynchronize(E->st));
   CK(cudaGetLastError());
-  return IRIS_OK;
+  return stream_status(E);
 }
 
 int iris_flux(iris_engine* E, int box, double* J) {
@@ -1723,6 +2090,8 @@ int iris_flux(iris_engine* E, int box, double* J) {
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(E->h_J, E->d_J, sizeof(double) * 6 * p.nof, cudaMemcpyDeviceToHost, E->st));
   CK(cudaStreamSynchronize(E->st));
+  int rc = stream_status(E);
+  if (rc) return rc;
   bool finite = true;
   for (int k = 0; k < 6 * p.nof; ++k) {
     J[k] = E->h_J[k];
@@ -1893,7 +2262,7 @@ int iris_timing_read(iris_engine* E, double* region_ms, double* kernel_ms, long*
     if (launches) launches[k] = (long)E->ev_used[k];
   }
   E->timing = false;
-  return IRIS_OK;
+  return stream_status(E);
 }
 
 int iris_info(const iris_engine* E, long* info) {
