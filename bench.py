@@ -305,7 +305,11 @@ def run_batch(args, rank, world, local):
     b = iris.Batch(params, fw, precision=iris.FP32, dft_faces=iris.DFT_Z, device=local)
     for i, m in enumerate(mats):
         b.set_material(i, m)
-    tile, tune_ms = b.tune(reps=2)
+    if args.tile is not None:
+        b.set_tile(args.tile)
+        tile, tune_ms = iris.TILES[args.tile], {}
+    else:
+        tile, tune_ms = b.tune(reps=2)
     b.step(1, K)
     J = [b.flux(i) for i in range(ncells)]
     t_e2e = D.max(time.perf_counter() - t0)
@@ -341,7 +345,8 @@ def run_batch(args, rank, world, local):
         "config": {"workload": f"batch of {ncells} uneven Bloch cells (configs[3])", "grid_cells": cells,
                    "nof": 128, "dft_points": info["dft_points"], "dft_block": info["dft_block"],
                    "dft_faces": "z planes (reflection, transmission)", "tile": list(tile),
-                   "tune_ms_per_eh_pass": {"x".join(map(str, k)): round(v, 3) for k, v in tune_ms.items()},
+                   "tune_ms_per_eh_pass": {"_".join(map(str, k)) if k[0] == "flat" else "x".join(map(str, k)): round(v, 3)
+                                           for k, v in tune_ms.items()},
                    "l2": "working set >> 129 MB L2; no flush needed",
                    "parallelism": f"replicas x{world} (independent batches, one per GPU)"},
         "e2e": {"value": round(world * cells * K / t_e2e / 1e9, 3), "unit": "Gcell/s",
@@ -590,6 +595,7 @@ def main():
     ap.add_argument("--stencil", type=int, default=0, choices=[0, 1, 2, 3],
                     help="0: engine default, 1: split E and H passes, 2: fused E+H pass (fp32), 3: streamed split passes (fp32)")
     ap.add_argument("--cells", type=int, default=256, help="cells in the batch (workload 4)")
+    ap.add_argument("--tile", type=int, default=None, help="workload 4: this work-list tile instead of the autotuner's")
     ap.add_argument("--adjoint-steps", type=int, default=0, help="workload 5: forward steps (0: the workload's 6000)")
     ap.add_argument("--fd-voxels", type=int, default=4,
                     help="workload 5: voxels checked against central differences of the FP64 forward")

@@ -285,11 +285,13 @@ int iris_batch_get_field(iris_batch* b, int cell, int which, double* re, double*
 /*
  * Tile-shape autotuner: times every candidate tile of the E/H work list
  * (reps E+H passes each) on this batch and keeps the fastest; ms[i]
- * (optional, 5 entries) receives the time per E+H pass of candidate i.  Call
+ * (optional, 7 entries) receives the time per E+H pass of candidate i.  Call
  * before the first step (the passes run on the zero initial state).
  */
 int iris_batch_tune(iris_batch* b, int reps, int* best, double* ms);
-/* Force a candidate tile (0..4: 32x8x1, 32x4x2, 64x4x1, 16x16x1, 32x2x4). */
+/* Force a candidate tile (0..4: x*y*z blocks 32x8x1, 32x4x2, 64x4x1,
+ * 16x16x1, 32x2x4; 5, 6: runs of 256 consecutive cells of one plane, with
+ * registers capped for five resident blocks per SM (5) or not (6)). */
 int iris_batch_set_tile(iris_batch* b, int tile);
 int iris_batch_timing(iris_batch* b, int enable);
 int iris_batch_timing_read(iris_batch* b, double* region_ms, double* kernel_ms, long* launches);

@@ -2383,8 +2383,13 @@ struct BSeg {
   int cell, pad;
 };
 
-constexpr int NTILES = 5;
-constexpr int TILES[NTILES][3] = {{32, 8, 1}, {32, 4, 2}, {64, 4, 1}, {16, 16, 1}, {32, 2, 4}};
+// Work-list shapes the autotuner chooses from: x * y * z blocks of cells,
+// and (FLAT) 256 consecutive cells of one plane in row-major order, which
+// keeps every lane busy whatever the cell's nx.
+// keeps every lane busy whatever the cell's nx (FLAT: register-capped for
+// five resident blocks per SM; FLAT + 1: uncapped).
+constexpr int NTILES = 7, FLAT = 5;
+constexpr int TILES[NTILES][3] = {{32, 8, 1}, {32, 4, 2}, {64, 4, 1}, {16, 16, 1}, {32, 2, 4}, {256, 1, 1}, {256, 1, 1}};
 
 // Copies the cell's arguments into shared memory when the item's cell changes.
 template <typename A>
@@ -2431,6 +2436,33 @@ __global__ void __launch_bounds__(TX* TY* TZ) k_batch_h(const FieldArgs<T>* __re
     cell_args(args, b.cell, sa, scell, tid);
     const int x = b.x0 + threadIdx.x, y = b.y0 + threadIdx.y, z = b.z0 + threadIdx.z;
     if (x <= sa.g.nx && y <= sa.g.ny && z <= sa.g.nz) h_split_cell<T>(sa, x, y, z);
+  }
+}
+
+// FLAT items: x0 = first row-major offset in the plane, z0 = the plane.
+// MINB: resident blocks per SM asked of the register allocator (0: none).
+template <typename T, bool EPASS, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_batch_flat(const FieldArgs<T>* __restrict__ args,
+                                                    const BItem* __restrict__ items, long nitems) {
+  __shared__ FieldArgs<T> sa;
+  __shared__ int scell;
+  const int tid = threadIdx.x;
+  if (tid == 0) scell = -1;
+  __syncthreads();
+  for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
+    const BItem b = items[k];
+    cell_args(args, b.cell, sa, scell, tid);
+    const int nx = sa.g.nx;
+    const int L = b.x0 + tid;
+    if (L < nx * sa.g.ny) {
+      const int y = L / nx, x = L - y * nx;
+      if (EPASS) {
+        if (sa.eps_c) e_split_cell<T, true>(sa, x + 1, y + 1, b.z0);
+        else e_split_cell<T, false>(sa, x + 1, y + 1, b.z0);
+      } else {
+        h_split_cell<T>(sa, x + 1, y + 1, b.z0);
+      }
+    }
   }
 }
 
@@ -2511,6 +2543,12 @@ int batch_build_items(iris_batch* B, int tile) {
   std::vector<BItem> items;
   for (int c = 0; c < B->n; ++c) {
     const iris_params& p = B->cells[c]->p;
+    if (tile >= FLAT) {
+      const int nxy = p.nx * p.ny;
+      for (int z = 1; z <= p.nz; ++z)
+        for (int l = 0; l < nxy; l += TX) items.push_back(BItem{c, l, 0, z});
+      continue;
+    }
     for (int z = 1; z <= p.nz; z += TZ)
       for (int y = 1; y <= p.ny; y += TY)
         for (int x = 1; x <= p.nx; x += TX) items.push_back(BItem{c, x, y, z});
@@ -2551,8 +2589,25 @@ template <typename T, int TX, int TY, int TZ> void launch_batch_eh(iris_batch* B
   }
 }
 
+template <typename T, int MINB> void launch_batch_flat(iris_batch* B, bool e) {
+  iris_engine* M = B->master;
+  const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
+  static int grid_e = 0, grid_h = 0;
+  int& grid = e ? grid_e : grid_h;
+  if (!grid) {
+    const void* kern = e ? (const void*)k_batch_flat<T, true, MINB> : (const void*)k_batch_flat<T, false, MINB>;
+    grid = persistent_grid<T, 256, 1, 1>(kern);
+  }
+  const long g = std::min<long>(grid, B->nitems);
+  KTimer tm(M, e ? IRIS_KC_E : IRIS_KC_H);
+  if (e) k_batch_flat<T, true, MINB><<<(unsigned)g, 256, 0, M->st>>>(args, B->d_items, B->nitems);
+  else k_batch_flat<T, false, MINB><<<(unsigned)g, 256, 0, M->st>>>(args, B->d_items, B->nitems);
+}
+
 template <typename T> void batch_eh(iris_batch* B, bool e) {
   switch (B->tile) {
+    case FLAT: launch_batch_flat<T, 5>(B, e); break;
+    case FLAT + 1: launch_batch_flat<T, 0>(B, e); break;
     case 0: launch_batch_eh<T, 32, 8, 1>(B, e); break;
     case 1: launch_batch_eh<T, 32, 4, 2>(B, e); break;
     case 2: launch_batch_eh<T, 64, 4, 1>(B, e); break;

@@ -40,11 +40,14 @@ def make_cells(oracle, tmp_path):
     return out
 
 
-def batch_and_singles(iris, cells, precision, tune=False):
+def batch_and_singles(iris, cells, precision, tune=False, tile=None):
     params = [engine_params_from_oracle(iris, op, precision=precision, ak=ak) for _, op, ak, _ in cells]
     b = iris.Batch(params, cells[0][1].fw, dft_faces=iris.DFT_Z)
     for c, (_, _, _, eps) in enumerate(cells):
         b.set_material(c, eps)
+    if tile is not None:
+        b.set_tile(tile)
+        assert b.info()["tile"] == iris.TILES[tile]
     if tune:
         tile, ms = b.tune(reps=2)
         assert tile in iris.TILES and len(ms) == len(iris.TILES)
@@ -64,10 +67,11 @@ def batch_and_singles(iris, cells, precision, tune=False):
     return b, singles
 
 
+@pytest.mark.parametrize("tile", [0, 3, 5, 6])
 @pytest.mark.parametrize("precision,tol", [(0, 1e-15), (1, 1e-6)])
-def test_batch_matches_single_engines(iris, oracle, tmp_path, precision, tol):
+def test_batch_matches_single_engines(iris, oracle, tmp_path, precision, tol, tile):
     cells = make_cells(oracle, tmp_path)
-    b, singles = batch_and_singles(iris, cells, precision)
+    b, singles = batch_and_singles(iris, cells, precision, tile=tile)
     assert b.info()["cells"] == len(CELLS)
     for c, (e, Js) in enumerate(singles):
         Jb = b.flux(c)
