@@ -1891,7 +1891,8 @@ long iris::engine_npts(const iris_engine* E, int box, int j) {
 
 extern "C" {
 
-static int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out);
+static int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out,
+                         bool packed = false);
 
 int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
   return create_engine(pin, fw, false, false, out);
@@ -1899,7 +1900,10 @@ int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
 
 }  // extern "C"
 
-static int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out) {
+// packed: rows of nx+2 cells back to back (no 128-byte alignment of x = 1),
+// for cells whose rows are short; component arrays stay 128-byte aligned.
+static int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out,
+                         bool packed) {
   clear_error();
   if (!pin || !fw || !out) return fail(IRIS_EINVAL, "null argument");
   *out = nullptr;
@@ -1925,14 +1929,14 @@ static int create_engine(const iris_params* pin, const double* fw, bool member, 
   if (cudaSetDevice(E->device) != cudaSuccess) return bail(fail(IRIS_ECUDA, "cudaSetDevice failed"));
   if (cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(IRIS_ECUDA, "cudaStreamCreate failed"));
-  // geometry: x = 1 on a 128-byte boundary
+  // geometry: x = 1 on a 128-byte boundary, or packed rows
   Geo& g = E->g;
   g.nx = p.nx;
   g.ny = p.ny;
   g.nz = p.nz;
   const int align = (int)(128 / E->esz);
-  g.xo = align - 1;
-  g.pitch = ((long)(g.xo + p.nx + 2) + align - 1) / align * align;
+  g.xo = packed ? 0 : align - 1;
+  g.pitch = packed ? (long)p.nx + 2 : ((long)(g.xo + p.nx + 2) + align - 1) / align * align;
   g.plane = g.pitch * (p.ny + 2);
   g.comp = (g.plane * (p.nz + 2) + align - 1) / align * align;
   const size_t fbytes = (size_t)3 * g.comp * E->esz;
@@ -2009,7 +2013,7 @@ static int create_engine(const iris_params* pin, const double* fw, bool member, 
   }
   if (cudaMalloc(&E->d_err, sizeof(int)) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "allocation failed"));
   cudaMemsetAsync(E->d_err, 0, sizeof(int), E->st);
-  E->stream = E->prec == IRIS_FP32 && p.stencil == IRIS_STENCIL_STREAM;
+  E->stream = E->prec == IRIS_FP32 && p.stencil == IRIS_STENCIL_STREAM && !packed;
   if (E->stream) {
     if (cudaFuncSetAttribute(k_stream_e, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STREAM_SMEM_E) !=
             cudaSuccess ||
@@ -2441,7 +2445,8 @@ __global__ void __launch_bounds__(TX* TY* TZ) k_batch_h(const FieldArgs<T>* __re
 
 // FLAT items: x0 = first row-major offset in the plane, z0 = the plane.
 // MINB: resident blocks per SM asked of the register allocator (0: none).
-template <typename T, bool EPASS, int MINB>
+// CEPS: some cell has a complex material (else every eps_c is null).
+template <typename T, bool EPASS, int MINB, bool CEPS>
 __global__ void __launch_bounds__(256, MINB) k_batch_flat(const FieldArgs<T>* __restrict__ args,
                                                     const BItem* __restrict__ items, long nitems) {
   __shared__ FieldArgs<T> sa;
@@ -2457,7 +2462,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_flat(const FieldArgs<T>* __
     if (L < nx * sa.g.ny) {
       const int y = L / nx, x = L - y * nx;
       if (EPASS) {
-        if (sa.eps_c) e_split_cell<T, true>(sa, x + 1, y + 1, b.z0);
+        if (CEPS && sa.eps_c) e_split_cell<T, true>(sa, x + 1, y + 1, b.z0);
         else e_split_cell<T, false>(sa, x + 1, y + 1, b.z0);
       } else {
         h_split_cell<T>(sa, x + 1, y + 1, b.z0);
@@ -2589,19 +2594,27 @@ template <typename T, int TX, int TY, int TZ> void launch_batch_eh(iris_batch* B
   }
 }
 
-template <typename T, int MINB> void launch_batch_flat(iris_batch* B, bool e) {
+template <typename T, int MINB, bool CEPS> void launch_flat(iris_batch* B, bool e) {
   iris_engine* M = B->master;
   const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
   static int grid_e = 0, grid_h = 0;
   int& grid = e ? grid_e : grid_h;
   if (!grid) {
-    const void* kern = e ? (const void*)k_batch_flat<T, true, MINB> : (const void*)k_batch_flat<T, false, MINB>;
+    const void* kern =
+        e ? (const void*)k_batch_flat<T, true, MINB, CEPS> : (const void*)k_batch_flat<T, false, MINB, false>;
     grid = persistent_grid<T, 256, 1, 1>(kern);
   }
   const long g = std::min<long>(grid, B->nitems);
   KTimer tm(M, e ? IRIS_KC_E : IRIS_KC_H);
-  if (e) k_batch_flat<T, true, MINB><<<(unsigned)g, 256, 0, M->st>>>(args, B->d_items, B->nitems);
-  else k_batch_flat<T, false, MINB><<<(unsigned)g, 256, 0, M->st>>>(args, B->d_items, B->nitems);
+  if (e) k_batch_flat<T, true, MINB, CEPS><<<(unsigned)g, 256, 0, M->st>>>(args, B->d_items, B->nitems);
+  else k_batch_flat<T, false, MINB, false><<<(unsigned)g, 256, 0, M->st>>>(args, B->d_items, B->nitems);
+}
+
+template <typename T, int MINB> void launch_batch_flat(iris_batch* B, bool e) {
+  bool cplx = false;
+  for (const iris_engine* E : B->cells) cplx |= E->eps_complex;
+  if (cplx) launch_flat<T, MINB, true>(B, e);
+  else launch_flat<T, MINB, false>(B, e);
 }
 
 template <typename T> void batch_eh(iris_batch* B, bool e) {
@@ -2690,7 +2703,7 @@ int iris_batch_create(int ncells, const iris_params* params, const double* fw, i
   for (int c = 0; c < ncells; ++c) {
     iris_params q = params[c];
     q.stencil = IRIS_STENCIL_SPLIT;
-    int rc = create_engine(&q, fw, true, dft_faces == IRIS_DFT_Z, &B->cells[c]);
+    int rc = create_engine(&q, fw, true, dft_faces == IRIS_DFT_Z, &B->cells[c], true);
     if (rc) return bail(rc);
     iris_engine* E = B->cells[c];
     B->pbase.push_back(P);
