@@ -334,7 +334,8 @@ def run_batch(args, rank, world, local):
     t_h = kms["update_h"] / kn["update_h"] * 1e-3
     dom, db, dt_ = ("update_h", hb, t_h) if t_h >= t_e else ("update_e", eb, t_e)
     achieved = db / dt_ / 1e9
-    launches = sum(kn[k] for k in ("update_e", "update_h", "tfsf", "dft_gather", "flux")) + 2 * kn["dft_block"]
+    launches = info["launches_per_pass"] * (kn["update_e"] + kn["update_h"]) + \
+        sum(kn[k] for k in ("tfsf", "dft_gather", "flux")) + 2 * kn["dft_block"]
     value = world * cells * K / (reg_ms * 1e-3) / 1e9
     h2d = sum(m.size * 16 for m in mats)
     out = {

@@ -296,7 +296,8 @@ int iris_batch_set_tile(iris_batch* b, int tile);
 int iris_batch_timing(iris_batch* b, int enable);
 int iris_batch_timing_read(iris_batch* b, double* region_ms, double* kernel_ms, long* launches);
 /* info[0] cells, [1] total grid cells, [2] DFT points, [3] DFT block K,
- * [4] tile index, [5] work items per pass. */
+ * [4] tile index, [5] work items per pass, [6] kernel launches per E or H
+ * pass (info: 7 entries). */
 int iris_batch_info(const iris_batch* b, long* info);
 
 /* ---- adjoint (gradient) form ------------------------------------------- */

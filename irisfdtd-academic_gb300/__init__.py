@@ -312,9 +312,10 @@ class Batch:
         return reg.value, dict(zip(Engine.KERNELS, ms.tolist())), dict(zip(Engine.KERNELS, list(n)))
 
     def info(self) -> dict:
-        a = (ctypes.c_long * 6)()
+        a = (ctypes.c_long * 7)()
         check(self.L.iris_batch_info(self.h, a), "iris_batch_info")
-        return dict(cells=a[0], grid_cells=a[1], dft_points=a[2], dft_block=a[3], tile=TILES[a[4]], items=a[5])
+        return dict(cells=a[0], grid_cells=a[1], dft_points=a[2], dft_block=a[3], tile=TILES[a[4]], items=a[5],
+                    launches_per_pass=a[6])
 
 
 from .adjoint import Adjoint, design_objective  # noqa: E402

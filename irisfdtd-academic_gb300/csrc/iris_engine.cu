@@ -111,13 +111,14 @@ template <typename T> struct FieldArgs {
 // when dnew is given, its new value written there (dnew == a.pml_d updates in
 // place).  With EPV the caller supplies the real structure eps_inv of the
 // cell (ep) instead of it being read from a.eps_r.  MASK selects the
-// components computed (bit k: E_{k+1}).
-template <typename T, bool CEPS, int MASK = 7, bool EPV = false>
+// components computed (bit k: E_{k+1}).  UPML = false: the caller knows the
+// cell lies outside the UPML slabs (the slab code is not compiled in).
+template <typename T, bool CEPS, int MASK = 7, bool EPV = false, bool UPML = true>
 __device__ __forceinline__ void e_apply(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
                                         const cx<T> c[3], cx<T> e[3], T ep = T(0)) {
   using V = typename V2<T>::t;
   const Geo& g = a.g;
-  if (z <= a.pmlzi || z >= a.pmlzf) {
+  if (UPML && (z <= a.pmlzi || z >= a.pmlzf)) {
     const int slab = z <= a.pmlzi ? 0 : 1;
     const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
     const int row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
@@ -159,7 +160,7 @@ __device__ __forceinline__ void e_apply(const FieldArgs<T>& a, typename V2<T>::t
 // below (hzm, components 1 and 2) and its old E (e, replaced by the new E);
 // the x-1 and y-1 neighbours are loaded here.  MASK selects the components
 // computed (bit k: E_{k+1}); loads only the others need are never issued.
-template <typename T, bool CEPS, int MASK = 7>
+template <typename T, bool CEPS, int MASK = 7, bool UPML = true>
 __device__ __forceinline__ void e_update(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
                                          const cx<T> h[3], const cx<T> hzm[3], cx<T> e[3]) {
   using V = typename V2<T>::t;
@@ -172,12 +173,12 @@ __device__ __forceinline__ void e_update(const FieldArgs<T>& a, typename V2<T>::
   if (MASK & 1) c[0] = cadd(csub(csub(h[2], ld<T>(H3 + i - g.pitch)), h[1]), hzm[1]);
   if (MASK & 2) c[1] = cadd(csub(csub(h[0], hzm[0]), h[2]), ld<T>(H3 + i - 1));
   if (MASK & 4) c[2] = cadd(csub(csub(h[1], ld<T>(H2 + i - 1)), h[0]), ld<T>(H1 + i - g.pitch));
-  e_apply<T, CEPS, MASK>(a, dnew, x, y, z, c, e);
+  e_apply<T, CEPS, MASK, false, UPML>(a, dnew, x, y, z, c, e);
 }
 
 // New E of interior cell (x, y, z) from the old E and H in memory: e_fdtd
 // (code/fdtd.f90:57-153) and UPML_Array_e (code/boundary_II.f90:60-138).
-template <typename T, bool CEPS, int MASK = 7>
+template <typename T, bool CEPS, int MASK = 7, bool UPML = true>
 __device__ __forceinline__ void e_cell(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
                                        cx<T> e[3]) {
   const Geo& g = a.g;
@@ -192,14 +193,15 @@ __device__ __forceinline__ void e_cell(const FieldArgs<T>& a, typename V2<T>::t*
 #pragma unroll
   for (int k = 0; k < 3; ++k)
     if (MASK & (1 << k)) e[k] = ld<T>(a.e + k * g.comp + i);
-  e_update<T, CEPS, MASK>(a, dnew, x, y, z, h, hzm, e);
+  e_update<T, CEPS, MASK, UPML>(a, dnew, x, y, z, h, hzm, e);
 }
 
 // New H of interior cell (x, y, z): h_fdtd (code/fdtd.f90:157-248) and
 // UPML_Array_h (code/boundary_II.f90:142-220), from the new E of the cell (ev)
 // and of its +x, +y, +z neighbours (xp: components 2,3; yp: 1,3; zp: 1,2),
-// the old H read from a.h, the UPML auxiliary B updated in place.
-template <typename T>
+// the old H read from a.h, the UPML auxiliary B updated in place.  UPML =
+// false: the cell lies outside the UPML slabs.
+template <typename T, bool UPML = true>
 __device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, int z, const cx<T> ev[3],
                                          const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3]) {
   using V = typename V2<T>::t;
@@ -208,7 +210,7 @@ __device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, in
   c[0] = cadd(csub(csub(yp[2], ev[2]), zp[1]), ev[1]);
   c[1] = cadd(csub(csub(zp[0], ev[0]), xp[2]), ev[2]);
   c[2] = cadd(csub(csub(xp[1], ev[1]), yp[0]), ev[0]);
-  if (z <= a.pmlzi || z >= a.pmlzf) {
+  if (UPML && (z <= a.pmlzi || z >= a.pmlzf)) {
     const int slab = z <= a.pmlzi ? 0 : 1;
     const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
     const int row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
@@ -230,25 +232,25 @@ __device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, in
 }
 
 // h_update with the old H of the cell loaded from a.h.
-template <typename T>
+template <typename T, bool UPML = true>
 __device__ __forceinline__ void h_cell(const FieldArgs<T>& a, int x, int y, int z, const cx<T> ev[3],
                                        const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3]) {
   const long i = a.g.at(x, y, z);
 #pragma unroll
   for (int k = 0; k < 3; ++k) h[k] = ld<T>(a.h + k * a.g.comp + i);
-  h_update<T>(a, x, y, z, ev, xp, yp, zp, h);
+  h_update<T, UPML>(a, x, y, z, ev, xp, yp, zp, h);
 }
 
 // Split E pass of one cell: e_cell in place + bc_{x,y,z}max_bloch
 // (code/boundary.f90:193-216,257-284,321-348) for the E ghosts.
-template <typename T, bool CEPS>
+template <typename T, bool CEPS, bool UPML = true>
 __device__ __forceinline__ void e_split_cell(const FieldArgs<T>& a, int x, int y, int z) {
   using V = typename V2<T>::t;
   const Geo& g = a.g;
   const long i = g.at(x, y, z);
   V* E[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
   cx<T> e[3];
-  e_cell<T, CEPS>(a, a.pml_d, x, y, z, e);
+  e_cell<T, CEPS, 7, UPML>(a, a.pml_d, x, y, z, e);
 #pragma unroll
   for (int k = 0; k < 3; ++k) st<T>(E[k] + i, e[k]);
   if (x == 1) {
@@ -281,7 +283,7 @@ __global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
 // (code/boundary.f90:163-187,224-251,288-315) for the H ghosts and the E
 // ghosts at 0.  The ghosts at nx+1/ny+1/nz+1 of H are never read by any
 // operator and are not maintained.
-template <typename T>
+template <typename T, bool UPML = true>
 __device__ __forceinline__ void h_split_cell(const FieldArgs<T>& a, int x, int y, int z) {
   using V = typename V2<T>::t;
   const Geo& g = a.g;
@@ -297,7 +299,7 @@ __device__ __forceinline__ void h_split_cell(const FieldArgs<T>& a, int x, int y
   yp[2] = ld<T>(Ec[2] + i + g.pitch);
   zp[0] = ld<T>(Ec[0] + i + g.plane);
   zp[1] = ld<T>(Ec[1] + i + g.plane);
-  h_cell<T>(a, x, y, z, ev, xp, yp, zp, h);
+  h_cell<T, UPML>(a, x, y, z, ev, xp, yp, zp, h);
 #pragma unroll
   for (int k = 0; k < 3; ++k) st<T>(H[k] + i, h[k]);
   if (x == g.nx) {
@@ -2446,7 +2448,8 @@ __global__ void __launch_bounds__(TX* TY* TZ) k_batch_h(const FieldArgs<T>* __re
 // FLAT items: x0 = first row-major offset in the plane, z0 = the plane.
 // MINB: resident blocks per SM asked of the register allocator (0: none).
 // CEPS: some cell has a complex material (else every eps_c is null).
-template <typename T, bool EPASS, int MINB, bool CEPS>
+// UPML = false: every item's plane lies outside its cell's UPML slabs.
+template <typename T, bool EPASS, int MINB, bool CEPS, bool UPML>
 __global__ void __launch_bounds__(256, MINB) k_batch_flat(const FieldArgs<T>* __restrict__ args,
                                                     const BItem* __restrict__ items, long nitems) {
   __shared__ FieldArgs<T> sa;
@@ -2454,18 +2457,21 @@ __global__ void __launch_bounds__(256, MINB) k_batch_flat(const FieldArgs<T>* __
   const int tid = threadIdx.x;
   if (tid == 0) scell = -1;
   __syncthreads();
+  // the next item's descriptor is loaded while this one is processed
+  BItem nb = blockIdx.x < nitems ? items[blockIdx.x] : BItem{};
   for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
-    const BItem b = items[k];
+    const BItem b = nb;
+    if (k + gridDim.x < nitems) nb = items[k + gridDim.x];
     cell_args(args, b.cell, sa, scell, tid);
     const int nx = sa.g.nx;
     const int L = b.x0 + tid;
     if (L < nx * sa.g.ny) {
       const int y = L / nx, x = L - y * nx;
       if (EPASS) {
-        if (CEPS && sa.eps_c) e_split_cell<T, true>(sa, x + 1, y + 1, b.z0);
-        else e_split_cell<T, false>(sa, x + 1, y + 1, b.z0);
+        if (CEPS && sa.eps_c) e_split_cell<T, true, UPML>(sa, x + 1, y + 1, b.z0);
+        else e_split_cell<T, false, UPML>(sa, x + 1, y + 1, b.z0);
       } else {
-        h_split_cell<T>(sa, x + 1, y + 1, b.z0);
+        h_split_cell<T, UPML>(sa, x + 1, y + 1, b.z0);
       }
     }
   }
@@ -2514,6 +2520,7 @@ struct iris_batch {
   SrcArgs* d_src = nullptr;
   BItem* d_items = nullptr;
   long nitems = 0;
+  long nitems_in = 0;  // flat work lists: items outside the UPML slabs come first
   int tile = 0;  // index into TILES
   int grid_e = 0, grid_h = 0;
   TItem* d_titems = nullptr;
@@ -2551,13 +2558,23 @@ int batch_build_items(iris_batch* B, int tile) {
     if (tile >= FLAT) {
       const int nxy = p.nx * p.ny;
       for (int z = 1; z <= p.nz; ++z)
-        for (int l = 0; l < nxy; l += TX) items.push_back(BItem{c, l, 0, z});
+        if (z > p.pmlzi && z < p.pmlzf)
+          for (int l = 0; l < nxy; l += TX) items.push_back(BItem{c, l, 0, z});
       continue;
     }
     for (int z = 1; z <= p.nz; z += TZ)
       for (int y = 1; y <= p.ny; y += TY)
         for (int x = 1; x <= p.nx; x += TX) items.push_back(BItem{c, x, y, z});
   }
+  B->nitems_in = tile >= FLAT ? (long)items.size() : 0;
+  if (tile >= FLAT)
+    for (int c = 0; c < B->n; ++c) {
+      const iris_params& p = B->cells[c]->p;
+      const int nxy = p.nx * p.ny;
+      for (int z = 1; z <= p.nz; ++z)
+        if (z <= p.pmlzi || z >= p.pmlzf)
+          for (int l = 0; l < nxy; l += TX) items.push_back(BItem{c, l, 0, z});
+    }
   if (B->d_items) cudaFree(B->d_items);
   B->d_items = nullptr;
   CK(cudaMalloc(&B->d_items, sizeof(BItem) * items.size()));
@@ -2594,20 +2611,25 @@ template <typename T, int TX, int TY, int TZ> void launch_batch_eh(iris_batch* B
   }
 }
 
-template <typename T, int MINB, bool CEPS> void launch_flat(iris_batch* B, bool e) {
+template <typename T, int MINB, bool CEPS, bool UPML>
+void launch_flat_part(iris_batch* B, bool e, const BItem* items, long n) {
+  if (n <= 0) return;
   iris_engine* M = B->master;
   const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
+  auto kern = e ? k_batch_flat<T, true, MINB, CEPS, UPML> : k_batch_flat<T, false, MINB, false, UPML>;
   static int grid_e = 0, grid_h = 0;
   int& grid = e ? grid_e : grid_h;
-  if (!grid) {
-    const void* kern =
-        e ? (const void*)k_batch_flat<T, true, MINB, CEPS> : (const void*)k_batch_flat<T, false, MINB, false>;
-    grid = persistent_grid<T, 256, 1, 1>(kern);
-  }
-  const long g = std::min<long>(grid, B->nitems);
-  KTimer tm(M, e ? IRIS_KC_E : IRIS_KC_H);
-  if (e) k_batch_flat<T, true, MINB, CEPS><<<(unsigned)g, 256, 0, M->st>>>(args, B->d_items, B->nitems);
-  else k_batch_flat<T, false, MINB, false><<<(unsigned)g, 256, 0, M->st>>>(args, B->d_items, B->nitems);
+  if (!grid) grid = persistent_grid<T, 256, 1, 1>((const void*)kern);
+  kern<<<(unsigned)std::min<long>(grid, n), 256, 0, M->st>>>(args, items, n);
+}
+
+// One pass over a flat work list: the planes outside the UPML slabs with a
+// kernel that has no slab code (fewer registers, more resident warps), then
+// the slab planes.
+template <typename T, int MINB, bool CEPS> void launch_flat(iris_batch* B, bool e) {
+  KTimer tm(B->master, e ? IRIS_KC_E : IRIS_KC_H);
+  launch_flat_part<T, MINB, CEPS, false>(B, e, B->d_items, B->nitems_in);
+  launch_flat_part<T, MINB, CEPS, true>(B, e, B->d_items + B->nitems_in, B->nitems - B->nitems_in);
 }
 
 template <typename T, int MINB> void launch_batch_flat(iris_batch* B, bool e) {
@@ -2884,6 +2906,7 @@ int iris_batch_info(const iris_batch* B, long* info) {
   info[3] = B->master->K;
   info[4] = B->tile;
   info[5] = B->nitems;
+  info[6] = B->tile >= FLAT ? (B->nitems_in > 0) + (B->nitems > B->nitems_in) : 1;
   return IRIS_OK;
 }
 
