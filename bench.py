@@ -186,7 +186,8 @@ def run_engine(args, rank, world, local):
     # --- end to end through the public API, host buffers in and out
     D.barrier()
     t0 = time.perf_counter()
-    eng = iris.Engine(p, fw, precision=prec, dft_block=args.dft_block, device=local, stencil=args.stencil)
+    eng = iris.Engine(p, fw, precision=prec, dft_block=args.dft_block, device=local, stencil=args.stencil,
+                      graph=args.graph)
     eng.set_material(eps)
     eng.step(1, K)
     J = eng.flux(0)
@@ -209,6 +210,17 @@ def run_engine(args, rank, world, local):
     clocks = stop_clocks(pr, cpath)
     it += K
     reg_ms = D.max(reg_ms)
+    graph_line = None
+    if args.graph:
+        # the same steps replayed from captured graphs (per-kernel events off)
+        eng.timing_start(per_kernel=False)
+        eng.step(it, K)
+        reg_g, _, _ = eng.timing_read()
+        it += K
+        reg_g = D.max(reg_g)
+        graph_line = {"value": round(world * cells * K / (reg_g * 1e-3) / 1e9, 3), "unit": "Gcell/s",
+                      "ms_per_step": round(reg_g / K, 4),
+                      "what": "device time of %d steps replayed as whole DFT blocks from one CUDA graph" % K}
     eng.close()
 
     sc, sm = (8, 4) if prec == iris.FP32 else (16, 8)
@@ -272,6 +284,8 @@ def run_engine(args, rank, world, local):
         "clocks": clocks,
         "material_setup_s": round(t_mat, 2),
     }
+    if graph_line:
+        out["graph"] = graph_line
     if rank == 0 and world == 1 and not args.no_fp64_compare and prec == iris.FP32:
         out["fp64_plain"] = fp64_compare(iris, p, fw, eps, cells, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -595,6 +609,8 @@ def main():
     ap.add_argument("--dft-block", type=int, default=0, help="DFT samples per accumulation block (0: engine default)")
     ap.add_argument("--stencil", type=int, default=0, choices=[0, 1, 2, 3],
                     help="0: engine default, 1: split E and H passes, 2: fused E+H pass (fp32), 3: streamed split passes (fp32)")
+    ap.add_argument("--graph", action="store_true",
+                    help="step whole DFT blocks from a captured CUDA graph (e2e run and an extra timed run)")
     ap.add_argument("--cells", type=int, default=256, help="cells in the batch (workload 4)")
     ap.add_argument("--tile", type=int, default=None, help="workload 4: this work-list tile instead of the autotuner's")
     ap.add_argument("--adjoint-steps", type=int, default=0, help="workload 5: forward steps (0: the workload's 6000)")

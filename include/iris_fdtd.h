@@ -112,6 +112,9 @@ typedef struct iris_params {
   int device;         /* CUDA device ordinal                               */
   int stencil;        /* IRIS_STENCIL_*: how E and H are stepped           */
   int dft_faces;      /* IRIS_DFT_ALL or IRIS_DFT_Z                        */
+  int graph;          /* 1: step whole DFT blocks (every step sampled) by
+                         replaying one captured CUDA graph; results are
+                         identical to launch-by-launch stepping            */
 } iris_params;
 
 /* ---- DFT faces (iris_params.dft_faces) -------------------------------- */

@@ -87,7 +87,7 @@ class Engine:
     """One run: device state of main()+driver() behind iris_create."""
 
     def __init__(self, p: IrisParams, fw=None, precision: int | None = None, dft_block: int = 0, device: int = 0,
-                 stencil: int = 0):
+                 stencil: int = 0, graph: bool = False):
         self.L = lib()
         q = p.copy()
         if precision is not None:
@@ -95,6 +95,7 @@ class Engine:
         q.dft_block = dft_block
         q.stencil = stencil
         q.device = device
+        q.graph = 1 if graph else 0
         self.p = q
         self.fw = np.ascontiguousarray(frequencies(q) if fw is None else np.asarray(fw, dtype=np.float64))
         h = ctypes.c_void_p()
@@ -241,7 +242,7 @@ class Batch:
     grid, structure, source and Bloch phases; shared precision, dt, frequencies."""
 
     def __init__(self, params, fw, precision: int | None = None, dft_faces: int = DFT_Z, device: int = 0,
-                 dft_block: int = 0):
+                 dft_block: int = 0, graph: bool = False):
         self.L = lib()
         arr = (IrisParams * len(params))()
         for i, p in enumerate(params):
@@ -250,6 +251,7 @@ class Batch:
                 q.precision = precision
             q.device = device
             q.dft_block = dft_block
+            q.graph = 1 if graph else 0
             arr[i] = q
         self.params = arr
         self.n = len(params)

@@ -337,6 +337,10 @@ __global__ void __launch_bounds__(256) k_update_h(FieldArgs<T> a) {
   h_split_cell<T>(a, x, y, z);
 }
 
+// The device-resident step base of captured graphs.
+__global__ void k_set_int(int* p, int v) { *p = v; }
+__global__ void k_add_int(int* p, int v) { *p += v; }
+
 // ---------------------------------------------------------------------------
 // Streamed split passes (FP32, real material).
 //
@@ -806,9 +810,13 @@ __device__ __forceinline__ void tfsf_column(typename V2<T>::t* e, typename V2<T>
 }
 
 template <typename T>
-__global__ void __launch_bounds__(64) k_tfsf(typename V2<T>::t* e, typename V2<T>::t* h, Geo g, SrcArgs s, int it) {
+// The step is it, or *itp + it when itp is given (a device-resident step
+// base, which lets a captured graph of steps be replayed at any step).
+__global__ void __launch_bounds__(64) k_tfsf(typename V2<T>::t* e, typename V2<T>::t* h, Geo g, SrcArgs s, int it,
+                                             const int* itp) {
   const int ix = blockIdx.x * blockDim.x + threadIdx.x;
   if (ix > s.nx + 1) return;
+  if (itp) it += *itp;
   const int y0 = blockIdx.y * TFSF_YCH;
   tfsf_column<T>(e, h, g, s, it, ix, y0, min(y0 + TFSF_YCH - 1, s.ny + 1));
 }
@@ -831,8 +839,8 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_dft_gather(const typename V2<T>::t* __restrict__ e,
                                                     const typename V2<T>::t* __restrict__ h, long comp,
                                                     const Seg* __restrict__ segs, typename V2<T>::t* __restrict__ slot,
-                                                    int* tk, int islot, int t) {
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = t;
+                                                    int* tk, int islot, int t, const int* tp) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = tp ? *tp + t : t;
   const Seg sg = segs[blockIdx.y];
   const long L = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long n = (long)sg.nu * sg.nv;
@@ -1358,6 +1366,11 @@ struct iris_engine {
   double2* d_inc = nullptr;
   int zchunk = 0;
   dim3 fblk, fgrd;
+  // CUDA graph of one DFT block of steps (iris_params.graph): d_it holds the
+  // step base the captured kernels add to their offsets, dev_it its value
+  cudaGraphExec_t gexec = nullptr;
+  int* d_it = nullptr;
+  int dev_it = -1;
   // streamed split passes (FP32, real material); d_err: a kernel's give-up record
   bool stream = false;
   dim3 sgrd;
@@ -1569,11 +1582,11 @@ template <typename T> void launch_h(iris_engine* E) {
   }
   k_update_h<T><<<E->grd, E->blk, 0, E->st>>>(field_args<T>(E));
 }
-template <typename T> void launch_tfsf(iris_engine* E, int it) {
+template <typename T> void launch_tfsf(iris_engine* E, int it, const int* itp = nullptr) {
   if (E->src.variant == 0) return;
   KTimer tm(E, IRIS_KC_TFSF);
   using V = typename V2<T>::t;
-  k_tfsf<T><<<E->tf_grd, E->tf_blk, 0, E->st>>>((V*)E->e, (V*)E->h, E->g, E->src, it);
+  k_tfsf<T><<<E->tf_grd, E->tf_blk, 0, E->st>>>((V*)E->e, (V*)E->h, E->g, E->src, it, itp);
 }
 
 void dft_flush(iris_engine* E) {
@@ -1596,7 +1609,7 @@ void dft_flush(iris_engine* E) {
   E->nslot = 0;
 }
 
-template <typename T> void dft_sample(iris_engine* E, int t) {
+template <typename T> void dft_sample(iris_engine* E, int t, const int* tp = nullptr) {
   if (E->P == 0) return;
   using V = typename V2<T>::t;
   {
@@ -1604,7 +1617,7 @@ template <typename T> void dft_sample(iris_engine* E, int t) {
   V* slot = (V*)E->S + (long)E->nslot * E->P;
   dim3 grid((unsigned)((E->max_seg + 255) / 256), (unsigned)E->segs.size());
   k_dft_gather<T><<<grid, 256, 0, E->st>>>((const V*)E->e, (const V*)E->h, E->g.comp, E->d_segs, slot, E->d_tk,
-                                          E->nslot, t);
+                                          E->nslot, t, tp);
   }
   if (++E->nslot == E->K) dft_flush(E);
 }
@@ -1681,13 +1694,71 @@ int step_fused(iris_engine* E, int it0, int n) {
   return IRIS_OK;
 }
 
+
+// A whole DFT block of steps from it on can be replayed from a graph: every
+// step of it is sampled and the block starts with an empty ring.
+bool graph_ready(const iris_engine* E, int it, int left) {
+  const iris_params& p = E->p;
+  return p.graph && !E->timing && !E->fused && E->P > 0 && E->nslot == 0 && p.sample_fourier == 1 &&
+         it >= p.to_fourier && left >= E->K;
+}
+
+void graph_reset(iris_engine* E) {
+  if (E->gexec) cudaGraphExecDestroy(E->gexec);
+  E->gexec = nullptr;
+}
+
+// Steps it .. it+K-1 from the engine's graph of one DFT block (captured on
+// first use from record(), which issues the K steps with step offsets
+// 0 .. K-1 relative to the device-resident base d_it, the block's sample
+// flush, and the base's advance by K).
+template <typename F> int graph_block(iris_engine* E, int it, F record) {
+  if (!E->d_it) {
+    CK(cudaMalloc(&E->d_it, sizeof(int)));
+    E->dev_it = -1;
+  }
+  if (E->dev_it != it) k_set_int<<<1, 1, 0, E->st>>>(E->d_it, it);
+  if (!E->gexec) {
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamBeginCapture(E->st, cudaStreamCaptureModeRelaxed));
+    record();
+    k_add_int<<<1, 1, 0, E->st>>>(E->d_it, E->K);
+    const cudaError_t ec = cudaStreamEndCapture(E->st, &gr);
+    if (ec != cudaSuccess) return fail(IRIS_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(&E->gexec, gr, 0);
+    cudaGraphDestroy(gr);
+    if (ei != cudaSuccess) {
+      E->gexec = nullptr;
+      return fail(IRIS_ECUDA, std::string("graph instantiation: ") + cudaGetErrorString(ei));
+    }
+  }
+  CK(cudaGraphLaunch(E->gexec, E->st));
+  E->dev_it = it + E->K;
+  return IRIS_OK;
+}
+
 template <typename T> int step_t(iris_engine* E, int it0, int n) {
   const iris_params& p = E->p;
-  for (int it = it0; it < it0 + n; ++it) {
+  int it = it0;
+  while (it < it0 + n) {
+    if (graph_ready(E, it, it0 + n - it)) {
+      int rc = graph_block(E, it, [&] {
+        for (int j = 0; j < E->K; ++j) {
+          launch_e<T>(E);
+          launch_h<T>(E);
+          launch_tfsf<T>(E, j, E->d_it);
+          dft_sample<T>(E, j + 1 - p.to_fourier, E->d_it);
+        }
+      });
+      if (rc) return rc;
+      it += E->K;
+      continue;
+    }
     launch_e<T>(E);
     launch_h<T>(E);
     launch_tfsf<T>(E, it);
     if (it >= p.to_fourier && it % p.sample_fourier == 0) dft_sample<T>(E, it + 1 - p.to_fourier);
+    ++it;
   }
   CK(cudaGetLastError());
   return IRIS_OK;
@@ -1727,6 +1798,7 @@ void default_material(const iris_params& p, std::vector<double>& re, std::vector
 
 int upload_material(iris_engine* E, const double* re, const double* im) {
   const iris_params& p = E->p;
+  graph_reset(E);  // captured launches hold the old material pointer
   const Geo& g = E->g;
   const int nzs = p.hf - p.hi + 1;  // planes stored: hi..hf
   bool cplx = false;
@@ -1869,10 +1941,11 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
 void free_engine(iris_engine* E) {
   void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
                   E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J, E->e2, E->h2, E->pml_d2[0],
-                  E->pml_d2[1], E->d_inc, E->d_err};
+                  E->pml_d2[1], E->d_inc, E->d_err, E->d_it};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (E->h_J) cudaFreeHost(E->h_J);
+  graph_reset(E);
   for (int k = 0; k < IRIS_NKC; ++k)
     for (auto& pr : E->ev[k]) {
       cudaEventDestroy(pr.first);
@@ -2480,7 +2553,8 @@ __global__ void __launch_bounds__(256, MINB) k_batch_flat(const FieldArgs<T>* __
 template <typename T>
 __global__ void __launch_bounds__(64) k_batch_tfsf(const FieldArgs<T>* __restrict__ args,
                                                    const SrcArgs* __restrict__ srcs, const TItem* __restrict__ items,
-                                                   long nitems, int it) {
+                                                   long nitems, int it, const int* itp) {
+  if (itp) it += *itp;
   for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
     const TItem b = items[k];
     const FieldArgs<T>& a = args[b.cell];
@@ -2495,8 +2569,8 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_batch_gather(const FieldArgs<T>* __restrict__ args,
                                                       const BSeg* __restrict__ segs,
                                                       typename V2<T>::t* __restrict__ slot, int* tk, int islot,
-                                                      int t) {
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = t;
+                                                      int t, const int* tp) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = tp ? *tp + t : t;
   const BSeg b = segs[blockIdx.y];
   const long L = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= (long)b.s.nu * b.s.nv) return;
@@ -2575,6 +2649,7 @@ int batch_build_items(iris_batch* B, int tile) {
         if (z <= p.pmlzi || z >= p.pmlzf)
           for (int l = 0; l < nxy; l += TX) items.push_back(BItem{c, l, 0, z});
     }
+  graph_reset(B->master);  // captured launches hold the old work list
   if (B->d_items) cudaFree(B->d_items);
   B->d_items = nullptr;
   CK(cudaMalloc(&B->d_items, sizeof(BItem) * items.size()));
@@ -2651,28 +2726,47 @@ template <typename T> void batch_eh(iris_batch* B, bool e) {
   }
 }
 
-template <typename T> int batch_step_t(iris_batch* B, int it0, int n) {
+// One step of every cell: step it, or *itp + it when itp is given; sampled
+// says whether the step's DFT sample is taken.
+template <typename T> void batch_one_step(iris_batch* B, int it, const int* itp, bool sampled) {
   iris_engine* M = B->master;
   const iris_params& p = M->p;
   using V = typename V2<T>::t;
   const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
-  for (int it = it0; it < it0 + n; ++it) {
-    batch_eh<T>(B, true);
-    batch_eh<T>(B, false);
-    if (B->ntitems) {
-      KTimer tm(M, IRIS_KC_TFSF);
-      const long g = std::min<long>(B->ntitems, 152L * 16);
-      k_batch_tfsf<T><<<(unsigned)g, 64, 0, M->st>>>(args, B->d_src, B->d_titems, B->ntitems, it);
+  batch_eh<T>(B, true);
+  batch_eh<T>(B, false);
+  if (B->ntitems) {
+    KTimer tm(M, IRIS_KC_TFSF);
+    const long g = std::min<long>(B->ntitems, 152L * 16);
+    k_batch_tfsf<T><<<(unsigned)g, 64, 0, M->st>>>(args, B->d_src, B->d_titems, B->ntitems, it, itp);
+  }
+  if (sampled) {
+    {
+      KTimer tm(M, IRIS_KC_GATHER);
+      V* slot = (V*)M->S + (long)M->nslot * M->P;
+      dim3 grid((unsigned)((B->max_seg + 255) / 256), (unsigned)B->nbsegs);
+      k_batch_gather<T><<<grid, 256, 0, M->st>>>(args, B->d_bsegs, slot, M->d_tk, M->nslot, it + 1 - p.to_fourier,
+                                                 itp);
     }
-    if (M->P > 0 && it >= p.to_fourier && it % p.sample_fourier == 0) {
-      {
-        KTimer tm(M, IRIS_KC_GATHER);
-        V* slot = (V*)M->S + (long)M->nslot * M->P;
-        dim3 grid((unsigned)((B->max_seg + 255) / 256), (unsigned)B->nbsegs);
-        k_batch_gather<T><<<grid, 256, 0, M->st>>>(args, B->d_bsegs, slot, M->d_tk, M->nslot, it + 1 - p.to_fourier);
-      }
-      if (++M->nslot == M->K) dft_flush(M);
+    if (++M->nslot == M->K) dft_flush(M);
+  }
+}
+
+template <typename T> int batch_step_t(iris_batch* B, int it0, int n) {
+  iris_engine* M = B->master;
+  const iris_params& p = M->p;
+  int it = it0;
+  while (it < it0 + n) {
+    if (graph_ready(M, it, it0 + n - it)) {
+      int rc = graph_block(M, it, [&] {
+        for (int j = 0; j < M->K; ++j) batch_one_step<T>(B, j, M->d_it, true);
+      });
+      if (rc) return rc;
+      it += M->K;
+      continue;
     }
+    batch_one_step<T>(B, it, nullptr, M->P > 0 && it >= p.to_fourier && it % p.sample_fourier == 0);
+    ++it;
   }
   B->steps_taken += n;
   CK(cudaGetLastError());
