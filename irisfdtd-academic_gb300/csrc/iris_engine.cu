@@ -3042,6 +3042,8 @@ struct Design {
 
 template <typename T> struct AdjArgs {
   FieldArgs<T> f;                // adjoint state; coef = adjoint rows, eps_r = forward material
+  int z0;                        // first plane of the launch (blockIdx.z counts from it)
+  int z1;                        // last plane of the launch
   Design d;
   const typename V2<T>::t* rec;  // forward curl of H at the design cells for this step, [3][n]
   double* grad;                  // dL/d eps_inv accumulators [n], or null
@@ -3067,10 +3069,12 @@ __device__ __forceinline__ void pml_at(const FieldArgs<T>& a, int x, int y, int 
   pi = ((long)zr * a.g.ny + (y - 1)) * (long)a.g.nx + (x - 1);
 }
 
-// V_k = b_h Bbar_k + be_h Hbar_k (UPML) or -dtcq2 Hbar_k at interior cell (x, y, z).
-template <typename T> __device__ __forceinline__ cx<T> adj_v(const FieldArgs<T>& a, int x, int y, int z, int k) {
+// V_k = b_h Bbar_k + be_h Hbar_k (UPML) or -dtcq2 Hbar_k at interior cell
+// (x, y, z); UPML = false: the caller knows z is outside the slabs.
+template <typename T, bool UPML>
+__device__ __forceinline__ cx<T> adj_v(const FieldArgs<T>& a, int x, int y, int z, int k) {
   const cx<T> hb = ld<T>(a.h + k * a.g.comp + a.g.at(x, y, z));
-  if (in_pml(a, z)) {
+  if (UPML && in_pml(a, z)) {
     int slab, row;
     long pi;
     pml_at(a, x, y, z, slab, row, pi);
@@ -3081,11 +3085,13 @@ template <typename T> __device__ __forceinline__ cx<T> adj_v(const FieldArgs<T>&
   return rmul(-a.dtcq2, hb);
 }
 
-// W_k = b_e Dbar_k + be_e Ebar_k (UPML) or m Ebar_k at interior cell (x, y, z).
-template <typename T> __device__ __forceinline__ cx<T> adj_w(const FieldArgs<T>& a, int x, int y, int z, int k) {
+// W_k = b_e Dbar_k + be_e Ebar_k (UPML) or m Ebar_k at interior cell
+// (x, y, z); UPML = false: the caller knows z is outside the slabs.
+template <typename T, bool UPML>
+__device__ __forceinline__ cx<T> adj_w(const FieldArgs<T>& a, int x, int y, int z, int k) {
   const Geo& g = a.g;
   const cx<T> eb = ld<T>(a.e + k * g.comp + g.at(x, y, z));
-  if (in_pml(a, z)) {
+  if (UPML && in_pml(a, z)) {
     int slab, row;
     long pi;
     pml_at(a, x, y, z, slab, row, pi);
@@ -3099,18 +3105,20 @@ template <typename T> __device__ __forceinline__ cx<T> adj_w(const FieldArgs<T>&
 
 // Adjoint of the H pass (plus the E pass transform deferred from the step
 // after it): Ebar += curl_b(V); the gradient term of the design cells.
-template <typename T, bool CURL> __global__ void __launch_bounds__(256) k_adj_h(AdjArgs<T> A) {
+// Planes z0 .. z1 of the launch; UPML = false: neither they nor the planes
+// below them lie in a UPML slab.
+template <typename T, bool CURL, bool UPML> __global__ void __launch_bounds__(256) k_adj_h(AdjArgs<T> A) {
   const FieldArgs<T>& a = A.f;
   const Geo& g = a.g;
   const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
-  if (x > g.nx || y > g.ny || z > g.nz) return;
+  const int z = A.z0 + blockIdx.z * blockDim.z + threadIdx.z;
+  if (x > g.nx || y > g.ny || z > A.z1) return;
   const long i = g.at(x, y, z);
   cx<T> e[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) e[k] = ld<T>(a.e + k * g.comp + i);
-  if (!A.first && in_pml(a, z)) {
+  if (UPML && !A.first && in_pml(a, z)) {
     int slab, row;
     long pi;
     pml_at(a, x, y, z, slab, row, pi);
@@ -3126,11 +3134,11 @@ template <typename T, bool CURL> __global__ void __launch_bounds__(256) k_adj_h(
   if (CURL) {
     cx<T> v[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) v[k] = adj_v(a, x, y, z, k);
+    for (int k = 0; k < 3; ++k) v[k] = adj_v<T, UPML>(a, x, y, z, k);
     const int xm = x == 1 ? g.nx : x - 1, ym = y == 1 ? g.ny : y - 1, zm = z == 1 ? g.nz : z - 1;
-    cx<T> v1x = adj_v(a, xm, y, z, 1), v2x = adj_v(a, xm, y, z, 2);
-    cx<T> v0y = adj_v(a, x, ym, z, 0), v2y = adj_v(a, x, ym, z, 2);
-    cx<T> v0z = adj_v(a, x, y, zm, 0), v1z = adj_v(a, x, y, zm, 1);
+    cx<T> v1x = adj_v<T, UPML>(a, xm, y, z, 1), v2x = adj_v<T, UPML>(a, xm, y, z, 2);
+    cx<T> v0y = adj_v<T, UPML>(a, x, ym, z, 0), v2y = adj_v<T, UPML>(a, x, ym, z, 2);
+    cx<T> v0z = adj_v<T, UPML>(a, x, y, zm, 0), v1z = adj_v<T, UPML>(a, x, y, zm, 1);
     if (x == 1) { v1x = cmul(a.pxm, v1x); v2x = cmul(a.pxm, v2x); }
     if (y == 1) { v0y = cmul(a.pym, v0y); v2y = cmul(a.pym, v2y); }
     if (z == 1) { v0z = cmul(a.pzm, v0z); v1z = cmul(a.pzm, v1z); }
@@ -3154,19 +3162,20 @@ template <typename T, bool CURL> __global__ void __launch_bounds__(256) k_adj_h(
 }
 
 // Adjoint of the E pass (plus the H pass transform of the same step):
-// Hbar <- al Hbar + curl_f(W), Bbar <- a Bbar + g_h Hbar.
-template <typename T> __global__ void __launch_bounds__(256) k_adj_e(AdjArgs<T> A) {
+// Hbar <- al Hbar + curl_f(W), Bbar <- a Bbar + g_h Hbar.  Planes z0 .. z1;
+// UPML = false: neither they nor the planes above them lie in a UPML slab.
+template <typename T, bool UPML> __global__ void __launch_bounds__(256) k_adj_e(AdjArgs<T> A) {
   const FieldArgs<T>& a = A.f;
   const Geo& g = a.g;
   const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
-  if (x > g.nx || y > g.ny || z > g.nz) return;
+  const int z = A.z0 + blockIdx.z * blockDim.z + threadIdx.z;
+  if (x > g.nx || y > g.ny || z > A.z1) return;
   const long i = g.at(x, y, z);
   cx<T> h[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) h[k] = ld<T>(a.h + k * g.comp + i);
-  if (in_pml(a, z)) {
+  if (UPML && in_pml(a, z)) {
     int slab, row;
     long pi;
     pml_at(a, x, y, z, slab, row, pi);
@@ -3181,11 +3190,11 @@ template <typename T> __global__ void __launch_bounds__(256) k_adj_e(AdjArgs<T> 
   }
   cx<T> w[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) w[k] = adj_w(a, x, y, z, k);
+  for (int k = 0; k < 3; ++k) w[k] = adj_w<T, UPML>(a, x, y, z, k);
   const int xp = x == g.nx ? 1 : x + 1, yp = y == g.ny ? 1 : y + 1, zp = z == g.nz ? 1 : z + 1;
-  cx<T> w1x = adj_w(a, xp, y, z, 1), w2x = adj_w(a, xp, y, z, 2);
-  cx<T> w0y = adj_w(a, x, yp, z, 0), w2y = adj_w(a, x, yp, z, 2);
-  cx<T> w0z = adj_w(a, x, y, zp, 0), w1z = adj_w(a, x, y, zp, 1);
+  cx<T> w1x = adj_w<T, UPML>(a, xp, y, z, 1), w2x = adj_w<T, UPML>(a, xp, y, z, 2);
+  cx<T> w0y = adj_w<T, UPML>(a, x, yp, z, 0), w2y = adj_w<T, UPML>(a, x, yp, z, 2);
+  cx<T> w0z = adj_w<T, UPML>(a, x, y, zp, 0), w1z = adj_w<T, UPML>(a, x, y, zp, 1);
   if (x == g.nx) { w1x = cmul(a.pxp, w1x); w2x = cmul(a.pxp, w2x); }
   if (y == g.ny) { w0y = cmul(a.pyp, w0y); w2y = cmul(a.pyp, w2y); }
   if (z == g.nz) { w0z = cmul(a.pzp, w0z); w1z = cmul(a.pzp, w1z); }
@@ -3335,17 +3344,54 @@ template <typename T> void adj_source(iris_adjoint* J, int t) {
   }
 }
 
-// One adjoint step (K1 then K2) for forward step it; rec slot or -1.
+// Launch shape of planes z0 .. z1 (none when z1 < z0).
+dim3 adj_grid(const iris_engine* F, int z0, int z1) {
+  return dim3(F->grd.x, F->grd.y, z1 < z0 ? 0u : (unsigned)((z1 - z0 + F->blk.z) / F->blk.z));
+}
+
+// One adjoint step (K1 then K2) for forward step it; rec slot or -1.  Each
+// kernel runs as the planes whose stencil stays outside the UPML slabs,
+// compiled without slab code, and the rest (the slabs and their neighbours).
 template <typename T> void adj_step(iris_adjoint* J, bool first, int slot) {
   iris_engine* F = J->F;
+  const iris_params& p = F->p;
   const bool grad = slot >= 0;
-  k_adj_h<T, true><<<F->grd, F->blk, 0, F->st>>>(adj_args<T>(J, first, slot, grad));
-  k_adj_e<T><<<F->grd, F->blk, 0, F->st>>>(adj_args<T>(J, first, -1, false));
+  AdjArgs<T> a = adj_args<T>(J, first, slot, grad);
+  auto k1 = [&](int z0, int z1, bool upml) {
+    a.z0 = z0;
+    a.z1 = z1;
+    const dim3 gr = adj_grid(F, z0, z1);
+    if (gr.z == 0) return;
+    if (upml) k_adj_h<T, true, true><<<gr, F->blk, 0, F->st>>>(a);
+    else k_adj_h<T, true, false><<<gr, F->blk, 0, F->st>>>(a);
+  };
+  // K1 reads planes z and z-1: free of slab code for z in [pmlzi+2, pmlzf-1]
+  const int a1 = std::min(p.pmlzi + 1, p.pmlzf - 1);
+  k1(1, a1, true);
+  k1(a1 + 1, p.pmlzf - 1, false);
+  k1(p.pmlzf, p.nz, true);
+  AdjArgs<T> b = adj_args<T>(J, first, -1, false);
+  auto k2 = [&](int z0, int z1, bool upml) {
+    b.z0 = z0;
+    b.z1 = z1;
+    const dim3 gr = adj_grid(F, z0, z1);
+    if (gr.z == 0) return;
+    if (upml) k_adj_e<T, true><<<gr, F->blk, 0, F->st>>>(b);
+    else k_adj_e<T, false><<<gr, F->blk, 0, F->st>>>(b);
+  };
+  // K2 reads planes z and z+1: free of slab code for z in [pmlzi+1, pmlzf-2]
+  const int b2 = std::max(p.pmlzf - 2, p.pmlzi);
+  k2(1, p.pmlzi, true);
+  k2(p.pmlzi + 1, b2, false);
+  k2(b2 + 1, p.nz, true);
 }
 
 template <typename T> void adj_finalize(iris_adjoint* J) {
   iris_engine* F = J->F;
-  k_adj_h<T, false><<<F->grd, F->blk, 0, F->st>>>(adj_args<T>(J, false, -1, false));
+  AdjArgs<T> a = adj_args<T>(J, false, -1, false);
+  a.z0 = 1;
+  a.z1 = F->p.nz;
+  k_adj_h<T, false, true><<<adj_grid(F, 1, F->p.nz), F->blk, 0, F->st>>>(a);
 }
 
 // The forward step without DFT sampling (recompute) or with it (forward).
