@@ -187,7 +187,7 @@ def run_engine(args, rank, world, local):
     D.barrier()
     t0 = time.perf_counter()
     eng = iris.Engine(p, fw, precision=prec, dft_block=args.dft_block, device=local, stencil=args.stencil,
-                      graph=args.graph)
+                      graph=args.graph, dft_kernel=args.dft_kernel)
     eng.set_material(eps)
     eng.step(1, K)
     J = eng.flux(0)
@@ -264,6 +264,7 @@ def run_engine(args, rank, world, local):
             "workload": wl_name,
             "grid": [w.nx, w.ny, w.nz], "upml": 24, "nof": w.nof, "dft_points": info["dft_points"],
             "dft_block": info["dft_block"], "precision": args.precision,
+            "dft_kernel": ["engine default", "cuda cores", "tensor cores (tcgen05 tf32x3)"][args.dft_kernel],
             "l2": "working set (fields %.1f GB, DFT accumulators %.1f GB) >> 129 MB L2; no flush needed" % (
                 2 * 3 * info["comp_elems"] * info["bytes_per_complex"] / 1e9,
                 info["dft_points"] * w.nof * 16 / 1e9),
@@ -609,6 +610,8 @@ def main():
     ap.add_argument("--dft-block", type=int, default=0, help="DFT samples per accumulation block (0: engine default)")
     ap.add_argument("--stencil", type=int, default=0, choices=[0, 1, 2, 3],
                     help="0: engine default, 1: split E and H passes, 2: fused E+H pass (fp32), 3: streamed split passes (fp32)")
+    ap.add_argument("--dft-kernel", type=int, default=0, choices=[0, 1, 2],
+                    help="FP32 DFT block: 0 engine default, 1 CUDA cores, 2 tensor cores (tcgen05)")
     ap.add_argument("--graph", action="store_true",
                     help="step whole DFT blocks from a captured CUDA graph (e2e run and an extra timed run)")
     ap.add_argument("--cells", type=int, default=256, help="cells in the batch (workload 4)")

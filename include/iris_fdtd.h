@@ -115,7 +115,15 @@ typedef struct iris_params {
   int graph;          /* 1: step whole DFT blocks (every step sampled) by
                          replaying one captured CUDA graph; results are
                          identical to launch-by-launch stepping            */
+  int dft_kernel;     /* IRIS_DFT_KERNEL_*: FP32 DFT block accumulation    */
 } iris_params;
+
+/* ---- FP32 DFT block kernels (iris_params.dft_kernel) ------------------ */
+#define IRIS_DFT_KERNEL_AUTO 0   /* the engine's choice (tensor cores)      */
+#define IRIS_DFT_KERNEL_CUDA 1   /* FP32 FMA on the CUDA cores              */
+/* tcgen05 tensor cores, TF32 operands split hi + lo (three MMAs per product,
+ * FP32-level accuracy), FP32 partial sums in TMEM, FP64 accumulators      */
+#define IRIS_DFT_KERNEL_TENSOR 2
 
 /* ---- DFT faces (iris_params.dft_faces) -------------------------------- */
 /* every face pair scattering_fourier accumulates (the reference)          */

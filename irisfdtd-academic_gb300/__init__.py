@@ -35,6 +35,7 @@ from .native import IrisError, IrisParams, build, check, lib
 
 FP64, FP32 = 0, 1
 STENCIL_DEFAULT, STENCIL_SPLIT, STENCIL_FUSED, STENCIL_STREAM = 0, 1, 2, 3
+DFT_KERNEL_AUTO, DFT_KERNEL_CUDA, DFT_KERNEL_TENSOR = 0, 1, 2
 E, H = 0, 1
 OP_E, OP_H, OP_TFSF, OP_DFT = 1, 2, 3, 4
 
@@ -87,7 +88,7 @@ class Engine:
     """One run: device state of main()+driver() behind iris_create."""
 
     def __init__(self, p: IrisParams, fw=None, precision: int | None = None, dft_block: int = 0, device: int = 0,
-                 stencil: int = 0, graph: bool = False):
+                 stencil: int = 0, graph: bool = False, dft_kernel: int = 0):
         self.L = lib()
         q = p.copy()
         if precision is not None:
@@ -96,6 +97,7 @@ class Engine:
         q.stencil = stencil
         q.device = device
         q.graph = 1 if graph else 0
+        q.dft_kernel = dft_kernel
         self.p = q
         self.fw = np.ascontiguousarray(frequencies(q) if fw is None else np.asarray(fw, dtype=np.float64))
         h = ctypes.c_void_p()

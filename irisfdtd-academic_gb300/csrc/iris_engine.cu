@@ -983,6 +983,229 @@ __global__ void __launch_bounds__(DFT_THREADS) k_dft_fp32(const float2* __restri
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 DFT block on the tensor cores (tcgen05.mma kind::tf32).
+//
+// fdata[iw][p] += sum_k F_k(p) W_k(iw), W_k(iw) = dt exp(i fw(iw) t_k), for a
+// block of nk samples is the real GEMM C = A B with
+//   A[p][2k+c]      = Re (c = 0) / Im (c = 1) of F_k(p)       M = points
+//   B[2k+c][2j+d]   = the real 2x2 form of W_k(iw0 + j)       N = 2 x frequencies
+// so that C[p][2j] and C[p][2j+1] are Re and Im of the (p, iw0+j) partial sum.
+// FP32 accuracy from TF32 operands: with X = Xh + Xl, Xh = X rounded to TF32,
+// A B ~ Ah Bh + Ah Bl + Al Bh (the Al Bl term is below FP32 rounding).
+//
+// A CTA owns TC_M = 128 points (the 128 TMEM lanes) and a group of up to
+// TC_NW = 128 frequencies (256 FP32 TMEM columns).  K is walked in chunks of
+// TC_KC = 16 (8 samples) through two shared-memory stages: the CTA's four
+// warps split the chunk's samples into the hi/lo A operands (K-major core
+// matrices, no swizzle) while the previous chunk's twelve MMAs run; the B
+// operands, identical for every CTA, are prepared once per block in global
+// memory in the same layout by k_twiddle_tc and bulk-copied (TMA) per chunk.
+// One elected thread issues the MMAs and commits them to an mbarrier; the
+// epilogue reads the accumulators back with tcgen05.ld and adds them to
+// fdata in FP64, one coalesced double2 row per frequency.  Every wait is
+// bounded; a CTA that gives up records it in err, still waits (bounded) for
+// its MMAs, frees its TMEM and exits.
+
+constexpr int TC_M = 128, TC_NW = 128, TC_KC = 16, TC_THREADS = 128;
+constexpr int TC_NMAX = 2 * TC_NW;                       // TMEM columns per CTA
+constexpr int TC_BROWS = TC_NMAX;                        // B rows per chunk buffer
+constexpr size_t TC_A_BYTES = (size_t)TC_M * TC_KC * 4;  // one of A hi / A lo
+constexpr size_t TC_B_BYTES = (size_t)TC_BROWS * TC_KC * 4;
+constexpr size_t TC_STAGE = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
+constexpr size_t TC_SMEM = 2 * TC_STAGE;
+
+// Offset (in floats) of element (row r, k) of a K-major, unswizzled operand
+// of TC_KC columns: 8-row x 16-byte core matrices, the K-neighbour core
+// matrix 128 bytes on, the next 8-row group TC_KC/4 core matrices on.
+__host__ __device__ __forceinline__ int tc_off(int r, int k) {
+  return ((r >> 3) * (TC_KC / 4) + (k >> 2)) * 32 + (r & 7) * 4 + (k & 3);
+}
+
+__device__ __forceinline__ float tf32_hi(float x) {
+  unsigned u;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
+  return __uint_as_float(u);
+}
+
+// B operands of every frequency group and chunk of one block, hi then lo:
+// Bt[((g * nch + c) * 2 + h) * TC_BROWS * TC_KC + tc_off(n, kk)].
+__global__ void k_twiddle_tc(const int* __restrict__ tk, int t0, int tstep, int nk, const double* __restrict__ fw,
+                             int nof, double dt, int ngroups, int nch, float* __restrict__ Bt) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long per = (long)TC_BROWS * TC_KC;
+  if (t >= (long)ngroups * nch * per) return;
+  const int g = (int)(t / (nch * per)), c = (int)((t / per) % nch);
+  const int n = (int)((t % per) / TC_KC), kk = (int)(t % TC_KC);
+  const int j = n >> 1, d = n & 1, iw = g * TC_NW + j;
+  const int k2 = c * TC_KC + kk, k = k2 >> 1, cc = k2 & 1;
+  float v = 0.f;
+  if (iw < nof && k < nk) {
+    const int tt = tk ? tk[k] : t0 + k * tstep;
+    double sn, cs;
+    sincos(fw[iw] * (double)tt, &sn, &cs);
+    const float wr = (float)(dt * cs), wi = (float)(dt * sn);
+    v = d == 0 ? (cc == 0 ? wr : -wi) : (cc == 0 ? wi : wr);
+  }
+  const float hi = tf32_hi(v);
+  float* base = Bt + ((long)(g * nch + c) * 2) * per;
+  base[tc_off(n, kk)] = hi;
+  base[per + tc_off(n, kk)] = v - hi;
+}
+
+__device__ __forceinline__ uint64_t tc_desc(const void* smem) {
+  // start address, leading (K) byte offset 128, stride (8-row) byte offset
+  // TC_KC/4 * 128, descriptor version 1, no swizzle
+  const uint64_t a = (smem_u32(smem) & 0x3FFFFu) >> 4;
+  const uint64_t lbo = 128u >> 4, sbo = (uint64_t)(TC_KC / 4 * 128) >> 4;
+  return a | (lbo << 16) | (sbo << 32) | (1ull << 46);
+}
+
+// kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t tc_idesc(int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, int acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// CTA (point tile, frequency group), the groups of one tile adjacent in
+// blockIdx.x so the tile's samples are read from HBM once.
+__global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict__ S, long P, int nk,
+                                                       const float* __restrict__ Bt, int nof, int ngroups,
+                                                       double2* __restrict__ fd, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint64_t bar_b[2], bar_mma[2];
+  __shared__ uint32_t taddr_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = blockIdx.x % ngroups;
+  const long p0 = (long)(blockIdx.x / ngroups) * TC_M;
+  const int nw = min(TC_NW, nof - g * TC_NW);   // frequencies of this group
+  const int ncol = ((2 * nw + 15) / 16) * 16;   // MMA N: a multiple of 16
+  const int nch = (2 * nk + TC_KC - 1) / TC_KC;
+  const long per = (long)TC_BROWS * TC_KC;
+  if (tid == 0) {
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(&bar_b[s], 1);
+      mbar_init(&bar_mma[s], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&taddr_s)),
+                 "r"(TC_NMAX)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = taddr_s;
+  const uint32_t idesc = tc_idesc(ncol);
+  unsigned par_b = 0, par_mma = 0;
+  bool bad = false;
+  const long p = p0 + tid;  // this thread's point (row of A)
+  for (int c = 0; c < nch; ++c) {
+    const int s = c & 1;
+    unsigned char* st = smem + s * TC_STAGE;
+    float* Ah = (float*)st;
+    float* Al = (float*)(st + TC_A_BYTES);
+    float* Bh = (float*)(st + 2 * TC_A_BYTES);
+    float* Bl = (float*)(st + 2 * TC_A_BYTES + TC_B_BYTES);
+    if (c >= 2) {  // the MMAs of chunk c-2 read this stage
+      bad |= !mbar_wait(&bar_mma[s], (par_mma >> s) & 1u, STREAM_WAIT_CYCLES);
+      par_mma ^= 1u << s;
+    }
+    if (tid == 0) {
+      const unsigned nb = (unsigned)(ncol * TC_KC * 4);
+      const float* src = Bt + ((long)(g * nch + c) * 2) * per;
+      mbar_expect_tx(&bar_b[s], 2 * nb);
+      fence_proxy_async();
+      bulk_g2s(Bh, src, nb, &bar_b[s]);
+      bulk_g2s(Bl, src + per, nb, &bar_b[s]);
+    }
+    // this thread's row of A: samples c*TC_KC/2 .. +TC_KC/2, split hi/lo
+#pragma unroll
+    for (int q = 0; q < TC_KC / 4; ++q) {
+      const int k = c * (TC_KC / 2) + 2 * q;
+      float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+      if (p < P) {
+        if (k < nk) a = S[(long)k * P + p];
+        if (k + 1 < nk) b = S[(long)(k + 1) * P + p];
+      }
+      const float4 v = make_float4(a.x, a.y, b.x, b.y);
+      const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+      *(float4*)(Ah + tc_off(tid, 4 * q)) = h;
+      *(float4*)(Al + tc_off(tid, 4 * q)) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+    }
+    fence_proxy_async();  // generic-proxy writes of A before the tensor core reads them
+    __syncthreads();
+    if (tid == 0) {
+      bad |= !mbar_wait(&bar_b[s], (par_b >> s) & 1u, STREAM_WAIT_CYCLES);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int ks = 0; ks < TC_KC / 8; ++ks) {
+        const uint64_t ah = tc_desc(Ah + 64 * ks), al = tc_desc(Al + 64 * ks);
+        const uint64_t bh = tc_desc(Bh + 64 * ks), bl = tc_desc(Bl + 64 * ks);
+        tc_mma(tmem, ah, bh, idesc, (c > 0 || ks > 0) ? 1 : 0);
+        tc_mma(tmem, ah, bl, idesc, 1);
+        tc_mma(tmem, al, bh, idesc, 1);
+      }
+      tc_commit(&bar_mma[s]);
+    }
+    par_b ^= 1u << s;
+  }
+  // the commits of the last two chunks (each covers every earlier MMA)
+  for (int c = max(0, nch - 2); c < nch; ++c) {
+    const int s = c & 1;
+    bad |= !mbar_wait(&bar_mma[s], (par_mma >> s) & 1u, STREAM_WAIT_CYCLES);
+    par_mma ^= 1u << s;
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (__syncthreads_or(bad)) {
+    if (tid == 0) atomicExch(err, 3);
+  } else {
+    // epilogue: warp w reads TMEM lanes 32w .. 32w+31 (points p0+32w+lane)
+    const long pp = p0 + 32 * warp + lane;
+    for (int c0 = 0; c0 < ncol; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(ta)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (pp < P) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int jw = c0 / 2 + j;
+          if (jw >= nw) break;
+          double2* q = fd + (long)(g * TC_NW + jw) * P + pp;
+          double2 f = *q;
+          f.x += (double)__uint_as_float(r[2 * j]);
+          f.y += (double)__uint_as_float(r[2 * j + 1]);
+          *q = f;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_NMAX) : "memory");
+}
+
 // Poynting flux of one face, code/dataprocess.f90:246-277:
 // J = sign * sum Re(a*conj(b) - c*conj(d)) * eps0*Q/(2 dt).
 struct FluxFace {
@@ -1351,6 +1574,8 @@ struct iris_engine {
   double* d_fw = nullptr;
   double2* fd = nullptr;
   float2* d_wt = nullptr;
+  bool dft_tc = false;     // FP32 block accumulation on the tensor cores
+  float* d_wtc = nullptr;  // its B operands (k_twiddle_tc)
   FluxFace* d_faces = nullptr;
   double* d_J = nullptr;
   double* h_J = nullptr;
@@ -1528,6 +1753,7 @@ int validate(const iris_params& p) {
   if (p.stencil == IRIS_STENCIL_FUSED && p.precision != IRIS_FP32) return bad("the fused stencil is FP32 only");
   if (p.stencil == IRIS_STENCIL_STREAM && p.precision != IRIS_FP32) return bad("the streamed stencil is FP32 only");
   if (p.dft_faces != IRIS_DFT_ALL && p.dft_faces != IRIS_DFT_Z) return bad("dft_faces must be IRIS_DFT_ALL or IRIS_DFT_Z");
+  if (p.dft_kernel < IRIS_DFT_KERNEL_AUTO || p.dft_kernel > IRIS_DFT_KERNEL_TENSOR) return bad("unknown dft_kernel");
   return IRIS_OK;
 }
 
@@ -1598,6 +1824,14 @@ void dft_flush(iris_engine* E) {
     const long nblk = (E->P + 127) / 128;
     k_dft_fp64<<<(unsigned)(nblk * nwc), 128, (size_t)nk * DFT64_WC * sizeof(double2), E->st>>>(
         (const double2*)E->S, E->P, nk, E->d_tk, E->d_fw, E->p.nof, nwc, E->p.dt, E->fd);
+  } else if (E->dft_tc) {
+    const int ng = (E->p.nof + TC_NW - 1) / TC_NW, nch = (2 * nk + TC_KC - 1) / TC_KC;
+    const long nt = (long)ng * nch * TC_BROWS * TC_KC;
+    k_twiddle_tc<<<(unsigned)((nt + 255) / 256), 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, ng,
+                                                                   nch, E->d_wtc);
+    const long ntiles = (E->P + TC_M - 1) / TC_M;
+    k_dft_tc<<<(unsigned)(ntiles * ng), TC_THREADS, TC_SMEM, E->st>>>((const float2*)E->S, E->P, nk, E->d_wtc,
+                                                                       E->p.nof, ng, E->fd, E->d_err);
   } else {
     const int nt = nk * E->p.nof;
     k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
@@ -1927,6 +2161,12 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
   CK(cudaMalloc(&E->d_fw, sizeof(double) * p.nof));
   CK(cudaMemcpy(E->d_fw, E->fw.data(), sizeof(double) * p.nof, cudaMemcpyHostToDevice));
   if (E->prec == IRIS_FP32) CK(cudaMalloc(&E->d_wt, sizeof(float2) * (size_t)E->K * p.nof));
+  E->dft_tc = E->prec == IRIS_FP32 && p.dft_kernel != IRIS_DFT_KERNEL_CUDA;
+  if (E->dft_tc) {
+    const int ng = (p.nof + TC_NW - 1) / TC_NW, nch = (2 * E->K + TC_KC - 1) / TC_KC;
+    CK(cudaMalloc(&E->d_wtc, sizeof(float) * (size_t)ng * nch * 2 * TC_BROWS * TC_KC));
+    CK(cudaFuncSetAttribute(k_dft_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+  }
   if (!E->segs.empty()) {
     CK(cudaMalloc(&E->d_segs, sizeof(Seg) * E->segs.size()));
     CK(cudaMemcpy(E->d_segs, E->segs.data(), sizeof(Seg) * E->segs.size(), cudaMemcpyHostToDevice));
@@ -1941,7 +2181,7 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
 void free_engine(iris_engine* E) {
   void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
                   E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J, E->e2, E->h2, E->pml_d2[0],
-                  E->pml_d2[1], E->d_inc, E->d_err, E->d_it};
+                  E->pml_d2[1], E->d_inc, E->d_err, E->d_it, E->d_wtc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (E->h_J) cudaFreeHost(E->h_J);
@@ -2117,8 +2357,9 @@ static int stream_status(iris_engine* E) {
   int h = 0;
   CK(cudaMemcpyAsync(&h, E->d_err, sizeof(int), cudaMemcpyDeviceToHost, E->st));
   CK(cudaStreamSynchronize(E->st));
-  if (h) return fail(IRIS_ETIMEOUT, std::string("a streamed ") + (h == 1 ? "E" : "H") +
-                                        " pass gave up waiting for its staged plane");
+  if (h) return fail(IRIS_ETIMEOUT, h == 3 ? std::string("the tensor-core DFT block gave up waiting")
+                                            : std::string("a streamed ") + (h == 1 ? "E" : "H") +
+                                                  " pass gave up waiting for its staged plane");
   return IRIS_OK;
 }
 

@@ -86,7 +86,7 @@ class IrisParams(ctypes.Structure):
         ("pmlalfa", _D),
         ("akx_re", _D), ("akx_im", _D), ("aky_re", _D), ("aky_im", _D), ("akz_re", _D), ("akz_im", _D),
         ("system_model", _I), ("precision", _I), ("dft_block", _I), ("device", _I), ("stencil", _I),
-        ("dft_faces", _I), ("graph", _I),
+        ("dft_faces", _I), ("graph", _I), ("dft_kernel", _I),
     ]
 
     def copy(self) -> "IrisParams":

@@ -4,7 +4,8 @@ same cell stepped on its own engine and against the FP64 oracle.
 The batch runs the same per-cell arithmetic as a single engine (the same
 device functions, one launch per operator over all cells), so FP64 cells
 agree with their single-engine runs to the last bit (asserted <= 1e-15) and
-with the oracle within 1e-12; FP32 cells within 1e-6 of FP32 single runs.
+with the oracle within 1e-12; FP32 fields within 1e-6 of FP32 single runs,
+FP32 spectra within 1e-5 (different DFT block boundaries).
 """
 import importlib
 import os
@@ -75,7 +76,11 @@ def test_batch_matches_single_engines(iris, oracle, tmp_path, precision, tol, ti
     assert b.info()["cells"] == len(CELLS)
     for c, (e, Js) in enumerate(singles):
         Jb = b.flux(c)
-        assert rel_err(Jb, Js) <= tol, c
+        # the single engines flush their DFT blocks at every output step, the
+        # batch only when its ring is full: in FP32 the partial sums group
+        # differently (and the tensor-core DFT's operand split rounds at ~4x
+        # FP32's unit), so the spectra agree to 1e-5 while the fields stay at tol
+        assert rel_err(Jb, Js) <= (tol if precision == 0 else 1e-5), c
         assert np.all(Jb[:4] == 0)  # only the z planes are accumulated
         for which in (iris.E, iris.H):
             fb = interior(b.get_field(c, which), cells[c][1])
