@@ -1007,13 +1007,14 @@ __global__ void __launch_bounds__(DFT_THREADS) k_dft_fp32(const float2* __restri
 // bounded; a CTA that gives up records it in err, still waits (bounded) for
 // its MMAs, frees its TMEM and exits.
 
-constexpr int TC_M = 128, TC_NW = 128, TC_KC = 16, TC_THREADS = 128;
+constexpr int TC_M = 128, TC_NW = 128, TC_KC = 16, TC_THREADS = 256;
 constexpr int TC_NMAX = 2 * TC_NW;                       // TMEM columns per CTA
 constexpr int TC_BROWS = TC_NMAX;                        // B rows per chunk buffer
 constexpr size_t TC_A_BYTES = (size_t)TC_M * TC_KC * 4;  // one of A hi / A lo
 constexpr size_t TC_B_BYTES = (size_t)TC_BROWS * TC_KC * 4;
+constexpr size_t TC_R_BYTES = (size_t)(TC_KC / 2) * TC_M * 8;  // raw samples of one chunk
 constexpr size_t TC_STAGE = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
-constexpr size_t TC_SMEM = 2 * TC_STAGE;
+constexpr size_t TC_SMEM = 2 * TC_STAGE + 2 * TC_R_BYTES;
 
 // Offset (in floats) of element (row r, k) of a K-major, unswizzled operand
 // of TC_KC columns: 8-row x 16-byte core matrices, the K-neighbour core
@@ -1079,23 +1080,29 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
 }
 
 // CTA (point tile, frequency group), the groups of one tile adjacent in
-// blockIdx.x so the tile's samples are read from HBM once.
+// blockIdx.x so the tile's samples are read from HBM once.  Eight warps: all
+// split samples into A; warp w reads TMEM lanes 32 (w % 4) .. +31 and the
+// w / 4 half of the columns in the epilogue.  The samples of a chunk (8 rows
+// of 128 points, 1 KB each; P is even, so every row starts 16-byte aligned)
+// and its B operands are bulk-copied one chunk ahead.
 __global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict__ S, long P, int nk,
                                                        const float* __restrict__ Bt, int nof, int ngroups,
                                                        double2* __restrict__ fd, int* err) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint64_t bar_b[2], bar_mma[2];
+  __shared__ uint64_t bar_in[2], bar_mma[2];
   __shared__ uint32_t taddr_s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int g = blockIdx.x % ngroups;
   const long p0 = (long)(blockIdx.x / ngroups) * TC_M;
+  const int np = (int)min((long)TC_M, P - p0);  // points of this tile (even)
   const int nw = min(TC_NW, nof - g * TC_NW);   // frequencies of this group
   const int ncol = ((2 * nw + 15) / 16) * 16;   // MMA N: a multiple of 16
   const int nch = (2 * nk + TC_KC - 1) / TC_KC;
   const long per = (long)TC_BROWS * TC_KC;
+  unsigned char* raw = smem + 2 * TC_STAGE;
   if (tid == 0) {
     for (int s = 0; s < 2; ++s) {
-      mbar_init(&bar_b[s], 1);
+      mbar_init(&bar_in[s], 1);
       mbar_init(&bar_mma[s], 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1111,46 +1118,63 @@ __global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict_
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = taddr_s;
   const uint32_t idesc = tc_idesc(ncol);
-  unsigned par_b = 0, par_mma = 0;
+  const unsigned nb = (unsigned)(ncol * TC_KC * 4);
+  // chunk c's inputs (its raw samples and B operands) into slot s
+  auto issue = [&](int c, int s) {
+    const int k0 = c * (TC_KC / 2), nr = min(TC_KC / 2, nk - k0);
+    unsigned char* st = smem + s * TC_STAGE;
+    const float* src = Bt + ((long)(g * nch + c) * 2) * per;
+    mbar_expect_tx(&bar_in[s], 2 * nb + (unsigned)(nr * np * 8));
+    fence_proxy_async();
+    bulk_g2s(st + 2 * TC_A_BYTES, src, nb, &bar_in[s]);
+    bulk_g2s(st + 2 * TC_A_BYTES + TC_B_BYTES, src + per, nb, &bar_in[s]);
+    for (int r = 0; r < nr; ++r)
+      bulk_g2s(raw + s * TC_R_BYTES + (size_t)r * TC_M * 8, S + (long)(k0 + r) * P + p0, (unsigned)(np * 8),
+               &bar_in[s]);
+  };
+  unsigned par_in = 0, par_mma = 0;
   bool bad = false;
-  const long p = p0 + tid;  // this thread's point (row of A)
+  if (tid == 0) issue(0, 0);
   for (int c = 0; c < nch; ++c) {
     const int s = c & 1;
     unsigned char* st = smem + s * TC_STAGE;
     float* Ah = (float*)st;
     float* Al = (float*)(st + TC_A_BYTES);
-    float* Bh = (float*)(st + 2 * TC_A_BYTES);
-    float* Bl = (float*)(st + 2 * TC_A_BYTES + TC_B_BYTES);
-    if (c >= 2) {  // the MMAs of chunk c-2 read this stage
-      bad |= !mbar_wait(&bar_mma[s], (par_mma >> s) & 1u, STREAM_WAIT_CYCLES);
-      par_mma ^= 1u << s;
-    }
-    if (tid == 0) {
-      const unsigned nb = (unsigned)(ncol * TC_KC * 4);
-      const float* src = Bt + ((long)(g * nch + c) * 2) * per;
-      mbar_expect_tx(&bar_b[s], 2 * nb);
-      fence_proxy_async();
-      bulk_g2s(Bh, src, nb, &bar_b[s]);
-      bulk_g2s(Bl, src + per, nb, &bar_b[s]);
-    }
-    // this thread's row of A: samples c*TC_KC/2 .. +TC_KC/2, split hi/lo
-#pragma unroll
-    for (int q = 0; q < TC_KC / 4; ++q) {
-      const int k = c * (TC_KC / 2) + 2 * q;
-      float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-      if (p < P) {
-        if (k < nk) a = S[(long)k * P + p];
-        if (k + 1 < nk) b = S[(long)(k + 1) * P + p];
+    const float* Bh = (const float*)(st + 2 * TC_A_BYTES);
+    const float* Bl = (const float*)(st + 2 * TC_A_BYTES + TC_B_BYTES);
+    if (c + 1 < nch) {
+      // slot s^1 was last read by the MMAs of chunk c-1 (its raw samples by
+      // this CTA's split of chunk c-1, finished at that iteration's barrier)
+      if (c >= 1) {
+        bad |= !mbar_wait(&bar_mma[s ^ 1], (par_mma >> (s ^ 1)) & 1u, STREAM_WAIT_CYCLES);
+        par_mma ^= 1u << (s ^ 1);
       }
-      const float4 v = make_float4(a.x, a.y, b.x, b.y);
-      const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-      *(float4*)(Ah + tc_off(tid, 4 * q)) = h;
-      *(float4*)(Al + tc_off(tid, 4 * q)) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      if (tid == 0) issue(c + 1, s ^ 1);
+    }
+    bad |= !mbar_wait(&bar_in[s], (par_in >> s) & 1u, STREAM_WAIT_CYCLES);
+    par_in ^= 1u << s;
+    // split: thread (row, half) takes samples 4 half .. 4 half + 3 of the chunk
+    {
+      const int row = tid & (TC_M - 1), half = tid >> 7;
+      const int k0 = c * (TC_KC / 2);
+      const float2* rw = (const float2*)(raw + s * TC_R_BYTES);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int kq = 4 * half + 2 * q;  // sample pair kq, kq+1 of the chunk
+        float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+        if (row < np) {
+          if (k0 + kq < nk) a = rw[kq * TC_M + row];
+          if (k0 + kq + 1 < nk) b = rw[(kq + 1) * TC_M + row];
+        }
+        const float4 v = make_float4(a.x, a.y, b.x, b.y);
+        const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+        *(float4*)(Ah + tc_off(row, 2 * kq)) = h;
+        *(float4*)(Al + tc_off(row, 2 * kq)) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      }
     }
     fence_proxy_async();  // generic-proxy writes of A before the tensor core reads them
     __syncthreads();
     if (tid == 0) {
-      bad |= !mbar_wait(&bar_b[s], (par_b >> s) & 1u, STREAM_WAIT_CYCLES);
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
       for (int ks = 0; ks < TC_KC / 8; ++ks) {
@@ -1162,7 +1186,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict_
       }
       tc_commit(&bar_mma[s]);
     }
-    par_b ^= 1u << s;
   }
   // the commits of the last two chunks (each covers every earlier MMA)
   for (int c = max(0, nch - 2); c < nch; ++c) {
@@ -1174,11 +1197,14 @@ __global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict_
   if (__syncthreads_or(bad)) {
     if (tid == 0) atomicExch(err, 3);
   } else {
-    // epilogue: warp w reads TMEM lanes 32w .. 32w+31 (points p0+32w+lane)
-    const long pp = p0 + 32 * warp + lane;
-    for (int c0 = 0; c0 < ncol; c0 += 16) {
+    // epilogue: lanes 32 (w % 4) + lane = points, columns of half w / 4
+    const int q4 = warp & 3, hw = warp >> 2;
+    const int row = 32 * q4 + lane;
+    const long pp = p0 + row;
+    const int cbeg = hw * (ncol / 2), cend = cbeg + ncol / 2;  // ncol / 2 is a multiple of 8
+    for (int c0 = cbeg; c0 < cend; c0 += 16) {
       uint32_t r[16];
-      const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+      const uint32_t ta = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)c0;
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
           : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
@@ -1186,17 +1212,19 @@ __global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict_
           : "r"(ta)
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (pp < P) {
+      if (row < np) {
+        const int j0 = c0 / 2, jn = min(8, min(nw, cend / 2) - j0);
+        double2 f[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int jw = c0 / 2 + j;
-          if (jw >= nw) break;
-          double2* q = fd + (long)(g * TC_NW + jw) * P + pp;
-          double2 f = *q;
-          f.x += (double)__uint_as_float(r[2 * j]);
-          f.y += (double)__uint_as_float(r[2 * j + 1]);
-          *q = f;
-        }
+        for (int j = 0; j < 8; ++j)
+          if (j < jn) f[j] = fd[(long)(g * TC_NW + j0 + j) * P + pp];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (j < jn) {
+            f[j].x += (double)__uint_as_float(r[2 * j]);
+            f[j].y += (double)__uint_as_float(r[2 * j + 1]);
+            fd[(long)(g * TC_NW + j0 + j) * P + pp] = f[j];
+          }
       }
     }
   }
