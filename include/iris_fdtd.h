@@ -227,6 +227,17 @@ int iris_get_pml(iris_engine* eng, int which, int slab, double* re, double* im);
 int iris_set_pml(iris_engine* eng, int which, int slab, const double* re, const double* im);
 
 /*
+ * One plane of E or H extracted on the device, for the SDL snapshots of
+ * SDL_output (code/sdl.f90:68-234): axis 1, 2, 3 = the plane x, y, z = index;
+ * the two in-plane coordinates run over [lo1, hi1] x [lo2, hi2] (y, z for
+ * axis 1; x, z for axis 2; x, y for axis 3), ghost cells 0 and n+1 allowed.
+ * re/im receive 3 * n1 * n2 values, component fastest, then the first
+ * in-plane coordinate.
+ */
+int iris_get_plane(iris_engine* eng, int which, int axis, int index, int lo1, int hi1, int lo2, int hi2,
+                   double* re, double* im);
+
+/*
  * DFT accumulator emg(j)%fdata(i_pts, iw) of box (0/1) and face pair
  * j (1..3) in the reference order, i_pts fastest
  * (code/dataprocess.f90:109-209); *npts receives the point count.

@@ -203,6 +203,15 @@ class Engine:
         re, im = np.ascontiguousarray(a.real), np.ascontiguousarray(a.imag)
         check(self.L.iris_set_pml(self.h, which, slab, _dp(re), _dp(im)), "iris_set_pml")
 
+    def get_plane(self, which: int, axis: int, index: int, r1, r2) -> np.ndarray:
+        """One plane (axis 1, 2, 3 = x, y, z = index) over the in-plane ranges
+        r1 = (lo, hi), r2 = (lo, hi), as complex [i2, i1, component]."""
+        n1, n2 = r1[1] - r1[0] + 1, r2[1] - r2[0] + 1
+        re, im = np.empty(3 * n1 * n2), np.empty(3 * n1 * n2)
+        check(self.L.iris_get_plane(self.h, which, axis, index, r1[0], r1[1], r2[0], r2[1], _dp(re), _dp(im)),
+              "iris_get_plane")
+        return (re + 1j * im).reshape(n2, n1, 3)
+
     # -- instrumentation
     KERNELS = ("update_e", "update_h", "tfsf", "dft_gather", "dft_block", "flux", "fused_eh")
 

@@ -1234,6 +1234,19 @@ __global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict_
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_NMAX) : "memory");
 }
 
+// One plane of a field (SDL snapshots): out[(i2 * n1 + i1) * 3 + k].
+template <typename T>
+__global__ void k_plane(const typename V2<T>::t* __restrict__ f, Geo g, int axis, int index, int lo1, int n1, int lo2,
+                        int n2, double2* __restrict__ out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3L * n1 * n2) return;
+  const int k = (int)(t % 3), i1 = (int)((t / 3) % n1), i2 = (int)(t / (3L * n1));
+  const int a = lo1 + i1, b = lo2 + i2;
+  const long i = axis == 1 ? g.at(index, a, b) : axis == 2 ? g.at(a, index, b) : g.at(a, b, index);
+  const typename V2<T>::t v = f[k * g.comp + i];
+  out[t] = make_double2((double)v.x, (double)v.y);
+}
+
 // Poynting flux of one face, code/dataprocess.f90:246-277:
 // J = sign * sum Re(a*conj(b) - c*conj(d)) * eps0*Q/(2 dt).
 struct FluxFace {
@@ -2546,6 +2559,39 @@ int iris_set_pml(iris_engine* E, int which, int slab, const double* re, const do
   clear_error();
   if (!re || !im) return fail(IRIS_EINVAL, "null buffer");
   return pml_io(E, which, slab, nullptr, nullptr, re, im);
+}
+
+int iris_get_plane(iris_engine* E, int which, int axis, int index, int lo1, int hi1, int lo2, int hi2, double* re,
+                   double* im) {
+  clear_error();
+  if (!E || !re || !im || (which != IRIS_E && which != IRIS_H) || axis < 1 || axis > 3)
+    return fail(IRIS_EINVAL, "bad argument");
+  const int n[3] = {E->p.nx, E->p.ny, E->p.nz};
+  const int ax1 = axis == 1 ? 1 : 0, ax2 = axis == 3 ? 1 : 2;
+  if (index < 0 || index > n[axis - 1] + 1 || lo1 < 0 || hi1 > n[ax1] + 1 || lo1 > hi1 || lo2 < 0 ||
+      hi2 > n[ax2] + 1 || lo2 > hi2)
+    return fail(IRIS_EINVAL, "plane outside the grid (ghost cells 0..n+1 included)");
+  CK(cudaSetDevice(E->device));
+  const int n1 = hi1 - lo1 + 1, n2 = hi2 - lo2 + 1;
+  const long m = 3L * n1 * n2;
+  double2* d = nullptr;
+  CK(cudaMalloc(&d, sizeof(double2) * m));
+  const void* f = which == IRIS_E ? E->e : E->h;
+  const unsigned nb = (unsigned)((m + 255) / 256);
+  if (E->prec == IRIS_FP64)
+    k_plane<double><<<nb, 256, 0, E->st>>>((const double2*)f, E->g, axis, index, lo1, n1, lo2, n2, d);
+  else
+    k_plane<float><<<nb, 256, 0, E->st>>>((const float2*)f, E->g, axis, index, lo1, n1, lo2, n2, d);
+  std::vector<double2> h((size_t)m);
+  cudaError_t e1 = cudaMemcpyAsync(h.data(), d, sizeof(double2) * m, cudaMemcpyDeviceToHost, E->st);
+  cudaError_t e2 = cudaStreamSynchronize(E->st);
+  cudaFree(d);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) return fail(IRIS_ECUDA, "plane extraction failed");
+  for (long q = 0; q < m; ++q) {
+    re[q] = h[q].x;
+    im[q] = h[q].y;
+  }
+  return IRIS_OK;
 }
 
 int iris_get_fdata(iris_engine* E, int box, int j, double* re, double* im, long* npts) {

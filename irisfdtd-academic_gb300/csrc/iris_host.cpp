@@ -4,6 +4,7 @@
 #include <cerrno>
 #include <cmath>
 #include <complex>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -344,6 +345,189 @@ void write_film_spectrum(const std::string& dir, const iris_params& p) {
   std::fclose(f);
 }
 
+// ---------------------------------------------------------------------------
+// SDL field snapshots (code/sdl.f90): the parameters of setparam_SDL
+// (:365-400) and of the optional "Extra parameters-SDLextended" section
+// (code/files.f90:291-320), and SDL_output's files (:68-234).
+
+struct SdlParams {
+  int copy_flag = 0, copy_no = 1;
+  int xi[3] = {}, xf[3] = {}, yi[3] = {}, yf[3] = {}, zi[3] = {}, zf[3] = {};
+  int module_e = 0;     // 1: |E| from E, 2: |H| from the previous step's H
+  int field[6] = {};    // Ex Ey Ez Hx Hy Hz: 1 Re, 2 Im, 3 modulus, 4 |Re|, 5 |Im|
+  std::vector<int> delta[3] = {{0}, {0}, {0}};  // extra layers per plane
+  bool extended() const { return delta[0].size() != 1 || delta[1].size() != 1 || delta[2].size() != 1; }
+  bool wants_e() const { return module_e == 1 || field[0] >= 1 || field[1] >= 1 || field[2] >= 1; }
+  bool wants_h() const { return module_e == 2 || field[3] >= 1 || field[4] >= 1 || field[5] >= 1; }
+};
+
+int read_sdl(const std::string& path, SdlParams& q) {
+  std::ifstream in(path);
+  std::vector<std::string> lines;
+  for (std::string l; std::getline(in, l);) lines.push_back(l);
+  ListReader R(lines);
+  std::vector<Tok> t;
+  auto seek = [&](const char* header) {
+    R.rewind();
+    while (!R.eof()) {
+      if (!R.read(1, t)) return false;
+      if (t[0].text == header) return true;
+    }
+    return false;
+  };
+  auto perr = [](const std::string& m) { return fail(IRIS_EPARSE, "invalid SDL section: " + m); };
+  if (!seek("Time evolution options")) return perr("no 'Time evolution options'");
+  if (!R.read(2, t) || !to_int(t[0], q.copy_flag) || !to_int(t[1], q.copy_no)) return perr("SDL_copy_flag");
+  int* rows[6] = {q.xi, q.xf, q.yi, q.yf, q.zi, q.zf};
+  for (int r = 0; r < 6; ++r)
+    if (!R.read(3, t) || !to_int(t[0], rows[r][0]) || !to_int(t[1], rows[r][1]) || !to_int(t[2], rows[r][2]))
+      return perr("plane ranges");
+  if (!R.read(1, t) || !to_int(t[0], q.module_e)) return perr("SDLModuleE");
+  for (int k = 0; k < 6; ++k)
+    if (!R.read(1, t) || !to_int(t[0], q.field[k])) return perr("SDLField");
+  if (seek("Extra parameters-SDLextended")) {
+    int n[3];
+    if (!R.read(3, t) || !to_int(t[0], n[0]) || !to_int(t[1], n[1]) || !to_int(t[2], n[2])) return perr("extra layers");
+    for (int a = 0; a < 3; ++a) {
+      if (n[a] < 1) return perr("extra layers must be >= 1");
+      q.delta[a].assign(n[a], 0);
+      for (int i = 0; i < n[a]; ++i)
+        if (!R.read(1, t) || !to_int(t[0], q.delta[a][i])) return perr("layer offsets");
+    }
+  }
+  if (q.copy_flag && q.copy_no < 1) return perr("SDL_copy_no");
+  return IRIS_OK;
+}
+
+// inttoASCII (code/common.f90:40-101): plain decimal digits
+std::string sdl_number(int n) { return std::to_string(n); }
+
+// One plane request: layer 1, 2, 3 (x, y, z = const), its index and ranges.
+struct SdlPlane {
+  int layer, index, lo1, hi1, lo2, hi2;
+};
+
+std::vector<SdlPlane> sdl_planes(const iris_params& p, const SdlParams& q) {
+  std::vector<SdlPlane> out;
+  for (int l = 1; l <= 3; ++l) {
+    if (!p.sdl_plane_on[l - 1]) continue;
+    for (int d : q.delta[l - 1]) {
+      const int j = l - 1;
+      if (l == 1) out.push_back({1, q.xi[j] + d, q.yi[j], q.yf[j], q.zi[j], q.zf[j]});
+      if (l == 2) out.push_back({2, q.yi[j] + d, q.xi[j], q.xf[j], q.zi[j], q.zf[j]});
+      if (l == 3) out.push_back({3, q.zi[j] + d, q.xi[j], q.xf[j], q.yi[j], q.yf[j]});
+    }
+  }
+  return out;
+}
+
+// One Fortran unformatted sequential record of REAL(4) values.
+int write_record(const std::string& path, const std::vector<float>& v) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) return fail(IRIS_EIO, "cannot write " + path);
+  const uint32_t n = (uint32_t)(v.size() * 4);
+  bool ok = std::fwrite(&n, 4, 1, f) == 1;
+  ok = ok && (v.empty() || std::fwrite(v.data(), 4, v.size(), f) == v.size());
+  ok = ok && std::fwrite(&n, 4, 1, f) == 1;
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? IRIS_OK : fail(IRIS_EIO, "write failed: " + path);
+}
+
+// SDL_output for one plane and one quantity: em 0 (modulus of all three
+// components), 1 (a component of E), 2 (a component of H); comp 0..2; the
+// plane's values re/im (component fastest) as iris_get_plane returns them.
+int sdl_output(const std::string& dir, const iris_params& p, const SdlParams& q, const SdlPlane& pl, int nos, int em,
+               int comp, int mode, bool module_h, const std::vector<double>& re, const std::vector<double>& im) {
+  const int n1 = pl.hi1 - pl.lo1 + 1, n2 = pl.hi2 - pl.lo2 + 1;
+  std::string ext, ext2;
+  if (em == 0) {
+    ext = ".e";
+    ext2 = module_h ? "_H" : "_E";
+  } else {
+    ext = std::string(em == 1 ? ".e" : ".h") + char('1' + comp);
+    static const char* m[6] = {"", "_R", "_I", "_MC", "_MR", "_MI"};
+    ext2 = mode >= 1 && mode <= 5 ? m[mode] : "";
+  }
+  static const char* axis_name[4] = {"", "X", "Y", "Z"};
+  std::string name = std::string("/") + axis_name[pl.layer] + "_SDL";
+  if (q.extended()) name += sdl_number(pl.index) + "layer";
+  name += ext2 + sdl_number(nos) + ext;
+  // Output(i1, i2), i1 fastest; values / (q * Epump) (the TF/SF amplitude)
+  double norm = p.Q * p.epump;
+  if (norm == 0.0) norm = 1.0;
+  std::vector<double> out((size_t)n1 * n2);
+  for (int b = 0; b < n2; ++b)
+    for (int a = 0; a < n1; ++a) {
+      const size_t c = (size_t)b * n1 + a;
+      double v = 0.0;
+      if (em == 0) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s += re[3 * c + k] * re[3 * c + k] + im[3 * c + k] * im[3 * c + k];
+        v = std::sqrt(s);
+      } else {
+        const double r = re[3 * c + comp], i = im[3 * c + comp];
+        switch (mode) {
+          case 1: v = r; break;
+          case 2: v = i; break;
+          case 3: v = std::sqrt(r * r + i * i); break;
+          case 4: v = std::sqrt(r * r); break;
+          case 5: v = std::sqrt(i * i); break;
+          default: v = 0.0;
+        }
+      }
+      out[c] = v / norm;
+    }
+  std::vector<float> rec;
+  if (q.copy_flag) {
+    // output_aux(ixo : copies*(ixf+1-ixo), iyo : ...) filled at ix + i*(ixf+1-ixo)
+    // (and, for z planes, iy + j*(iyf+1-iyo)); cells the copies do not reach
+    // (lower bounds below 1) are left 0 here
+    const int c1 = q.copy_no, c2 = pl.layer == 3 ? q.copy_no : 1;
+    const int m1 = c1 * (pl.hi1 + 1 - pl.lo1) - pl.lo1 + 1, m2 = pl.layer == 3 ? c2 * (pl.hi2 + 1 - pl.lo2) - pl.lo2 + 1 : n2;
+    rec.assign((size_t)std::max(m1, 0) * std::max(m2, 0), 0.0f);
+    for (int j = 0; j < c2; ++j)
+      for (int i = 0; i < c1; ++i)
+        for (int b = 0; b < n2; ++b)
+          for (int a = 0; a < n1; ++a) {
+            const int x = a + i * n1, y = b + j * n2;  // offsets from (lo1, lo2)
+            if (x < m1 && y < m2) rec[(size_t)y * m1 + x] = (float)out[(size_t)b * n1 + a];
+          }
+  } else {
+    rec.assign(out.begin(), out.end());
+  }
+  return write_record(dir + name, rec);
+}
+
+// setSDL_FILE (code/sdl.f90:404-448) for one plane: E quantities from e (the
+// current E), H quantities from h (the H of the step before).
+int sdl_files(const std::string& dir, const iris_params& p, const SdlParams& q, const SdlPlane& pl, int nos,
+              const std::vector<double>& ere, const std::vector<double>& eim, const std::vector<double>& hre,
+              const std::vector<double>& him) {
+  int rc = IRIS_OK;
+  if (q.module_e == 1) rc = sdl_output(dir, p, q, pl, nos, 0, 0, 0, false, ere, eim);
+  if (!rc && q.module_e == 2) rc = sdl_output(dir, p, q, pl, nos, 0, 0, 0, true, hre, him);
+  for (int k = 0; k < 3 && !rc; ++k)
+    if (q.field[k] >= 1) rc = sdl_output(dir, p, q, pl, nos, 1, k, q.field[k], false, ere, eim);
+  for (int k = 0; k < 3 && !rc; ++k)
+    if (q.field[3 + k] >= 1) rc = sdl_output(dir, p, q, pl, nos, 2, k, q.field[3 + k], false, hre, him);
+  return rc;
+}
+
+int get_planes(iris_engine* eng, int which, const std::vector<SdlPlane>& pls, std::vector<std::vector<double>>& re,
+               std::vector<std::vector<double>>& im) {
+  re.resize(pls.size());
+  im.resize(pls.size());
+  for (size_t i = 0; i < pls.size(); ++i) {
+    const SdlPlane& pl = pls[i];
+    const size_t m = 3 * (size_t)(pl.hi1 - pl.lo1 + 1) * (pl.hi2 - pl.lo2 + 1);
+    re[i].resize(m);
+    im[i].resize(m);
+    int rc = iris_get_plane(eng, which, pl.layer, pl.index, pl.lo1, pl.hi1, pl.lo2, pl.hi2, re[i].data(), im[i].data());
+    if (rc) return rc;
+  }
+  return IRIS_OK;
+}
+
 // main() + driver(), code/main.f90:43-213 and code/driver.f90:66-555
 int run_main(const std::string& dir, int precision) {
   iris_params p;
@@ -364,6 +548,18 @@ int run_main(const std::string& dir, int precision) {
   std::fprintf(log, "# pmlzi=%d pmlzf=%d hi=%d hf=%d aix=%d afx=%d\n", p.pmlzi, p.pmlzf, p.hi, p.hf, p.aix, p.afx);
   std::fprintf(log, "# precision=%s\n", precision == IRIS_FP64 ? "fp64" : "fp32");
   write_film_spectrum(dir, p);
+  const bool sdl_on = p.sdl_plane_on[0] || p.sdl_plane_on[1] || p.sdl_plane_on[2];
+  SdlParams sdl;
+  std::vector<SdlPlane> planes;
+  if (sdl_on) {
+    rc = read_sdl(dir + "/inputFDTD.dat", sdl);
+    if (rc) { std::fclose(log); return rc; }
+    planes = sdl_planes(p, sdl);
+    std::fprintf(log, "#SDL planes=%d (x %d, y %d, z %d)\n", (int)planes.size(), p.sdl_plane_on[0], p.sdl_plane_on[1],
+                 p.sdl_plane_on[2]);
+  }
+  const bool sdl_h = sdl_on && sdl.wants_h();
+  std::vector<std::vector<double>> ere, eim, hre, him;
   iris_engine* eng = nullptr;
   rc = iris_create(&p, fw.data(), &eng);
   if (rc) { std::fclose(log); return rc; }
@@ -379,9 +575,23 @@ int run_main(const std::string& dir, int precision) {
     if (p.to_fourier + p.no_downloads * nos >= it && p.to_fourier + p.no_downloads * nos < next)
       next = p.to_fourier + p.no_downloads * nos;
     if (next < it) next = it;
-    rc = iris_step(eng, it, next - it + 1);
+    const bool output = next >= p.to_fourier && (next == p.to_fourier + p.no_downloads * nos || next == p.texit);
+    if (output && sdl_h) {
+      // the SDL's H is h_prev: the H of the step before the output step
+      if (next > it) rc = iris_step(eng, it, next - it);
+      if (!rc) rc = get_planes(eng, IRIS_H, planes, hre, him);
+      if (!rc) rc = iris_step(eng, next, 1);
+    } else {
+      rc = iris_step(eng, it, next - it + 1);
+    }
     if (rc) break;
     it = next;
+    if (output && sdl_on) {
+      rc = get_planes(eng, IRIS_E, planes, ere, eim);
+      for (size_t i = 0; i < planes.size() && !rc; ++i)
+        rc = sdl_files(dir, p, sdl, planes[i], nos, ere[i], eim[i], sdl_h ? hre[i] : ere[i], sdl_h ? him[i] : eim[i]);
+      if (rc) break;
+    }
     if (it >= p.to_fourier && (it == p.to_fourier + p.no_downloads * nos || it == p.texit)) {
       rc = iris_flux(eng, 0, J.data());
       if (rc == IRIS_OK || rc == IRIS_ENAN) rc = iris_write_scatt(dir.c_str(), 0, it, p.nof, J.data()) ? IRIS_EIO : rc;

@@ -99,7 +99,7 @@ EXPORTS = [
     "iris_strerror", "iris_last_error", "iris_setparam", "iris_physconsts", "iris_frequencies",
     "iris_create", "iris_destroy", "iris_set_material", "iris_step", "iris_sync", "iris_flux",
     "iris_write_scatt", "iris_get_field", "iris_set_field", "iris_get_pml", "iris_set_pml",
-    "iris_get_fdata", "iris_apply", "iris_run_input", "iris_timing", "iris_timing_read", "iris_info",
+    "iris_get_fdata", "iris_get_plane", "iris_apply", "iris_run_input", "iris_timing", "iris_timing_read", "iris_info",
     "iris_dft_block_noalloc", "iris_batch_create", "iris_batch_destroy", "iris_batch_set_material",
     "iris_batch_step", "iris_batch_flux", "iris_batch_get_field", "iris_batch_tune", "iris_batch_set_tile",
     "iris_batch_timing", "iris_batch_timing_read", "iris_batch_info",
@@ -142,6 +142,7 @@ def lib():
     L.iris_get_pml.argtypes = [vp, ip, ip, dp, dp]
     L.iris_set_pml.argtypes = [vp, ip, ip, dp, dp]
     L.iris_get_fdata.argtypes = [vp, ip, ip, dp, dp, ctypes.POINTER(ctypes.c_long)]
+    L.iris_get_plane.argtypes = [vp, ip, ip, ip, ip, ip, ip, ip, dp, dp]
     L.iris_apply.argtypes = [vp, ip, ip]
     L.iris_run_input.argtypes = [cp, ip]
     L.iris_timing.argtypes = [vp, ip]
