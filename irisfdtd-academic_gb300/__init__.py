@@ -49,6 +49,16 @@ def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
+def _split_material(eps_inv):
+    """(re, im) float64 C-contiguous arrays; im None for a real material (a
+    real array is passed on without a copy)."""
+    a = np.asarray(eps_inv)
+    if not np.iscomplexobj(a):
+        return np.ascontiguousarray(a, dtype=np.float64), None
+    im = np.ascontiguousarray(a.imag, dtype=np.float64)
+    return np.ascontiguousarray(a.real, dtype=np.float64), (im if np.any(im) else None)
+
+
 def physconsts(single_literals: bool = True) -> IrisParams:
     p = IrisParams()
     lib().iris_physconsts(ctypes.byref(p), 1 if single_literals else 0)
@@ -144,14 +154,13 @@ class Engine:
 
     # -- material
     def set_material(self, eps_inv: np.ndarray):
-        a = np.asarray(eps_inv, dtype=np.complex128)
+        """eps_inv over (hi-1:hf+1, 0:ny+1, 0:nx+1) as [z, y, x], real or complex."""
         p = self.p
         want = (p.hf - p.hi + 3, p.ny + 2, p.nx + 2)
-        if a.shape != want:
-            raise ValueError(f"eps_inv shape {a.shape} != {want}")
-        re = np.ascontiguousarray(a.real)
-        im = np.ascontiguousarray(a.imag)
-        check(self.L.iris_set_material(self.h, _dp(re), _dp(im) if np.any(im) else None), "iris_set_material")
+        if np.shape(eps_inv) != want:
+            raise ValueError(f"eps_inv shape {np.shape(eps_inv)} != {want}")
+        re, im = _split_material(eps_inv)
+        check(self.L.iris_set_material(self.h, _dp(re), _dp(im) if im is not None else None), "iris_set_material")
 
     # -- stepping
     def step(self, it0: int, n: int):
@@ -283,9 +292,8 @@ class Batch:
             pass
 
     def set_material(self, cell: int, eps_inv: np.ndarray):
-        a = np.asarray(eps_inv, dtype=np.complex128)
-        re, im = np.ascontiguousarray(a.real), np.ascontiguousarray(a.imag)
-        check(self.L.iris_batch_set_material(self.h, cell, _dp(re), _dp(im) if np.any(im) else None),
+        re, im = _split_material(eps_inv)
+        check(self.L.iris_batch_set_material(self.h, cell, _dp(re), _dp(im) if im is not None else None),
               "iris_batch_set_material")
 
     def step(self, it0: int, n: int):

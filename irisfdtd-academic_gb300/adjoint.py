@@ -70,14 +70,14 @@ class Adjoint:
             pass
 
     def set_material(self, eps_inv: np.ndarray):
-        a = np.asarray(eps_inv, dtype=np.complex128)
+        from . import _split_material
+
         p = self.p
         want = (p.hf - p.hi + 3, p.ny + 2, p.nx + 2)
-        if a.shape != want:
-            raise ValueError(f"eps_inv shape {a.shape} != {want}")
-        re = np.ascontiguousarray(a.real)
-        im = np.ascontiguousarray(a.imag)
-        check(self.L.iris_adjoint_set_material(self.h, _dp(re), _dp(im) if np.any(im) else None),
+        if np.shape(eps_inv) != want:
+            raise ValueError(f"eps_inv shape {np.shape(eps_inv)} != {want}")
+        re, im = _split_material(eps_inv)
+        check(self.L.iris_adjoint_set_material(self.h, _dp(re), _dp(im) if im is not None else None),
               "iris_adjoint_set_material")
 
     def set_design(self, eps_inv: np.ndarray):

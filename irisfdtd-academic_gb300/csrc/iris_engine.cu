@@ -1247,6 +1247,38 @@ __global__ void k_plane(const typename V2<T>::t* __restrict__ f, Geo g, int axis
   out[t] = make_double2((double)v.x, (double)v.y);
 }
 
+// Structure material into the padded layout: planes hi..hf of eps_inv given
+// over (hi-1:hf+1, 0:ny+1, 0:nx+1) as re/im (im may be null), or, with
+// re == null, the default of set_emconstants and slit() (code/mesh.f90:57-109):
+// 1/eps_bbox (vr, vi) with the slit columns aix..afx set to 1.
+template <typename T>
+__global__ void k_material(const double* __restrict__ re, const double* __restrict__ im, Geo g, int nzs, double vr,
+                           double vi, int aix, int afx, T* __restrict__ out_r, typename V2<T>::t* __restrict__ out_c) {
+  const long nx2 = g.nx + 2, nxy = nx2 * (g.ny + 2);
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nxy * nzs) return;
+  const int zz = (int)(t / nxy);
+  const long r = t % nxy;
+  const int y = (int)(r / nx2), x = (int)(r % nx2);
+  double a = vr, b = vi;
+  if (re) {
+    a = re[t];
+    b = im ? im[t] : 0.0;
+  } else if (x >= aix && x <= afx) {
+    a = 1.0;
+    b = 0.0;
+  }
+  const long dst = (long)zz * g.plane + (long)y * g.pitch + (x + g.xo);
+  if (out_c) {
+    typename V2<T>::t v;
+    v.x = (T)a;
+    v.y = (T)b;
+    out_c[dst] = v;
+  } else {
+    out_r[dst] = (T)a;
+  }
+}
+
 // Poynting flux of one face, code/dataprocess.f90:246-277:
 // J = sign * sum Re(a*conj(b) - c*conj(d)) * eps0*Q/(2 dt).
 struct FluxFace {
@@ -2039,14 +2071,13 @@ template <typename T> int step_t(iris_engine* E, int it0, int n) {
   return IRIS_OK;
 }
 
-// Reference material of set_emconstants() and slit() (code/mesh.f90:57-109)
-// over (0:nx+1, 0:ny+1, hi-1:hf+1), x fastest.
-void default_material(const iris_params& p, std::vector<double>& re, std::vector<double>& im) {
+int upload_material(iris_engine* E, const double* re, const double* im) {
+  const iris_params& p = E->p;
+  graph_reset(E);  // captured launches hold the old material pointer
+  const Geo& g = E->g;
+  const int nzs = p.hf - p.hi + 1;  // planes stored: hi..hf
   const long nxy = (long)(p.nx + 2) * (p.ny + 2);
-  const int nzs = p.hf - p.hi + 3;
-  re.assign(nxy * nzs, 0.0);
-  im.assign(nxy * nzs, 0.0);
-  // 1.0/eps_bbox as a complex division (Smith's algorithm)
+  // 1/eps_bbox as a complex division (Smith's algorithm), for the default
   double c = p.eps_bbox_re, d = p.eps_bbox_im, ir, ii;
   if (std::fabs(c) >= std::fabs(d)) {
     const double r = d / c, den = c + d * r;
@@ -2057,54 +2088,45 @@ void default_material(const iris_params& p, std::vector<double>& re, std::vector
     ir = (1.0 * r + 0.0) / den;
     ii = (0.0 * r - 1.0) / den;
   }
-  for (long i = 0; i < nxy * nzs; ++i) { re[i] = ir; im[i] = ii; }
-  for (long i = 0; i < nxy; ++i) {
-    re[i] = 1.0 / p.eps1; im[i] = 0.0;
-    re[(long)(nzs - 1) * nxy + i] = 1.0 / p.eps3; im[(long)(nzs - 1) * nxy + i] = 0.0;
-  }
-  for (int z = p.hi; z <= p.hf; ++z)
-    for (int y = 0; y <= p.ny + 1; ++y)
-      for (int x = p.aix; x <= p.afx; ++x) {
-        const long i = (long)(z - (p.hi - 1)) * nxy + (long)y * (p.nx + 2) + x;
-        re[i] = 1.0;
-        im[i] = 0.0;
-      }
-}
-
-int upload_material(iris_engine* E, const double* re, const double* im) {
-  const iris_params& p = E->p;
-  graph_reset(E);  // captured launches hold the old material pointer
-  const Geo& g = E->g;
-  const int nzs = p.hf - p.hi + 1;  // planes stored: hi..hf
   bool cplx = false;
-  const long nxy = (long)(p.nx + 2) * (p.ny + 2);
-  if (im)
-    for (long i = nxy; i < nxy * (nzs + 1); ++i)
-      if (im[i] != 0.0) { cplx = true; break; }
+  if (re) {
+    if (im)
+      for (long i = nxy; i < nxy * (nzs + 1); ++i)
+        if (im[i] != 0.0) { cplx = true; break; }
+  } else {
+    cplx = ii != 0.0;
+  }
   if (E->eps) { cudaFree(E->eps); E->eps = nullptr; }
   if (nzs <= 0) { E->eps_complex = false; return IRIS_OK; }
   const long n = (long)nzs * g.plane;
   const size_t rsz = E->prec == IRIS_FP64 ? 8 : 4;
   const size_t bytes = (size_t)n * rsz * (cplx ? 2 : 1);
-  std::vector<unsigned char> host(bytes, 0);
-  for (int zz = 0; zz < nzs; ++zz)
-    for (int y = 0; y <= p.ny + 1; ++y)
-      for (int x = 0; x <= p.nx + 1; ++x) {
-        const long src = (long)(zz + 1) * nxy + (long)y * (p.nx + 2) + x;
-        const long dst = (long)zz * g.plane + (long)y * g.pitch + (x + g.xo);
-        const double vr = re[src], vi = im ? im[src] : 0.0;
-        if (E->prec == IRIS_FP64) {
-          double* h = (double*)host.data();
-          if (cplx) { h[2 * dst] = vr; h[2 * dst + 1] = vi; }
-          else h[dst] = vr;
-        } else {
-          float* h = (float*)host.data();
-          if (cplx) { h[2 * dst] = (float)vr; h[2 * dst + 1] = (float)vi; }
-          else h[dst] = (float)vr;
-        }
-      }
   CK(cudaMalloc(&E->eps, bytes));
-  CK(cudaMemcpy(E->eps, host.data(), bytes, cudaMemcpyHostToDevice));
+  CK(cudaMemsetAsync(E->eps, 0, bytes, E->st));
+  double* dre = nullptr;
+  double* dim = nullptr;
+  const size_t vb = sizeof(double) * (size_t)nxy * nzs;
+  if (re) {
+    // planes hi..hf of the host array (its plane 0 is hi-1)
+    CK(cudaMalloc(&dre, vb));
+    CK(cudaMemcpyAsync(dre, re + nxy, vb, cudaMemcpyHostToDevice, E->st));
+    if (cplx) {
+      CK(cudaMalloc(&dim, vb));
+      CK(cudaMemcpyAsync(dim, im + nxy, vb, cudaMemcpyHostToDevice, E->st));
+    }
+  }
+  const unsigned nb = (unsigned)((nxy * nzs + 255) / 256);
+  if (E->prec == IRIS_FP64)
+    k_material<double><<<nb, 256, 0, E->st>>>(dre, dim, g, nzs, ir, ii, p.aix, p.afx,
+                                               cplx ? nullptr : (double*)E->eps, cplx ? (double2*)E->eps : nullptr);
+  else
+    k_material<float><<<nb, 256, 0, E->st>>>(dre, dim, g, nzs, ir, ii, p.aix, p.afx,
+                                              cplx ? nullptr : (float*)E->eps, cplx ? (float2*)E->eps : nullptr);
+  const cudaError_t e1 = cudaGetLastError();
+  const cudaError_t e2 = cudaStreamSynchronize(E->st);
+  if (dre) cudaFree(dre);
+  if (dim) cudaFree(dim);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) return fail(IRIS_ECUDA, "material upload failed");
   E->eps_complex = cplx;
   return IRIS_OK;
 }
@@ -2378,12 +2400,8 @@ static int create_engine(const iris_params* pin, const double* fw, bool member, 
       return bail(fail(IRIS_ECUDA, "streamed stencil: shared memory opt-in failed"));
     E->sgrd = dim3((p.nx + SX - 1) / SX, (p.ny + SY - 1) / SY, (p.nz + SZC - 1) / SZC);
   }
-  {
-    std::vector<double> re, im;
-    default_material(p, re, im);
-    rc = upload_material(E, re.data(), im.data());
-    if (rc) return bail(rc);
-  }
+  rc = upload_material(E, nullptr, nullptr);  // the reference's default material
+  if (rc) return bail(rc);
   rc = build_dft(E);
   if (rc) return bail(rc);
   if (cudaStreamSynchronize(E->st) != cudaSuccess) return bail(fail(IRIS_ECUDA, "initialisation failed"));
