@@ -132,12 +132,13 @@ typedef struct iris_params {
 #define IRIS_DFT_Z 1
 
 /* ---- stencil variants (iris_params.stencil) -------------------------- */
-/* default: the split passes (the faster variant on GB300 at present)      */
+/* default: the fused pass in IRIS_FP32 (the faster variant on GB300), the
+ * split passes in IRIS_FP64                                               */
 #define IRIS_STENCIL_DEFAULT 0
 /* separate in-place E and H passes (18 complex values per cell per step)  */
 #define IRIS_STENCIL_SPLIT 1
-/* one fused E+H pass over double-buffered fields (12 values per cell);
- * IRIS_FP32 only                                                          */
+/* one fused E+H pass over double-buffered fields (12 values per cell, twice
+ * the field memory); IRIS_FP32 only                                       */
 #define IRIS_STENCIL_FUSED 2
 /* the split passes with each plane staged in shared memory by bulk (TMA)
  * copies, z-marching tiles; IRIS_FP32 with a real material (a complex

@@ -1310,269 +1310,225 @@ __global__ void __launch_bounds__(256) k_flux(const double2* __restrict__ fd, lo
 }
 
 // ---------------------------------------------------------------------------
-// Fused E+H step (FP32 mode).
+// Fused E+H pass (FP32, IRIS_STENCIL_FUSED).
 //
-// One pass per time step over double-buffered fields: E_new and H_new from
-// E_old and H_old, so each field value is read once and written once per step
-// (12 complex values per cell instead of the 18 of separate E and H passes).
-// A CTA owns an FX x FY column tile and marches z over a chunk of planes.  At
-// plane z it first computes E_new(z+1) for its cells and for the one-cell
-// high halo (x = x0+FX column, y = y0+FY row) that H_new needs, exchanging
-// them through shared memory, then H_new(z).  Halo values are recomputed from
-// the old fields, never read from another CTA's output, so CTAs never wait on
-// each other; this is why E, H and the UPML auxiliary D are double buffered
-// here (B is only ever touched by its owner and stays in place).  The
-// reference's Bloch ghost planes of E become index mapping with a phase:
-// E_new at x = nx+1 is exp(i akx) E_new(1), and likewise for y and z.  TF/SF
-// corrections (FP64 values per x, from k_incident) are added as each plane is
-// written, H's ghosts at x = 0, y = 0, z = 0 (the only ghosts any operator
-// reads) are written with the reference's Bloch copy plus their own TF/SF
-// correction, and DFT face samples are stored straight from registers.
+// One pass per time step from (E, H, D) into double buffers (E', H', D'):
+// each field value is read once and written once per step (12 complex values
+// per cell instead of the split passes' 18).  A CTA is 16 warps; warp w holds
+// row y0 + w and lane l column x0 + l of a 32 x 16 tile, and the CTA marches z
+// over a chunk of planes.  At plane z every thread computes E'(z) of its cell
+// and H'(z-1) of the cell below it, so H' has E'(z-1) and E'(z) at hand: the
+// x neighbours come from the next / previous lane by warp shuffle, the y
+// neighbours from the next / previous warp through one shared-memory row
+// exchange per plane (one barrier).  Tiles overlap by one column and one row:
+// lane 31 and the last warp compute the E' that H' needs at +x / +y but write
+// nothing, so tiles advance by 31 x 15 and no CTA reads another's output.
+// Cells one past nx or ny, and plane nz+1, are the Bloch images of x = 1,
+// y = 1, z = 1: their threads compute E' at the image cell and apply the
+// phase.  TF/SF and the DFT sample follow as their own kernels on the new
+// buffers, as after the split passes.  B is touched only by its owner and
+// stays in place; D is double buffered because image and overlap threads
+// read the old D of cells another CTA owns.
 
-struct FusedSrc {
-  int zE, zH;  // planes of the E and H corrections (-1: none)
-  int cE, cH;  // corrected components
-  int sE, sH;  // +1 add, -1 subtract
-};
+constexpr int FZ_X = 32, FZ_Y = 16, FZ_OX = FZ_X - 1, FZ_OY = FZ_Y - 1;
 
-struct FusedFace {  // one face pair of one box, as accumulated by scattering_fourier
-  int active;
-  int lo[3], hi[3];  // box bounds in x, y, z
-  int nu;            // extent of the fast in-face axis
-  long base[2][6];   // first sample index per [side][component]
-};
-
-template <typename T> struct FusedArgs {
-  FieldArgs<T> f;  // the old state: f.e, f.h, f.pml_d (D old), f.pml_b (B, in place)
-  typename V2<T>::t* e_new;
-  typename V2<T>::t* h_new;
-  typename V2<T>::t* d_new[2];
-  const double2* inc;  // [2][nx+2]: E and H corrections per ix, FP64
-  FusedSrc src;
-  typename V2<T>::t* slot;  // DFT sample slot of this step, or null
-  int* tk;
-  int islot, t;
-  int nboxes;
-  FusedFace faces[2][3];
+struct FusedArgs {
+  FieldArgs<float> f;  // the old state: f.e, f.h, f.pml_d (D old), f.pml_b (B, in place)
+  float2* e_new;
+  float2* h_new;
+  float2* d_new[2];
   int zchunk;  // planes per CTA
 };
 
-constexpr int FX = 32, FY = 8;
-
-__device__ __forceinline__ void corr_f(cx<float>& v, double2 c, int sgn) {
-  if (sgn > 0) { v.re = (float)((double)v.re + c.x); v.im = (float)((double)v.im + c.y); }
-  else { v.re = (float)((double)v.re - c.x); v.im = (float)((double)v.im - c.y); }
+__device__ __forceinline__ cx<float> shfl_cx(cx<float> v, int d, bool up) {
+  cx<float> r;
+  r.re = up ? __shfl_up_sync(0xffffffffu, v.re, d) : __shfl_down_sync(0xffffffffu, v.re, d);
+  r.im = up ? __shfl_up_sync(0xffffffffu, v.im, d) : __shfl_down_sync(0xffffffffu, v.im, d);
+  return r;
 }
 
-// Store the six samples of cell (x, y, z) for every face (pair) it lies on.
-__device__ __forceinline__ void dft_store(const FusedArgs<float>& a, int x, int y, int z, const cx<float> e[3],
-                                          const cx<float> h[3]) {
-  for (int b = 0; b < a.nboxes; ++b)
+template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(FusedArgs A) {
+  const FieldArgs<float>& a = A.f;
+  const Geo& g = a.g;
+  // per row and plane parity: H(z) components 1, 3 and E'(z-1) components 1, 3
+  __shared__ float2 xr[2][FZ_Y][4][FZ_X];
+  const int lane = threadIdx.x, w = threadIdx.y;
+  const int x = 1 + blockIdx.x * FZ_OX + lane, y = 1 + blockIdx.y * FZ_OY + w;
+  const int z0 = 1 + blockIdx.z * A.zchunk, z1 = min(z0 + A.zchunk - 1, g.nz);
+  const bool act = x <= g.nx + 1 && y <= g.ny + 1;
+  const bool ximg = x == g.nx + 1, yimg = y == g.ny + 1;
+  const int cxx = ximg ? 1 : x, cyy = yimg ? 1 : y;  // the cell whose E' this thread computes
+  const bool own = lane < FZ_OX && w < FZ_OY && x <= g.nx && y <= g.ny;
+  cx<float> ph = {1.f, 0.f};
+  if (ximg) ph = cmul(ph, a.pxp);
+  if (yimg) ph = cmul(ph, a.pyp);
+  const float2* E = a.e;
+  const float2* H = a.h;
+  auto ldc = [&](const float2* f, int k, int xx, int yy, int zz) {
+    return ld<float>(f + k * g.comp + g.at(xx, yy, zz));
+  };
+  const cx<float> zero = {0.f, 0.f};
+  // Carried from plane z-1 in this thread's own slots of the exchange rows
+  // (written there for the neighbours anyway): components 1, 3 of H(z-1) in
+  // rows of parity (z-1)&1 and of E'(z-1) in rows of parity z&1 (stored at
+  // the end of the previous plane); component 2 of both in registers.
+  cx<float> ep1 = zero, hp1 = act ? ldc(H, 1, cxx, cyy, z0 - 1) : zero;
+  {
+    const cx<float> h0 = act ? ldc(H, 0, cxx, cyy, z0 - 1) : zero, h2 = act ? ldc(H, 2, cxx, cyy, z0 - 1) : zero;
+    xr[(z0 - 1) & 1][w][0][lane] = make_float2(h0.re, h0.im);
+    xr[(z0 - 1) & 1][w][1][lane] = make_float2(h2.re, h2.im);
+    xr[z0 & 1][w][2][lane] = make_float2(0.f, 0.f);
+    xr[z0 & 1][w][3][lane] = make_float2(0.f, 0.f);
+  }
+  cx<float> en[3], hn_[3];  // E and H of the next plane, loaded one plane ahead
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      const FusedFace& F = a.faces[b][j];
-      if (!F.active) continue;
-      // normal axis j; in-face axes u (fast) and v: x faces (y, z), y faces (x, z), z faces (x, y)
-      const int cn = j == 0 ? x : (j == 1 ? y : z);
-      const int cu = j == 0 ? y : x, cv = j == 2 ? y : z;
-      const int lu = j == 0 ? F.lo[1] : F.lo[0], hu = j == 0 ? F.hi[1] : F.hi[0];
-      const int lv = j == 2 ? F.lo[1] : F.lo[2], hv = j == 2 ? F.hi[1] : F.hi[2];
-      const int ln = j == 0 ? F.lo[0] : (j == 1 ? F.lo[1] : F.lo[2]);
-      const int hn = j == 0 ? F.hi[0] : (j == 1 ? F.hi[1] : F.hi[2]);
-      if (cu < lu || cu > hu || cv < lv || cv > hv) continue;
-      const long L = (long)(cu - lu) + (long)F.nu * (cv - lv);
-      for (int side = 0; side < 2; ++side) {
-        if (cn != (side ? hn : ln)) continue;
+  for (int k = 0; k < 3; ++k) {
+    en[k] = act ? ldc(E, k, cxx, cyy, z0) : zero;
+    hn_[k] = act ? ldc(H, k, cxx, cyy, z0) : zero;
+  }
+  for (int z = z0; z <= z1 + 1; ++z) {
+    const int buf = z & 1;
+    const bool zimg = z == g.nz + 1;
+    const int cz = zimg ? 1 : z;
+    cx<float> e[3], h[3], hzm0, hzm1, ep[3], hp[3];
+    {
+      const float2 a0 = xr[buf ^ 1][w][0][lane], a2 = xr[buf ^ 1][w][1][lane];
+      const float2 b0 = xr[buf][w][2][lane], b2 = xr[buf][w][3][lane];
+      hp[0] = {a0.x, a0.y};
+      hp[1] = hp1;
+      hp[2] = {a2.x, a2.y};
+      ep[0] = {b0.x, b0.y};
+      ep[1] = ep1;
+      ep[2] = {b2.x, b2.y};
+    }
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          st<float>(a.slot + F.base[side][k] + L, e[k]);
-          st<float>(a.slot + F.base[side][k + 3] + L, h[k]);
+    for (int k = 0; k < 3; ++k) {
+      e[k] = en[k];
+      h[k] = hn_[k];
+    }
+    if (act && z + 1 <= z1 + 1) {
+      const int zn = z + 1 == g.nz + 1 ? 1 : z + 1;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        en[k] = ldc(E, k, cxx, cyy, zn);
+        hn_[k] = ldc(H, k, cxx, cyy, zn);
+      }
+    }
+    if (zimg && act) {
+      hzm0 = ldc(H, 0, cxx, cyy, 0);
+      hzm1 = ldc(H, 1, cxx, cyy, 0);
+    } else {
+      hzm0 = hp[0];
+      hzm1 = hp[1];
+    }
+    xr[buf][w][0][lane] = make_float2(h[0].re, h[0].im);
+    xr[buf][w][1][lane] = make_float2(h[2].re, h[2].im);
+    cx<float> hx1 = shfl_cx(h[1], 1, true), hx2 = shfl_cx(h[2], 1, true);
+    const cx<float> ex1 = shfl_cx(ep[1], 1, false), ex2 = shfl_cx(ep[2], 1, false);
+    __syncthreads();
+    cx<float> enew[3];
+    if (act) {
+      if (lane == 0 || ximg) {
+        hx1 = ldc(H, 1, cxx - 1, cyy, cz);
+        hx2 = ldc(H, 2, cxx - 1, cyy, cz);
+      }
+      cx<float> hy0, hy2;
+      if (w == 0 || yimg) {
+        hy0 = ldc(H, 0, cxx, cyy - 1, cz);
+        hy2 = ldc(H, 2, cxx, cyy - 1, cz);
+      } else {
+        const float2 u = xr[buf][w - 1][0][lane], v = xr[buf][w - 1][1][lane];
+        hy0 = {u.x, u.y};
+        hy2 = {v.x, v.y};
+      }
+      // the curl of e_update, then its material / UPML part
+      cx<float> c[3];
+      c[0] = cadd(csub(csub(h[2], hy2), h[1]), hzm1);
+      c[1] = cadd(csub(csub(h[0], hzm0), h[2]), hx2);
+      c[2] = cadd(csub(csub(h[1], hx1), h[0]), hy0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) enew[k] = e[k];
+      e_apply<float, CEPS>(a, (own && z <= z1) ? A.d_new : nullptr, cxx, cyy, cz, c, enew);
+      if (ximg || yimg) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) enew[k] = cmul(ph, enew[k]);
+      }
+      if (zimg) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) enew[k] = cmul(a.pzp, enew[k]);
+      }
+      if (own && z > z0) {
+        // H'(z-1) of (x, y): h_update from E'(z-1), its +x and +y neighbours and E'(z)
+        cx<float> xp[3], yp[3], zp[3], hn[3];
+        xp[1] = ex1;
+        xp[2] = ex2;
+        const float2 u = xr[buf][w + 1][2][lane], v = xr[buf][w + 1][3][lane];
+        yp[0] = {u.x, u.y};
+        yp[2] = {v.x, v.y};
+        zp[0] = enew[0];
+        zp[1] = enew[1];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) hn[k] = hp[k];
+        h_update<float>(a, x, y, z - 1, ep, xp, yp, zp, hn);
+        const long i = g.at(x, y, z - 1);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) st<float>(A.h_new + k * g.comp + i, hn[k]);
+        if (x == g.nx) {
+          const long q = g.at(0, y, z - 1);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            st<float>(A.e_new + k * g.comp + q, cmul(a.pxm, ep[k]));
+            st<float>(A.h_new + k * g.comp + q, cmul(a.pxm, hn[k]));
+          }
+        }
+        if (y == g.ny) {
+          const long q = g.at(x, 0, z - 1);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            st<float>(A.e_new + k * g.comp + q, cmul(a.pym, ep[k]));
+            st<float>(A.h_new + k * g.comp + q, cmul(a.pym, hn[k]));
+          }
+        }
+        if (z - 1 == g.nz) {
+          const long q = g.at(x, y, 0);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            st<float>(A.e_new + k * g.comp + q, cmul(a.pzm, ep[k]));
+            st<float>(A.h_new + k * g.comp + q, cmul(a.pzm, hn[k]));
+          }
         }
       }
-    }
-}
-
-// Per-thread asynchronous global -> shared copies (8 bytes, cached in L1).
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-// Bloch image: multiply the listed components by the phase when wrapped.
-template <int MASK>
-__device__ __forceinline__ void image(bool wrapped, cx<float> ph, cx<float> v[3]) {
-  if (!wrapped) return;
+      if (own && z <= z1) {
+        const long i = g.at(x, y, z);
 #pragma unroll
-  for (int k = 0; k < 3; ++k)
-    if (MASK & (1 << k)) v[k] = cmul(ph, v[k]);
-}
-
-// One thread per (x, y) column of a FX x FY tile, marching z over the CTA's
-// chunk with no shared memory and no barriers: at plane z the thread computes
-// E_new(z+1) of its cell and the two components H_new needs at its +x
-// neighbour (E2, E3) and +y neighbour (E1, E3), recomputing those from the old
-// fields itself (their loads hit L1/L2: the neighbour thread loads the same
-// values), then H_new(z).  DRAM traffic stays at one read and one write of E
-// and H per cell.  Neighbours past nx or ny are the Bloch images of x = 1 or
-// y = 1; the plane past nz is the image of z = 1.
-template <bool CEPS>
-__global__ void __launch_bounds__(FX* FY) k_fused(FusedArgs<float> a) {
-  using T = float;
-  const Geo g = a.f.g;
-  const int x = blockIdx.x * FX + threadIdx.x + 1;
-  const int y = blockIdx.y * FY + threadIdx.y + 1;
-  if (a.slot && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
-    a.tk[a.islot] = a.t;
-  if (x > g.nx || y > g.ny) return;
-  const int z0 = blockIdx.z * a.zchunk + 1;
-  const int z1 = min(z0 + a.zchunk - 1, g.nz);
-  const bool wx = x == g.nx, wy = y == g.ny;
-  const int xs = wx ? 1 : x + 1, ys = wy ? 1 : y + 1;
-  // The cell's own old H and E of plane p are copied asynchronously into
-  // stage slot p % 3 two planes before they are used; each thread waits only
-  // for its own copies, so no barrier is involved.
-  __shared__ float2 stg[3][6][FY][FX];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int pmax = min(z1 + 1, g.nz);
-  auto stage = [&](int pz) {
-    if (pz <= pmax) {
-      const long ip = g.at(x, y, pz);
+        for (int k = 0; k < 3; ++k) st<float>(A.e_new + k * g.comp + i, enew[k]);
+        if (x == 1) {
+          const long q = g.at(g.nx + 1, y, z);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        cp_async8(&stg[pz % 3][c][ty][tx], a.f.h + c * g.comp + ip);
-        cp_async8(&stg[pz % 3][3 + c][ty][tx], a.f.e + c * g.comp + ip);
-      }
-    }
-    cp_commit();
-  };
-  auto staged = [&](int pz, int c) {
-    const float2 q = stg[pz % 3][c][ty][tx];
-    return cx<T>{q.x, q.y};
-  };
-  cx<T> ecur[3], xcur[3], ycur[3], enxt[3], xnxt[3], ynxt[3];
-  stage(z0);
-  stage(z0 + 1);
-  cp_wait<1>();
-  {
-    cx<T> hh[3], hzm[3];
-    const long im = g.at(x, y, z0 - 1);
-    hzm[0] = ld<T>(a.f.h + im);
-    hzm[1] = ld<T>(a.f.h + g.comp + im);
+          for (int k = 0; k < 3; ++k) st<float>(A.e_new + k * g.comp + q, cmul(a.pxp, enew[k]));
+        }
+        if (y == 1) {
+          const long q = g.at(x, g.ny + 1, z);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      hh[c] = staged(z0, c);
-      ecur[c] = staged(z0, 3 + c);
-    }
-    e_update<T, CEPS, 7>(a.f, a.d_new, x, y, z0, hh, hzm, ecur);
-  }
-  e_cell<T, CEPS, 6>(a.f, nullptr, xs, y, z0, xcur);
-  image<6>(wx, a.f.pxp, xcur);
-  e_cell<T, CEPS, 5>(a.f, nullptr, x, ys, z0, ycur);
-  image<5>(wy, a.f.pyp, ycur);
-  const double2* incE = a.inc;
-  const double2* incH = a.inc + (g.nx + 2);
-  for (int z = z0; z <= z1; ++z) {
-    const int zn = z + 1;
-    stage(z + 2);
-    cp_wait<1>();  // plane z+1 has landed
-    if (zn <= g.nz) {
-      cx<T> hh[3], hzm[3];
+          for (int k = 0; k < 3; ++k) st<float>(A.e_new + k * g.comp + q, cmul(a.pyp, enew[k]));
+        }
+        if (z == 1) {
+          const long q = g.at(x, y, g.nz + 1);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        hh[c] = staged(zn, c);
-        enxt[c] = staged(zn, 3 + c);
-      }
-      hzm[0] = staged(z, 0);
-      hzm[1] = staged(z, 1);
-      e_update<T, CEPS, 7>(a.f, zn <= z1 ? a.d_new : nullptr, x, y, zn, hh, hzm, enxt);
-      if (z < z1) {
-        e_cell<T, CEPS, 6>(a.f, nullptr, xs, y, zn, xnxt);
-        image<6>(wx, a.f.pxp, xnxt);
-        e_cell<T, CEPS, 5>(a.f, nullptr, x, ys, zn, ynxt);
-        image<5>(wy, a.f.pyp, ynxt);
+          for (int k = 0; k < 3; ++k) st<float>(A.e_new + k * g.comp + q, cmul(a.pzp, enew[k]));
+        }
       }
     } else {
-      e_cell<T, CEPS, 7>(a.f, nullptr, x, y, 1, enxt);
-      image<7>(true, a.f.pzp, enxt);
-    }
-    cx<T> h[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) h[c] = staged(z, c);
-    h_update<T>(a.f, x, y, z, ecur, xcur, ycur, enxt, h);
-    const long i = g.at(x, y, z);
-    const bool onH = z == a.src.zH, onE = z == a.src.zE;
-    // H ghosts read by the next step: the Bloch copy, then their own TF/SF correction
-    if (wx) {
-      const long j = g.at(0, y, z);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        cx<T> v = cmul(a.f.pxm, h[k]);
-        if (onH && k == a.src.cH) corr_f(v, incH[0], a.src.sH);
-        st<T>(a.h_new + k * g.comp + j, v);
-      }
+      for (int k = 0; k < 3; ++k) enew[k] = zero;
     }
-    if (wy) {
-      const long j = g.at(x, 0, z);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        cx<T> v = cmul(a.f.pym, h[k]);
-        if (onH && k == a.src.cH) corr_f(v, incH[x], a.src.sH);
-        st<T>(a.h_new + k * g.comp + j, v);
-      }
-    }
-    if (z == g.nz) {
-      const long j = g.at(x, y, 0);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        cx<T> v = cmul(a.f.pzm, h[k]);
-        if (a.src.zH == 0 && k == a.src.cH) corr_f(v, incH[x], a.src.sH);
-        st<T>(a.h_new + k * g.comp + j, v);
-      }
-    }
-    cx<T> e[3] = {ecur[0], ecur[1], ecur[2]};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {  // static indices keep h and e in registers
-      if (onH && k == a.src.cH) corr_f(h[k], incH[x], a.src.sH);
-      if (onE && k == a.src.cE) corr_f(e[k], incE[x], a.src.sE);
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      st<T>(a.h_new + k * g.comp + i, h[k]);
-      st<T>(a.e_new + k * g.comp + i, e[k]);
-    }
-    if (a.slot) dft_store(a, x, y, z, e, h);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      ecur[k] = enxt[k];
-      xcur[k] = xnxt[k];
-      ycur[k] = ynxt[k];
-    }
+    // carry E'(z) to the next plane: components 1, 3 into the rows of the
+    // other parity (last read during plane z-1, before this plane's barrier)
+    xr[buf ^ 1][w][2][lane] = make_float2(enew[0].re, enew[0].im);
+    xr[buf ^ 1][w][3][lane] = make_float2(enew[2].re, enew[2].im);
+    ep1 = enew[1];
+    hp1 = h[1];
   }
-}
-
-// The FP64 TF/SF correction values of one step per ix in [0, nx+1]: inc[ix]
-// for E, inc[nx+2+ix] for H (the values k_tfsf adds, see there).
-__global__ void k_incident(SrcArgs s, int it, double2* inc) {
-  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ix > s.nx + 1) return;
-  cx<double> a0, b0, a1, b1, vE, vH;
-  const int zm = s.iz_min;
-  if (s.variant == 1) {
-    incident(s, ix, zm - 1, it, a0, b0);
-    incident(s, ix, zm, it, a1, b1);
-    vE = {dm(s.eps_in1, b0.re), dm(s.eps_in1, b0.im)};
-    vH = {dm(s.dtcq2, a1.re), dm(s.dtcq2, a1.im)};
-  } else {
-    incident(s, ix, zm, it, a1, b1);
-    vE = {dq(b1.re, s.eps_src), dq(b1.im, s.eps_src)};
-    vH = {dm(s.dtcq2, a1.re), dm(s.dtcq2, a1.im)};
-  }
-  inc[ix] = make_double2(vE.re, vE.im);
-  inc[s.nx + 2 + ix] = make_double2(vH.re, vH.im);
 }
 
 }  // namespace
@@ -1661,7 +1617,6 @@ struct iris_engine {
   void* e2 = nullptr;
   void* h2 = nullptr;
   void* pml_d2[2] = {nullptr, nullptr};
-  double2* d_inc = nullptr;
   int zchunk = 0;
   dim3 fblk, fgrd;
   // CUDA graph of one DFT block of steps (iris_params.graph): d_it holds the
@@ -1929,85 +1884,23 @@ template <typename T> void dft_sample(iris_engine* E, int t, const int* tp = nul
   if (++E->nslot == E->K) dft_flush(E);
 }
 
-FusedArgs<float> fused_args(const iris_engine* E) {
-  const iris_params& p = E->p;
-  FusedArgs<float> a{};
+FusedArgs fused_args(const iris_engine* E) {
+  FusedArgs a{};
   a.f = field_args<float>(E);
   a.e_new = (float2*)E->e2;
   a.h_new = (float2*)E->h2;
   for (int s = 0; s < 2; ++s) a.d_new[s] = (float2*)E->pml_d2[s];
-  a.inc = E->d_inc;
-  const SrcArgs& s = E->src;
-  a.src.zE = a.src.zH = -1;
-  if (s.variant == 1) {
-    a.src.zE = s.iz_min;
-    a.src.zH = s.iz_min - 1;
-    const bool ex = s.i_pol == 2;
-    a.src.cE = ex ? 0 : 1;
-    a.src.cH = ex ? 1 : 0;
-    a.src.sE = a.src.sH = ex ? +1 : -1;
-  } else if (s.variant == 2) {
-    a.src.zE = a.src.zH = s.iz_min;
-    a.src.cE = 0;
-    a.src.cH = 1;
-    a.src.sE = a.src.sH = +1;
-  }
-  a.nboxes = E->nboxes;
-  for (int b = 0; b < E->nboxes; ++b) {
-    const int* bx = b == 0 ? p.box1 : p.box2;
-    for (int j = 0; j < 3; ++j) {
-      const FaceMap& F = E->fm[b][j];
-      FusedFace& f = a.faces[b][j];
-      f.active = F.active ? 1 : 0;
-      for (int d = 0; d < 3; ++d) {
-        f.lo[d] = bx[2 * d];
-        f.hi[d] = bx[2 * d + 1];
-      }
-      f.nu = F.nu;
-      for (int side = 0; side < 2; ++side)
-        for (int c = 0; c < 6; ++c) f.base[side][c] = F.base[side][c];
-    }
-  }
   a.zchunk = E->zchunk;
   return a;
 }
-
-int step_fused(iris_engine* E, int it0, int n) {
-  const iris_params& p = E->p;
-  for (int it = it0; it < it0 + n; ++it) {
-    if (E->src.variant != 0) {
-      KTimer tm(E, IRIS_KC_TFSF);
-      k_incident<<<(p.nx + 2 + 127) / 128, 128, 0, E->st>>>(E->src, it, E->d_inc);
-    }
-    FusedArgs<float> a = fused_args(E);
-    const bool sampled = E->P > 0 && it >= p.to_fourier && it % p.sample_fourier == 0;
-    if (sampled) {
-      a.slot = (float2*)E->S + (long)E->nslot * E->P;
-      a.tk = E->d_tk;
-      a.islot = E->nslot;
-      a.t = it + 1 - p.to_fourier;
-    }
-    {
-      KTimer tm(E, IRIS_KC_FUSED);
-      if (E->eps_complex) k_fused<true><<<E->fgrd, E->fblk, 0, E->st>>>(a);
-      else k_fused<false><<<E->fgrd, E->fblk, 0, E->st>>>(a);
-    }
-    std::swap(E->e, E->e2);
-    std::swap(E->h, E->h2);
-    for (int s = 0; s < 2; ++s) std::swap(E->pml_d[s], E->pml_d2[s]);
-    if (sampled && ++E->nslot == E->K) dft_flush(E);
-  }
-  CK(cudaGetLastError());
-  return IRIS_OK;
-}
-
 
 // A whole DFT block of steps from it on can be replayed from a graph: every
 // step of it is sampled and the block starts with an empty ring.
 bool graph_ready(const iris_engine* E, int it, int left) {
   const iris_params& p = E->p;
-  return p.graph && !E->timing && !E->fused && E->P > 0 && E->nslot == 0 && p.sample_fourier == 1 &&
-         it >= p.to_fourier && left >= E->K;
+  // the fused passes swap buffers every step: an even block brings them back
+  return p.graph && !E->timing && (!E->fused || E->K % 2 == 0) && E->P > 0 && E->nslot == 0 &&
+         p.sample_fourier == 1 && it >= p.to_fourier && left >= E->K;
 }
 
 void graph_reset(iris_engine* E) {
@@ -2041,6 +1934,42 @@ template <typename F> int graph_block(iris_engine* E, int it, F record) {
   }
   CK(cudaGraphLaunch(E->gexec, E->st));
   E->dev_it = it + E->K;
+  return IRIS_OK;
+}
+
+// One fused step into the second buffers, swap, then TF/SF and the DFT
+// sample on the new state, in the operator order of the split passes; step
+// it, or *itp + it when itp is given.
+void fused_one(iris_engine* E, int it, const int* itp, bool sampled) {
+  {
+    KTimer tm(E, IRIS_KC_FUSED);
+    const FusedArgs a = fused_args(E);
+    if (E->eps_complex) k_fused<true><<<E->fgrd, E->fblk, 0, E->st>>>(a);
+    else k_fused<false><<<E->fgrd, E->fblk, 0, E->st>>>(a);
+  }
+  std::swap(E->e, E->e2);
+  std::swap(E->h, E->h2);
+  for (int s = 0; s < 2; ++s) std::swap(E->pml_d[s], E->pml_d2[s]);
+  launch_tfsf<float>(E, it, itp);
+  if (sampled) dft_sample<float>(E, it + 1 - E->p.to_fourier, itp);
+}
+
+int step_fused(iris_engine* E, int it0, int n) {
+  const iris_params& p = E->p;
+  int it = it0;
+  while (it < it0 + n) {
+    if (graph_ready(E, it, it0 + n - it)) {
+      int rc = graph_block(E, it, [&] {
+        for (int j = 0; j < E->K; ++j) fused_one(E, j, E->d_it, true);
+      });
+      if (rc) return rc;
+      it += E->K;
+      continue;
+    }
+    fused_one(E, it, nullptr, it >= p.to_fourier && it % p.sample_fourier == 0);
+    ++it;
+  }
+  CK(cudaGetLastError());
   return IRIS_OK;
 }
 
@@ -2244,7 +2173,7 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
 void free_engine(iris_engine* E) {
   void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
                   E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J, E->e2, E->h2, E->pml_d2[0],
-                  E->pml_d2[1], E->d_inc, E->d_err, E->d_it, E->d_wtc};
+                  E->pml_d2[1], E->d_err, E->d_it, E->d_wtc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (E->h_J) cudaFreeHost(E->h_J);
@@ -2367,7 +2296,8 @@ static int create_engine(const iris_params* pin, const double* fw, bool member, 
   // fused E+H pass: FP32 only
   // fused on request only: it moves fewer bytes but issues ~1.6x the
   // instructions of the split passes and measures slower on GB300 for now
-  E->fused = E->prec == IRIS_FP32 && p.stencil == IRIS_STENCIL_FUSED;
+  // FP32 steps with the fused pass unless the split or streamed passes are asked for
+  E->fused = E->prec == IRIS_FP32 && (p.stencil == IRIS_STENCIL_FUSED || p.stencil == IRIS_STENCIL_DEFAULT);
   if (E->fused) {
     if (cudaMalloc(&E->e2, fbytes) != cudaSuccess || cudaMalloc(&E->h2, fbytes) != cudaSuccess)
       return bail(fail(IRIS_ENOMEM, "second field buffers: allocation failed"));
@@ -2378,16 +2308,13 @@ static int create_engine(const iris_params* pin, const double* fw, bool member, 
       if (cudaMalloc(&E->pml_d2[s], b) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "UPML allocation failed"));
       cudaMemsetAsync(E->pml_d2[s], 0, b, E->st);
     }
-    if (cudaMalloc(&E->d_inc, sizeof(double2) * 2 * (p.nx + 2)) != cudaSuccess)
-      return bail(fail(IRIS_ENOMEM, "TF/SF table allocation failed"));
-    cudaMemsetAsync(E->d_inc, 0, sizeof(double2) * 2 * (p.nx + 2), E->st);
-    // z chunks: enough CTAs for many waves over 152 SMs, at least 8 planes each
-    const long tiles = (long)((p.nx + FX - 1) / FX) * ((p.ny + FY - 1) / FY);
-    long nch = std::max(1L, (8L * 152 * 4 + tiles - 1) / tiles);
-    nch = std::min<long>(nch, std::max(1, p.nz / 8));
+    // z chunks: about eight waves of two CTAs per SM, at least 16 planes each
+    const long tiles = (long)((p.nx + FZ_OX - 1) / FZ_OX) * ((p.ny + FZ_OY - 1) / FZ_OY);
+    long nch = std::max(1L, (8L * 152 * 2 + tiles - 1) / tiles);
+    nch = std::min<long>(nch, std::max(1, p.nz / 16));
     E->zchunk = (int)((p.nz + nch - 1) / nch);
-    E->fblk = dim3(FX, FY, 1);
-    E->fgrd = dim3((p.nx + FX - 1) / FX, (p.ny + FY - 1) / FY, (p.nz + E->zchunk - 1) / E->zchunk);
+    E->fblk = dim3(FZ_X, FZ_Y, 1);
+    E->fgrd = dim3((p.nx + FZ_OX - 1) / FZ_OX, (p.ny + FZ_OY - 1) / FZ_OY, (p.nz + E->zchunk - 1) / E->zchunk);
   }
   if (cudaMalloc(&E->d_err, sizeof(int)) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "allocation failed"));
   cudaMemsetAsync(E->d_err, 0, sizeof(int), E->st);

@@ -3,8 +3,9 @@ and against the FP64 oracle.
 
 The fused pass computes every cell with the same per-cell arithmetic as the
 split passes but reorders the work (one z-marching pass over double buffers,
-halo cells recomputed, Bloch ghosts as index images, TF/SF and DFT samples
-applied in-kernel).  Tolerances: 1e-5 norm-wise relative against the split
+overlapping tiles whose edge cells are recomputed, Bloch ghosts as index
+images; TF/SF and the DFT sample run after it as after the split passes).
+Tolerances: 1e-5 norm-wise relative against the split
 FP32 run (only FP32 rounding differs), 1e-4 against the FP64 oracle, and the
 reference-order DFT accumulators of every face pair within 1e-5 of the split
 run.
@@ -102,9 +103,10 @@ def test_fused_rejected_in_fp64(iris, oracle, tmp_path):
 
 
 def test_stencil_selection(iris, oracle, tmp_path):
-    """The per-kernel timers show which pass ran: split by default, fused on request."""
+    """The per-kernel timers show which pass ran: fused by default in FP32,
+    split on request."""
     w, op = make_case(oracle, tmp_path, (16, 8, 40, 6, 35, 15, 10, 4.0, 10, (1, 16, 1, 8, 8, 32)), 2)
-    for stencil, fused in ((0, False), (1, False), (2, True)):
+    for stencil, fused in ((0, True), (1, False), (2, True)):
         eng = iris.Engine(engine_params_from_oracle(iris, op, precision=1), op.fw, stencil=stencil)
         eng.timing_start()
         eng.step(1, 5)

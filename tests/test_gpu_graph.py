@@ -36,7 +36,7 @@ def same(a, b, op, iris):
     assert np.array_equal(a.flux(0), b.flux(0))
 
 
-@pytest.mark.parametrize("precision,stencil", [(0, 0), (1, 1), (1, 3)])
+@pytest.mark.parametrize("precision,stencil", [(0, 0), (1, 1), (1, 2), (1, 3)])
 def test_graph_steps_identical(iris, oracle, tmp_path, precision, stencil):
     w, op, eps, (plain, graphed) = engines(iris, oracle, tmp_path, precision, stencil)
     for it0, n in CALLS:
