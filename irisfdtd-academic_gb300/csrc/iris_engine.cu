@@ -850,45 +850,54 @@ __global__ void __launch_bounds__(256) k_dft_gather(const typename V2<T>::t* __r
   slot[sg.p0 + L] = src[sg.src + (long)u * sg.su + (long)v * sg.sv];
 }
 
-// FP64 mode: fdata(p, iw) += dt*F_k(p)*exp(i*fw(iw)*t_k), k in order, one
-// rounding per reference operation (code/dataprocess.f90:143-147).
+// FP64 mode: fdata(p, iw) += (dt*F_k(p))*exp(i*fw(iw)*t_k), k in the
+// reference's order (code/dataprocess.f90:143-147), each complex
+// multiply-add as four FP64 FMAs (GB300's FP64 rate makes the unfused eight
+// operations the cost of the FP64 mode; the difference is one rounding per
+// term).  The twiddles exp(i*fw*t_k) come from one table per block.
 constexpr int DFT64_WC = 8;
+__global__ void k_twiddle64(const int* __restrict__ tk, int nk, const double* __restrict__ fw, int nof,
+                            double2* __restrict__ W) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nk * nof) return;
+  const int k = t / nof, j = t % nof;
+  double sn, cs;
+  sincos(dm(fw[j], (double)tk[k]), &sn, &cs);
+  W[t] = make_double2(cs, sn);
+}
+
 __global__ void __launch_bounds__(128) k_dft_fp64(const double2* __restrict__ S, long P, int nk,
-                                                  const int* __restrict__ tk, const double* __restrict__ fw, int nof,
-                                                  int nwc, double dt, double2* __restrict__ fd) {
+                                                  const double2* __restrict__ W, int nof, int nwc, double dt,
+                                                  double2* __restrict__ fd) {
   extern __shared__ double2 W64[];  // [nk][WC]
   // 1-D grid, frequency chunks fastest: the chunks of one point block share its samples in L2
   const int w0 = (blockIdx.x % nwc) * DFT64_WC;
   const long pblk = blockIdx.x / nwc;
   for (int t = threadIdx.x; t < nk * DFT64_WC; t += blockDim.x) {
     const int k = t / DFT64_WC, j = t % DFT64_WC;
-    double2 v = make_double2(0.0, 0.0);
-    if (w0 + j < nof) {
-      double sn, cs;
-      sincos(dm(fw[w0 + j], (double)tk[k]), &sn, &cs);
-      v = make_double2(cs, sn);
-    }
-    W64[t] = v;
+    W64[t] = w0 + j < nof ? W[(long)k * nof + w0 + j] : make_double2(0.0, 0.0);
   }
   __syncthreads();
   const long p = pblk * blockDim.x + threadIdx.x;
   if (p >= P) return;
   const int nw = min(DFT64_WC, nof - w0);
-  cx<double> acc[DFT64_WC];
+  double2 acc[DFT64_WC];
 #pragma unroll
   for (int j = 0; j < DFT64_WC; ++j)
-    if (j < nw) acc[j] = ld<double>(fd + (long)(w0 + j) * P + p);
+    if (j < nw) acc[j] = fd[(long)(w0 + j) * P + p];
   for (int k = 0; k < nk; ++k) {
-    const cx<double> a = rmul(dt, ld<double>(S + (long)k * P + p));
+    const double2 f = S[(long)k * P + p];
+    const double ar = dm(dt, f.x), ai = dm(dt, f.y);
 #pragma unroll
     for (int j = 0; j < DFT64_WC; ++j) {
       const double2 w = W64[k * DFT64_WC + j];
-      acc[j] = cadd(acc[j], cmul(a, cx<double>{w.x, w.y}));
+      acc[j].x = fma(ar, w.x, fma(-ai, w.y, acc[j].x));
+      acc[j].y = fma(ar, w.y, fma(ai, w.x, acc[j].y));
     }
   }
 #pragma unroll
   for (int j = 0; j < DFT64_WC; ++j)
-    if (j < nw) st<double>(fd + (long)(w0 + j) * P + p, acc[j]);
+    if (j < nw) fd[(long)(w0 + j) * P + p] = acc[j];
 }
 
 // FP32 mode twiddles: Wt[k][iw] = dt*exp(i*fw(iw)*t_k), phase formed in FP64
@@ -1603,6 +1612,7 @@ struct iris_engine {
   double* d_fw = nullptr;
   double2* fd = nullptr;
   float2* d_wt = nullptr;
+  double2* d_wt64 = nullptr;  // FP64 mode twiddles of one block
   bool dft_tc = false;     // FP32 block accumulation on the tensor cores
   float* d_wtc = nullptr;  // its B operands (k_twiddle_tc)
   FluxFace* d_faces = nullptr;
@@ -1850,8 +1860,9 @@ void dft_flush(iris_engine* E) {
   if (E->prec == IRIS_FP64) {
     const int nwc = (E->p.nof + DFT64_WC - 1) / DFT64_WC;
     const long nblk = (E->P + 127) / 128;
+    k_twiddle64<<<(nk * E->p.nof + 255) / 256, 256, 0, E->st>>>(E->d_tk, nk, E->d_fw, E->p.nof, E->d_wt64);
     k_dft_fp64<<<(unsigned)(nblk * nwc), 128, (size_t)nk * DFT64_WC * sizeof(double2), E->st>>>(
-        (const double2*)E->S, E->P, nk, E->d_tk, E->d_fw, E->p.nof, nwc, E->p.dt, E->fd);
+        (const double2*)E->S, E->P, nk, E->d_wt64, E->p.nof, nwc, E->p.dt, E->fd);
   } else if (E->dft_tc) {
     const int ng = (E->p.nof + TC_NW - 1) / TC_NW, nch = (2 * nk + TC_KC - 1) / TC_KC;
     const long nt = (long)ng * nch * TC_BROWS * TC_KC;
@@ -2153,6 +2164,7 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
   CK(cudaMalloc(&E->d_fw, sizeof(double) * p.nof));
   CK(cudaMemcpy(E->d_fw, E->fw.data(), sizeof(double) * p.nof, cudaMemcpyHostToDevice));
   if (E->prec == IRIS_FP32) CK(cudaMalloc(&E->d_wt, sizeof(float2) * (size_t)E->K * p.nof));
+  if (E->prec == IRIS_FP64) CK(cudaMalloc(&E->d_wt64, sizeof(double2) * (size_t)E->K * p.nof));
   E->dft_tc = E->prec == IRIS_FP32 && p.dft_kernel != IRIS_DFT_KERNEL_CUDA;
   if (E->dft_tc) {
     const int ng = (p.nof + TC_NW - 1) / TC_NW, nch = (2 * E->K + TC_KC - 1) / TC_KC;
@@ -2173,7 +2185,7 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
 void free_engine(iris_engine* E) {
   void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
                   E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J, E->e2, E->h2, E->pml_d2[0],
-                  E->pml_d2[1], E->d_err, E->d_it, E->d_wtc};
+                  E->pml_d2[1], E->d_err, E->d_it, E->d_wtc, E->d_wt64};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (E->h_J) cudaFreeHost(E->h_J);
