@@ -244,7 +244,7 @@ def run_engine(args, rank, world, local):
         dom, db, dt_ = ("update_h", hb, t_h) if t_h >= t_e else ("update_e", eb, t_e)
         min_bytes = db
     achieved = db / dt_ / 1e9
-    wl_name = f"{w.name} (configs[2])" if not args.grid else w.name
+    wl_name = f"{w.name} (configs[{args.workload - 1}])" if not args.grid else w.name
     traffic, tsrc = ncu_traffic(dom, w.name + "_" + args.precision)
     launches = kn["update_e"] + kn["update_h"] + kn["tfsf"] + kn["dft_gather"] + kn["flux"] + kn["fused_eh"] + \
         kn["dft_block"] * (2 if prec == iris.FP32 else 1)
@@ -261,10 +261,11 @@ def run_engine(args, rank, world, local):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "c64 fields (fp32), fp64 incident field and DFT accumulation" if prec == iris.FP32 else "c128 (fp64)",
-        "data": "synthetic (seeded spheres, numpy PCG64 seed 0)",
+        "data": ("synthetic (seeded spheres, numpy PCG64 seed 0)" if w.structure == "spheres"
+                 else f"synthetic ({w.structure} geometry)"),
         "config": {
             "workload": wl_name,
-            "grid": [w.nx, w.ny, w.nz], "upml": 24, "nof": w.nof, "dft_points": info["dft_points"],
+            "grid": [w.nx, w.ny, w.nz], "upml": p.pmlzi, "nof": w.nof, "dft_points": info["dft_points"],
             "dft_block": info["dft_block"], "precision": args.precision,
             "dft_kernel": ["engine default", "cuda cores", "tensor cores (tcgen05 tf32x3)"][args.dft_kernel],
             "l2": "working set (fields %.1f GB, DFT accumulators %.1f GB) >> 129 MB L2; no flush needed" % (
@@ -289,6 +290,8 @@ def run_engine(args, rank, world, local):
     }
     if graph_line:
         out["graph"] = graph_line
+    if rank == 0 and world == 1 and args.workload == 2 and not args.grid:
+        out["tr_error"] = tr_error(iris, p, fw, eps, local)
     if rank == 0 and world == 1 and not args.no_fp64_compare and prec == iris.FP32:
         out["fp64_plain"] = fp64_compare(iris, p, fw, eps, cells, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -508,6 +511,32 @@ def loop_plain(iris, ws, params, mats, fw, local, nsample, steps):
         tot_ms += reg
     return {"value": round(tot_cells / (tot_ms * 1e-3) / 1e9, 3), "unit": "Gcell/s", "cells_sampled": len(idx),
             "steps": steps, "note": "each sampled cell on its own engine, device time summed"}
+
+
+def tr_error(iris, p, fw, eps, local):
+    """FP32 against FP64 over the whole run (texit steps): R = J5/(J5+J6) and
+    T = J6/(J5+J6) of box 1 per wavelength, their largest absolute
+    differences.  The FP64 engine stands for the FP64 oracle (the parity
+    tests hold it within 1e-12 of the oracle); z-plane DFTs only."""
+    out = {}
+    for prec in (iris.FP64, iris.FP32):
+        q = p.copy()
+        q.dft_faces = iris.DFT_Z
+        e = iris.Engine(q, fw, precision=prec, device=local)
+        e.set_material(eps)
+        t0 = time.perf_counter()
+        e.step(1, p.texit)
+        J = e.flux(0)
+        out[prec] = (iris.tr_normalise(J[4], J[5]), time.perf_counter() - t0)
+        e.close()
+    (r64, t64), s64 = out[iris.FP64]
+    (r32, t32), s32 = out[iris.FP32]
+    return {"steps": p.texit, "nof": p.nof, "R_max_abs_err": float(np.max(np.abs(r32 - r64))),
+            "T_max_abs_err": float(np.max(np.abs(t32 - t64))),
+            "R_rel_err": float(np.max(np.abs(r32 - r64)) / np.max(np.abs(r64))),
+            "T_rel_err": float(np.max(np.abs(t32 - t64)) / np.max(np.abs(t64))),
+            "wall_s": {"fp64": round(s64, 2), "fp32": round(s32, 2)},
+            "note": "FP32 (fused pass, tensor-core DFT) against FP64 over the full run, per spectrum"}
 
 
 def fp64_compare(iris, p, fw, eps, cells, local, K=32, W=3):
