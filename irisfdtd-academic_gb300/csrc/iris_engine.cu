@@ -17,9 +17,9 @@
 //     each sampled step, accumulated into fdata [nof][P] (complex double)
 //     one block of samples at a time.
 //
-// Arithmetic: the FP64 mode uses __dmul_rn/__dadd_rn (never contracted to
-// FMA) so the stencil rounds exactly like the reference build; the FP32 mode
-// lets the compiler contract.
+// The batched form lives in iris_batch.cu, the adjoint form in
+// iris_adjoint.cu; the per-cell operators they share are in iris_device.cuh.
+
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,243 +32,10 @@
 #include <type_traits>
 #include <vector>
 
-#include "iris_internal.h"
+#include "iris_engine.h"
 
 namespace iris {
 namespace {
-
-// ---------------------------------------------------------------------------
-// device arithmetic
-
-template <typename T> struct V2;
-template <> struct V2<double> { using t = double2; };
-template <> struct V2<float> { using t = float2; };
-
-template <typename T> __device__ __forceinline__ T mul_(T a, T b);
-template <typename T> __device__ __forceinline__ T add_(T a, T b);
-template <typename T> __device__ __forceinline__ T sub_(T a, T b);
-template <> __device__ __forceinline__ double mul_<double>(double a, double b) { return __dmul_rn(a, b); }
-template <> __device__ __forceinline__ double add_<double>(double a, double b) { return __dadd_rn(a, b); }
-template <> __device__ __forceinline__ double sub_<double>(double a, double b) { return __dsub_rn(a, b); }
-template <> __device__ __forceinline__ float mul_<float>(float a, float b) { return a * b; }
-template <> __device__ __forceinline__ float add_<float>(float a, float b) { return a + b; }
-template <> __device__ __forceinline__ float sub_<float>(float a, float b) { return a - b; }
-
-template <typename T> struct cx { T re, im; };
-
-template <typename T> __device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) { return {add_(a.re, b.re), add_(a.im, b.im)}; }
-template <typename T> __device__ __forceinline__ cx<T> csub(cx<T> a, cx<T> b) { return {sub_(a.re, b.re), sub_(a.im, b.im)}; }
-template <typename T> __device__ __forceinline__ cx<T> rmul(T r, cx<T> a) { return {mul_(r, a.re), mul_(r, a.im)}; }
-template <typename T> __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
-  return {sub_(mul_(a.re, b.re), mul_(a.im, b.im)), add_(mul_(a.re, b.im), mul_(a.im, b.re))};
-}
-template <typename T> __device__ __forceinline__ cx<T> ld(const typename V2<T>::t* p) {
-  typename V2<T>::t v = *p;
-  return {v.x, v.y};
-}
-template <typename T> __device__ __forceinline__ void st(typename V2<T>::t* p, cx<T> a) {
-  typename V2<T>::t v;
-  v.x = a.re;
-  v.y = a.im;
-  *p = v;
-}
-
-// ---------------------------------------------------------------------------
-// geometry of a ghost-padded field component
-
-struct Geo {
-  int nx, ny, nz;
-  long pitch, plane, comp;  // in elements
-  int xo;                   // storage index of x is x + xo
-  __host__ __device__ __forceinline__ long at(int x, int y, int z) const {
-    return (long)z * plane + (long)y * pitch + (long)(x + xo);
-  }
-};
-
-// UPML coefficient row (24 per PML z-plane), see make_coef()
-enum { CD_A = 0, CD_B = 3, CE_A = 6, CE_B = 9, C_FP = 12, C_FM = 15, CB_B = 18, CH_B = 21, NCOEF = 24 };
-
-template <typename T> struct FieldArgs {
-  typename V2<T>::t* e;  // component 0; components 1,2 at +comp, +2 comp
-  typename V2<T>::t* h;
-  Geo g;
-  typename V2<T>::t* pml_d[2];
-  typename V2<T>::t* pml_b[2];
-  long pcomp[2];
-  const T* coef;
-  int pmlzi, pmlzf, hi, hf;
-  const typename V2<T>::t* eps_c;  // complex structure material or null
-  const T* eps_r;                  // real structure material or null
-  T m1, m3, eps0sq, dtcq2;
-  cx<T> pxp, pyp, pzp, pxm, pym, pzm;  // Bloch phases exp(+-i ak)
-};
-
-// New E of interior cell (x, y, z) from the curl of the old H (c) and the
-// old E (e, replaced): the material and UPML part of e_fdtd
-// (code/fdtd.f90:57-153) and UPML_Array_e (code/boundary_II.f90:60-138).
-// Per z the reference's region order decides: the UPML slabs overwrite
-// whatever e_fdtd wrote there.  The UPML auxiliary is read from a.pml_d and,
-// when dnew is given, its new value written there (dnew == a.pml_d updates in
-// place).  With EPV the caller supplies the real structure eps_inv of the
-// cell (ep) instead of it being read from a.eps_r.  MASK selects the
-// components computed (bit k: E_{k+1}).  UPML = false: the caller knows the
-// cell lies outside the UPML slabs (the slab code is not compiled in).
-template <typename T, bool CEPS, int MASK = 7, bool EPV = false, bool UPML = true>
-__device__ __forceinline__ void e_apply(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
-                                        const cx<T> c[3], cx<T> e[3], T ep = T(0)) {
-  using V = typename V2<T>::t;
-  const Geo& g = a.g;
-  if (UPML && (z <= a.pmlzi || z >= a.pmlzf)) {
-    const int slab = z <= a.pmlzi ? 0 : 1;
-    const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
-    const int row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
-    const T* cf = a.coef + NCOEF * row;
-    const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
-    const V* D = a.pml_d[slab];
-    const long pc = a.pcomp[slab];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      if (!(MASK & (1 << k))) continue;
-      const cx<T> ck = rmul(a.eps0sq, c[k]);
-      const cx<T> dold = ld<T>(D + k * pc + pi);
-      const cx<T> dn = cadd(rmul(cf[CD_A + k], dold), rmul(cf[CD_B + k], ck));
-      if (dnew) st<T>(dnew[slab] + k * pc + pi, dn);
-      e[k] = cadd(rmul(cf[CE_A + k], e[k]), rmul(cf[CE_B + k], csub(rmul(cf[C_FP + k], dn), rmul(cf[C_FM + k], dold))));
-    }
-  } else if (z >= a.hi && z <= a.hf) {
-    const long ie = (long)(z - a.hi) * g.plane + (long)y * g.pitch + (long)(x + g.xo);
-    if (CEPS) {
-      const cx<T> epc = ld<T>(a.eps_c + ie);
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        if (MASK & (1 << k)) e[k] = cadd(e[k], cmul(epc, c[k]));
-    } else {
-      const T epr = EPV ? ep : a.eps_r[ie];
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        if (MASK & (1 << k)) e[k] = cadd(e[k], rmul(epr, c[k]));
-    }
-  } else {
-    const T m = z < a.hi ? a.m1 : a.m3;
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-      if (MASK & (1 << k)) e[k] = cadd(e[k], rmul(m, c[k]));
-  }
-}
-
-// The E update of one cell given its own old H (h), the old H one plane
-// below (hzm, components 1 and 2) and its old E (e, replaced by the new E);
-// the x-1 and y-1 neighbours are loaded here.  MASK selects the components
-// computed (bit k: E_{k+1}); loads only the others need are never issued.
-template <typename T, bool CEPS, int MASK = 7, bool UPML = true>
-__device__ __forceinline__ void e_update(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
-                                         const cx<T> h[3], const cx<T> hzm[3], cx<T> e[3]) {
-  using V = typename V2<T>::t;
-  const Geo& g = a.g;
-  const long i = g.at(x, y, z);
-  const V* H1 = a.h;
-  const V* H2 = a.h + g.comp;
-  const V* H3 = a.h + 2 * g.comp;
-  cx<T> c[3];
-  if (MASK & 1) c[0] = cadd(csub(csub(h[2], ld<T>(H3 + i - g.pitch)), h[1]), hzm[1]);
-  if (MASK & 2) c[1] = cadd(csub(csub(h[0], hzm[0]), h[2]), ld<T>(H3 + i - 1));
-  if (MASK & 4) c[2] = cadd(csub(csub(h[1], ld<T>(H2 + i - 1)), h[0]), ld<T>(H1 + i - g.pitch));
-  e_apply<T, CEPS, MASK, false, UPML>(a, dnew, x, y, z, c, e);
-}
-
-// New E of interior cell (x, y, z) from the old E and H in memory: e_fdtd
-// (code/fdtd.f90:57-153) and UPML_Array_e (code/boundary_II.f90:60-138).
-template <typename T, bool CEPS, int MASK = 7, bool UPML = true>
-__device__ __forceinline__ void e_cell(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
-                                       cx<T> e[3]) {
-  const Geo& g = a.g;
-  const long i = g.at(x, y, z);
-  cx<T> h[3], hzm[3];
-  // own H: c1 uses H3, H2; c2 uses H1, H3; c3 uses H2, H1
-  if (MASK & 6) h[0] = ld<T>(a.h + i);
-  if (MASK & 5) h[1] = ld<T>(a.h + g.comp + i);
-  if (MASK & 3) h[2] = ld<T>(a.h + 2 * g.comp + i);
-  if (MASK & 2) hzm[0] = ld<T>(a.h + i - g.plane);
-  if (MASK & 1) hzm[1] = ld<T>(a.h + g.comp + i - g.plane);
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-    if (MASK & (1 << k)) e[k] = ld<T>(a.e + k * g.comp + i);
-  e_update<T, CEPS, MASK, UPML>(a, dnew, x, y, z, h, hzm, e);
-}
-
-// New H of interior cell (x, y, z): h_fdtd (code/fdtd.f90:157-248) and
-// UPML_Array_h (code/boundary_II.f90:142-220), from the new E of the cell (ev)
-// and of its +x, +y, +z neighbours (xp: components 2,3; yp: 1,3; zp: 1,2),
-// the old H read from a.h, the UPML auxiliary B updated in place.  UPML =
-// false: the cell lies outside the UPML slabs.
-template <typename T, bool UPML = true>
-__device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, int z, const cx<T> ev[3],
-                                         const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3]) {
-  using V = typename V2<T>::t;
-  const Geo& g = a.g;
-  cx<T> c[3];
-  c[0] = cadd(csub(csub(yp[2], ev[2]), zp[1]), ev[1]);
-  c[1] = cadd(csub(csub(zp[0], ev[0]), xp[2]), ev[2]);
-  c[2] = cadd(csub(csub(xp[1], ev[1]), yp[0]), ev[0]);
-  if (UPML && (z <= a.pmlzi || z >= a.pmlzf)) {
-    const int slab = z <= a.pmlzi ? 0 : 1;
-    const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
-    const int row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
-    const T* cf = a.coef + NCOEF * row;
-    const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
-    V* B = a.pml_b[slab];
-    const long pc = a.pcomp[slab];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const cx<T> bold = ld<T>(B + k * pc + pi);
-      const cx<T> bn = csub(rmul(cf[CD_A + k], bold), rmul(cf[CB_B + k], c[k]));
-      st<T>(B + k * pc + pi, bn);
-      h[k] = cadd(rmul(cf[CE_A + k], h[k]), rmul(cf[CH_B + k], csub(rmul(cf[C_FP + k], bn), rmul(cf[C_FM + k], bold))));
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) h[k] = csub(h[k], rmul(a.dtcq2, c[k]));
-  }
-}
-
-// h_update with the old H of the cell loaded from a.h.
-template <typename T, bool UPML = true>
-__device__ __forceinline__ void h_cell(const FieldArgs<T>& a, int x, int y, int z, const cx<T> ev[3],
-                                       const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3]) {
-  const long i = a.g.at(x, y, z);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) h[k] = ld<T>(a.h + k * a.g.comp + i);
-  h_update<T, UPML>(a, x, y, z, ev, xp, yp, zp, h);
-}
-
-// Split E pass of one cell: e_cell in place + bc_{x,y,z}max_bloch
-// (code/boundary.f90:193-216,257-284,321-348) for the E ghosts.
-template <typename T, bool CEPS, bool UPML = true>
-__device__ __forceinline__ void e_split_cell(const FieldArgs<T>& a, int x, int y, int z) {
-  using V = typename V2<T>::t;
-  const Geo& g = a.g;
-  const long i = g.at(x, y, z);
-  V* E[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
-  cx<T> e[3];
-  e_cell<T, CEPS, 7, UPML>(a, a.pml_d, x, y, z, e);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) st<T>(E[k] + i, e[k]);
-  if (x == 1) {
-    const long j = g.at(g.nx + 1, y, z);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pxp, e[k]));
-  }
-  if (y == 1) {
-    const long j = g.at(x, g.ny + 1, z);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pyp, e[k]));
-  }
-  if (z == 1) {
-    const long j = g.at(x, y, g.nz + 1);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pzp, e[k]));
-  }
-}
 
 template <typename T, bool CEPS>
 __global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
@@ -277,55 +44,6 @@ __global__ void __launch_bounds__(256) k_update_e(FieldArgs<T> a) {
   const int z = blockIdx.z * blockDim.z + threadIdx.z + 1;
   if (x > a.g.nx || y > a.g.ny || z > a.g.nz) return;
   e_split_cell<T, CEPS>(a, x, y, z);
-}
-
-// Split H pass of one cell: h_cell in place + bc_{x,y,z}min_bloch
-// (code/boundary.f90:163-187,224-251,288-315) for the H ghosts and the E
-// ghosts at 0.  The ghosts at nx+1/ny+1/nz+1 of H are never read by any
-// operator and are not maintained.
-template <typename T, bool UPML = true>
-__device__ __forceinline__ void h_split_cell(const FieldArgs<T>& a, int x, int y, int z) {
-  using V = typename V2<T>::t;
-  const Geo& g = a.g;
-  const long i = g.at(x, y, z);
-  V* Ec[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
-  V* H[3] = {a.h, a.h + g.comp, a.h + 2 * g.comp};
-  cx<T> ev[3], xp[3], yp[3], zp[3], h[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) ev[k] = ld<T>(Ec[k] + i);
-  xp[1] = ld<T>(Ec[1] + i + 1);
-  xp[2] = ld<T>(Ec[2] + i + 1);
-  yp[0] = ld<T>(Ec[0] + i + g.pitch);
-  yp[2] = ld<T>(Ec[2] + i + g.pitch);
-  zp[0] = ld<T>(Ec[0] + i + g.plane);
-  zp[1] = ld<T>(Ec[1] + i + g.plane);
-  h_cell<T, UPML>(a, x, y, z, ev, xp, yp, zp, h);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) st<T>(H[k] + i, h[k]);
-  if (x == g.nx) {
-    const long j = g.at(0, y, z);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      st<T>(Ec[k] + j, cmul(a.pxm, ev[k]));
-      st<T>(H[k] + j, cmul(a.pxm, h[k]));
-    }
-  }
-  if (y == g.ny) {
-    const long j = g.at(x, 0, z);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      st<T>(Ec[k] + j, cmul(a.pym, ev[k]));
-      st<T>(H[k] + j, cmul(a.pym, h[k]));
-    }
-  }
-  if (z == g.nz) {
-    const long j = g.at(x, y, 0);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      st<T>(Ec[k] + j, cmul(a.pzm, ev[k]));
-      st<T>(H[k] + j, cmul(a.pzm, h[k]));
-    }
-  }
 }
 
 template <typename T>
@@ -656,159 +374,6 @@ __global__ void __launch_bounds__(SX* SY) k_stream_h(FieldArgs<float> a, int* er
   stream_tile_h(a, 1 + blockIdx.x * SX, 1 + blockIdx.y * SY, 1 + blockIdx.z * SZC, (StageH*)smem, bar, par, err);
 }
 
-// ---------------------------------------------------------------------------
-// TF/SF source: tfsf_gauss (code/tfsf.f90:231-355) or tfsf_plane_wave
-// (code/tfsf.f90:359-517) evaluated in FP64 at the two planes the update
-// reads, then tfsf_update_3DArray (code/tfsf.f90:76-153) or
-// tfsf_update_2DArray (code/tfsf.f90:163-227) over the reference's ranges,
-// ghosts included.  The incident field is y-independent, so each thread
-// evaluates it once for its ix and walks a chunk of iy.
-
-struct SrcArgs {
-  int variant;  // 0 none, 1 update_3DArray, 2 update_2DArray
-  int i_pol, plane_wave, cosine;
-  int nx, ny, iz_min;
-  int ixo, izo_i;  // izo_i: the INTEGER izo of tfsf_plane_wave
-  double izo;      // the REAL izo of tfsf_gauss (zopump)
-  double Q, c0dt, ko, Dk, ux, uz;
-  double sign_kz;  // +1 source in the cover, -1 in the substrate
-  double sq_eps;   // sqrt(eps of the source medium)
-  double sqs;      // sqrt(eps)*sign_kz
-  double uzs;      // u_z*sign_kz
-  double amp;      // Epump*Q
-  double hcoef;    // Epump*Q*(dt*c0/Q)
-  double eps_in1, eps_src, dtcq2, s1, tincr, tdecay;
-};
-
-
-__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dq(double a, double b) { return __ddiv_rn(a, b); }
-
-// Incident field at (ix, iz), step it.  i_pol = 2: ta = tf1 (E_x), tb = tf5
-// (H_y, scaled by dt*c0/Q); i_pol = 1: ta = tf2 (E_y), tb = tf4 (H_x).  The
-// expressions keep the reference's association (code/tfsf.f90:306-347 and
-// :430-508), with exact shortcuts only where a factor is (1,0) or +-1.
-__device__ void incident(const SrcArgs& s, int ix, int iz, int it, cx<double>& ta, cx<double>& tb) {
-  double cs, sn, env;
-  const double t = dm(s.c0dt, (double)it);  // c0*dt*(it-ito), ito = 0
-  const bool gauss = s.plane_wave == 1;
-  if (gauss) {
-    const double A = da(dm(dm(s.Q, (double)(ix - s.ixo)), s.ux), dm(dm(s.Q, ds((double)iz, s.izo)), s.uz));
-    const double kzz = dm(s.ko, ds(dm(s.sqs, A), t));
-    const double arg = dq(ds(A, dq(t, s.sq_eps)), s.Dk);
-    env = exp(-dm(arg, arg));
-    sincos(kzz, &sn, &cs);
-  } else {
-    const double A = da(dm(dm(s.Q, (double)(ix - s.ixo)), s.ux), dm(dm(s.Q, (double)(iz - s.izo_i)), s.uz));
-    const double kzz = dm(s.ko, ds(A, dq(t, s.s1)));
-    const double d = dm(s.Q, fabs((double)(iz - s.izo_i)));
-    const double ton = dm(s.c0dt, ds((double)it, s.tincr));
-    const double toff = dm(s.c0dt, ds((double)it, s.tdecay));
-    if (ton <= d) env = exp(dq(-ds(d, ton), s.Dk));
-    else if (toff >= d) env = exp(dq(ds(d, toff), s.Dk));
-    else env = 1.0;
-    sincos(kzz, &sn, &cs);
-  }
-  const double sg = gauss ? s.sign_kz : 1.0;
-  // sign*(1,0)*exp(i kzz)*env  ->  (env*(sign*c), env*(sign*s))
-  const cx<double> w{dm(env, dm(sg, cs)), dm(env, dm(sg, sn))};
-  const cx<double> w1{dm(env, cs), dm(env, sn)};  // (1,0)*exp(i kzz)*env
-  if (s.i_pol == 2) {
-    const cx<double> ex{dm(s.uz, w.re), dm(s.uz, w.im)};
-    const cx<double> ez{-dm(s.ux, w1.re), -dm(s.ux, w1.im)};
-    cx<double> hy;
-    if (gauss) hy = {ds(dm(s.uzs, ex.re), dm(s.ux, ez.re)), ds(dm(s.uzs, ex.im), dm(s.ux, ez.im))};
-    else hy = {dm(s.s1, ds(dm(s.uz, ex.re), dm(s.ux, ez.re))), dm(s.s1, ds(dm(s.uz, ex.im), dm(s.ux, ez.im)))};
-    cx<double> exo = ex;
-    if (s.cosine == 1) {
-      exo.im = 0.0;
-      hy.im = 0.0;
-    }
-    ta = {dm(s.amp, exo.re), dm(s.amp, exo.im)};
-    tb = {dm(s.hcoef, hy.re), dm(s.hcoef, hy.im)};
-  } else if (s.i_pol == 1) {
-    const cx<double> hx{-dm(s.uz, w.re), -dm(s.uz, w.im)};
-    const cx<double> hz{dm(s.ux, w1.re), dm(s.ux, w1.im)};
-    cx<double> ey;
-    if (gauss) ey = {ds(dm(s.ux, hz.re), dm(s.uzs, hx.re)), ds(dm(s.ux, hz.im), dm(s.uzs, hx.im))};
-    else ey = {dm(s.s1, ds(dm(s.ux, hz.re), dm(s.uz, hx.re))), dm(s.s1, ds(dm(s.ux, hz.im), dm(s.uz, hx.im)))};
-    cx<double> hxo = hx;
-    if (s.cosine == 1) {
-      ey.im = 0.0;
-      hxo.im = 0.0;
-    }
-    ta = {dm(s.amp, ey.re), dm(s.amp, ey.im)};
-    tb = {dm(s.hcoef, hxo.re), dm(s.hcoef, hxo.im)};
-  } else {
-    ta = {0.0, 0.0};
-    tb = {0.0, 0.0};
-  }
-}
-
-// Add (sgn=+1) or subtract an FP64 correction to a stored field value.
-template <typename T> __device__ __forceinline__ void corr(typename V2<T>::t* p, cx<double> v, int sgn);
-template <> __device__ __forceinline__ void corr<double>(double2* p, cx<double> v, int sgn) {
-  double2 a = *p;
-  if (sgn > 0) { a.x = da(a.x, v.re); a.y = da(a.y, v.im); }
-  else { a.x = ds(a.x, v.re); a.y = ds(a.y, v.im); }
-  *p = a;
-}
-template <> __device__ __forceinline__ void corr<float>(float2* p, cx<double> v, int sgn) {
-  float2 a = *p;
-  if (sgn > 0) { a.x = (float)((double)a.x + v.re); a.y = (float)((double)a.y + v.im); }
-  else { a.x = (float)((double)a.x - v.re); a.y = (float)((double)a.y - v.im); }
-  *p = a;
-}
-
-constexpr int TFSF_YCH = 16;
-
-// Incident field at ix and the corrections of the rows iy in [y0, y1].
-template <typename T>
-__device__ __forceinline__ void tfsf_column(typename V2<T>::t* e, typename V2<T>::t* h, const Geo& g,
-                                            const SrcArgs& s, int it, int ix, int y0, int y1) {
-  const int zm = s.iz_min;
-  cx<double> ta, tb, vE, vH;
-  typename V2<T>::t *pe, *ph;
-  int sE, sH, exE, exH, eyE, eyH;  // ix limit and iy limit per update
-  if (s.variant == 1) {
-    cx<double> a0, b0, a1, b1;
-    incident(s, ix, zm - 1, it, a0, b0);  // tfsf_data(:, ix, iy, iz_min-1)
-    incident(s, ix, zm, it, a1, b1);      // tfsf_data(:, ix, iy, iz_min)
-    vE = {dm(s.eps_in1, b0.re), dm(s.eps_in1, b0.im)};
-    vH = {dm(s.dtcq2, a1.re), dm(s.dtcq2, a1.im)};
-    if (s.i_pol == 2) {
-      // E_x(iz_min) += eps_in(1)*tf5(iz_min-1): ix in [0,nx], iy in [0,ny+1]
-      // H_y(iz_min-1) += dtcq2*tf1(iz_min):      ix in [0,nx], iy in [0,ny+1]
-      pe = e;
-      ph = h + g.comp;
-      sE = +1; sH = +1;
-      exE = s.nx; exH = s.nx; eyE = s.ny + 1; eyH = s.ny + 1;
-    } else {
-      // E_y(iz_min) -= eps_in(1)*tf4(iz_min-1): ix in [0,nx+1], iy in [0,ny]
-      // H_x(iz_min-1) -= dtcq2*tf2(iz_min):      ix in [0,nx+1], iy in [0,ny]
-      pe = e + g.comp;
-      ph = h;
-      sE = -1; sH = -1;
-      exE = s.nx + 1; exH = s.nx + 1; eyE = s.ny; eyH = s.ny;
-    }
-    for (int iy = y0; iy <= y1; ++iy) {
-      if (ix <= exE && iy <= eyE) corr<T>(pe + g.at(ix, iy, zm), vE, sE);
-      if (ix <= exH && iy <= eyH) corr<T>(ph + g.at(ix, iy, zm - 1), vH, sH);
-    }
-  } else if (s.variant == 2) {
-    // E_x(iz_min) += tf5(iz_min)/eps ; H_y(iz_min) += dtcq2*tf1(iz_min)
-    incident(s, ix, zm, it, ta, tb);
-    vE = {dq(tb.re, s.eps_src), dq(tb.im, s.eps_src)};
-    vH = {dm(s.dtcq2, ta.re), dm(s.dtcq2, ta.im)};
-    for (int iy = y0; iy <= y1; ++iy) {
-      corr<T>(e + g.at(ix, iy, zm), vE, +1);
-      corr<T>(h + g.comp + g.at(ix, iy, zm), vH, +1);
-    }
-  }
-}
-
 template <typename T>
 // The step is it, or *itp + it when itp is given (a device-resident step
 // base, which lets a captured graph of steps be replayed at any step).
@@ -821,19 +386,6 @@ __global__ void __launch_bounds__(64) k_tfsf(typename V2<T>::t* e, typename V2<T
   tfsf_column<T>(e, h, g, s, it, ix, y0, min(y0 + TFSF_YCH - 1, s.ny + 1));
 }
 
-// ---------------------------------------------------------------------------
-// On-the-fly DFT (code/dataprocess.f90:109-209)
-
-// One contiguous run of sample points: one component on one face of a box,
-// locations in the reference's order (code/dataprocess.f90:813-900).
-struct Seg {
-  long src;    // storage index of the first location
-  long su, sv; // storage strides of the two in-face axes
-  int nu, nv;  // extents (u fastest)
-  int field;   // 0..2 E components, 3..5 H components
-  int pad;
-  long p0;     // first sample index
-};
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_dft_gather(const typename V2<T>::t* __restrict__ e,
@@ -1288,13 +840,6 @@ __global__ void k_material(const double* __restrict__ re, const double* __restri
   }
 }
 
-// Poynting flux of one face, code/dataprocess.f90:246-277:
-// J = sign * sum Re(a*conj(b) - c*conj(d)) * eps0*Q/(2 dt).
-struct FluxFace {
-  long pa, pb, pc, pd;  // first sample index of the four components
-  long n;               // locations on the face
-  int sign, active;
-};
 
 __global__ void __launch_bounds__(256) k_flux(const double2* __restrict__ fd, long P, const FluxFace* __restrict__ faces,
                                               int nof, double scale, double* __restrict__ J) {
@@ -1557,119 +1102,7 @@ void clear_error() { g_last_error.clear(); }
 
 using namespace iris;
 
-#define CK(call)                                                                                      \
-  do {                                                                                                \
-    cudaError_t err_ = (call);                                                                        \
-    if (err_ != cudaSuccess)                                                                          \
-      return fail(err_ == cudaErrorMemoryAllocation ? IRIS_ENOMEM : IRIS_ECUDA,                      \
-                  std::string(#call) + ": " + cudaGetErrorString(err_));                              \
-  } while (0)
-
-
 namespace {
-
-struct FaceMap {
-  bool active = false;  // this face pair is accumulated by scattering_fourier
-  int nu = 0, nv = 0;
-  long nloc = 0;         // locations per face
-  long base[2][6] = {};  // first sample index per [side][component]
-};
-
-}  // namespace
-
-struct iris_engine {
-  iris_params p{};
-  std::vector<double> fw;
-  int prec = IRIS_FP64;
-  size_t esz = 16;  // bytes per stored complex value
-  int device = 0;
-  cudaStream_t st = nullptr;
-  Geo g{};
-  dim3 blk, grd;
-  void* e = nullptr;
-  void* h = nullptr;
-  void* pml_d[2] = {nullptr, nullptr};
-  void* pml_b[2] = {nullptr, nullptr};
-  long pcomp[2] = {0, 0};
-  int nbot = 0, ntop = 0;
-  void* coef = nullptr;
-  std::vector<double> coef_h;
-  void* eps = nullptr;
-  bool eps_complex = false;
-  double ph[6][2] = {};  // exp(+i akx), exp(+i aky), exp(+i akz), exp(-i akx), ...
-  SrcArgs src{};
-  dim3 tf_blk, tf_grd;
-  // DFT
-  int nboxes = 1;
-  FaceMap fm[2][3];
-  long P = 0;
-  int K = 0, nslot = 0;
-  std::vector<Seg> segs;
-  long max_seg = 0;
-  Seg* d_segs = nullptr;
-  void* S = nullptr;
-  int* d_tk = nullptr;
-  double* d_fw = nullptr;
-  double2* fd = nullptr;
-  float2* d_wt = nullptr;
-  double2* d_wt64 = nullptr;  // FP64 mode twiddles of one block
-  bool dft_tc = false;     // FP32 block accumulation on the tensor cores
-  float* d_wtc = nullptr;  // its B operands (k_twiddle_tc)
-  FluxFace* d_faces = nullptr;
-  double* d_J = nullptr;
-  double* h_J = nullptr;
-  // batch member: no DFT buffers of its own; z-plane DFT only on request
-  bool member = false;
-  bool dft_z_only = false;
-  std::vector<FluxFace> host_faces;
-  // fused E+H stepping (FP32): second field buffers and D, per-step TF/SF table
-  bool fused = false;
-  void* e2 = nullptr;
-  void* h2 = nullptr;
-  void* pml_d2[2] = {nullptr, nullptr};
-  int zchunk = 0;
-  dim3 fblk, fgrd;
-  // CUDA graph of one DFT block of steps (iris_params.graph): d_it holds the
-  // step base the captured kernels add to their offsets, dev_it its value
-  cudaGraphExec_t gexec = nullptr;
-  int* d_it = nullptr;
-  int dev_it = -1;
-  // streamed split passes (FP32, real material); d_err: a kernel's give-up record
-  bool stream = false;
-  dim3 sgrd;
-  int* d_err = nullptr;
-  // timing: CUDA events on the engine stream, per kernel class
-  bool timing = false;
-  cudaEvent_t t0 = nullptr, t1 = nullptr;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[IRIS_NKC];
-  size_t ev_used[IRIS_NKC] = {};
-};
-
-namespace {
-
-// Brackets one kernel launch with a pair of events when timing is on.
-struct KTimer {
-  iris_engine* E;
-  int k;
-  cudaEvent_t b = nullptr, e = nullptr;
-  KTimer(iris_engine* eng, int kind) : E(eng), k(kind) {
-    if (!E->timing) return;
-    auto& v = E->ev[k];
-    if (E->ev_used[k] == v.size()) {
-      cudaEvent_t x, y;
-      cudaEventCreate(&x);
-      cudaEventCreate(&y);
-      v.push_back({x, y});
-    }
-    b = v[E->ev_used[k]].first;
-    e = v[E->ev_used[k]].second;
-    ++E->ev_used[k];
-    cudaEventRecord(b, E->st);
-  }
-  ~KTimer() {
-    if (b) cudaEventRecord(e, E->st);
-  }
-};
 
 int p2ceil(int n) {
   int v = 1;
@@ -1795,35 +1228,6 @@ int validate(const iris_params& p) {
   return IRIS_OK;
 }
 
-template <typename T> FieldArgs<T> field_args(const iris_engine* E) {
-  using V = typename V2<T>::t;
-  const iris_params& p = E->p;
-  FieldArgs<T> a{};
-  a.e = (V*)E->e;
-  a.h = (V*)E->h;
-  a.g = E->g;
-  for (int s = 0; s < 2; ++s) {
-    a.pml_d[s] = (V*)E->pml_d[s];
-    a.pml_b[s] = (V*)E->pml_b[s];
-    a.pcomp[s] = E->pcomp[s];
-  }
-  a.coef = (const T*)E->coef;
-  a.pmlzi = p.pmlzi;
-  a.pmlzf = p.pmlzf;
-  a.hi = p.hi;
-  a.hf = p.hf;
-  a.eps_c = E->eps_complex ? (const V*)E->eps : nullptr;
-  a.eps_r = E->eps_complex ? nullptr : (const T*)E->eps;
-  a.m1 = (T)(1.0 / p.eps1);
-  a.m3 = (T)(1.0 / p.eps3);
-  a.eps0sq = (T)(p.eps0 * p.eps0);
-  const double dtc = p.dt * p.c0 / p.Q;
-  a.dtcq2 = (T)(dtc * dtc);
-  cx<T>* ph[6] = {&a.pxp, &a.pyp, &a.pzp, &a.pxm, &a.pym, &a.pzm};
-  for (int k = 0; k < 6; ++k) *ph[k] = cx<T>{(T)E->ph[k][0], (T)E->ph[k][1]};
-  return a;
-}
-
 template <typename T> void launch_e(iris_engine* E) {
   KTimer tm(E, IRIS_KC_E);
   FieldArgs<T> a = field_args<T>(E);
@@ -1853,35 +1257,6 @@ template <typename T> void launch_tfsf(iris_engine* E, int it, const int* itp = 
   k_tfsf<T><<<E->tf_grd, E->tf_blk, 0, E->st>>>((V*)E->e, (V*)E->h, E->g, E->src, it, itp);
 }
 
-void dft_flush(iris_engine* E) {
-  if (E->nslot == 0) return;
-  KTimer tm(E, IRIS_KC_DFT);
-  const int nk = E->nslot;
-  if (E->prec == IRIS_FP64) {
-    const int nwc = (E->p.nof + DFT64_WC - 1) / DFT64_WC;
-    const long nblk = (E->P + 127) / 128;
-    k_twiddle64<<<(nk * E->p.nof + 255) / 256, 256, 0, E->st>>>(E->d_tk, nk, E->d_fw, E->p.nof, E->d_wt64);
-    k_dft_fp64<<<(unsigned)(nblk * nwc), 128, (size_t)nk * DFT64_WC * sizeof(double2), E->st>>>(
-        (const double2*)E->S, E->P, nk, E->d_wt64, E->p.nof, nwc, E->p.dt, E->fd);
-  } else if (E->dft_tc) {
-    const int ng = (E->p.nof + TC_NW - 1) / TC_NW, nch = (2 * nk + TC_KC - 1) / TC_KC;
-    const long nt = (long)ng * nch * TC_BROWS * TC_KC;
-    k_twiddle_tc<<<(unsigned)((nt + 255) / 256), 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, ng,
-                                                                   nch, E->d_wtc);
-    const long ntiles = (E->P + TC_M - 1) / TC_M;
-    k_dft_tc<<<(unsigned)(ntiles * ng), TC_THREADS, TC_SMEM, E->st>>>((const float2*)E->S, E->P, nk, E->d_wtc,
-                                                                       E->p.nof, ng, E->fd, E->d_err);
-  } else {
-    const int nt = nk * E->p.nof;
-    k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
-    const int nwc = (E->p.nof + DFT_TW - 1) / DFT_TW;
-    const long nblk = (E->P + DFT_TP - 1) / DFT_TP;
-    k_dft_fp32<<<(unsigned)(nblk * nwc), DFT_THREADS, 0, E->st>>>((const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, nwc,
-                                                        E->fd);
-  }
-  E->nslot = 0;
-}
-
 template <typename T> void dft_sample(iris_engine* E, int t, const int* tp = nullptr) {
   if (E->P == 0) return;
   using V = typename V2<T>::t;
@@ -1905,48 +1280,6 @@ FusedArgs fused_args(const iris_engine* E) {
   return a;
 }
 
-// A whole DFT block of steps from it on can be replayed from a graph: every
-// step of it is sampled and the block starts with an empty ring.
-bool graph_ready(const iris_engine* E, int it, int left) {
-  const iris_params& p = E->p;
-  // the fused passes swap buffers every step: an even block brings them back
-  return p.graph && !E->timing && (!E->fused || E->K % 2 == 0) && E->P > 0 && E->nslot == 0 &&
-         p.sample_fourier == 1 && it >= p.to_fourier && left >= E->K;
-}
-
-void graph_reset(iris_engine* E) {
-  if (E->gexec) cudaGraphExecDestroy(E->gexec);
-  E->gexec = nullptr;
-}
-
-// Steps it .. it+K-1 from the engine's graph of one DFT block (captured on
-// first use from record(), which issues the K steps with step offsets
-// 0 .. K-1 relative to the device-resident base d_it, the block's sample
-// flush, and the base's advance by K).
-template <typename F> int graph_block(iris_engine* E, int it, F record) {
-  if (!E->d_it) {
-    CK(cudaMalloc(&E->d_it, sizeof(int)));
-    E->dev_it = -1;
-  }
-  if (E->dev_it != it) k_set_int<<<1, 1, 0, E->st>>>(E->d_it, it);
-  if (!E->gexec) {
-    cudaGraph_t gr = nullptr;
-    CK(cudaStreamBeginCapture(E->st, cudaStreamCaptureModeRelaxed));
-    record();
-    k_add_int<<<1, 1, 0, E->st>>>(E->d_it, E->K);
-    const cudaError_t ec = cudaStreamEndCapture(E->st, &gr);
-    if (ec != cudaSuccess) return fail(IRIS_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
-    const cudaError_t ei = cudaGraphInstantiate(&E->gexec, gr, 0);
-    cudaGraphDestroy(gr);
-    if (ei != cudaSuccess) {
-      E->gexec = nullptr;
-      return fail(IRIS_ECUDA, std::string("graph instantiation: ") + cudaGetErrorString(ei));
-    }
-  }
-  CK(cudaGraphLaunch(E->gexec, E->st));
-  E->dev_it = it + E->K;
-  return IRIS_OK;
-}
 
 // One fused step into the second buffers, swap, then TF/SF and the DFT
 // sample on the new state, in the operator order of the split passes; step
@@ -2071,8 +1404,6 @@ int upload_material(iris_engine* E, const double* re, const double* im) {
   return IRIS_OK;
 }
 
-int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces);
-
 int build_dft(iris_engine* E) {
   const iris_params& p = E->p;
   bool single = true;
@@ -2139,6 +1470,82 @@ int build_dft(iris_engine* E) {
   return alloc_dft(E, faces.data(), 12);
 }
 
+}  // namespace
+
+namespace iris {
+
+void dft_flush(iris_engine* E) {
+  if (E->nslot == 0) return;
+  KTimer tm(E, IRIS_KC_DFT);
+  const int nk = E->nslot;
+  if (E->prec == IRIS_FP64) {
+    const int nwc = (E->p.nof + DFT64_WC - 1) / DFT64_WC;
+    const long nblk = (E->P + 127) / 128;
+    k_twiddle64<<<(nk * E->p.nof + 255) / 256, 256, 0, E->st>>>(E->d_tk, nk, E->d_fw, E->p.nof, E->d_wt64);
+    k_dft_fp64<<<(unsigned)(nblk * nwc), 128, (size_t)nk * DFT64_WC * sizeof(double2), E->st>>>(
+        (const double2*)E->S, E->P, nk, E->d_wt64, E->p.nof, nwc, E->p.dt, E->fd);
+  } else if (E->dft_tc) {
+    const int ng = (E->p.nof + TC_NW - 1) / TC_NW, nch = (2 * nk + TC_KC - 1) / TC_KC;
+    const long nt = (long)ng * nch * TC_BROWS * TC_KC;
+    k_twiddle_tc<<<(unsigned)((nt + 255) / 256), 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, ng,
+                                                                   nch, E->d_wtc);
+    const long ntiles = (E->P + TC_M - 1) / TC_M;
+    k_dft_tc<<<(unsigned)(ntiles * ng), TC_THREADS, TC_SMEM, E->st>>>((const float2*)E->S, E->P, nk, E->d_wtc,
+                                                                       E->p.nof, ng, E->fd, E->d_err);
+  } else {
+    const int nt = nk * E->p.nof;
+    k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
+    const int nwc = (E->p.nof + DFT_TW - 1) / DFT_TW;
+    const long nblk = (E->P + DFT_TP - 1) / DFT_TP;
+    k_dft_fp32<<<(unsigned)(nblk * nwc), DFT_THREADS, 0, E->st>>>((const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, nwc,
+                                                        E->fd);
+  }
+  E->nslot = 0;
+}
+
+// A whole DFT block of steps from it on can be replayed from a graph: every
+// step of it is sampled and the block starts with an empty ring.
+bool graph_ready(const iris_engine* E, int it, int left) {
+  const iris_params& p = E->p;
+  // the fused passes swap buffers every step: an even block brings them back
+  return p.graph && !E->timing && (!E->fused || E->K % 2 == 0) && E->P > 0 && E->nslot == 0 &&
+         p.sample_fourier == 1 && it >= p.to_fourier && left >= E->K;
+}
+
+void graph_reset(iris_engine* E) {
+  if (E->gexec) cudaGraphExecDestroy(E->gexec);
+  E->gexec = nullptr;
+}
+
+// Steps it .. it+K-1 from the engine's graph of one DFT block (captured on
+// first use from record(), which issues the K steps with step offsets
+// 0 .. K-1 relative to the device-resident base d_it, the block's sample
+// flush, and the base's advance by K).
+int graph_block(iris_engine* E, int it, const std::function<void()>& record) {
+  if (!E->d_it) {
+    CK(cudaMalloc(&E->d_it, sizeof(int)));
+    E->dev_it = -1;
+  }
+  if (E->dev_it != it) k_set_int<<<1, 1, 0, E->st>>>(E->d_it, it);
+  if (!E->gexec) {
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamBeginCapture(E->st, cudaStreamCaptureModeRelaxed));
+    record();
+    k_add_int<<<1, 1, 0, E->st>>>(E->d_it, E->K);
+    const cudaError_t ec = cudaStreamEndCapture(E->st, &gr);
+    if (ec != cudaSuccess) return fail(IRIS_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(&E->gexec, gr, 0);
+    cudaGraphDestroy(gr);
+    if (ei != cudaSuccess) {
+      E->gexec = nullptr;
+      return fail(IRIS_ECUDA, std::string("graph instantiation: ") + cudaGetErrorString(ei));
+    }
+  }
+  CK(cudaGraphLaunch(E->gexec, E->st));
+  E->dev_it = it + E->K;
+  return IRIS_OK;
+}
+
 // DFT buffers for E->P sample points: accumulators, the K-slot sample ring,
 // twiddles, the flux faces (nfaces FluxFace) and the flux output.
 int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
@@ -2200,29 +1607,27 @@ void free_engine(iris_engine* E) {
   if (E->st) cudaStreamDestroy(E->st);
 }
 
-}  // namespace
 
-long iris::engine_npts(const iris_engine* E, int box, int j) {
-  if (box < 0 || box >= E->nboxes || j < 1 || j > 3) return 0;
-  const FaceMap& F = E->fm[box][j - 1];
-  return F.active ? 12 * F.nloc : 0;
+void split_step(iris_engine* E, int it, bool dft) {
+  const iris_params& p = E->p;
+  const bool sampled = dft && it >= p.to_fourier && it % p.sample_fourier == 0;
+  if (E->prec == IRIS_FP64) {
+    launch_e<double>(E);
+    launch_h<double>(E);
+    launch_tfsf<double>(E, it);
+    if (sampled) dft_sample<double>(E, it + 1 - p.to_fourier);
+  } else {
+    launch_e<float>(E);
+    launch_h<float>(E);
+    launch_tfsf<float>(E, it);
+    if (sampled) dft_sample<float>(E, it + 1 - p.to_fourier);
+  }
 }
-
-extern "C" {
-
-static int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out,
-                         bool packed = false);
-
-int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
-  return create_engine(pin, fw, false, false, out);
-}
-
-}  // extern "C"
 
 // packed: rows of nx+2 cells back to back (no 128-byte alignment of x = 1),
 // for cells whose rows are short; component arrays stay 128-byte aligned.
-static int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out,
-                         bool packed) {
+int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out,
+                  bool packed) {
   clear_error();
   if (!pin || !fw || !out) return fail(IRIS_EINVAL, "null argument");
   *out = nullptr;
@@ -2348,6 +1753,14 @@ static int create_engine(const iris_params* pin, const double* fw, bool member, 
   return IRIS_OK;
 }
 
+}  // namespace iris
+
+long iris::engine_npts(const iris_engine* E, int box, int j) {
+  if (box < 0 || box >= E->nboxes || j < 1 || j > 3) return 0;
+  const FaceMap& F = E->fm[box][j - 1];
+  return F.active ? 12 * F.nloc : 0;
+}
+
 // Status of the engine's bounded device waits: IRIS_ETIMEOUT once a kernel
 // gave up on one (the stream is synchronised first).
 static int stream_status(iris_engine* E) {
@@ -2361,7 +1774,32 @@ static int stream_status(iris_engine* E) {
   return IRIS_OK;
 }
 
+int iris::read_flux(iris_engine* E, int set, double* J) {
+  const iris_params& p = E->p;
+  dft_flush(E);
+  const double scale = p.eps0 * p.Q / (2.0 * p.dt);
+  {
+    KTimer tm(E, IRIS_KC_FLUX);
+    k_flux<<<dim3(p.nof, 6), 256, 0, E->st>>>(E->fd, E->P, E->d_faces + 6 * set, p.nof, scale, E->d_J);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(E->h_J, E->d_J, sizeof(double) * 6 * p.nof, cudaMemcpyDeviceToHost, E->st));
+  CK(cudaStreamSynchronize(E->st));
+  int rc = stream_status(E);
+  if (rc) return rc;
+  bool finite = true;
+  for (int k = 0; k < 6 * p.nof; ++k) {
+    J[k] = E->h_J[k];
+    if (!std::isfinite(J[k])) finite = false;
+  }
+  return finite ? IRIS_OK : fail(IRIS_ENAN, "non-finite flux");
+}
+
 extern "C" {
+
+int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
+  return create_engine(pin, fw, false, false, out);
+}
 
 void iris_destroy(iris_engine* E) {
   if (!E) return;
@@ -2399,24 +1837,8 @@ int iris_flux(iris_engine* E, int box, double* J) {
   clear_error();
   if (!E || !J || box < 0 || box > 1) return fail(IRIS_EINVAL, "bad argument");
   CK(cudaSetDevice(E->device));
-  const iris_params& p = E->p;
   if (box >= E->nboxes) box = 0;  // a single box: the second one is the same box
-  dft_flush(E);
-  const double scale = p.eps0 * p.Q / (2.0 * p.dt);
-  KTimer tm(E, IRIS_KC_FLUX);
-  k_flux<<<dim3(p.nof, 6), 256, 0, E->st>>>(E->fd, E->P, E->d_faces + 6 * box, p.nof, scale, E->d_J);
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(E->h_J, E->d_J, sizeof(double) * 6 * p.nof, cudaMemcpyDeviceToHost, E->st));
-  CK(cudaStreamSynchronize(E->st));
-  int rc = stream_status(E);
-  if (rc) return rc;
-  bool finite = true;
-  for (int k = 0; k < 6 * p.nof; ++k) {
-    J[k] = E->h_J[k];
-    if (!std::isfinite(J[k])) finite = false;
-  }
-  if (!finite) return fail(IRIS_ENAN, "non-finite flux");
-  return IRIS_OK;
+  return read_flux(E, box, J);
 }
 
 int iris_get_field(iris_engine* E, int which, double* re, double* im) {
@@ -2706,1281 +2128,3 @@ extern "C" int iris_dft_block_noalloc(const void* samples, int nk, long npts, in
   CK(cudaGetLastError());
   return IRIS_OK;
 }
-
-// ---------------------------------------------------------------------------
-// Batched form: many independent Bloch cells (or k-points) stepped together.
-//
-// Each cell is a member engine (its own fields, UPML, material, source and
-// DFT point layout, but no DFT buffers).  One launch per operator covers
-// every cell: a persistent kernel walks a work list of (cell, tile) items in
-// cell, z, y, x order, so the CTAs running together touch neighbouring tiles
-// of one cell and the neighbour loads hit L2.  The DFT samples of all cells go
-// to one shared ring and one accumulator array (all cells share dt and the
-// frequency list) and are accumulated by the single-engine block kernel.  The
-// tile shape is picked by iris_batch_tune, which times the candidates on the
-// batch itself.
-
-namespace iris {
-namespace {
-
-struct BItem {
-  int cell, x0, y0, z0;  // tile origin (1-based)
-};
-struct TItem {
-  int cell, ix0, iy0, pad;
-};
-struct BSeg {
-  Seg s;
-  int cell, pad;
-};
-
-// Work-list shapes the autotuner chooses from: x * y * z blocks of cells,
-// and (FLAT) 256 consecutive cells of one plane in row-major order, which
-// keeps every lane busy whatever the cell's nx.
-// keeps every lane busy whatever the cell's nx (FLAT: register-capped for
-// five resident blocks per SM; FLAT + 1: uncapped).
-constexpr int NTILES = 7, FLAT = 5;
-constexpr int TILES[NTILES][3] = {{32, 8, 1}, {32, 4, 2}, {64, 4, 1}, {16, 16, 1}, {32, 2, 4}, {256, 1, 1}, {256, 1, 1}};
-
-// Copies the cell's arguments into shared memory when the item's cell changes.
-template <typename A>
-__device__ __forceinline__ void cell_args(const A* args, int cell, A& sa, int& scell, int tid) {
-  if (cell != scell) {
-    __syncthreads();
-    if (tid == 0) {
-      sa = args[cell];
-      scell = cell;
-    }
-    __syncthreads();
-  }
-}
-
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX* TY* TZ) k_batch_e(const FieldArgs<T>* __restrict__ args,
-                                                        const BItem* __restrict__ items, long nitems) {
-  __shared__ FieldArgs<T> sa;
-  __shared__ int scell;
-  const int tid = (threadIdx.z * TY + threadIdx.y) * TX + threadIdx.x;
-  if (tid == 0) scell = -1;
-  __syncthreads();
-  for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
-    const BItem b = items[k];
-    cell_args(args, b.cell, sa, scell, tid);
-    const int x = b.x0 + threadIdx.x, y = b.y0 + threadIdx.y, z = b.z0 + threadIdx.z;
-    if (x <= sa.g.nx && y <= sa.g.ny && z <= sa.g.nz) {
-      if (sa.eps_c) e_split_cell<T, true>(sa, x, y, z);
-      else e_split_cell<T, false>(sa, x, y, z);
-    }
-  }
-}
-
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX* TY* TZ) k_batch_h(const FieldArgs<T>* __restrict__ args,
-                                                        const BItem* __restrict__ items, long nitems) {
-  __shared__ FieldArgs<T> sa;
-  __shared__ int scell;
-  const int tid = (threadIdx.z * TY + threadIdx.y) * TX + threadIdx.x;
-  if (tid == 0) scell = -1;
-  __syncthreads();
-  for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
-    const BItem b = items[k];
-    cell_args(args, b.cell, sa, scell, tid);
-    const int x = b.x0 + threadIdx.x, y = b.y0 + threadIdx.y, z = b.z0 + threadIdx.z;
-    if (x <= sa.g.nx && y <= sa.g.ny && z <= sa.g.nz) h_split_cell<T>(sa, x, y, z);
-  }
-}
-
-// FLAT items: x0 = first row-major offset in the plane, z0 = the plane.
-// MINB: resident blocks per SM asked of the register allocator (0: none).
-// CEPS: some cell has a complex material (else every eps_c is null).
-// UPML = false: every item's plane lies outside its cell's UPML slabs.
-template <typename T, bool EPASS, int MINB, bool CEPS, bool UPML>
-__global__ void __launch_bounds__(256, MINB) k_batch_flat(const FieldArgs<T>* __restrict__ args,
-                                                    const BItem* __restrict__ items, long nitems) {
-  __shared__ FieldArgs<T> sa;
-  __shared__ int scell;
-  const int tid = threadIdx.x;
-  if (tid == 0) scell = -1;
-  __syncthreads();
-  // the next item's descriptor is loaded while this one is processed
-  BItem nb = blockIdx.x < nitems ? items[blockIdx.x] : BItem{};
-  for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
-    const BItem b = nb;
-    if (k + gridDim.x < nitems) nb = items[k + gridDim.x];
-    cell_args(args, b.cell, sa, scell, tid);
-    const int nx = sa.g.nx;
-    const int L = b.x0 + tid;
-    if (L < nx * sa.g.ny) {
-      const int y = L / nx, x = L - y * nx;
-      if (EPASS) {
-        if (CEPS && sa.eps_c) e_split_cell<T, true, UPML>(sa, x + 1, y + 1, b.z0);
-        else e_split_cell<T, false, UPML>(sa, x + 1, y + 1, b.z0);
-      } else {
-        h_split_cell<T, UPML>(sa, x + 1, y + 1, b.z0);
-      }
-    }
-  }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(64) k_batch_tfsf(const FieldArgs<T>* __restrict__ args,
-                                                   const SrcArgs* __restrict__ srcs, const TItem* __restrict__ items,
-                                                   long nitems, int it, const int* itp) {
-  if (itp) it += *itp;
-  for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
-    const TItem b = items[k];
-    const FieldArgs<T>& a = args[b.cell];
-    const SrcArgs& s = srcs[b.cell];
-    const int ix = b.ix0 + threadIdx.x;
-    if (s.variant == 0 || ix > s.nx + 1) continue;
-    tfsf_column<T>(a.e, a.h, a.g, s, it, ix, b.iy0, min(b.iy0 + TFSF_YCH - 1, s.ny + 1));
-  }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_batch_gather(const FieldArgs<T>* __restrict__ args,
-                                                      const BSeg* __restrict__ segs,
-                                                      typename V2<T>::t* __restrict__ slot, int* tk, int islot,
-                                                      int t, const int* tp) {
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = tp ? *tp + t : t;
-  const BSeg b = segs[blockIdx.y];
-  const long L = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (L >= (long)b.s.nu * b.s.nv) return;
-  const FieldArgs<T>& a = args[b.cell];
-  const int u = (int)(L % b.s.nu), v = (int)(L / b.s.nu);
-  const typename V2<T>::t* src = b.s.field < 3 ? a.e + b.s.field * a.g.comp : a.h + (b.s.field - 3) * a.g.comp;
-  slot[b.s.p0 + L] = src[b.s.src + (long)u * b.s.su + (long)v * b.s.sv];
-}
-
-}  // namespace
-}  // namespace iris
-
-struct iris_batch {
-  int n = 0;
-  int prec = IRIS_FP64;
-  int device = 0;
-  iris_engine* master = nullptr;  // stream, timing and the shared DFT buffers
-  std::vector<iris_engine*> cells;
-  std::vector<long> pbase;
-  void* d_args = nullptr;  // FieldArgs<T>[n]
-  SrcArgs* d_src = nullptr;
-  BItem* d_items = nullptr;
-  long nitems = 0;
-  long nitems_in = 0;  // flat work lists: items outside the UPML slabs come first
-  int tile = 0;  // index into TILES
-  int grid_e = 0, grid_h = 0;
-  TItem* d_titems = nullptr;
-  long ntitems = 0;
-  BSeg* d_bsegs = nullptr;
-  int nbsegs = 0;
-  long max_seg = 0;
-  long steps_taken = 0;
-};
-
-namespace {
-
-int batch_upload_args(iris_batch* B) {
-  const size_t sz = B->prec == IRIS_FP64 ? sizeof(FieldArgs<double>) : sizeof(FieldArgs<float>);
-  std::vector<unsigned char> h(sz * B->n);
-  for (int c = 0; c < B->n; ++c) {
-    if (B->prec == IRIS_FP64) {
-      FieldArgs<double> a = field_args<double>(B->cells[c]);
-      std::memcpy(h.data() + sz * c, &a, sz);
-    } else {
-      FieldArgs<float> a = field_args<float>(B->cells[c]);
-      std::memcpy(h.data() + sz * c, &a, sz);
-    }
-  }
-  if (!B->d_args) CK(cudaMalloc(&B->d_args, h.size()));
-  CK(cudaMemcpy(B->d_args, h.data(), h.size(), cudaMemcpyHostToDevice));
-  return IRIS_OK;
-}
-
-int batch_build_items(iris_batch* B, int tile) {
-  const int TX = TILES[tile][0], TY = TILES[tile][1], TZ = TILES[tile][2];
-  std::vector<BItem> items;
-  for (int c = 0; c < B->n; ++c) {
-    const iris_params& p = B->cells[c]->p;
-    if (tile >= FLAT) {
-      const int nxy = p.nx * p.ny;
-      for (int z = 1; z <= p.nz; ++z)
-        if (z > p.pmlzi && z < p.pmlzf)
-          for (int l = 0; l < nxy; l += TX) items.push_back(BItem{c, l, 0, z});
-      continue;
-    }
-    for (int z = 1; z <= p.nz; z += TZ)
-      for (int y = 1; y <= p.ny; y += TY)
-        for (int x = 1; x <= p.nx; x += TX) items.push_back(BItem{c, x, y, z});
-  }
-  B->nitems_in = tile >= FLAT ? (long)items.size() : 0;
-  if (tile >= FLAT)
-    for (int c = 0; c < B->n; ++c) {
-      const iris_params& p = B->cells[c]->p;
-      const int nxy = p.nx * p.ny;
-      for (int z = 1; z <= p.nz; ++z)
-        if (z <= p.pmlzi || z >= p.pmlzf)
-          for (int l = 0; l < nxy; l += TX) items.push_back(BItem{c, l, 0, z});
-    }
-  graph_reset(B->master);  // captured launches hold the old work list
-  if (B->d_items) cudaFree(B->d_items);
-  B->d_items = nullptr;
-  CK(cudaMalloc(&B->d_items, sizeof(BItem) * items.size()));
-  CK(cudaMemcpy(B->d_items, items.data(), sizeof(BItem) * items.size(), cudaMemcpyHostToDevice));
-  B->nitems = (long)items.size();
-  B->tile = tile;
-  return IRIS_OK;
-}
-
-template <typename T, int TX, int TY, int TZ> int persistent_grid(const void* kern) {
-  int nsm = 0, per = 0, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TX * TY * TZ, 0);
-  return std::max(1, nsm * std::max(1, per));
-}
-
-template <typename T, int TX, int TY, int TZ> void launch_batch_eh(iris_batch* B, bool e) {
-  iris_engine* M = B->master;
-  const dim3 blk(TX, TY, TZ);
-  const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
-  if (e) {
-    static int grid = 0;
-    if (!grid) grid = persistent_grid<T, TX, TY, TZ>((const void*)k_batch_e<T, TX, TY, TZ>);
-    const long g = std::min<long>(grid, B->nitems);
-    KTimer tm(M, IRIS_KC_E);
-    k_batch_e<T, TX, TY, TZ><<<(unsigned)g, blk, 0, M->st>>>(args, B->d_items, B->nitems);
-  } else {
-    static int grid = 0;
-    if (!grid) grid = persistent_grid<T, TX, TY, TZ>((const void*)k_batch_h<T, TX, TY, TZ>);
-    const long g = std::min<long>(grid, B->nitems);
-    KTimer tm(M, IRIS_KC_H);
-    k_batch_h<T, TX, TY, TZ><<<(unsigned)g, blk, 0, M->st>>>(args, B->d_items, B->nitems);
-  }
-}
-
-template <typename T, int MINB, bool CEPS, bool UPML>
-void launch_flat_part(iris_batch* B, bool e, const BItem* items, long n) {
-  if (n <= 0) return;
-  iris_engine* M = B->master;
-  const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
-  auto kern = e ? k_batch_flat<T, true, MINB, CEPS, UPML> : k_batch_flat<T, false, MINB, false, UPML>;
-  static int grid_e = 0, grid_h = 0;
-  int& grid = e ? grid_e : grid_h;
-  if (!grid) grid = persistent_grid<T, 256, 1, 1>((const void*)kern);
-  kern<<<(unsigned)std::min<long>(grid, n), 256, 0, M->st>>>(args, items, n);
-}
-
-// One pass over a flat work list: the planes outside the UPML slabs with a
-// kernel that has no slab code (fewer registers, more resident warps), then
-// the slab planes.
-template <typename T, int MINB, bool CEPS> void launch_flat(iris_batch* B, bool e) {
-  KTimer tm(B->master, e ? IRIS_KC_E : IRIS_KC_H);
-  launch_flat_part<T, MINB, CEPS, false>(B, e, B->d_items, B->nitems_in);
-  launch_flat_part<T, MINB, CEPS, true>(B, e, B->d_items + B->nitems_in, B->nitems - B->nitems_in);
-}
-
-template <typename T, int MINB> void launch_batch_flat(iris_batch* B, bool e) {
-  bool cplx = false;
-  for (const iris_engine* E : B->cells) cplx |= E->eps_complex;
-  if (cplx) launch_flat<T, MINB, true>(B, e);
-  else launch_flat<T, MINB, false>(B, e);
-}
-
-template <typename T> void batch_eh(iris_batch* B, bool e) {
-  switch (B->tile) {
-    case FLAT: launch_batch_flat<T, 5>(B, e); break;
-    case FLAT + 1: launch_batch_flat<T, 0>(B, e); break;
-    case 0: launch_batch_eh<T, 32, 8, 1>(B, e); break;
-    case 1: launch_batch_eh<T, 32, 4, 2>(B, e); break;
-    case 2: launch_batch_eh<T, 64, 4, 1>(B, e); break;
-    case 3: launch_batch_eh<T, 16, 16, 1>(B, e); break;
-    default: launch_batch_eh<T, 32, 2, 4>(B, e); break;
-  }
-}
-
-// One step of every cell: step it, or *itp + it when itp is given; sampled
-// says whether the step's DFT sample is taken.
-template <typename T> void batch_one_step(iris_batch* B, int it, const int* itp, bool sampled) {
-  iris_engine* M = B->master;
-  const iris_params& p = M->p;
-  using V = typename V2<T>::t;
-  const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
-  batch_eh<T>(B, true);
-  batch_eh<T>(B, false);
-  if (B->ntitems) {
-    KTimer tm(M, IRIS_KC_TFSF);
-    const long g = std::min<long>(B->ntitems, 152L * 16);
-    k_batch_tfsf<T><<<(unsigned)g, 64, 0, M->st>>>(args, B->d_src, B->d_titems, B->ntitems, it, itp);
-  }
-  if (sampled) {
-    {
-      KTimer tm(M, IRIS_KC_GATHER);
-      V* slot = (V*)M->S + (long)M->nslot * M->P;
-      dim3 grid((unsigned)((B->max_seg + 255) / 256), (unsigned)B->nbsegs);
-      k_batch_gather<T><<<grid, 256, 0, M->st>>>(args, B->d_bsegs, slot, M->d_tk, M->nslot, it + 1 - p.to_fourier,
-                                                 itp);
-    }
-    if (++M->nslot == M->K) dft_flush(M);
-  }
-}
-
-template <typename T> int batch_step_t(iris_batch* B, int it0, int n) {
-  iris_engine* M = B->master;
-  const iris_params& p = M->p;
-  int it = it0;
-  while (it < it0 + n) {
-    if (graph_ready(M, it, it0 + n - it)) {
-      int rc = graph_block(M, it, [&] {
-        for (int j = 0; j < M->K; ++j) batch_one_step<T>(B, j, M->d_it, true);
-      });
-      if (rc) return rc;
-      it += M->K;
-      continue;
-    }
-    batch_one_step<T>(B, it, nullptr, M->P > 0 && it >= p.to_fourier && it % p.sample_fourier == 0);
-    ++it;
-  }
-  B->steps_taken += n;
-  CK(cudaGetLastError());
-  return IRIS_OK;
-}
-
-void batch_free(iris_batch* B) {
-  for (iris_engine* E : B->cells)
-    if (E) iris_destroy(E);
-  void* ptrs[] = {B->d_args, B->d_src, B->d_items, B->d_titems, B->d_bsegs};
-  for (void* q : ptrs)
-    if (q) cudaFree(q);
-  if (B->master) {
-    free_engine(B->master);
-    delete B->master;
-  }
-}
-
-}  // namespace
-
-extern "C" {
-
-int iris_batch_create(int ncells, const iris_params* params, const double* fw, int dft_faces, iris_batch** out) {
-  clear_error();
-  if (ncells < 1 || !params || !fw || !out) return fail(IRIS_EINVAL, "bad argument");
-  *out = nullptr;
-  const iris_params& p0 = params[0];
-  for (int c = 1; c < ncells; ++c) {
-    const iris_params& q = params[c];
-    if (q.precision != p0.precision || q.nof != p0.nof || q.dt != p0.dt || q.to_fourier != p0.to_fourier ||
-        q.sample_fourier != p0.sample_fourier || q.device != p0.device || q.Q != p0.Q)
-      return fail(IRIS_EINVAL, "batch cells must share precision, dt, Q, nof, DFT sampling and device");
-  }
-  if (p0.stencil == IRIS_STENCIL_FUSED) return fail(IRIS_EINVAL, "the batch steps with the split passes");
-  iris_batch* B = new iris_batch();
-  B->n = ncells;
-  B->prec = p0.precision;
-  B->device = p0.device;
-  auto bail = [&](int code) {
-    batch_free(B);
-    delete B;
-    return code;
-  };
-  B->cells.assign(ncells, nullptr);
-  long P = 0;
-  std::vector<BSeg> bsegs;
-  std::vector<FluxFace> faces(6 * (size_t)ncells);
-  std::vector<SrcArgs> srcs(ncells);
-  std::vector<TItem> titems;
-  for (int c = 0; c < ncells; ++c) {
-    iris_params q = params[c];
-    q.stencil = IRIS_STENCIL_SPLIT;
-    int rc = create_engine(&q, fw, true, dft_faces == IRIS_DFT_Z, &B->cells[c], true);
-    if (rc) return bail(rc);
-    iris_engine* E = B->cells[c];
-    B->pbase.push_back(P);
-    for (const Seg& s : E->segs) {
-      BSeg b{};
-      b.s = s;
-      b.s.p0 += P;
-      b.cell = c;
-      bsegs.push_back(b);
-      B->max_seg = std::max(B->max_seg, (long)s.nu * s.nv);
-    }
-    for (int f = 0; f < 6; ++f) {
-      FluxFace ff = E->host_faces[f];
-      if (ff.active) {
-        ff.pa += P;
-        ff.pb += P;
-        ff.pc += P;
-        ff.pd += P;
-      }
-      faces[6 * c + f] = ff;
-    }
-    srcs[c] = E->src;
-    if (E->src.variant != 0)
-      for (int iy = 0; iy <= q.ny + 1; iy += TFSF_YCH)
-        for (int ix = 0; ix <= q.nx + 1; ix += 64) titems.push_back(TItem{c, ix, iy, 0});
-    P += E->P;
-  }
-  // the shell: one stream, the timers and the shared DFT buffers
-  iris_engine* M = new iris_engine();
-  B->master = M;
-  M->p = params[0];
-  M->fw.assign(fw, fw + p0.nof);
-  M->prec = p0.precision;
-  M->esz = p0.precision == IRIS_FP64 ? 16 : 8;
-  M->device = p0.device;
-  M->P = P;
-  if (cudaSetDevice(M->device) != cudaSuccess) return bail(fail(IRIS_ECUDA, "cudaSetDevice failed"));
-  if (cudaStreamCreateWithFlags(&M->st, cudaStreamNonBlocking) != cudaSuccess)
-    return bail(fail(IRIS_ECUDA, "cudaStreamCreate failed"));
-  int rc = alloc_dft(M, faces.data(), (int)faces.size());
-  if (rc) return bail(rc);
-  if (cudaMalloc(&B->d_bsegs, sizeof(BSeg) * std::max<size_t>(1, bsegs.size())) != cudaSuccess ||
-      cudaMalloc(&B->d_src, sizeof(SrcArgs) * ncells) != cudaSuccess ||
-      cudaMalloc(&B->d_titems, sizeof(TItem) * std::max<size_t>(1, titems.size())) != cudaSuccess)
-    return bail(fail(IRIS_ENOMEM, "batch tables: allocation failed"));
-  cudaMemcpy(B->d_bsegs, bsegs.data(), sizeof(BSeg) * bsegs.size(), cudaMemcpyHostToDevice);
-  cudaMemcpy(B->d_src, srcs.data(), sizeof(SrcArgs) * ncells, cudaMemcpyHostToDevice);
-  cudaMemcpy(B->d_titems, titems.data(), sizeof(TItem) * titems.size(), cudaMemcpyHostToDevice);
-  B->nbsegs = (int)bsegs.size();
-  B->ntitems = (long)titems.size();
-  rc = batch_upload_args(B);
-  if (rc) return bail(rc);
-  rc = batch_build_items(B, 0);
-  if (rc) return bail(rc);
-  if (cudaStreamSynchronize(M->st) != cudaSuccess) return bail(fail(IRIS_ECUDA, "batch initialisation failed"));
-  *out = B;
-  return IRIS_OK;
-}
-
-void iris_batch_destroy(iris_batch* B) {
-  if (!B) return;
-  cudaSetDevice(B->device);
-  if (B->master && B->master->st) cudaStreamSynchronize(B->master->st);
-  batch_free(B);
-  delete B;
-}
-
-int iris_batch_set_material(iris_batch* B, int cell, const double* re, const double* im) {
-  clear_error();
-  if (!B || cell < 0 || cell >= B->n) return fail(IRIS_EINVAL, "bad argument");
-  CK(cudaSetDevice(B->device));
-  CK(cudaStreamSynchronize(B->master->st));
-  int rc = iris_set_material(B->cells[cell], re, im);
-  if (rc) return rc;
-  return batch_upload_args(B);  // the material pointer may have changed
-}
-
-int iris_batch_step(iris_batch* B, int it0, int nsteps) {
-  clear_error();
-  if (!B || nsteps < 0) return fail(IRIS_EINVAL, "bad argument");
-  CK(cudaSetDevice(B->device));
-  return B->prec == IRIS_FP64 ? batch_step_t<double>(B, it0, nsteps) : batch_step_t<float>(B, it0, nsteps);
-}
-
-int iris_batch_flux(iris_batch* B, int cell, double* J) {
-  clear_error();
-  if (!B || !J || cell < 0 || cell >= B->n) return fail(IRIS_EINVAL, "bad argument");
-  CK(cudaSetDevice(B->device));
-  iris_engine* M = B->master;
-  const iris_params& p = M->p;
-  dft_flush(M);
-  const double scale = p.eps0 * p.Q / (2.0 * p.dt);
-  k_flux<<<dim3(p.nof, 6), 256, 0, M->st>>>(M->fd, M->P, M->d_faces + 6 * cell, p.nof, scale, M->d_J);
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(M->h_J, M->d_J, sizeof(double) * 6 * p.nof, cudaMemcpyDeviceToHost, M->st));
-  CK(cudaStreamSynchronize(M->st));
-  bool finite = true;
-  for (int k = 0; k < 6 * p.nof; ++k) {
-    J[k] = M->h_J[k];
-    if (!std::isfinite(J[k])) finite = false;
-  }
-  return finite ? IRIS_OK : fail(IRIS_ENAN, "non-finite flux");
-}
-
-int iris_batch_get_field(iris_batch* B, int cell, int which, double* re, double* im) {
-  clear_error();
-  if (!B || cell < 0 || cell >= B->n) return fail(IRIS_EINVAL, "bad argument");
-  CK(cudaSetDevice(B->device));
-  CK(cudaStreamSynchronize(B->master->st));
-  return iris_get_field(B->cells[cell], which, re, im);
-}
-
-int iris_batch_set_tile(iris_batch* B, int tile) {
-  clear_error();
-  if (!B || tile < 0 || tile >= NTILES) return fail(IRIS_EINVAL, "bad argument");
-  CK(cudaSetDevice(B->device));
-  CK(cudaStreamSynchronize(B->master->st));
-  return batch_build_items(B, tile);
-}
-
-int iris_batch_tune(iris_batch* B, int reps, int* best, double* ms) {
-  clear_error();
-  if (!B || reps < 1) return fail(IRIS_EINVAL, "bad argument");
-  if (B->steps_taken) return fail(IRIS_EINVAL, "tune before the first step (it runs E and H passes on the state)");
-  CK(cudaSetDevice(B->device));
-  iris_engine* M = B->master;
-  cudaEvent_t a, b;
-  CK(cudaEventCreate(&a));
-  CK(cudaEventCreate(&b));
-  int arg = 0;
-  double bestms = 1e30;
-  for (int t = 0; t < NTILES; ++t) {
-    int rc = batch_build_items(B, t);
-    if (rc) return rc;
-    // fields are still zero, so E and H passes leave the state unchanged
-    for (int r = 0; r < 2; ++r) {
-      B->prec == IRIS_FP64 ? batch_eh<double>(B, true) : batch_eh<float>(B, true);
-      B->prec == IRIS_FP64 ? batch_eh<double>(B, false) : batch_eh<float>(B, false);
-    }
-    CK(cudaEventRecord(a, M->st));
-    for (int r = 0; r < reps; ++r) {
-      B->prec == IRIS_FP64 ? batch_eh<double>(B, true) : batch_eh<float>(B, true);
-      B->prec == IRIS_FP64 ? batch_eh<double>(B, false) : batch_eh<float>(B, false);
-    }
-    CK(cudaEventRecord(b, M->st));
-    CK(cudaEventSynchronize(b));
-    float x = 0;
-    CK(cudaEventElapsedTime(&x, a, b));
-    if (ms) ms[t] = x / reps;
-    if (x < bestms) {
-      bestms = x;
-      arg = t;
-    }
-  }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  if (best) *best = arg;
-  return batch_build_items(B, arg);
-}
-
-int iris_batch_timing(iris_batch* B, int enable) {
-  if (!B) return fail(IRIS_EINVAL, "null batch");
-  return iris_timing(B->master, enable);
-}
-
-int iris_batch_timing_read(iris_batch* B, double* region_ms, double* kernel_ms, long* launches) {
-  if (!B) return fail(IRIS_EINVAL, "null batch");
-  return iris_timing_read(B->master, region_ms, kernel_ms, launches);
-}
-
-int iris_batch_info(const iris_batch* B, long* info) {
-  if (!B || !info) return fail(IRIS_EINVAL, "bad argument");
-  long cells = 0;
-  for (const iris_engine* E : B->cells) cells += (long)E->p.nx * E->p.ny * E->p.nz;
-  info[0] = B->n;
-  info[1] = cells;
-  info[2] = B->master->P;
-  info[3] = B->master->K;
-  info[4] = B->tile;
-  info[5] = B->nitems;
-  info[6] = B->tile >= FLAT ? (B->nitems_in > 0) + (B->nitems > B->nitems_in) : 1;
-  return IRIS_OK;
-}
-
-}  // extern "C"
-
-// ---------------------------------------------------------------------------
-// Adjoint (gradient) form: the exact discrete adjoint of the time loop of
-// code/driver.f90:338-451 as the engine runs it.
-//
-// One forward step maps the interior state (E, D, H, B; ghosts are Bloch
-// images of interior cells) linearly, plus a TF/SF source that does not
-// depend on the state:
-//   E pass  D' = a D + b_e C,  E' = al E + g_e D + be_e C,   C  = curl_b H
-//   H pass  B' = a B + b_h C', H' = al H + g_h B + be_h C',  C' = curl_f E'
-// with, outside the UPML slabs, E' = E + m C (m = eps_inv, or 1/eps1, 1/eps3)
-// and H' = H - dtcq2 C'.  Its conjugate transpose, applied in reverse order,
-// uses curl_b^H = curl_f and curl_f^H = curl_b, whose Bloch ghosts carry the
-// conjugated phase of the opposite side:
-//   adjoint H pass  Ebar += curl_b(V),  V = b_h Bbar + be_h Hbar,
-//                   then Hbar <- al Hbar, Bbar <- a Bbar + g_h Hbar
-//   adjoint E pass  Hbar += curl_f(W),  W = b_e Dbar + be_e Ebar,
-//                   then Ebar <- al Ebar, Dbar <- a Dbar + g_e Ebar
-// Each "then" part touches one cell of a field whose neighbours the same
-// kernel still reads, so it is deferred to the next kernel, which reads only
-// its own cell of that field: both kernels update in place.
-// dL/d eps_inv(c) = sum_n Re <Ebar'_n(c), C_n(c)>, Ebar'_n the adjoint of the
-// E pass output of step n, C_n the forward curl of H that pass used.
-
-namespace iris {
-namespace {
-
-// adjoint UPML rows, 24 per UPML plane (+k: component)
-enum { AJ_A = 0, AJ_AL = 3, AJ_GE = 6, AJ_BE = 9, AJ_DE = 12, AJ_GH = 15, AJ_BH = 18, AJ_DH = 21 };
-
-struct Design {
-  int x0, y0, z0, nx, ny, nz;
-  long n;
-};
-
-template <typename T> struct AdjArgs {
-  FieldArgs<T> f;                // adjoint state; coef = adjoint rows, eps_r = forward material
-  int z0;                        // first plane of the launch (blockIdx.z counts from it)
-  int z1;                        // last plane of the launch
-  Design d;
-  const typename V2<T>::t* rec;  // forward curl of H at the design cells for this step, [3][n]
-  double* grad;                  // dL/d eps_inv accumulators [n], or null
-  int first;                     // no deferred E transform pending
-};
-
-struct AdjFace {
-  long b[6];  // first sample index per component (Ex, Ey, Ez, Hx, Hy, Hz)
-  long n;
-  int nu, x0, y0, z;
-};
-
-template <typename T> __device__ __forceinline__ bool in_pml(const FieldArgs<T>& a, int z) {
-  return z <= a.pmlzi || z >= a.pmlzf;
-}
-
-// UPML row and auxiliary index of interior cell (x, y, z) inside a slab.
-template <typename T>
-__device__ __forceinline__ void pml_at(const FieldArgs<T>& a, int x, int y, int z, int& slab, int& row, long& pi) {
-  slab = z <= a.pmlzi ? 0 : 1;
-  const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
-  row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
-  pi = ((long)zr * a.g.ny + (y - 1)) * (long)a.g.nx + (x - 1);
-}
-
-// V_k = b_h Bbar_k + be_h Hbar_k (UPML) or -dtcq2 Hbar_k at interior cell
-// (x, y, z); UPML = false: the caller knows z is outside the slabs.
-template <typename T, bool UPML>
-__device__ __forceinline__ cx<T> adj_v(const FieldArgs<T>& a, int x, int y, int z, int k) {
-  const cx<T> hb = ld<T>(a.h + k * a.g.comp + a.g.at(x, y, z));
-  if (UPML && in_pml(a, z)) {
-    int slab, row;
-    long pi;
-    pml_at(a, x, y, z, slab, row, pi);
-    const T* cf = a.coef + NCOEF * row;
-    const cx<T> bb = ld<T>(a.pml_b[slab] + k * a.pcomp[slab] + pi);
-    return cadd(rmul(cf[AJ_DH + k], bb), rmul(cf[AJ_BH + k], hb));
-  }
-  return rmul(-a.dtcq2, hb);
-}
-
-// W_k = b_e Dbar_k + be_e Ebar_k (UPML) or m Ebar_k at interior cell
-// (x, y, z); UPML = false: the caller knows z is outside the slabs.
-template <typename T, bool UPML>
-__device__ __forceinline__ cx<T> adj_w(const FieldArgs<T>& a, int x, int y, int z, int k) {
-  const Geo& g = a.g;
-  const cx<T> eb = ld<T>(a.e + k * g.comp + g.at(x, y, z));
-  if (UPML && in_pml(a, z)) {
-    int slab, row;
-    long pi;
-    pml_at(a, x, y, z, slab, row, pi);
-    const T* cf = a.coef + NCOEF * row;
-    const cx<T> dd = ld<T>(a.pml_d[slab] + k * a.pcomp[slab] + pi);
-    return cadd(rmul(cf[AJ_DE + k], dd), rmul(cf[AJ_BE + k], eb));
-  }
-  if (z >= a.hi && z <= a.hf) return rmul(a.eps_r[(long)(z - a.hi) * g.plane + (long)y * g.pitch + (x + g.xo)], eb);
-  return rmul(z < a.hi ? a.m1 : a.m3, eb);
-}
-
-// Adjoint of the H pass (plus the E pass transform deferred from the step
-// after it): Ebar += curl_b(V); the gradient term of the design cells.
-// Planes z0 .. z1 of the launch; UPML = false: neither they nor the planes
-// below them lie in a UPML slab.
-template <typename T, bool CURL, bool UPML> __global__ void __launch_bounds__(256) k_adj_h(AdjArgs<T> A) {
-  const FieldArgs<T>& a = A.f;
-  const Geo& g = a.g;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int z = A.z0 + blockIdx.z * blockDim.z + threadIdx.z;
-  if (x > g.nx || y > g.ny || z > A.z1) return;
-  const long i = g.at(x, y, z);
-  cx<T> e[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) e[k] = ld<T>(a.e + k * g.comp + i);
-  if (UPML && !A.first && in_pml(a, z)) {
-    int slab, row;
-    long pi;
-    pml_at(a, x, y, z, slab, row, pi);
-    const T* cf = a.coef + NCOEF * row;
-    auto* D = a.pml_d[slab];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const long j = k * a.pcomp[slab] + pi;
-      st<T>(D + j, cadd(rmul(cf[AJ_A + k], ld<T>(D + j)), rmul(cf[AJ_GE + k], e[k])));
-      e[k] = rmul(cf[AJ_AL + k], e[k]);
-    }
-  }
-  if (CURL) {
-    cx<T> v[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) v[k] = adj_v<T, UPML>(a, x, y, z, k);
-    const int xm = x == 1 ? g.nx : x - 1, ym = y == 1 ? g.ny : y - 1, zm = z == 1 ? g.nz : z - 1;
-    cx<T> v1x = adj_v<T, UPML>(a, xm, y, z, 1), v2x = adj_v<T, UPML>(a, xm, y, z, 2);
-    cx<T> v0y = adj_v<T, UPML>(a, x, ym, z, 0), v2y = adj_v<T, UPML>(a, x, ym, z, 2);
-    cx<T> v0z = adj_v<T, UPML>(a, x, y, zm, 0), v1z = adj_v<T, UPML>(a, x, y, zm, 1);
-    if (x == 1) { v1x = cmul(a.pxm, v1x); v2x = cmul(a.pxm, v2x); }
-    if (y == 1) { v0y = cmul(a.pym, v0y); v2y = cmul(a.pym, v2y); }
-    if (z == 1) { v0z = cmul(a.pzm, v0z); v1z = cmul(a.pzm, v1z); }
-    e[0] = cadd(e[0], cadd(csub(csub(v[2], v2y), v[1]), v1z));
-    e[1] = cadd(e[1], cadd(csub(csub(v[0], v0z), v[2]), v2x));
-    e[2] = cadd(e[2], cadd(csub(csub(v[1], v1x), v[0]), v0y));
-    const Design& d = A.d;
-    if (A.grad && x >= d.x0 && x < d.x0 + d.nx && y >= d.y0 && y < d.y0 + d.ny && z >= d.z0 && z < d.z0 + d.nz) {
-      const long q = ((long)(z - d.z0) * d.ny + (y - d.y0)) * d.nx + (x - d.x0);
-      T s = 0;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const cx<T> c = ld<T>(A.rec + k * d.n + q);
-        s = add_(s, add_(mul_(e[k].re, c.re), mul_(e[k].im, c.im)));
-      }
-      A.grad[q] += (double)s;
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) st<T>(a.e + k * g.comp + i, e[k]);
-}
-
-// Adjoint of the E pass (plus the H pass transform of the same step):
-// Hbar <- al Hbar + curl_f(W), Bbar <- a Bbar + g_h Hbar.  Planes z0 .. z1;
-// UPML = false: neither they nor the planes above them lie in a UPML slab.
-template <typename T, bool UPML> __global__ void __launch_bounds__(256) k_adj_e(AdjArgs<T> A) {
-  const FieldArgs<T>& a = A.f;
-  const Geo& g = a.g;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int z = A.z0 + blockIdx.z * blockDim.z + threadIdx.z;
-  if (x > g.nx || y > g.ny || z > A.z1) return;
-  const long i = g.at(x, y, z);
-  cx<T> h[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) h[k] = ld<T>(a.h + k * g.comp + i);
-  if (UPML && in_pml(a, z)) {
-    int slab, row;
-    long pi;
-    pml_at(a, x, y, z, slab, row, pi);
-    const T* cf = a.coef + NCOEF * row;
-    auto* B = a.pml_b[slab];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const long j = k * a.pcomp[slab] + pi;
-      st<T>(B + j, cadd(rmul(cf[AJ_A + k], ld<T>(B + j)), rmul(cf[AJ_GH + k], h[k])));
-      h[k] = rmul(cf[AJ_AL + k], h[k]);
-    }
-  }
-  cx<T> w[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) w[k] = adj_w<T, UPML>(a, x, y, z, k);
-  const int xp = x == g.nx ? 1 : x + 1, yp = y == g.ny ? 1 : y + 1, zp = z == g.nz ? 1 : z + 1;
-  cx<T> w1x = adj_w<T, UPML>(a, xp, y, z, 1), w2x = adj_w<T, UPML>(a, xp, y, z, 2);
-  cx<T> w0y = adj_w<T, UPML>(a, x, yp, z, 0), w2y = adj_w<T, UPML>(a, x, yp, z, 2);
-  cx<T> w0z = adj_w<T, UPML>(a, x, y, zp, 0), w1z = adj_w<T, UPML>(a, x, y, zp, 1);
-  if (x == g.nx) { w1x = cmul(a.pxp, w1x); w2x = cmul(a.pxp, w2x); }
-  if (y == g.ny) { w0y = cmul(a.pyp, w0y); w2y = cmul(a.pyp, w2y); }
-  if (z == g.nz) { w0z = cmul(a.pzp, w0z); w1z = cmul(a.pzp, w1z); }
-  h[0] = cadd(h[0], cadd(csub(csub(w2y, w[2]), w1z), w[1]));
-  h[1] = cadd(h[1], cadd(csub(csub(w0z, w[0]), w2x), w[2]));
-  h[2] = cadd(h[2], cadd(csub(csub(w1x, w[1]), w0y), w[0]));
-#pragma unroll
-  for (int k = 0; k < 3; ++k) st<T>(a.h + k * g.comp + i, h[k]);
-}
-
-// Forward curl_b H of the E pass at the design cells (the H the next E pass
-// reads, ghosts included), as e_update forms it.
-template <typename T>
-__global__ void __launch_bounds__(256) k_adj_record(FieldArgs<T> a, Design d, typename V2<T>::t* __restrict__ rec) {
-  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= d.n) return;
-  const int x = d.x0 + (int)(q % d.nx), y = d.y0 + (int)((q / d.nx) % d.ny), z = d.z0 + (int)(q / ((long)d.nx * d.ny));
-  const Geo& g = a.g;
-  const long i = g.at(x, y, z);
-  const auto* H1 = a.h;
-  const auto* H2 = a.h + g.comp;
-  const auto* H3 = a.h + 2 * g.comp;
-  const cx<T> h0 = ld<T>(H1 + i), h1 = ld<T>(H2 + i), h2 = ld<T>(H3 + i);
-  st<T>(rec + q, cadd(csub(csub(h2, ld<T>(H3 + i - g.pitch)), h1), ld<T>(H2 + i - g.plane)));
-  st<T>(rec + d.n + q, cadd(csub(csub(h0, ld<T>(H1 + i - g.plane)), h2), ld<T>(H3 + i - 1)));
-  st<T>(rec + 2 * d.n + q, cadd(csub(csub(h1, ld<T>(H2 + i - 1)), h0), ld<T>(H1 + i - g.pitch)));
-}
-
-// Adjoint DFT source of one sampled step on one z face:
-//   Ebar_x += c Y_Hy, Ebar_y -= c Y_Hx, Hbar_x -= c Y_Ey, Hbar_y += c Y_Ex
-// summed over frequencies, c = w * exp(-i fw t), Y the final DFT values.
-template <typename T>
-__global__ void __launch_bounds__(256) k_adj_source(typename V2<T>::t* __restrict__ ae, typename V2<T>::t* __restrict__ ah,
-                                                    Geo g, const double2* __restrict__ fd, long P, AdjFace f,
-                                                    const double* __restrict__ w, const double* __restrict__ fw,
-                                                    int nof, int t) {
-  extern __shared__ double2 tw[];
-  for (int iw = threadIdx.x; iw < nof; iw += blockDim.x) {
-    double s, c;
-    sincos(fw[iw] * (double)t, &s, &c);
-    tw[iw] = make_double2(w[iw] * c, -w[iw] * s);
-  }
-  __syncthreads();
-  const long L = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (L >= f.n) return;
-  double2 gex = {0, 0}, gey = {0, 0}, ghx = {0, 0}, ghy = {0, 0};
-  for (int iw = 0; iw < nof; ++iw) {
-    const double2* row = fd + (long)iw * P;
-    const double2 xe = row[f.b[0] + L], ye = row[f.b[1] + L], xh = row[f.b[3] + L], yh = row[f.b[4] + L];
-    const double2 c = tw[iw];
-    gex.x += c.x * yh.x - c.y * yh.y; gex.y += c.x * yh.y + c.y * yh.x;
-    ghy.x += c.x * xe.x - c.y * xe.y; ghy.y += c.x * xe.y + c.y * xe.x;
-    gey.x -= c.x * xh.x - c.y * xh.y; gey.y -= c.x * xh.y + c.y * xh.x;
-    ghx.x -= c.x * ye.x - c.y * ye.y; ghx.y -= c.x * ye.y + c.y * ye.x;
-  }
-  const long i = g.at(f.x0 + (int)(L % f.nu), f.y0 + (int)(L / f.nu), f.z);
-  auto addv = [](typename V2<T>::t* p, double2 v) {
-    typename V2<T>::t o = *p;
-    o.x = (T)((double)o.x + v.x);
-    o.y = (T)((double)o.y + v.y);
-    *p = o;
-  };
-  addv(ae + i, gex);
-  addv(ae + g.comp + i, gey);
-  addv(ah + i, ghx);
-  addv(ah + g.comp + i, ghy);
-}
-
-template <typename T> __global__ void k_adj_scatter(T* __restrict__ eps, Geo g, int hi, Design d, const T* __restrict__ v) {
-  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= d.n) return;
-  const int x = d.x0 + (int)(q % d.nx), y = d.y0 + (int)((q / d.nx) % d.ny), z = d.z0 + (int)(q / ((long)d.nx * d.ny));
-  eps[(long)(z - hi) * g.plane + (long)y * g.pitch + (x + g.xo)] = v[q];
-}
-
-}  // namespace
-}  // namespace iris
-
-struct iris_adjoint {
-  iris_engine* F = nullptr;  // forward engine (z-face DFT of box 1)
-  iris_engine* A = nullptr;  // adjoint state: e, h, pml_d, pml_b
-  void* acoef = nullptr;     // adjoint UPML rows
-  Design d{};
-  int K = 256;                 // checkpoint interval
-  std::vector<double> w;       // [2][nof] objective weights
-  double* d_w = nullptr;       // [2][nof] weight * sign * flux scale * dt
-  bool side_on[2] = {false, false};
-  double* d_grad = nullptr;    // [n]
-  void* rec = nullptr;         // [K][3][n]
-  int rec_seg = -1;            // segment whose curls rec holds
-  void* d_design = nullptr;    // [n] staging for set_design
-  std::vector<void*> ckpt;     // per segment: e, h, d0, d1, b0, b1
-  size_t fbytes = 0, sbytes[2] = {0, 0};
-  int nsteps = 0;
-  double ms[3] = {0, 0, 0};
-  cudaEvent_t ev[2] = {nullptr, nullptr};
-};
-
-namespace {
-
-template <typename T> AdjArgs<T> adj_args(const iris_adjoint* J, bool first, int slot, bool grad) {
-  AdjArgs<T> A{};
-  A.f = field_args<T>(J->A);
-  const FieldArgs<T> f = field_args<T>(J->F);
-  A.f.coef = (const T*)J->acoef;
-  A.f.eps_r = f.eps_r;
-  A.f.eps_c = nullptr;
-  auto conj = [](cx<T> c) { return cx<T>{c.re, -c.im}; };
-  A.f.pxm = conj(f.pxp);
-  A.f.pym = conj(f.pyp);
-  A.f.pzm = conj(f.pzp);
-  A.f.pxp = conj(f.pxm);
-  A.f.pyp = conj(f.pym);
-  A.f.pzp = conj(f.pzm);
-  A.d = J->d;
-  A.first = first ? 1 : 0;
-  if (grad) {
-    A.grad = J->d_grad;
-    A.rec = (const typename V2<T>::t*)J->rec + (long)slot * 3 * J->d.n;
-  }
-  return A;
-}
-
-template <typename T> void adj_record(iris_adjoint* J, int slot) {
-  iris_engine* F = J->F;
-  using V = typename V2<T>::t;
-  V* r = (V*)J->rec + (long)slot * 3 * J->d.n;
-  k_adj_record<T><<<(unsigned)((J->d.n + 255) / 256), 256, 0, F->st>>>(field_args<T>(F), J->d, r);
-}
-
-template <typename T> void adj_source(iris_adjoint* J, int t) {
-  iris_engine* F = J->F;
-  const FaceMap& M = F->fm[0][2];
-  const iris_params& p = F->p;
-  using V = typename V2<T>::t;
-  for (int side = 0; side < 2; ++side) {
-    if (!J->side_on[side]) continue;
-    AdjFace f{};
-    for (int c = 0; c < 6; ++c) f.b[c] = M.base[side][c];
-    f.n = M.nloc;
-    f.nu = M.nu;
-    f.x0 = p.box1[0];
-    f.y0 = p.box1[2];
-    f.z = side == 0 ? p.box1[4] : p.box1[5];
-    k_adj_source<T><<<(unsigned)((f.n + 255) / 256), 256, sizeof(double2) * p.nof, F->st>>>(
-        (V*)J->A->e, (V*)J->A->h, F->g, F->fd, F->P, f, J->d_w + side * p.nof, F->d_fw, p.nof, t);
-  }
-}
-
-// Launch shape of planes z0 .. z1 (none when z1 < z0).
-dim3 adj_grid(const iris_engine* F, int z0, int z1) {
-  return dim3(F->grd.x, F->grd.y, z1 < z0 ? 0u : (unsigned)((z1 - z0 + F->blk.z) / F->blk.z));
-}
-
-// One adjoint step (K1 then K2) for forward step it; rec slot or -1.  Each
-// kernel runs as the planes whose stencil stays outside the UPML slabs,
-// compiled without slab code, and the rest (the slabs and their neighbours).
-template <typename T> void adj_step(iris_adjoint* J, bool first, int slot) {
-  iris_engine* F = J->F;
-  const iris_params& p = F->p;
-  const bool grad = slot >= 0;
-  AdjArgs<T> a = adj_args<T>(J, first, slot, grad);
-  auto k1 = [&](int z0, int z1, bool upml) {
-    a.z0 = z0;
-    a.z1 = z1;
-    const dim3 gr = adj_grid(F, z0, z1);
-    if (gr.z == 0) return;
-    if (upml) k_adj_h<T, true, true><<<gr, F->blk, 0, F->st>>>(a);
-    else k_adj_h<T, true, false><<<gr, F->blk, 0, F->st>>>(a);
-  };
-  // K1 reads planes z and z-1: free of slab code for z in [pmlzi+2, pmlzf-1]
-  const int a1 = std::min(p.pmlzi + 1, p.pmlzf - 1);
-  k1(1, a1, true);
-  k1(a1 + 1, p.pmlzf - 1, false);
-  k1(p.pmlzf, p.nz, true);
-  AdjArgs<T> b = adj_args<T>(J, first, -1, false);
-  auto k2 = [&](int z0, int z1, bool upml) {
-    b.z0 = z0;
-    b.z1 = z1;
-    const dim3 gr = adj_grid(F, z0, z1);
-    if (gr.z == 0) return;
-    if (upml) k_adj_e<T, true><<<gr, F->blk, 0, F->st>>>(b);
-    else k_adj_e<T, false><<<gr, F->blk, 0, F->st>>>(b);
-  };
-  // K2 reads planes z and z+1: free of slab code for z in [pmlzi+1, pmlzf-2]
-  const int b2 = std::max(p.pmlzf - 2, p.pmlzi);
-  k2(1, p.pmlzi, true);
-  k2(p.pmlzi + 1, b2, false);
-  k2(b2 + 1, p.nz, true);
-}
-
-template <typename T> void adj_finalize(iris_adjoint* J) {
-  iris_engine* F = J->F;
-  AdjArgs<T> a = adj_args<T>(J, false, -1, false);
-  a.z0 = 1;
-  a.z1 = F->p.nz;
-  k_adj_h<T, false, true><<<adj_grid(F, 1, F->p.nz), F->blk, 0, F->st>>>(a);
-}
-
-// The forward step without DFT sampling (recompute) or with it (forward).
-template <typename T> void fwd_step(iris_engine* F, int it, bool dft) {
-  launch_e<T>(F);
-  launch_h<T>(F);
-  launch_tfsf<T>(F, it);
-  const iris_params& p = F->p;
-  if (dft && it >= p.to_fourier && it % p.sample_fourier == 0) dft_sample<T>(F, it + 1 - p.to_fourier);
-}
-
-int ckpt_io(iris_adjoint* J, int seg, bool save) {
-  iris_engine* F = J->F;
-  unsigned char* c = (unsigned char*)J->ckpt[seg];
-  void* parts[6] = {F->e, F->h, F->pml_d[0], F->pml_d[1], F->pml_b[0], F->pml_b[1]};
-  const size_t sz[6] = {J->fbytes, J->fbytes, J->sbytes[0], J->sbytes[1], J->sbytes[0], J->sbytes[1]};
-  size_t off = 0;
-  for (int k = 0; k < 6; ++k) {
-    if (save) CK(cudaMemcpyAsync(c + off, parts[k], sz[k], cudaMemcpyDeviceToDevice, F->st));
-    else CK(cudaMemcpyAsync(parts[k], c + off, sz[k], cudaMemcpyDeviceToDevice, F->st));
-    off += sz[k];
-  }
-  return IRIS_OK;
-}
-
-int zero_state(iris_engine* E, size_t fbytes, const size_t* sbytes) {
-  CK(cudaMemsetAsync(E->e, 0, fbytes, E->st));
-  CK(cudaMemsetAsync(E->h, 0, fbytes, E->st));
-  for (int s = 0; s < 2; ++s) {
-    CK(cudaMemsetAsync(E->pml_d[s], 0, sbytes[s], E->st));
-    CK(cudaMemsetAsync(E->pml_b[s], 0, sbytes[s], E->st));
-  }
-  return IRIS_OK;
-}
-
-template <typename T> int adj_forward(iris_adjoint* J, int nsteps) {
-  iris_engine* F = J->F;
-  const int S = (nsteps + J->K - 1) / J->K;
-  const size_t cbytes = 2 * J->fbytes + 2 * (J->sbytes[0] + J->sbytes[1]);
-  while ((int)J->ckpt.size() < S) {
-    void* q = nullptr;
-    if (cudaMalloc(&q, cbytes) != cudaSuccess) {
-      cudaGetLastError();
-      return fail(IRIS_ENOMEM, "checkpoint allocation failed (" + std::to_string(S) + " checkpoints of " +
-                                   std::to_string(cbytes) + " bytes)");
-    }
-    J->ckpt.push_back(q);
-  }
-  int rc = zero_state(F, J->fbytes, J->sbytes);
-  if (rc) return rc;
-  CK(cudaMemsetAsync(F->fd, 0, (size_t)F->P * F->p.nof * sizeof(double2), F->st));
-  F->nslot = 0;
-  CK(cudaEventRecord(J->ev[0], F->st));
-  for (int it = 1; it <= nsteps; ++it) {
-    const int seg = (it - 1) / J->K;
-    if ((it - 1) % J->K == 0) {
-      rc = ckpt_io(J, seg, true);
-      if (rc) return rc;
-    }
-    if (seg == S - 1) adj_record<T>(J, it - 1 - seg * J->K);
-    fwd_step<T>(F, it, true);
-  }
-  dft_flush(F);
-  CK(cudaEventRecord(J->ev[1], F->st));
-  CK(cudaEventSynchronize(J->ev[1]));
-  float x = 0.f;
-  CK(cudaEventElapsedTime(&x, J->ev[0], J->ev[1]));
-  J->ms[0] = x;
-  J->rec_seg = S - 1;
-  J->nsteps = nsteps;
-  CK(cudaGetLastError());
-  return IRIS_OK;
-}
-
-template <typename T> int adj_backward(iris_adjoint* J) {
-  iris_engine* F = J->F;
-  const iris_params& p = F->p;
-  const int N = J->nsteps, S = (N + J->K - 1) / J->K;
-  int rc = zero_state(J->A, J->fbytes, J->sbytes);
-  if (rc) return rc;
-  CK(cudaMemsetAsync(J->d_grad, 0, sizeof(double) * J->d.n, F->st));
-  double t_rec = 0, t_adj = 0;
-  bool first = true;
-  for (int seg = S - 1; seg >= 0; --seg) {
-    const int s0 = seg * J->K + 1, s1 = std::min(N, (seg + 1) * J->K);
-    float x = 0.f;
-    if (J->rec_seg != seg) {
-      CK(cudaEventRecord(J->ev[0], F->st));
-      rc = ckpt_io(J, seg, false);
-      if (rc) return rc;
-      for (int it = s0; it <= s1; ++it) {
-        adj_record<T>(J, it - s0);
-        fwd_step<T>(F, it, false);
-      }
-      CK(cudaEventRecord(J->ev[1], F->st));
-      CK(cudaEventSynchronize(J->ev[1]));
-      CK(cudaEventElapsedTime(&x, J->ev[0], J->ev[1]));
-      t_rec += x;
-      J->rec_seg = seg;
-    }
-    CK(cudaEventRecord(J->ev[0], F->st));
-    for (int it = s1; it >= s0; --it) {
-      if (it >= p.to_fourier && it % p.sample_fourier == 0) adj_source<T>(J, it + 1 - p.to_fourier);
-      adj_step<T>(J, first, it - s0);
-      first = false;
-    }
-    CK(cudaEventRecord(J->ev[1], F->st));
-    CK(cudaEventSynchronize(J->ev[1]));
-    CK(cudaEventElapsedTime(&x, J->ev[0], J->ev[1]));
-    t_adj += x;
-  }
-  J->ms[1] = t_rec;
-  J->ms[2] = t_adj;
-  CK(cudaGetLastError());
-  return IRIS_OK;
-}
-
-void adj_free(iris_adjoint* J) {
-  if (J->F) iris_destroy(J->F);
-  if (J->A) iris_destroy(J->A);
-  void* ptrs[] = {J->acoef, J->d_w, J->d_grad, J->rec, J->d_design};
-  for (void* q : ptrs)
-    if (q) cudaFree(q);
-  for (void* q : J->ckpt)
-    if (q) cudaFree(q);
-  for (cudaEvent_t e : J->ev)
-    if (e) cudaEventDestroy(e);
-}
-
-}  // namespace
-
-extern "C" {
-
-int iris_adjoint_create(const iris_params* pin, const double* fw, const int design[6], int checkpoint_every,
-                        const double* weights, iris_adjoint** out) {
-  clear_error();
-  if (!pin || !fw || !design || !out) return fail(IRIS_EINVAL, "null argument");
-  *out = nullptr;
-  const iris_params& p = *pin;
-  if (checkpoint_every < 1) return fail(IRIS_EINVAL, "checkpoint_every must be >= 1");
-  const int* D = design;
-  if (D[0] < 1 || D[1] > p.nx || D[0] > D[1] || D[2] < 1 || D[3] > p.ny || D[2] > D[3] || D[4] < p.hi ||
-      D[5] > p.hf || D[4] > D[5])
-    return fail(IRIS_EINVAL, "design region must lie in [1,nx] x [1,ny] x [hi,hf]");
-  if (p.hi <= p.pmlzi || p.hf >= p.pmlzf) return fail(IRIS_EINVAL, "the structure layer must lie outside the UPML slabs");
-  if (p.box1[4] <= p.pmlzi || p.box1[5] >= p.pmlzf)
-    return fail(IRIS_EINVAL, "the DFT z planes of box 1 must lie outside the UPML slabs");
-  iris_adjoint* J = new iris_adjoint();
-  auto bail = [&](int code) {
-    adj_free(J);
-    delete J;
-    return code;
-  };
-  iris_params q = p;
-  q.stencil = IRIS_STENCIL_SPLIT;
-  for (int i = 0; i < 6; ++i) q.box2[i] = q.box1[i];
-  int rc = create_engine(&q, fw, false, true, &J->F);
-  if (rc) return bail(rc);
-  rc = create_engine(&q, fw, true, true, &J->A);
-  if (rc) return bail(rc);
-  iris_engine* F = J->F;
-  J->K = checkpoint_every;
-  J->d = Design{D[0], D[2], D[4], D[1] - D[0] + 1, D[3] - D[2] + 1, D[5] - D[4] + 1, 0};
-  J->d.n = (long)J->d.nx * J->d.ny * J->d.nz;
-  J->fbytes = (size_t)3 * F->g.comp * F->esz;
-  for (int s = 0; s < 2; ++s) J->sbytes[s] = (size_t)3 * F->pcomp[s] * F->esz;
-  // objective weights, folded with the flux sign and scale and the DFT's dt
-  const int nof = p.nof;
-  J->w.assign(2 * (size_t)nof, 0.0);
-  for (int k = 0; k < nof; ++k) J->w[nof + k] = 1.0;
-  if (weights) J->w.assign(weights, weights + 2 * nof);
-  std::vector<double> wd(2 * (size_t)nof);
-  const double scale = p.eps0 * p.Q / (2.0 * p.dt);
-  for (int side = 0; side < 2; ++side)
-    for (int k = 0; k < nof; ++k) {
-      const double v = J->w[side * nof + k];
-      wd[side * nof + k] = (side == 0 ? -1.0 : 1.0) * scale * p.dt * v;
-      if (v != 0.0) J->side_on[side] = true;
-    }
-  // adjoint UPML rows from the forward ones
-  const std::vector<double>& c = F->coef_h;
-  const size_t nrow = c.size() / NCOEF;
-  std::vector<double> ac(c.size());
-  const double e2 = p.eps0 * p.eps0;
-  for (size_t r = 0; r < nrow; ++r) {
-    const double* f = c.data() + NCOEF * r;
-    double* a = ac.data() + NCOEF * r;
-    for (int k = 0; k < 3; ++k) {
-      a[AJ_A + k] = f[CD_A + k];
-      a[AJ_AL + k] = f[CE_A + k];
-      a[AJ_GE + k] = f[CE_B + k] * (f[C_FP + k] * f[CD_A + k] - f[C_FM + k]);
-      a[AJ_BE + k] = f[CE_B + k] * f[C_FP + k] * f[CD_B + k] * e2;
-      a[AJ_DE + k] = f[CD_B + k] * e2;
-      a[AJ_GH + k] = f[CH_B + k] * (f[C_FP + k] * f[CD_A + k] - f[C_FM + k]);
-      a[AJ_BH + k] = -f[CH_B + k] * f[C_FP + k] * f[CB_B + k];
-      a[AJ_DH + k] = -f[CB_B + k];
-    }
-  }
-  const size_t rsz = F->prec == IRIS_FP64 ? 8 : 4;
-  const size_t csz = F->prec == IRIS_FP64 ? 16 : 8;
-  auto dev_alloc = [&](void** q2, size_t b) { return cudaMalloc(q2, std::max<size_t>(b, 16)) == cudaSuccess; };
-  if (!dev_alloc(&J->acoef, ac.size() * rsz) || !dev_alloc((void**)&J->d_w, sizeof(double) * 2 * nof) ||
-      !dev_alloc((void**)&J->d_grad, sizeof(double) * J->d.n) ||
-      !dev_alloc(&J->rec, (size_t)J->K * 3 * J->d.n * csz) || !dev_alloc(&J->d_design, J->d.n * rsz)) {
-    cudaGetLastError();
-    return bail(fail(IRIS_ENOMEM, "adjoint buffers: allocation failed"));
-  }
-  if (F->prec == IRIS_FP64) {
-    if (cudaMemcpy(J->acoef, ac.data(), ac.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
-      return bail(fail(IRIS_ECUDA, "adjoint rows upload failed"));
-  } else {
-    std::vector<float> af(ac.begin(), ac.end());
-    if (cudaMemcpy(J->acoef, af.data(), af.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
-      return bail(fail(IRIS_ECUDA, "adjoint rows upload failed"));
-  }
-  if (cudaMemcpy(J->d_w, wd.data(), sizeof(double) * 2 * nof, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaEventCreate(&J->ev[0]) != cudaSuccess || cudaEventCreate(&J->ev[1]) != cudaSuccess)
-    return bail(fail(IRIS_ECUDA, "adjoint initialisation failed"));
-  *out = J;
-  return IRIS_OK;
-}
-
-void iris_adjoint_destroy(iris_adjoint* J) {
-  if (!J) return;
-  cudaSetDevice(J->F ? J->F->device : 0);
-  if (J->F) cudaStreamSynchronize(J->F->st);
-  adj_free(J);
-  delete J;
-}
-
-int iris_adjoint_set_material(iris_adjoint* J, const double* re, const double* im) {
-  clear_error();
-  if (!J || !re) return fail(IRIS_EINVAL, "null argument");
-  int rc = iris_set_material(J->F, re, im);
-  if (rc) return rc;
-  if (J->F->eps_complex) return fail(IRIS_EINVAL, "the adjoint form needs a real material");
-  return IRIS_OK;
-}
-
-int iris_adjoint_set_design(iris_adjoint* J, const double* v) {
-  clear_error();
-  if (!J || !v) return fail(IRIS_EINVAL, "null argument");
-  iris_engine* F = J->F;
-  CK(cudaSetDevice(F->device));
-  if (F->eps_complex) return fail(IRIS_EINVAL, "the adjoint form needs a real material");
-  const unsigned nb = (unsigned)((J->d.n + 255) / 256);
-  if (F->prec == IRIS_FP64) {
-    CK(cudaMemcpyAsync(J->d_design, v, sizeof(double) * J->d.n, cudaMemcpyHostToDevice, F->st));
-    k_adj_scatter<double><<<nb, 256, 0, F->st>>>((double*)F->eps, F->g, F->p.hi, J->d, (const double*)J->d_design);
-  } else {
-    std::vector<float> f(v, v + J->d.n);
-    CK(cudaMemcpyAsync(J->d_design, f.data(), sizeof(float) * J->d.n, cudaMemcpyHostToDevice, F->st));
-    k_adj_scatter<float><<<nb, 256, 0, F->st>>>((float*)F->eps, F->g, F->p.hi, J->d, (const float*)J->d_design);
-  }
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(F->st));
-  return IRIS_OK;
-}
-
-int iris_adjoint_forward(iris_adjoint* J, int nsteps, double* L, double* Jout) {
-  clear_error();
-  if (!J || nsteps < 1) return fail(IRIS_EINVAL, "bad argument");
-  iris_engine* F = J->F;
-  CK(cudaSetDevice(F->device));
-  if (F->eps_complex) return fail(IRIS_EINVAL, "the adjoint form needs a real material");
-  int rc = F->prec == IRIS_FP64 ? adj_forward<double>(J, nsteps) : adj_forward<float>(J, nsteps);
-  if (rc) return rc;
-  const int nof = F->p.nof;
-  std::vector<double> flux(6 * (size_t)nof);
-  rc = iris_flux(F, 0, flux.data());
-  if (rc) return rc;
-  double s = 0.0;
-  for (int k = 0; k < nof; ++k) s += J->w[k] * flux[4 * nof + k] + J->w[nof + k] * flux[5 * nof + k];
-  if (L) *L = s;
-  if (Jout) std::copy(flux.begin(), flux.end(), Jout);
-  return IRIS_OK;
-}
-
-int iris_adjoint_backward(iris_adjoint* J, double* grad) {
-  clear_error();
-  if (!J || !grad) return fail(IRIS_EINVAL, "null argument");
-  if (J->nsteps < 1) return fail(IRIS_EINVAL, "no forward solve to differentiate");
-  iris_engine* F = J->F;
-  CK(cudaSetDevice(F->device));
-  int rc = F->prec == IRIS_FP64 ? adj_backward<double>(J) : adj_backward<float>(J);
-  if (rc) return rc;
-  CK(cudaMemcpyAsync(grad, J->d_grad, sizeof(double) * J->d.n, cudaMemcpyDeviceToHost, F->st));
-  CK(cudaStreamSynchronize(F->st));
-  for (long q = 0; q < J->d.n; ++q)
-    if (!std::isfinite(grad[q])) return fail(IRIS_ENAN, "non-finite gradient");
-  return IRIS_OK;
-}
-
-int iris_adjoint_engine(iris_adjoint* J, int which, iris_engine** eng) {
-  if (!J || !eng || (which != 0 && which != 1)) return fail(IRIS_EINVAL, "bad argument");
-  *eng = which == 0 ? J->F : J->A;
-  return IRIS_OK;
-}
-
-int iris_adjoint_apply(iris_adjoint* J, int nsteps) {
-  clear_error();
-  if (!J || nsteps < 0) return fail(IRIS_EINVAL, "bad argument");
-  iris_engine* F = J->F;
-  CK(cudaSetDevice(F->device));
-  CK(cudaStreamSynchronize(J->A->st));
-  const bool d = F->prec == IRIS_FP64;
-  for (int k = 0; k < nsteps; ++k) d ? adj_step<double>(J, k == 0, -1) : adj_step<float>(J, k == 0, -1);
-  if (nsteps > 0) d ? adj_finalize<double>(J) : adj_finalize<float>(J);
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(F->st));
-  return IRIS_OK;
-}
-
-int iris_adjoint_timing(const iris_adjoint* J, double* ms) {
-  if (!J || !ms) return fail(IRIS_EINVAL, "bad argument");
-  for (int k = 0; k < 3; ++k) ms[k] = J->ms[k];
-  return IRIS_OK;
-}
-
-}  // extern "C"

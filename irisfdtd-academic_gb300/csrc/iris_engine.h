@@ -1,0 +1,181 @@
+// Engine internals shared by the CUDA translation units (iris_engine.cu,
+// iris_batch.cu, iris_adjoint.cu): the engine state and the host helpers
+// that build its kernel arguments, flush its DFT ring and replay its graphs.
+// Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <functional>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "iris_device.cuh"
+#include "iris_internal.h"
+
+// Return IRIS_ECUDA (IRIS_ENOMEM for an allocation) with the failing call's
+// text when a CUDA runtime call fails.
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t err_ = (call);                                                          \
+    if (err_ != cudaSuccess)                                                            \
+      return iris::fail(err_ == cudaErrorMemoryAllocation ? IRIS_ENOMEM : IRIS_ECUDA,   \
+                        std::string(#call) + ": " + cudaGetErrorString(err_));          \
+  } while (0)
+
+namespace iris {
+
+struct FaceMap {
+  bool active = false;  // this face pair is accumulated by scattering_fourier
+  int nu = 0, nv = 0;
+  long nloc = 0;         // locations per face
+  long base[2][6] = {};  // first sample index per [side][component]
+};
+
+}  // namespace iris
+
+struct iris_engine {
+  iris_params p{};
+  std::vector<double> fw;
+  int prec = IRIS_FP64;
+  size_t esz = 16;  // bytes per stored complex value
+  int device = 0;
+  cudaStream_t st = nullptr;
+  iris::Geo g{};
+  dim3 blk, grd;
+  void* e = nullptr;
+  void* h = nullptr;
+  void* pml_d[2] = {nullptr, nullptr};
+  void* pml_b[2] = {nullptr, nullptr};
+  long pcomp[2] = {0, 0};
+  int nbot = 0, ntop = 0;
+  void* coef = nullptr;
+  std::vector<double> coef_h;
+  void* eps = nullptr;
+  bool eps_complex = false;
+  double ph[6][2] = {};  // exp(+i akx), exp(+i aky), exp(+i akz), exp(-i akx), ...
+  iris::SrcArgs src{};
+  dim3 tf_blk, tf_grd;
+  // DFT
+  int nboxes = 1;
+  iris::FaceMap fm[2][3];
+  long P = 0;
+  int K = 0, nslot = 0;
+  std::vector<iris::Seg> segs;
+  long max_seg = 0;
+  iris::Seg* d_segs = nullptr;
+  void* S = nullptr;
+  int* d_tk = nullptr;
+  double* d_fw = nullptr;
+  double2* fd = nullptr;
+  float2* d_wt = nullptr;
+  double2* d_wt64 = nullptr;  // FP64 mode twiddles of one block
+  bool dft_tc = false;     // FP32 block accumulation on the tensor cores
+  float* d_wtc = nullptr;  // its B operands (k_twiddle_tc)
+  iris::FluxFace* d_faces = nullptr;
+  double* d_J = nullptr;
+  double* h_J = nullptr;
+  // batch member: no DFT buffers of its own; z-plane DFT only on request
+  bool member = false;
+  bool dft_z_only = false;
+  std::vector<iris::FluxFace> host_faces;
+  // fused E+H stepping (FP32): second field buffers and D, per-step TF/SF table
+  bool fused = false;
+  void* e2 = nullptr;
+  void* h2 = nullptr;
+  void* pml_d2[2] = {nullptr, nullptr};
+  int zchunk = 0;
+  dim3 fblk, fgrd;
+  // CUDA graph of one DFT block of steps (iris_params.graph): d_it holds the
+  // step base the captured kernels add to their offsets, dev_it its value
+  cudaGraphExec_t gexec = nullptr;
+  int* d_it = nullptr;
+  int dev_it = -1;
+  // streamed split passes (FP32, real material); d_err: a kernel's give-up record
+  bool stream = false;
+  dim3 sgrd;
+  int* d_err = nullptr;
+  // timing: CUDA events on the engine stream, per kernel class
+  bool timing = false;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[IRIS_NKC];
+  size_t ev_used[IRIS_NKC] = {};
+};
+
+namespace iris {
+
+// Brackets one kernel launch with a pair of events when timing is on.
+struct KTimer {
+  iris_engine* E;
+  int k;
+  cudaEvent_t b = nullptr, e = nullptr;
+  KTimer(iris_engine* eng, int kind) : E(eng), k(kind) {
+    if (!E->timing) return;
+    auto& v = E->ev[k];
+    if (E->ev_used[k] == v.size()) {
+      cudaEvent_t x, y;
+      cudaEventCreate(&x);
+      cudaEventCreate(&y);
+      v.push_back({x, y});
+    }
+    b = v[E->ev_used[k]].first;
+    e = v[E->ev_used[k]].second;
+    ++E->ev_used[k];
+    cudaEventRecord(b, E->st);
+  }
+  ~KTimer() {
+    if (b) cudaEventRecord(e, E->st);
+  }
+};
+
+template <typename T> FieldArgs<T> field_args(const iris_engine* E) {
+  using V = typename V2<T>::t;
+  const iris_params& p = E->p;
+  FieldArgs<T> a{};
+  a.e = (V*)E->e;
+  a.h = (V*)E->h;
+  a.g = E->g;
+  for (int s = 0; s < 2; ++s) {
+    a.pml_d[s] = (V*)E->pml_d[s];
+    a.pml_b[s] = (V*)E->pml_b[s];
+    a.pcomp[s] = E->pcomp[s];
+  }
+  a.coef = (const T*)E->coef;
+  a.pmlzi = p.pmlzi;
+  a.pmlzf = p.pmlzf;
+  a.hi = p.hi;
+  a.hf = p.hf;
+  a.eps_c = E->eps_complex ? (const V*)E->eps : nullptr;
+  a.eps_r = E->eps_complex ? nullptr : (const T*)E->eps;
+  a.m1 = (T)(1.0 / p.eps1);
+  a.m3 = (T)(1.0 / p.eps3);
+  a.eps0sq = (T)(p.eps0 * p.eps0);
+  const double dtc = p.dt * p.c0 / p.Q;
+  a.dtcq2 = (T)(dtc * dtc);
+  cx<T>* ph[6] = {&a.pxp, &a.pyp, &a.pzp, &a.pxm, &a.pym, &a.pzm};
+  for (int k = 0; k < 6; ++k) *ph[k] = cx<T>{(T)E->ph[k][0], (T)E->ph[k][1]};
+  return a;
+}
+
+// Engine lifetime.  member: a batch member (no DFT buffers of its own);
+// z_only: DFT points on the z faces only; packed: rows of nx+2 cells back to
+// back (no 128-byte alignment of x = 1), for cells whose rows are short.
+int create_engine(const iris_params* pin, const double* fw, bool member, bool z_only, iris_engine** out,
+                  bool packed = false);
+void free_engine(iris_engine* E);
+// DFT buffers for E->P sample points and nfaces flux faces.
+int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces);
+// Accumulate the sample ring into fdata (one block kernel pass).
+void dft_flush(iris_engine* E);
+// Flux of face set `set` (6 FluxFace from d_faces + 6 set) into J[6][nof].
+int read_flux(iris_engine* E, int set, double* J);
+// One split-pass step (E, H, TF/SF), with the DFT sample of step it when
+// dft is set and the step is sampled.
+void split_step(iris_engine* E, int it, bool dft);
+
+// CUDA graph of one DFT block of steps.
+bool graph_ready(const iris_engine* E, int it, int left);
+void graph_reset(iris_engine* E);
+int graph_block(iris_engine* E, int it, const std::function<void()>& record);
+
+}  // namespace iris

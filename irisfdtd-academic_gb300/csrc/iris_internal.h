@@ -1,5 +1,6 @@
 // Shared declarations between the host driver (iris_host.cpp) and the CUDA
-// engine (iris_engine.cu).  Not part of the public ABI.
+// engine (iris_engine.cu, iris_batch.cu, iris_adjoint.cu).  Not part of the
+// public ABI.
 #pragma once
 #include <string>
 
