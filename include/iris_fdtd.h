@@ -51,6 +51,13 @@ extern "C" {
 #define IRIS_OP_H 2    /* h_fdtd + UPML_Array_h + bc_{x,y,z}min_bloch      */
 #define IRIS_OP_TFSF 3 /* tfsf_gauss/tfsf_plane_wave + tfsf_update_{2D,3D} */
 #define IRIS_OP_DFT 4  /* scattering_fourier for every box, arg = time idx */
+/* Check of the bounded device waits: one CTA arms an mbarrier for bytes
+ * that are never sent, waits on it with the limit the streamed passes use
+ * divided by 2^arg (arg 0..30), gives up, records it like a real give-up
+ * and returns.  iris_apply then returns IRIS_ETIMEOUT; the engine and its
+ * CUDA context stay usable.  No memory is touched but the engine's
+ * error word.                                                          */
+#define IRIS_OP_WAIT_CHECK 5
 
 /* ---- field selectors (iris_get_field / iris_set_field) --------------- */
 #define IRIS_E 0
@@ -247,7 +254,9 @@ int iris_get_plane(iris_engine* eng, int which, int axis, int index, int lo1, in
 int iris_get_fdata(iris_engine* eng, int box, int j, double* re, double* im, long* npts);
 
 /* Run one operator group (IRIS_OP_*) for parity checks; arg is `it` for
- * IRIS_OP_TFSF and the DFT time index for IRIS_OP_DFT. */
+ * IRIS_OP_TFSF and the DFT time index for IRIS_OP_DFT.  Returns
+ * IRIS_ETIMEOUT when a bounded device wait gave up (the engine's error
+ * word is cleared once reported, by any call that reports it). */
 int iris_apply(iris_engine* eng, int op, int arg);
 
 /*

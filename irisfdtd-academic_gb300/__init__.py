@@ -37,7 +37,7 @@ FP64, FP32 = 0, 1
 STENCIL_DEFAULT, STENCIL_SPLIT, STENCIL_FUSED, STENCIL_STREAM = 0, 1, 2, 3
 DFT_KERNEL_AUTO, DFT_KERNEL_CUDA, DFT_KERNEL_TENSOR = 0, 1, 2
 E, H = 0, 1
-OP_E, OP_H, OP_TFSF, OP_DFT = 1, 2, 3, 4
+OP_E, OP_H, OP_TFSF, OP_DFT, OP_WAIT_CHECK = 1, 2, 3, 4, 5
 
 __all__ = [
     "FP64", "FP32", "E", "H", "IrisError", "IrisParams", "Engine", "build", "lib", "setparam",

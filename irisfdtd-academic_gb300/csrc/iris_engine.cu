@@ -123,6 +123,18 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 
 constexpr long long STREAM_WAIT_CYCLES = 1LL << 31;  // about a second
 
+// IRIS_OP_WAIT_CHECK: an mbarrier armed for 16 bytes that no copy delivers,
+// waited on with the streamed passes' limit divided by 2^shift; the give-up
+// is recorded (code 4) as the passes record theirs.
+__global__ void k_wait_check(int* err, int shift) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  mbar_expect_tx(&bar, 16);
+  if (!mbar_wait(&bar, 0, STREAM_WAIT_CYCLES >> shift)) atomicExch(err, 4);
+}
+
 // Issue (warp 0) the bulk copies of plane z into stage S of the E pass:
 // full: H (3 components, rows y0-1 .. y0+nye-1), E (3 components, own rows)
 // and, on structure planes, eps_inv; otherwise H components 1, 2 of the own
@@ -1763,15 +1775,20 @@ long iris::engine_npts(const iris_engine* E, int box, int j) {
 
 // Status of the engine's bounded device waits: IRIS_ETIMEOUT once a kernel
 // gave up on one (the stream is synchronised first).
+// The word is cleared once reported.
 static int stream_status(iris_engine* E) {
   if (!E->d_err) return IRIS_OK;
   int h = 0;
   CK(cudaMemcpyAsync(&h, E->d_err, sizeof(int), cudaMemcpyDeviceToHost, E->st));
   CK(cudaStreamSynchronize(E->st));
-  if (h) return fail(IRIS_ETIMEOUT, h == 3 ? std::string("the tensor-core DFT block gave up waiting")
-                                            : std::string("a streamed ") + (h == 1 ? "E" : "H") +
-                                                  " pass gave up waiting for its staged plane");
-  return IRIS_OK;
+  if (!h) return IRIS_OK;
+  CK(cudaMemsetAsync(E->d_err, 0, sizeof(int), E->st));
+  CK(cudaStreamSynchronize(E->st));
+  const char* what = h == 1   ? "a streamed E pass gave up waiting for its staged plane"
+                     : h == 2 ? "a streamed H pass gave up waiting for its staged plane"
+                     : h == 3 ? "the tensor-core DFT block gave up waiting"
+                              : "the wait check gave up (as it must)";
+  return fail(IRIS_ETIMEOUT, what);
 }
 
 int iris::read_flux(iris_engine* E, int set, double* J) {
@@ -2063,11 +2080,15 @@ int iris_apply(iris_engine* E, int op, int arg) {
       d ? dft_sample<double>(E, arg) : dft_sample<float>(E, arg);
       dft_flush(E);
       break;
+    case IRIS_OP_WAIT_CHECK:
+      if (arg < 0 || arg > 30) return fail(IRIS_EINVAL, "wait check: arg must be 0..30");
+      k_wait_check<<<1, 32, 0, E->st>>>(E->d_err, arg);
+      break;
     default: return fail(IRIS_EINVAL, "unknown operator");
   }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(E->st));
-  return IRIS_OK;
+  return stream_status(E);
 }
 
 }  // extern "C"

@@ -14,7 +14,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import interior, output_steps, rel_err
+from helpers import interior, output_steps, rel_err, run_engine_blocks
 from test_gpu_fused import CASES, make_case, material, run
 
 pytestmark = pytest.mark.gpu
@@ -80,3 +80,33 @@ def test_stream_selection_and_fp64_rejected(iris, oracle, tmp_path):
 def engine_params_from_oracle_fp(iris, op, precision):
     from helpers import engine_params_from_oracle
     return engine_params_from_oracle(iris, op, precision=precision)
+
+
+
+IRIS_EINVAL, IRIS_ETIMEOUT = -1, -7
+
+
+@pytest.mark.parametrize("stencil", [STREAM, 2])
+def test_bounded_wait_gives_up_and_engine_stays_usable(iris, oracle, tmp_path, stencil):
+    """A device wait on an mbarrier that nothing completes (IRIS_OP_WAIT_CHECK)
+    gives up after its limit and is reported once as IRIS_ETIMEOUT; the engine
+    then steps exactly like a twin that never waited."""
+    w, op = make_case(oracle, tmp_path, (24, 12, 48, 6, 43, 18, 10, 4.0, 10, (1, 24, 1, 12, 8, 40)), 2)
+    op.texit = 40
+    eps = cfg.spheres_material(w, seed=3)
+
+    def engine():
+        e = iris.Engine(engine_params_from_oracle_fp(iris, op, 1), op.fw, stencil=stencil)
+        e.set_material(eps)
+        return e
+
+    eng, twin = engine(), engine()
+    assert eng.L.iris_apply(eng.h, iris.OP_WAIT_CHECK, 10) == IRIS_ETIMEOUT  # about a millisecond
+    assert "wait check" in eng.L.iris_last_error().decode()
+    eng.sync()  # reported once: the error word is clear again
+    assert eng.L.iris_apply(eng.h, iris.OP_WAIT_CHECK, 31) == IRIS_EINVAL
+    J = run_engine_blocks(eng, op, output_steps(op))
+    Jt = run_engine_blocks(twin, op, output_steps(op))
+    assert np.array_equal(J, Jt)
+    for which in (iris.E, iris.H):
+        assert np.array_equal(eng.get_field(which), twin.get_field(which))
