@@ -257,7 +257,7 @@ def run_engine(args, rank, world, local):
         dom, db, dt_ = ("update_h", hb, t_h) if t_h >= t_e else ("update_e", eb, t_e)
         min_bytes = db
     achieved = db / dt_ / 1e9
-    wl_name = f"{w.name} (configs[{args.workload - 1}])" if not args.grid else w.name
+    wl_name = w.name
     traffic, tsrc = ncu_traffic(dom, w.name + "_" + args.precision)
     launches = kn["update_e"] + kn["update_h"] + kn["tfsf"] + kn["dft_gather"] + kn["flux"] + kn["fused_eh"] + \
         kn["dft_block"] * (2 if prec == iris.FP32 else 1)
@@ -315,7 +315,7 @@ def run_engine(args, rank, world, local):
 
 
 def run_batch(args, rank, world, local):
-    """configs[3]: 256 independent Bloch cells of uneven size (seed+i per cell),
+    """The batched workload: 256 independent Bloch cells of uneven size (seed+i per cell),
     FP32 fields, FP64 DFT at 128 frequencies on the reflection and transmission
     planes, all cells stepped by one launch per operator."""
     iris = importlib.import_module(PKG)
@@ -377,7 +377,7 @@ def run_batch(args, rank, world, local):
         "ms_per_step": round(reg_ms / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64 fields (fp32), fp64 incident field and DFT accumulation",
         "data": "synthetic (seeded binary eps patterns, numpy PCG64 seed+i per cell)",
-        "config": {"workload": f"batch of {ncells} uneven Bloch cells (configs[3])", "grid_cells": cells,
+        "config": {"workload": f"batch of {ncells} uneven Bloch cells", "grid_cells": cells,
                    "nof": 128, "dft_points": info["dft_points"], "dft_block": info["dft_block"],
                    "dft_faces": "z planes (reflection, transmission)", "tile": list(tile),
                    "tune_ms_per_eh_pass": {"_".join(map(str, k)) if k[0] == "flat" else "x".join(map(str, k)): round(v, 3)
@@ -403,7 +403,7 @@ def run_batch(args, rank, world, local):
 
 
 def run_adjoint(args, rank, world, local):
-    """configs[4]: dL/d eps over a 128x128x32 design region (eps ~U[1,12],
+    """The gradient workload: dL/d eps over a 128x128x32 design region (eps ~U[1,12],
     seed 0) of a 160x160x512 cell, L = sum over 64 frequencies of J6, FP32
     forward and adjoint, checkpoints every 256 steps.  Reports the gradient
     throughput, its cost against the forward solve, and its error against
@@ -448,7 +448,7 @@ def run_adjoint(args, rank, world, local):
         "ms_per_step": round((fwd_ms + bwd_ms) / N, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 fields and adjoint (fp32), fp64 DFT and gradient accumulation",
         "data": "synthetic (design eps ~U[1,12], numpy PCG64 seed = rank)",
-        "config": {"workload": f"{w.name} gradient (configs[4])", "grid": [w.nx, w.ny, w.nz],
+        "config": {"workload": f"{w.name} gradient", "grid": [w.nx, w.ny, w.nz],
                    "design_region": list(design), "nof": w.nof, "checkpoint_every": 256,
                    "objective": "sum_w J6(w)",
                    "l2": "fields 2 x %.2f GB >> 129 MB L2" % (cells * 24 / 1e9),
@@ -642,8 +642,8 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)",
         "data": "synthetic (seeded inputs of the workload's shape)",
-        "config": {"workload": (f"batch of {args.cells} cells (configs[3]), per-cell costs of {w.name}"
-                                if args.workload == 4 else f"{w.name} (configs[{args.workload - 1}])"),
+        "config": {"workload": (f"batch of {args.cells} cells, per-cell costs of {w.name}"
+                                if args.workload == 4 else w.name),
                    "grid": [w.nx, w.ny, w.nz], "grid_cells": cells, "nof": w.nof},
         "cpu_baseline": {"value": round(v, 6), "unit": "Gcell/s", "cores": threads, "kind": "port",
                          "sample": sample},

@@ -23,7 +23,7 @@
 // irisfdtd_movie.py:25) and the analytic film spectrum the reference writes
 // (code/common.f90:104-131).  The reference itself cannot be compiled here
 // (no Fortran compiler), so bit-level pinning against a reference run is not
-// possible; see the design doc.
+// possible.
 
 #include <chrono>
 #include <cmath>
