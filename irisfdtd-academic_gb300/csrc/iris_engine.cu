@@ -895,6 +895,14 @@ __global__ void __launch_bounds__(256) k_flux(const double2* __restrict__ fd, lo
 // buffers, as after the split passes.  B is touched only by its owner and
 // stays in place; D is double buffered because image and overlap threads
 // read the old D of cells another CTA owns.
+//
+// Loads: a thread's own E and H of the next plane go to registers one plane
+// ahead.  What it reads after the barrier from outside the tile (the H
+// neighbours at x-1 for lane 0 and at y-1 for warp 0, and the ghosts the
+// image threads read) and the eps_inv of structure planes would otherwise be
+// dependent loads right after the barrier, which every warp waits for; they
+// are copied into shared memory by cp.async one plane ahead instead, into
+// slots only the issuing thread reads.
 
 constexpr int FZ_X = 32, FZ_Y = 16, FZ_OX = FZ_X - 1, FZ_OY = FZ_Y - 1;
 
@@ -913,11 +921,26 @@ __device__ __forceinline__ cx<float> shfl_cx(cx<float> v, int d, bool up) {
   return r;
 }
 
+__device__ __forceinline__ void cpa8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(FusedArgs A) {
   const FieldArgs<float>& a = A.f;
   const Geo& g = a.g;
   // per row and plane parity: H(z) components 1, 3 and E'(z-1) components 1, 3
   __shared__ float2 xr[2][FZ_Y][4][FZ_X];
+  // H neighbours outside the tile, copied one plane ahead (plane parity):
+  // x-1 components 1, 2 for lane 0 [0] and the x-image lane [1]; y-1
+  // components 0, 2 for warp 0 [0] and the y-image warp [1]
+  __shared__ float2 xh[2][FZ_Y][2][2];
+  __shared__ float2 yh[2][2][2][FZ_X];
+  __shared__ float epsh[2][FZ_Y][FZ_X];  // eps_inv of a structure plane (real material)
   const int lane = threadIdx.x, w = threadIdx.y;
   const int x = 1 + blockIdx.x * FZ_OX + lane, y = 1 + blockIdx.y * FZ_OY + w;
   const int z0 = 1 + blockIdx.z * A.zchunk, z1 = min(z0 + A.zchunk - 1, g.nz);
@@ -933,6 +956,29 @@ template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(Fu
   auto ldc = [&](const float2* f, int k, int xx, int yy, int zz) {
     return ld<float>(f + k * g.comp + g.at(xx, yy, zz));
   };
+  const bool xhalo = act && (lane == 0 || ximg), yhalo = act && (w == 0 || yimg);
+  const int xs = lane == 0 ? 0 : 1, ys = w == 0 ? 0 : 1;
+  // The copies of plane p in [z0, z1 + 1] (plane nz + 1 is the image of
+  // plane 1) into the slots of parity p & 1: one commit group per plane.
+  auto ahead = [&](int p) {
+    if (p <= z1 + 1) {
+      const int zp = p == g.nz + 1 ? 1 : p;
+      if (!CEPS && act && zp >= a.hi && zp <= a.hf)
+        cpa4(&epsh[p & 1][w][lane], a.eps_r + (long)(zp - a.hi) * g.plane + (long)cyy * g.pitch + (cxx + g.xo));
+      if (xhalo) {
+        const long q = g.at(cxx - 1, cyy, zp);
+        cpa8(&xh[p & 1][w][xs][0], H + g.comp + q);
+        cpa8(&xh[p & 1][w][xs][1], H + 2 * g.comp + q);
+      }
+      if (yhalo) {
+        const long q = g.at(cxx, cyy - 1, zp);
+        cpa8(&yh[p & 1][ys][0][lane], H + q);
+        cpa8(&yh[p & 1][ys][1][lane], H + 2 * g.comp + q);
+      }
+    }
+    cpa_commit();
+  };
+  ahead(z0);
   const cx<float> zero = {0.f, 0.f};
   // Carried from plane z-1 in this thread's own slots of the exchange rows
   // (written there for the neighbours anyway): components 1, 3 of H(z-1) in
@@ -980,6 +1026,7 @@ template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(Fu
         hn_[k] = ldc(H, k, cxx, cyy, zn);
       }
     }
+    ahead(z + 1);
     if (zimg && act) {
       hzm0 = ldc(H, 0, cxx, cyy, 0);
       hzm1 = ldc(H, 1, cxx, cyy, 0);
@@ -993,15 +1040,18 @@ template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(Fu
     const cx<float> ex1 = shfl_cx(ep[1], 1, false), ex2 = shfl_cx(ep[2], 1, false);
     __syncthreads();
     cx<float> enew[3];
+    cpa_wait<1>();  // the copies of plane z have landed (those of z + 1 may not)
     if (act) {
-      if (lane == 0 || ximg) {
-        hx1 = ldc(H, 1, cxx - 1, cyy, cz);
-        hx2 = ldc(H, 2, cxx - 1, cyy, cz);
+      if (xhalo) {
+        const float2 u = xh[z & 1][w][xs][0], v = xh[z & 1][w][xs][1];
+        hx1 = {u.x, u.y};
+        hx2 = {v.x, v.y};
       }
       cx<float> hy0, hy2;
-      if (w == 0 || yimg) {
-        hy0 = ldc(H, 0, cxx, cyy - 1, cz);
-        hy2 = ldc(H, 2, cxx, cyy - 1, cz);
+      if (yhalo) {
+        const float2 u = yh[z & 1][ys][0][lane], v = yh[z & 1][ys][1][lane];
+        hy0 = {u.x, u.y};
+        hy2 = {v.x, v.y};
       } else {
         const float2 u = xr[buf][w - 1][0][lane], v = xr[buf][w - 1][1][lane];
         hy0 = {u.x, u.y};
@@ -1014,7 +1064,8 @@ template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(Fu
       c[2] = cadd(csub(csub(h[1], hx1), h[0]), hy0);
 #pragma unroll
       for (int k = 0; k < 3; ++k) enew[k] = e[k];
-      e_apply<float, CEPS>(a, (own && z <= z1) ? A.d_new : nullptr, cxx, cyy, cz, c, enew);
+      e_apply<float, CEPS, 7, !CEPS>(a, (own && z <= z1) ? A.d_new : nullptr, cxx, cyy, cz, c, enew,
+                                     CEPS ? 0.f : epsh[z & 1][w][lane]);
       if (ximg || yimg) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) enew[k] = cmul(ph, enew[k]);
