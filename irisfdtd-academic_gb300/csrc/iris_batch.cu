@@ -150,12 +150,10 @@ __global__ void __launch_bounds__(256) k_batch_gather(const FieldArgs<T>* __rest
                                                       int t, const int* tp) {
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = tp ? *tp + t : t;
   const BSeg b = segs[blockIdx.y];
-  const long L = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (L >= (long)b.s.nu * b.s.nv) return;
+  if (blockIdx.x * (unsigned)GATHER_BLOCK >= (unsigned)b.s.nu * (unsigned)b.s.nv) return;
   const FieldArgs<T>& a = args[b.cell];
-  const int u = (int)(L % b.s.nu), v = (int)(L / b.s.nu);
   const typename V2<T>::t* src = b.s.field < 3 ? a.e + b.s.field * a.g.comp : a.h + (b.s.field - 3) * a.g.comp;
-  slot[b.s.p0 + L] = src[b.s.src + (long)u * b.s.su + (long)v * b.s.sv];
+  gather_run<T>(b.s, src, slot);
 }
 
 }  // namespace
@@ -322,7 +320,7 @@ template <typename T> void batch_one_step(iris_batch* B, int it, const int* itp,
     {
       KTimer tm(M, IRIS_KC_GATHER);
       V* slot = (V*)M->S + (long)M->nslot * M->P;
-      dim3 grid((unsigned)((B->max_seg + 255) / 256), (unsigned)B->nbsegs);
+      dim3 grid((unsigned)((B->max_seg + GATHER_BLOCK - 1) / GATHER_BLOCK), (unsigned)B->nbsegs);
       k_batch_gather<T><<<grid, 256, 0, M->st>>>(args, B->d_bsegs, slot, M->d_tk, M->nslot, it + 1 - p.to_fourier,
                                                  itp);
     }

@@ -463,6 +463,32 @@ struct Seg {
   int pad;
   long p0;     // first sample index
 };
+// Samples of one run handled by a block of 256 threads: GATHER_PER per
+// thread, their loads issued before their stores.  Sample L of the run is
+// location (u, v) = (L mod nu, L div nu); runs hold fewer than 2^31 samples.
+constexpr int GATHER_PER = 4, GATHER_BLOCK = 256 * GATHER_PER;
+template <typename T>
+__device__ __forceinline__ void gather_run(const Seg& sg, const typename V2<T>::t* __restrict__ src,
+                                           typename V2<T>::t* __restrict__ slot) {
+  using V = typename V2<T>::t;
+  const unsigned n = (unsigned)sg.nu * (unsigned)sg.nv, nu = (unsigned)sg.nu;
+  const unsigned L0 = blockIdx.x * (unsigned)GATHER_BLOCK + threadIdx.x;
+  V val[GATHER_PER];
+#pragma unroll
+  for (int j = 0; j < GATHER_PER; ++j) {
+    const unsigned L = L0 + 256u * j;
+    if (L < n) {
+      const unsigned v = L / nu, u = L - v * nu;
+      val[j] = src[sg.src + (long)u * sg.su + (long)v * sg.sv];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < GATHER_PER; ++j) {
+    const unsigned L = L0 + 256u * j;
+    if (L < n) slot[sg.p0 + L] = val[j];
+  }
+}
+
 // Poynting flux of one face, code/dataprocess.f90:246-277:
 // J = sign * sum Re(a*conj(b) - c*conj(d)) * eps0*Q/(2 dt).
 struct FluxFace {

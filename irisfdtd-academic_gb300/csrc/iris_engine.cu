@@ -406,12 +406,8 @@ __global__ void __launch_bounds__(256) k_dft_gather(const typename V2<T>::t* __r
                                                     int* tk, int islot, int t, const int* tp) {
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = tp ? *tp + t : t;
   const Seg sg = segs[blockIdx.y];
-  const long L = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long n = (long)sg.nu * sg.nv;
-  if (L >= n) return;
-  const int u = (int)(L % sg.nu), v = (int)(L / sg.nu);
   const typename V2<T>::t* src = sg.field < 3 ? e + sg.field * comp : h + (sg.field - 3) * comp;
-  slot[sg.p0 + L] = src[sg.src + (long)u * sg.su + (long)v * sg.sv];
+  gather_run<T>(sg, src, slot);
 }
 
 // FP64 mode: fdata(p, iw) += (dt*F_k(p))*exp(i*fw(iw)*t_k), k in the
@@ -1326,7 +1322,7 @@ template <typename T> void dft_sample(iris_engine* E, int t, const int* tp = nul
   {
   KTimer tm(E, IRIS_KC_GATHER);
   V* slot = (V*)E->S + (long)E->nslot * E->P;
-  dim3 grid((unsigned)((E->max_seg + 255) / 256), (unsigned)E->segs.size());
+  dim3 grid((unsigned)((E->max_seg + GATHER_BLOCK - 1) / GATHER_BLOCK), (unsigned)E->segs.size());
   k_dft_gather<T><<<grid, 256, 0, E->st>>>((const V*)E->e, (const V*)E->h, E->g.comp, E->d_segs, slot, E->d_tk,
                                           E->nslot, t, tp);
   }
@@ -1527,6 +1523,7 @@ int build_dft(iris_engine* E) {
       }
     }
   }
+  if (E->max_seg >= (1L << 31) - GATHER_BLOCK) return fail(IRIS_EINVAL, "a DFT face has 2^31 or more locations");
   E->P = P;
   E->host_faces = faces;
   if (E->member) return IRIS_OK;  // a batch member: the batch owns the DFT buffers
