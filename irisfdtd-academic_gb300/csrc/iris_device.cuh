@@ -90,17 +90,20 @@ template <typename T> struct FieldArgs {
 // place).  With EPV the caller supplies the real structure eps_inv of the
 // cell (ep) instead of it being read from a.eps_r.  MASK selects the
 // components computed (bit k: E_{k+1}).  UPML = false: the caller knows the
-// cell lies outside the UPML slabs (the slab code is not compiled in).
+// cell lies outside the UPML slabs (the slab code is not compiled in).  A
+// caller that has copied the cell's old D (dv, 3 values) or the plane's
+// coefficient row (cfv) ahead passes them instead of their global copies.
 template <typename T, bool CEPS, int MASK = 7, bool EPV = false, bool UPML = true>
 __device__ __forceinline__ void e_apply(const FieldArgs<T>& a, typename V2<T>::t* const* dnew, int x, int y, int z,
-                                        const cx<T> c[3], cx<T> e[3], T ep = T(0)) {
+                                        const cx<T> c[3], cx<T> e[3], T ep = T(0), const cx<T>* dv = nullptr,
+                                        const T* cfv = nullptr) {
   using V = typename V2<T>::t;
   const Geo& g = a.g;
   if (UPML && (z <= a.pmlzi || z >= a.pmlzf)) {
     const int slab = z <= a.pmlzi ? 0 : 1;
     const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
     const int row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
-    const T* cf = a.coef + NCOEF * row;
+    const T* cf = cfv ? cfv : a.coef + NCOEF * row;
     const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
     const V* D = a.pml_d[slab];
     const long pc = a.pcomp[slab];
@@ -108,7 +111,7 @@ __device__ __forceinline__ void e_apply(const FieldArgs<T>& a, typename V2<T>::t
     for (int k = 0; k < 3; ++k) {
       if (!(MASK & (1 << k))) continue;
       const cx<T> ck = rmul(a.eps0sq, c[k]);
-      const cx<T> dold = ld<T>(D + k * pc + pi);
+      const cx<T> dold = dv ? dv[k] : ld<T>(D + k * pc + pi);
       const cx<T> dn = cadd(rmul(cf[CD_A + k], dold), rmul(cf[CD_B + k], ck));
       if (dnew) st<T>(dnew[slab] + k * pc + pi, dn);
       e[k] = cadd(rmul(cf[CE_A + k], e[k]), rmul(cf[CE_B + k], csub(rmul(cf[C_FP + k], dn), rmul(cf[C_FM + k], dold))));
@@ -178,10 +181,12 @@ __device__ __forceinline__ void e_cell(const FieldArgs<T>& a, typename V2<T>::t*
 // UPML_Array_h (code/boundary_II.f90:142-220), from the new E of the cell (ev)
 // and of its +x, +y, +z neighbours (xp: components 2,3; yp: 1,3; zp: 1,2),
 // the old H read from a.h, the UPML auxiliary B updated in place.  UPML =
-// false: the cell lies outside the UPML slabs.
+// false: the cell lies outside the UPML slabs.  bv / cfv: the cell's old B and
+// the plane's coefficient row when the caller has copied them ahead.
 template <typename T, bool UPML = true>
 __device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, int z, const cx<T> ev[3],
-                                         const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3]) {
+                                         const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3],
+                                         const cx<T>* bv = nullptr, const T* cfv = nullptr) {
   using V = typename V2<T>::t;
   const Geo& g = a.g;
   cx<T> c[3];
@@ -192,13 +197,13 @@ __device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, in
     const int slab = z <= a.pmlzi ? 0 : 1;
     const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
     const int row = slab == 0 ? z - 1 : a.pmlzi + z - a.pmlzf;
-    const T* cf = a.coef + NCOEF * row;
+    const T* cf = cfv ? cfv : a.coef + NCOEF * row;
     const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
     V* B = a.pml_b[slab];
     const long pc = a.pcomp[slab];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const cx<T> bold = ld<T>(B + k * pc + pi);
+      const cx<T> bold = bv ? bv[k] : ld<T>(B + k * pc + pi);
       const cx<T> bn = csub(rmul(cf[CD_A + k], bold), rmul(cf[CB_B + k], c[k]));
       st<T>(B + k * pc + pi, bn);
       h[k] = cadd(rmul(cf[CE_A + k], h[k]), rmul(cf[CH_B + k], csub(rmul(cf[C_FP + k], bn), rmul(cf[C_FM + k], bold))));

@@ -899,6 +899,14 @@ __global__ void __launch_bounds__(256) k_flux(const double2* __restrict__ fd, lo
 // dependent loads right after the barrier, which every warp waits for; they
 // are copied into shared memory by cp.async one plane ahead instead, into
 // slots only the issuing thread reads.
+//
+// A step is two launches over z chunks (chunks are independent: each reads
+// the old state of its planes and the plane below and above it): the planes
+// pmlzi+1 .. pmlzf-2 by the kernel compiled without UPML code (UPML =
+// false), and the two slabs, each with the one plane next to it, by the
+// kernel with it.  The interior range stops at pmlzf-2 because a chunk also
+// computes E' one plane past its end (its last H' needs it), and that plane
+// must not lie in a slab.
 
 constexpr int FZ_X = 32, FZ_Y = 16, FZ_OX = FZ_X - 1, FZ_OY = FZ_Y - 1;
 
@@ -907,8 +915,20 @@ struct FusedArgs {
   float2* e_new;
   float2* h_new;
   float2* d_new[2];
-  int zchunk;  // planes per CTA
+  // z chunks: blockIdx.z < nc0 covers planes za0 + zc0 * blockIdx.z on (at
+  // most zc0, up to zb0), the rest the same over za1..zb1
+  int za0, zb0, zc0, nc0, za1, zb1, zc1;
 };
+
+// Dynamic shared memory of the slab kernel (UPML = true): this thread's old
+// D of the plane and B of the plane below, and the two planes' coefficient
+// rows, copied one plane ahead like the halo.
+struct FusedUpml {
+  cx<float> d[2][FZ_Y][FZ_X][3];
+  cx<float> b[2][FZ_Y][FZ_X][3];
+  float cf[2][2][NCOEF];  // [parity][E row of the plane, H row of the plane below]
+};
+constexpr size_t FZ_UPML_SMEM = sizeof(FusedUpml);
 
 __device__ __forceinline__ cx<float> shfl_cx(cx<float> v, int d, bool up) {
   cx<float> r;
@@ -926,7 +946,7 @@ __device__ __forceinline__ void cpa4(void* dst, const void* src) {
 __device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(FusedArgs A) {
+template <bool CEPS, bool UPML> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(FusedArgs A) {
   const FieldArgs<float>& a = A.f;
   const Geo& g = a.g;
   // per row and plane parity: H(z) components 1, 3 and E'(z-1) components 1, 3
@@ -937,9 +957,13 @@ template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(Fu
   __shared__ float2 xh[2][FZ_Y][2][2];
   __shared__ float2 yh[2][2][2][FZ_X];
   __shared__ float epsh[2][FZ_Y][FZ_X];  // eps_inv of a structure plane (real material)
+  extern __shared__ __align__(16) unsigned char fz_dyn[];
+  FusedUpml& U = *reinterpret_cast<FusedUpml*>(fz_dyn);  // UPML = true only
   const int lane = threadIdx.x, w = threadIdx.y;
   const int x = 1 + blockIdx.x * FZ_OX + lane, y = 1 + blockIdx.y * FZ_OY + w;
-  const int z0 = 1 + blockIdx.z * A.zchunk, z1 = min(z0 + A.zchunk - 1, g.nz);
+  const bool r0 = (int)blockIdx.z < A.nc0;
+  const int z0 = r0 ? A.za0 + A.zc0 * (int)blockIdx.z : A.za1 + A.zc1 * ((int)blockIdx.z - A.nc0);
+  const int z1 = min(z0 + (r0 ? A.zc0 : A.zc1) - 1, r0 ? A.zb0 : A.zb1);
   const bool act = x <= g.nx + 1 && y <= g.ny + 1;
   const bool ximg = x == g.nx + 1, yimg = y == g.ny + 1;
   const int cxx = ximg ? 1 : x, cyy = yimg ? 1 : y;  // the cell whose E' this thread computes
@@ -970,6 +994,29 @@ template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(Fu
         const long q = g.at(cxx, cyy - 1, zp);
         cpa8(&yh[p & 1][ys][0][lane], H + q);
         cpa8(&yh[p & 1][ys][1][lane], H + 2 * g.comp + q);
+      }
+      if (UPML) {
+        // the old D of this thread's E' cell on plane zp, the B of its H'
+        // cell on plane p-1, and both planes' coefficient rows (warps 0, 1)
+        const int zb = p - 1;
+        const bool pe = zp <= a.pmlzi || zp >= a.pmlzf, pb = zb >= z0 && (zb <= a.pmlzi || zb >= a.pmlzf);
+        if (act && pe) {
+          const int slab = zp <= a.pmlzi ? 0 : 1, zr = slab == 0 ? zp - 1 : zp - a.pmlzf;
+          const long pi = ((long)zr * g.ny + (cyy - 1)) * (long)g.nx + (cxx - 1);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) cpa8(&U.d[p & 1][w][lane][k], a.pml_d[slab] + k * a.pcomp[slab] + pi);
+        }
+        if (own && pb) {
+          const int slab = zb <= a.pmlzi ? 0 : 1, zr = slab == 0 ? zb - 1 : zb - a.pmlzf;
+          const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) cpa8(&U.b[p & 1][w][lane][k], a.pml_b[slab] + k * a.pcomp[slab] + pi);
+        }
+        if (w < 2 && lane < NCOEF && (w == 0 ? pe : pb)) {
+          const int zz = w == 0 ? zp : zb;
+          const int row = zz <= a.pmlzi ? zz - 1 : a.pmlzi + zz - a.pmlzf;
+          cpa4(&U.cf[p & 1][w][lane], a.coef + NCOEF * row + lane);
+        }
       }
     }
     cpa_commit();
@@ -1034,9 +1081,11 @@ template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(Fu
     xr[buf][w][1][lane] = make_float2(h[2].re, h[2].im);
     cx<float> hx1 = shfl_cx(h[1], 1, true), hx2 = shfl_cx(h[2], 1, true);
     const cx<float> ex1 = shfl_cx(ep[1], 1, false), ex2 = shfl_cx(ep[2], 1, false);
+    // this thread's copies of plane z have landed (those of z + 1 may not);
+    // the barrier then shows the coefficient rows to every thread
+    cpa_wait<1>();
     __syncthreads();
     cx<float> enew[3];
-    cpa_wait<1>();  // the copies of plane z have landed (those of z + 1 may not)
     if (act) {
       if (xhalo) {
         const float2 u = xh[z & 1][w][xs][0], v = xh[z & 1][w][xs][1];
@@ -1060,8 +1109,9 @@ template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(Fu
       c[2] = cadd(csub(csub(h[1], hx1), h[0]), hy0);
 #pragma unroll
       for (int k = 0; k < 3; ++k) enew[k] = e[k];
-      e_apply<float, CEPS, 7, !CEPS>(a, (own && z <= z1) ? A.d_new : nullptr, cxx, cyy, cz, c, enew,
-                                     CEPS ? 0.f : epsh[z & 1][w][lane]);
+      e_apply<float, CEPS, 7, !CEPS, UPML>(a, (own && z <= z1) ? A.d_new : nullptr, cxx, cyy, cz, c, enew,
+                                           CEPS ? 0.f : epsh[z & 1][w][lane], UPML ? U.d[z & 1][w][lane] : nullptr,
+                                           UPML ? U.cf[z & 1][0] : nullptr);
       if (ximg || yimg) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) enew[k] = cmul(ph, enew[k]);
@@ -1082,7 +1132,8 @@ template <bool CEPS> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(Fu
         zp[1] = enew[1];
 #pragma unroll
         for (int k = 0; k < 3; ++k) hn[k] = hp[k];
-        h_update<float>(a, x, y, z - 1, ep, xp, yp, zp, hn);
+        h_update<float, UPML>(a, x, y, z - 1, ep, xp, yp, zp, hn, UPML ? U.b[z & 1][w][lane] : nullptr,
+                              UPML ? U.cf[z & 1][1] : nullptr);
         const long i = g.at(x, y, z - 1);
 #pragma unroll
         for (int k = 0; k < 3; ++k) st<float>(A.h_new + k * g.comp + i, hn[k]);
@@ -1329,14 +1380,28 @@ template <typename T> void dft_sample(iris_engine* E, int t, const int* tp = nul
   if (++E->nslot == E->K) dft_flush(E);
 }
 
-FusedArgs fused_args(const iris_engine* E) {
+FusedArgs fused_args(const iris_engine* E, int part) {
   FusedArgs a{};
   a.f = field_args<float>(E);
   a.e_new = (float2*)E->e2;
   a.h_new = (float2*)E->h2;
   for (int s = 0; s < 2; ++s) a.d_new[s] = (float2*)E->pml_d2[s];
-  a.zchunk = E->zchunk;
+  const std::vector<int>& r = E->fzr[part];  // (za, zb, zc, n) per range
+  a.za0 = r[0], a.zb0 = r[1], a.zc0 = r[2], a.nc0 = r[3];
+  a.za1 = r.size() > 4 ? r[4] : 0, a.zb1 = r.size() > 4 ? r[5] : 0, a.zc1 = r.size() > 4 ? r[6] : 1;
   return a;
+}
+
+// z chunks of planes za..zb for a launch over `tiles` column tiles: about
+// eight waves of two CTAs per SM, at least 16 planes each; appends
+// (za, zb, planes per chunk, chunks) to r.
+void fused_chunks(std::vector<int>& r, int za, int zb, long tiles) {
+  if (zb < za) return;
+  const int len = zb - za + 1;
+  long nch = std::max(1L, (8L * 152 * 2 + tiles - 1) / tiles);
+  nch = std::min<long>(nch, std::max(1, len / 16));
+  const int zc = (int)((len + nch - 1) / nch);
+  r.insert(r.end(), {za, zb, zc, (len + zc - 1) / zc});
 }
 
 
@@ -1345,10 +1410,21 @@ FusedArgs fused_args(const iris_engine* E) {
 // it, or *itp + it when itp is given.
 void fused_one(iris_engine* E, int it, const int* itp, bool sampled) {
   {
-    KTimer tm(E, IRIS_KC_FUSED);
-    const FusedArgs a = fused_args(E);
-    if (E->eps_complex) k_fused<true><<<E->fgrd, E->fblk, 0, E->st>>>(a);
-    else k_fused<false><<<E->fgrd, E->fblk, 0, E->st>>>(a);
+    // the planes outside the UPML slabs with a kernel without slab code, then the slabs
+    for (int part = 0; part < 2; ++part) {
+      const std::vector<int>& r = E->fzr[part];
+      if (r.empty()) continue;
+      KTimer tm(E, IRIS_KC_FUSED);
+      const FusedArgs a = fused_args(E, part);
+      const dim3 grd(E->fgrd.x, E->fgrd.y, (unsigned)(r[3] + (r.size() > 4 ? r[7] : 0)));
+      if (part == 0) {
+        if (E->eps_complex) k_fused<true, false><<<grd, E->fblk, 0, E->st>>>(a);
+        else k_fused<false, false><<<grd, E->fblk, 0, E->st>>>(a);
+      } else {
+        if (E->eps_complex) k_fused<true, true><<<grd, E->fblk, FZ_UPML_SMEM, E->st>>>(a);
+        else k_fused<false, true><<<grd, E->fblk, FZ_UPML_SMEM, E->st>>>(a);
+      }
+    }
   }
   std::swap(E->e, E->e2);
   std::swap(E->h, E->h2);
@@ -1785,13 +1861,24 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
       if (cudaMalloc(&E->pml_d2[s], b) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "UPML allocation failed"));
       cudaMemsetAsync(E->pml_d2[s], 0, b, E->st);
     }
-    // z chunks: about eight waves of two CTAs per SM, at least 16 planes each
+    // z chunks: planes pmlzi+1 .. pmlzf-2 (the last chunk's extra plane,
+    // whose E' its H' needs, is then still outside the slabs) by the kernel
+    // without slab code, the slabs with the plane next to each by the other
     const long tiles = (long)((p.nx + FZ_OX - 1) / FZ_OX) * ((p.ny + FZ_OY - 1) / FZ_OY);
-    long nch = std::max(1L, (8L * 152 * 2 + tiles - 1) / tiles);
-    nch = std::min<long>(nch, std::max(1, p.nz / 16));
-    E->zchunk = (int)((p.nz + nch - 1) / nch);
+    const int ia = p.pmlzi + 1, ib = p.pmlzf - 2;
+    for (int part = 0; part < 2; ++part) E->fzr[part].clear();
+    if (ib >= ia) {
+      fused_chunks(E->fzr[0], ia, ib, tiles);
+      fused_chunks(E->fzr[1], 1, ia - 1, tiles);
+      fused_chunks(E->fzr[1], ib + 1, p.nz, tiles);
+    } else {
+      fused_chunks(E->fzr[1], 1, p.nz, tiles);
+    }
     E->fblk = dim3(FZ_X, FZ_Y, 1);
-    E->fgrd = dim3((p.nx + FZ_OX - 1) / FZ_OX, (p.ny + FZ_OY - 1) / FZ_OY, (p.nz + E->zchunk - 1) / E->zchunk);
+    for (const void* kf : {(const void*)k_fused<false, true>, (const void*)k_fused<true, true>})
+      if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FZ_UPML_SMEM) != cudaSuccess)
+        return bail(fail(IRIS_ECUDA, "fused pass: shared memory configuration failed"));
+    E->fgrd = dim3((p.nx + FZ_OX - 1) / FZ_OX, (p.ny + FZ_OY - 1) / FZ_OY, 1);
   }
   if (cudaMalloc(&E->d_err, sizeof(int)) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "allocation failed"));
   cudaMemsetAsync(E->d_err, 0, sizeof(int), E->st);

@@ -84,7 +84,9 @@ struct iris_engine {
   void* e2 = nullptr;
   void* h2 = nullptr;
   void* pml_d2[2] = {nullptr, nullptr};
-  int zchunk = 0;
+  // z chunks (first, last plane) of its two launches: [0] the planes outside
+  // the UPML slabs, [1] the slabs
+  std::vector<int> fzr[2];
   dim3 fblk, fgrd;
   // CUDA graph of one DFT block of steps (iris_params.graph): d_it holds the
   // step base the captured kernels add to their offsets, dev_it its value
