@@ -315,21 +315,27 @@ int iris_batch_flux(iris_batch* b, int cell, double* J);
 /* iris_get_field of one cell. */
 int iris_batch_get_field(iris_batch* b, int cell, int which, double* re, double* im);
 /*
- * Tile-shape autotuner: times every candidate tile of the E/H work list
- * (reps E+H passes each) on this batch and keeps the fastest; ms[i]
- * (optional, 7 entries) receives the time per E+H pass of candidate i.  Call
+ * Tile-shape autotuner: times every candidate work list (reps E+H passes,
+ * or fused passes, each) on this batch and keeps the fastest; ms[i]
+ * (optional, IRIS_BATCH_NTILES entries) receives the time per E+H pass of
+ * candidate i (-1 for a candidate the precision does not offer).  Call
  * before the first step (the passes run on the zero initial state).
  */
+#define IRIS_BATCH_NTILES 8
 int iris_batch_tune(iris_batch* b, int reps, int* best, double* ms);
-/* Force a candidate tile (0..4: x*y*z blocks 32x8x1, 32x4x2, 64x4x1,
- * 16x16x1, 32x2x4; 5, 6: runs of 256 consecutive cells of one plane, with
- * registers capped for five resident blocks per SM (5) or not (6)). */
+/* Force a candidate work list (0..4: x*y*z blocks 32x8x1, 32x4x2, 64x4x1,
+ * 16x16x1, 32x2x4 of the split E and H passes; 5, 6: runs of 256
+ * consecutive cells of one plane, with registers capped for five resident
+ * blocks per SM (5) or not (6); 7, FP32 only: the fused E+H pass over
+ * 32x16 column tiles and z chunks, which first allocates every cell's
+ * second field buffers (the fields then alternate between the two sets;
+ * iris_batch_get_field always reads the current one)). */
 int iris_batch_set_tile(iris_batch* b, int tile);
 int iris_batch_timing(iris_batch* b, int enable);
 int iris_batch_timing_read(iris_batch* b, double* region_ms, double* kernel_ms, long* launches);
 /* info[0] cells, [1] total grid cells, [2] DFT points, [3] DFT block K,
  * [4] tile index, [5] work items per pass, [6] kernel launches per E or H
- * pass (info: 7 entries). */
+ * pass, or per fused pass (info: 7 entries). */
 int iris_batch_info(const iris_batch* b, long* info);
 
 /* ---- adjoint (gradient) form ------------------------------------------- */

@@ -254,7 +254,8 @@ class Engine:
 
 
 DFT_ALL, DFT_Z = 0, 1
-TILES = ((32, 8, 1), (32, 4, 2), (64, 4, 1), (16, 16, 1), (32, 2, 4), ("flat", 256), ("flat", 256, "uncapped"))
+TILES = ((32, 8, 1), (32, 4, 2), (64, 4, 1), (16, 16, 1), (32, 2, 4), ("flat", 256), ("flat", 256, "uncapped"),
+         ("fused", 32, 16))
 
 
 class Batch:

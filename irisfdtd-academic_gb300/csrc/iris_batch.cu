@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "iris_engine.h"
+#include "iris_fused.cuh"
 
 using namespace iris;
 
@@ -39,14 +40,20 @@ struct BSeg {
   Seg s;
   int cell, pad;
 };
+struct FItem {
+  int cell, bx, by, z0, z1, pad;  // column tile (bx, by) of cell, planes z0..z1
+};
 
 // Work-list shapes the autotuner chooses from: x * y * z blocks of cells,
-// and (FLAT) 256 consecutive cells of one plane in row-major order, which
-// keeps every lane busy whatever the cell's nx.
-// keeps every lane busy whatever the cell's nx (FLAT: register-capped for
-// five resident blocks per SM; FLAT + 1: uncapped).
-constexpr int NTILES = 7, FLAT = 5;
-constexpr int TILES[NTILES][3] = {{32, 8, 1}, {32, 4, 2}, {64, 4, 1}, {16, 16, 1}, {32, 2, 4}, {256, 1, 1}, {256, 1, 1}};
+// (FLAT) 256 consecutive cells of one plane in row-major order, which keeps
+// every lane busy whatever the cell's nx (FLAT: register-capped for five
+// resident blocks per SM; FLAT + 1: uncapped), and (FUSED, FP32 only) the
+// fused E+H pass over 32 x 16 column tiles and z chunks of every cell.
+constexpr int NTILES = 8, FLAT = 5, FUSED = 7;
+constexpr int TILES[NTILES][3] = {{32, 8, 1}, {32, 4, 2}, {64, 4, 1}, {16, 16, 1},
+                                  {32, 2, 4}, {256, 1, 1}, {256, 1, 1}, {FZ_X, FZ_Y, 1}};
+constexpr int FB_CHUNK = 64;  // planes per FUSED item outside the UPML slabs
+static_assert(NTILES == IRIS_BATCH_NTILES, "the ABI's candidate count");
 
 // Copies the cell's arguments into shared memory when the item's cell changes.
 template <typename A>
@@ -128,6 +135,33 @@ __global__ void __launch_bounds__(256, MINB) k_batch_flat(const FieldArgs<T>* __
   }
 }
 
+// The fused E+H pass over FUSED items: one tile column of one cell per
+// item, the cell's FusedArgs (for the current buffer parity) copied to
+// shared memory when the item's cell changes.  UPML as in k_fused: items
+// outside the slabs with the kernel compiled without slab code.
+template <bool CEPS, bool UPML>
+__global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_batch_fused(const FusedArgs* __restrict__ args,
+                                                             const FItem* __restrict__ items, long nitems) {
+  __shared__ FusedSmem S;
+  __shared__ __align__(16) FusedArgs sa;
+  __shared__ int scell;
+  extern __shared__ __align__(16) unsigned char fz_dyn[];
+  FusedUpml& U = *reinterpret_cast<FusedUpml*>(fz_dyn);  // UPML = true only
+  const int tid = threadIdx.y * FZ_X + threadIdx.x;
+  if (tid == 0) scell = -1;
+  for (long k = blockIdx.x; k < nitems; k += gridDim.x) {
+    const FItem it = items[k];
+    __syncthreads();  // the previous item's last reads of S and sa are done
+    if (it.cell != scell) {
+      const int* src = (const int*)(args + it.cell);
+      for (int i = tid; i < (int)(sizeof(FusedArgs) / 4); i += FZ_X * FZ_Y) ((int*)&sa)[i] = src[i];
+      __syncthreads();
+      if (tid == 0) scell = it.cell;
+    }
+    fused_column<CEPS, UPML>(sa, S, U, it.bx, it.by, it.z0, it.z1);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(64) k_batch_tfsf(const FieldArgs<T>* __restrict__ args,
                                                    const SrcArgs* __restrict__ srcs, const TItem* __restrict__ items,
@@ -166,7 +200,14 @@ struct iris_batch {
   iris_engine* master = nullptr;  // stream, timing and the shared DFT buffers
   std::vector<iris_engine*> cells;
   std::vector<long> pbase;
-  void* d_args = nullptr;  // FieldArgs<T>[n]
+  void* d_args = nullptr;  // FieldArgs<T>[2][n]: the cells' current fields at buffer parity 0, 1
+  // FUSED: the members' second field buffers exist; parity: which buffer set
+  // holds the current fields (0 = the members' first buffers); d_fargs:
+  // FusedArgs[2][n] (old fields at parity q, new ones in the other set)
+  bool second = false;
+  int parity = 0;
+  void* d_fargs = nullptr;
+  FItem* d_fitems = nullptr;
   SrcArgs* d_src = nullptr;
   BItem* d_items = nullptr;
   long nitems = 0;
@@ -183,24 +224,115 @@ struct iris_batch {
 
 namespace {
 
+// Swaps a member's field, second-field and D buffers.
+void swap_sets(iris_engine* E) {
+  std::swap(E->e, E->e2);
+  std::swap(E->h, E->h2);
+  for (int s = 0; s < 2; ++s) std::swap(E->pml_d[s], E->pml_d2[s]);
+}
+
+// The cells' kernel arguments for both buffer parities.  A member's own
+// pointers always name its current fields (parity B->parity).
 int batch_upload_args(iris_batch* B) {
   const size_t sz = B->prec == IRIS_FP64 ? sizeof(FieldArgs<double>) : sizeof(FieldArgs<float>);
-  std::vector<unsigned char> h(sz * B->n);
-  for (int c = 0; c < B->n; ++c) {
-    if (B->prec == IRIS_FP64) {
-      FieldArgs<double> a = field_args<double>(B->cells[c]);
-      std::memcpy(h.data() + sz * c, &a, sz);
-    } else {
-      FieldArgs<float> a = field_args<float>(B->cells[c]);
-      std::memcpy(h.data() + sz * c, &a, sz);
+  std::vector<unsigned char> h(2 * sz * B->n);
+  std::vector<FusedArgs> fa(B->second ? 2 * B->n : 0);
+  for (int q = 0; q < 2; ++q)
+    for (int c = 0; c < B->n; ++c) {
+      iris_engine* E = B->cells[c];
+      const bool other = q != B->parity && B->second;
+      if (other) swap_sets(E);  // view the set that is current at parity q
+      if (B->prec == IRIS_FP64) {
+        FieldArgs<double> a = field_args<double>(E);
+        std::memcpy(h.data() + sz * ((size_t)q * B->n + c), &a, sz);
+      } else {
+        FieldArgs<float> a = field_args<float>(E);
+        std::memcpy(h.data() + sz * ((size_t)q * B->n + c), &a, sz);
+        if (B->second) {
+          FusedArgs& f = fa[(size_t)q * B->n + c];
+          f = FusedArgs{};
+          f.f = a;
+          f.e_new = (float2*)E->e2;
+          f.h_new = (float2*)E->h2;
+          for (int s = 0; s < 2; ++s) f.d_new[s] = (float2*)E->pml_d2[s];
+        }
+      }
+      if (other) swap_sets(E);
     }
-  }
   if (!B->d_args) CK(cudaMalloc(&B->d_args, h.size()));
   CK(cudaMemcpy(B->d_args, h.data(), h.size(), cudaMemcpyHostToDevice));
+  if (B->second) {
+    if (!B->d_fargs) CK(cudaMalloc(&B->d_fargs, sizeof(FusedArgs) * fa.size()));
+    CK(cudaMemcpy(B->d_fargs, fa.data(), sizeof(FusedArgs) * fa.size(), cudaMemcpyHostToDevice));
+  }
+  return IRIS_OK;
+}
+
+// The members' second field buffers and D (zero), for the FUSED work list.
+int batch_second_buffers(iris_batch* B) {
+  if (B->second) return IRIS_OK;
+  for (iris_engine* E : B->cells) {
+    const size_t fbytes = (size_t)3 * E->g.comp * E->esz;
+    if (!E->e2) CK(cudaMalloc(&E->e2, fbytes));
+    if (!E->h2) CK(cudaMalloc(&E->h2, fbytes));
+    CK(cudaMemsetAsync(E->e2, 0, fbytes, B->master->st));
+    CK(cudaMemsetAsync(E->h2, 0, fbytes, B->master->st));
+    for (int s = 0; s < 2; ++s) {
+      const size_t b = (size_t)3 * E->pcomp[s] * E->esz;
+      if (!E->pml_d2[s]) CK(cudaMalloc(&E->pml_d2[s], std::max<size_t>(b, 16)));
+      CK(cudaMemsetAsync(E->pml_d2[s], 0, std::max<size_t>(b, 16), B->master->st));
+    }
+  }
+  B->second = true;
+  return batch_upload_args(B);
+}
+
+// FUSED items: every cell's planes outside its UPML slabs in chunks of
+// FB_CHUNK (stopping at pmlzf-2, as the single-engine launch does) first,
+// then its two slabs each with the plane next to it; within a chunk, tile
+// rows of the cell in order.
+int batch_build_fused_items(iris_batch* B) {
+  std::vector<FItem> in, slab;
+  for (int c = 0; c < B->n; ++c) {
+    const iris_params& p = B->cells[c]->p;
+    const int tx = (p.nx + FZ_OX - 1) / FZ_OX, ty = (p.ny + FZ_OY - 1) / FZ_OY;
+    auto add = [&](std::vector<FItem>& v, int za, int zb, int len) {
+      for (int z = za; z <= zb; z += len)
+        for (int by = 0; by < ty; ++by)
+          for (int bx = 0; bx < tx; ++bx) v.push_back(FItem{c, bx, by, z, std::min(z + len - 1, zb), 0});
+    };
+    const int ia = p.pmlzi + 1, ib = p.pmlzf - 2;
+    if (ib >= ia) {
+      add(in, ia, ib, FB_CHUNK);
+      add(slab, 1, ia - 1, p.nz);
+      add(slab, ib + 1, p.nz, p.nz);
+    } else {
+      add(slab, 1, p.nz, p.nz);
+    }
+  }
+  B->nitems_in = (long)in.size();
+  in.insert(in.end(), slab.begin(), slab.end());
+  for (const void* kf : {(const void*)k_batch_fused<false, true>, (const void*)k_batch_fused<true, true>})
+    CK(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FZ_UPML_SMEM));
+  graph_reset(B->master);
+  if (B->d_fitems) cudaFree(B->d_fitems);
+  B->d_fitems = nullptr;
+  CK(cudaMalloc(&B->d_fitems, sizeof(FItem) * std::max<size_t>(1, in.size())));
+  CK(cudaMemcpy(B->d_fitems, in.data(), sizeof(FItem) * in.size(), cudaMemcpyHostToDevice));
+  B->nitems = (long)in.size();
+  B->tile = FUSED;
+  B->master->fused = true;  // graphs of an even number of steps only (the buffer sets alternate)
   return IRIS_OK;
 }
 
 int batch_build_items(iris_batch* B, int tile) {
+  if (tile == FUSED) {
+    if (B->prec != IRIS_FP32) return fail(IRIS_EINVAL, "the fused work list is FP32 only");
+    int rc = batch_second_buffers(B);
+    if (rc) return rc;
+    return batch_build_fused_items(B);
+  }
+  B->master->fused = false;
   const int TX = TILES[tile][0], TY = TILES[tile][1], TZ = TILES[tile][2];
   std::vector<BItem> items;
   for (int c = 0; c < B->n; ++c) {
@@ -243,10 +375,15 @@ template <typename T, int TX, int TY, int TZ> int persistent_grid(const void* ke
   return std::max(1, nsm * std::max(1, per));
 }
 
+// The cells' FieldArgs<T> for the current buffer parity.
+template <typename T> const FieldArgs<T>* cur_args(const iris_batch* B) {
+  return (const FieldArgs<T>*)B->d_args + (size_t)B->parity * B->n;
+}
+
 template <typename T, int TX, int TY, int TZ> void launch_batch_eh(iris_batch* B, bool e) {
   iris_engine* M = B->master;
   const dim3 blk(TX, TY, TZ);
-  const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
+  const FieldArgs<T>* args = cur_args<T>(B);
   if (e) {
     static int grid = 0;
     if (!grid) grid = persistent_grid<T, TX, TY, TZ>((const void*)k_batch_e<T, TX, TY, TZ>);
@@ -266,7 +403,7 @@ template <typename T, int MINB, bool CEPS, bool UPML>
 void launch_flat_part(iris_batch* B, bool e, const BItem* items, long n) {
   if (n <= 0) return;
   iris_engine* M = B->master;
-  const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
+  const FieldArgs<T>* args = cur_args<T>(B);
   auto kern = e ? k_batch_flat<T, true, MINB, CEPS, UPML> : k_batch_flat<T, false, MINB, false, UPML>;
   static int grid_e = 0, grid_h = 0;
   int& grid = e ? grid_e : grid_h;
@@ -290,6 +427,37 @@ template <typename T, int MINB> void launch_batch_flat(iris_batch* B, bool e) {
   else launch_flat<T, MINB, false>(B, e);
 }
 
+// One fused E+H pass of every cell (FUSED work list, FP32): the items
+// outside the slabs, then the slab items; the buffer sets then swap.
+template <bool CEPS> void launch_batch_fused(iris_batch* B) {
+  iris_engine* M = B->master;
+  const FusedArgs* args = (const FusedArgs*)B->d_fargs + (size_t)B->parity * B->n;
+  for (int part = 0; part < 2; ++part) {
+    const long n = part == 0 ? B->nitems_in : B->nitems - B->nitems_in;
+    if (n <= 0) continue;
+    const FItem* items = B->d_fitems + (part == 0 ? 0 : B->nitems_in);
+    const void* kern = part == 0 ? (const void*)k_batch_fused<CEPS, false> : (const void*)k_batch_fused<CEPS, true>;
+    const size_t dyn = part == 0 ? 0 : FZ_UPML_SMEM;
+    static int per[2] = {0, 0};
+    if (!per[part]) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[part], kern, FZ_X * FZ_Y, dyn);
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, B->device);
+    const unsigned g = (unsigned)std::min<long>(n, (long)nsm * std::max(1, per[part]));
+    KTimer tm(M, IRIS_KC_FUSED);
+    if (part == 0) k_batch_fused<CEPS, false><<<g, dim3(FZ_X, FZ_Y), 0, M->st>>>(args, items, n);
+    else k_batch_fused<CEPS, true><<<g, dim3(FZ_X, FZ_Y), FZ_UPML_SMEM, M->st>>>(args, items, n);
+  }
+  B->parity ^= 1;
+  for (iris_engine* E : B->cells) swap_sets(E);
+}
+
+void batch_fused(iris_batch* B) {
+  bool cplx = false;
+  for (const iris_engine* E : B->cells) cplx |= E->eps_complex;
+  if (cplx) launch_batch_fused<true>(B);
+  else launch_batch_fused<false>(B);
+}
+
 template <typename T> void batch_eh(iris_batch* B, bool e) {
   switch (B->tile) {
     case FLAT: launch_batch_flat<T, 5>(B, e); break;
@@ -308,9 +476,13 @@ template <typename T> void batch_one_step(iris_batch* B, int it, const int* itp,
   iris_engine* M = B->master;
   const iris_params& p = M->p;
   using V = typename V2<T>::t;
-  const FieldArgs<T>* args = (const FieldArgs<T>*)B->d_args;
-  batch_eh<T>(B, true);
-  batch_eh<T>(B, false);
+  if (B->tile == FUSED) {
+    batch_fused(B);
+  } else {
+    batch_eh<T>(B, true);
+    batch_eh<T>(B, false);
+  }
+  const FieldArgs<T>* args = cur_args<T>(B);  // after the fused pass: the new set
   if (B->ntitems) {
     KTimer tm(M, IRIS_KC_TFSF);
     const long g = std::min<long>(B->ntitems, 152L * 16);
@@ -352,7 +524,7 @@ template <typename T> int batch_step_t(iris_batch* B, int it0, int n) {
 void batch_free(iris_batch* B) {
   for (iris_engine* E : B->cells)
     if (E) iris_destroy(E);
-  void* ptrs[] = {B->d_args, B->d_src, B->d_items, B->d_titems, B->d_bsegs};
+  void* ptrs[] = {B->d_args, B->d_src, B->d_items, B->d_titems, B->d_bsegs, B->d_fargs, B->d_fitems};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (B->master) {
@@ -514,19 +686,27 @@ int iris_batch_tune(iris_batch* B, int reps, int* best, double* ms) {
   CK(cudaEventCreate(&b));
   int arg = 0;
   double bestms = 1e30;
-  for (int t = 0; t < NTILES; ++t) {
+  // one E and one H pass, or one fused pass
+  auto pass = [&] {
+    if (B->tile == FUSED) batch_fused(B);
+    else if (B->prec == IRIS_FP64) {
+      batch_eh<double>(B, true);
+      batch_eh<double>(B, false);
+    } else {
+      batch_eh<float>(B, true);
+      batch_eh<float>(B, false);
+    }
+  };
+  const int ntry = B->prec == IRIS_FP32 ? NTILES : FUSED;  // FUSED is FP32 only
+  if (ms)
+    for (int t = ntry; t < NTILES; ++t) ms[t] = -1.0;
+  for (int t = 0; t < ntry; ++t) {
     int rc = batch_build_items(B, t);
     if (rc) return rc;
-    // fields are still zero, so E and H passes leave the state unchanged
-    for (int r = 0; r < 2; ++r) {
-      B->prec == IRIS_FP64 ? batch_eh<double>(B, true) : batch_eh<float>(B, true);
-      B->prec == IRIS_FP64 ? batch_eh<double>(B, false) : batch_eh<float>(B, false);
-    }
+    // fields are still zero (both buffer sets), so the passes leave the state unchanged
+    for (int r = 0; r < 2; ++r) pass();
     CK(cudaEventRecord(a, M->st));
-    for (int r = 0; r < reps; ++r) {
-      B->prec == IRIS_FP64 ? batch_eh<double>(B, true) : batch_eh<float>(B, true);
-      B->prec == IRIS_FP64 ? batch_eh<double>(B, false) : batch_eh<float>(B, false);
-    }
+    for (int r = 0; r < reps; ++r) pass();
     CK(cudaEventRecord(b, M->st));
     CK(cudaEventSynchronize(b));
     float x = 0;
@@ -540,6 +720,27 @@ int iris_batch_tune(iris_batch* B, int reps, int* best, double* ms) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (best) *best = arg;
+  if (arg != FUSED && B->second) {
+    // the second buffer sets are not needed; every set still holds the zero
+    // state, so the first one can be made current without a copy
+    CK(cudaStreamSynchronize(M->st));
+    if (B->parity) {
+      for (iris_engine* E : B->cells) swap_sets(E);
+      B->parity = 0;
+    }
+    for (iris_engine* E : B->cells) {
+      cudaFree(E->e2);
+      cudaFree(E->h2);
+      E->e2 = E->h2 = nullptr;
+      for (int s = 0; s < 2; ++s) {
+        cudaFree(E->pml_d2[s]);
+        E->pml_d2[s] = nullptr;
+      }
+    }
+    B->second = false;
+    int rc = batch_upload_args(B);
+    if (rc) return rc;
+  }
   return batch_build_items(B, arg);
 }
 
@@ -563,7 +764,7 @@ int iris_batch_info(const iris_batch* B, long* info) {
   info[3] = B->master->K;
   info[4] = B->tile;
   info[5] = B->nitems;
-  info[6] = B->tile >= FLAT ? (B->nitems_in > 0) + (B->nitems > B->nitems_in) : 1;
+  info[6] = B->tile >= FLAT ? (B->nitems_in > 0) + (B->nitems > B->nitems_in) : 1;  // per E, H or fused pass
   return IRIS_OK;
 }
 

@@ -34,6 +34,8 @@ template <> __device__ __forceinline__ float sub_<float>(float a, float b) { ret
 
 template <typename T> struct cx { T re, im; };
 
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
 template <typename T> __device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) { return {add_(a.re, b.re), add_(a.im, b.im)}; }
 template <typename T> __device__ __forceinline__ cx<T> csub(cx<T> a, cx<T> b) { return {sub_(a.re, b.re), sub_(a.im, b.im)}; }
 template <typename T> __device__ __forceinline__ cx<T> rmul(T r, cx<T> a) { return {mul_(r, a.re), mul_(r, a.im)}; }

@@ -17,7 +17,8 @@ INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(PKG, "libiris_fdtd.so")
 SOURCES = ["iris_engine.cu", "iris_batch.cu", "iris_adjoint.cu", "iris_host.cpp"]
 HEADERS = [os.path.join(INCLUDE, "iris_fdtd.h")] + [os.path.join(CSRC, h) for h in
-                                                   ("iris_internal.h", "iris_device.cuh", "iris_engine.h")]
+                                                   ("iris_internal.h", "iris_device.cuh", "iris_engine.h",
+                                                    "iris_fused.cuh")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

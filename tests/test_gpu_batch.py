@@ -5,7 +5,8 @@ The batch runs the same per-cell arithmetic as a single engine (the same
 device functions, one launch per operator over all cells), so FP64 cells
 agree with their single-engine runs to the last bit (asserted <= 1e-15) and
 with the oracle within 1e-12; FP32 fields within 1e-6 of FP32 single runs,
-FP32 spectra within 1e-5 (different DFT block boundaries).
+FP32 spectra within 1e-5 (different DFT block boundaries).  Work list 7 is
+the fused E+H pass (FP32 only; its fields alternate between two buffer sets).
 """
 import importlib
 import os
@@ -68,10 +69,18 @@ def batch_and_singles(iris, cells, precision, tune=False, tile=None):
     return b, singles
 
 
-@pytest.mark.parametrize("tile", [0, 3, 5, 6])
+@pytest.mark.parametrize("tile", [0, 3, 5, 6, 7])
 @pytest.mark.parametrize("precision,tol", [(0, 1e-15), (1, 1e-6)])
 def test_batch_matches_single_engines(iris, oracle, tmp_path, precision, tol, tile):
     cells = make_cells(oracle, tmp_path)
+    if tile == 7 and precision == 0:
+        # the fused work list is FP32 only
+        params = [engine_params_from_oracle(iris, op, precision=0, ak=ak) for _, op, ak, _ in cells]
+        b = iris.Batch(params, cells[0][1].fw, dft_faces=iris.DFT_Z)
+        with pytest.raises(iris.IrisError) as e:
+            b.set_tile(7)
+        assert e.value.code == -1
+        return
     b, singles = batch_and_singles(iris, cells, precision, tile=tile)
     assert b.info()["cells"] == len(CELLS)
     for c, (e, Js) in enumerate(singles):

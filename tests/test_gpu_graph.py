@@ -62,7 +62,8 @@ def test_graph_not_used_under_per_kernel_timing(iris, oracle, tmp_path):
     assert n["update_e"] == 32
 
 
-def test_batch_graph_identical(iris, oracle, tmp_path):
+@pytest.mark.parametrize("tile", [5, 7])
+def test_batch_graph_identical(iris, oracle, tmp_path, tile):
     from test_gpu_batch import make_cells
     cells = make_cells(oracle, tmp_path)
     params = [engine_params_from_oracle(iris, op, precision=1, ak=ak) for _, op, ak, _ in cells]
@@ -73,7 +74,7 @@ def test_batch_graph_identical(iris, oracle, tmp_path):
         b = iris.Batch(params, cells[0][1].fw, dft_faces=iris.DFT_Z, dft_block=16, graph=graph)
         for c, (_, _, _, eps) in enumerate(cells):
             b.set_material(c, eps)
-        b.set_tile(5)
+        b.set_tile(tile)
         for it0, n in CALLS:
             b.step(it0, n)
         bs.append(b)
