@@ -450,7 +450,7 @@ template <typename T> int adj_forward(iris_adjoint* J, int nsteps) {
       if (rc) return rc;
     }
     if (seg == S - 1) adj_record<T>(J, it - 1 - seg * J->K);
-    split_step(F, it, true);
+    one_step(F, it, true);
   }
   dft_flush(F);
   CK(cudaEventRecord(J->ev[1], F->st));
@@ -482,7 +482,7 @@ template <typename T> int adj_backward(iris_adjoint* J) {
       if (rc) return rc;
       for (int it = s0; it <= s1; ++it) {
         adj_record<T>(J, it - s0);
-        split_step(F, it, false);
+        one_step(F, it, false);
       }
       CK(cudaEventRecord(J->ev[1], F->st));
       CK(cudaEventSynchronize(J->ev[1]));
@@ -543,11 +543,13 @@ int iris_adjoint_create(const iris_params* pin, const double* fw, const int desi
     delete J;
     return code;
   };
+  // the forward engine steps as the parameters ask (FP32: the fused pass by
+  // default); the adjoint state is a member engine that only holds fields
   iris_params q = p;
-  q.stencil = IRIS_STENCIL_SPLIT;
   for (int i = 0; i < 6; ++i) q.box2[i] = q.box1[i];
   int rc = create_engine(&q, fw, false, true, &J->F);
   if (rc) return bail(rc);
+  q.stencil = IRIS_STENCIL_SPLIT;
   rc = create_engine(&q, fw, true, true, &J->A);
   if (rc) return bail(rc);
   iris_engine* F = J->F;

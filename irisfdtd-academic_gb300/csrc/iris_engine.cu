@@ -1434,10 +1434,12 @@ void free_engine(iris_engine* E) {
 }
 
 
-void split_step(iris_engine* E, int it, bool dft) {
+void one_step(iris_engine* E, int it, bool dft) {
   const iris_params& p = E->p;
   const bool sampled = dft && it >= p.to_fourier && it % p.sample_fourier == 0;
-  if (E->prec == IRIS_FP64) {
+  if (E->fused) {
+    fused_one(E, it, nullptr, sampled);
+  } else if (E->prec == IRIS_FP64) {
     launch_e<double>(E);
     launch_h<double>(E);
     launch_tfsf<double>(E, it);
@@ -1536,10 +1538,8 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
   E->src = make_src(p);
   E->tf_blk = dim3(64);
   E->tf_grd = dim3((p.nx + 2 + 63) / 64, (p.ny + 2 + TFSF_YCH - 1) / TFSF_YCH);
-  // fused E+H pass: FP32 only
-  // fused on request only: it moves fewer bytes but issues ~1.6x the
-  // instructions of the split passes and measures slower on GB300 for now
-  // FP32 steps with the fused pass unless the split or streamed passes are asked for
+  // FP32 steps with the fused E+H pass unless the split or streamed passes
+  // are asked for (FP64 always steps with the split passes)
   E->fused = E->prec == IRIS_FP32 && (p.stencil == IRIS_STENCIL_FUSED || p.stencil == IRIS_STENCIL_DEFAULT);
   if (E->fused) {
     if (cudaMalloc(&E->e2, fbytes) != cudaSuccess || cudaMalloc(&E->h2, fbytes) != cudaSuccess)

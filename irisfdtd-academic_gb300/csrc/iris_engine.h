@@ -171,9 +171,10 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces);
 void dft_flush(iris_engine* E);
 // Flux of face set `set` (6 FluxFace from d_faces + 6 set) into J[6][nof].
 int read_flux(iris_engine* E, int set, double* J);
-// One split-pass step (E, H, TF/SF), with the DFT sample of step it when
-// dft is set and the step is sampled.
-void split_step(iris_engine* E, int it, bool dft);
+// One step (the fused pass or the split E and H passes, as the engine
+// steps, then TF/SF), with the DFT sample of step it when dft is set and the
+// step is sampled.
+void one_step(iris_engine* E, int it, bool dft);
 
 // CUDA graph of one DFT block of steps.
 bool graph_ready(const iris_engine* E, int it, int left);

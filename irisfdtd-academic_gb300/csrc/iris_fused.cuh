@@ -62,7 +62,11 @@ struct FusedArgs {
 struct FusedUpml {
   cx<float> d[2][FZ_Y][FZ_X][3];
   cx<float> b[2][FZ_Y][FZ_X][3];
-  float cf[2][2][NCOEF];  // [parity][E row of the plane, H row of the plane below]
+  // [plane mod 3][E row of the plane, H row of the plane below]: read by
+  // every thread, so three slots: the refill for plane z+1, issued before
+  // plane z's barrier, must not land in the slot that slower warps may
+  // still be reading for plane z-1
+  float cf[3][2][NCOEF];
 };
 constexpr size_t FZ_UPML_SMEM = sizeof(FusedUpml);
 
@@ -158,7 +162,7 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
         if (w < 2 && lane < NCOEF && (w == 0 ? pe : pb)) {
           const int zz = w == 0 ? zp : zb;
           const int row = zz <= a.pmlzi ? zz - 1 : a.pmlzi + zz - a.pmlzf;
-          cpa4(&U.cf[p & 1][w][lane], a.coef + NCOEF * row + lane);
+          cpa4(&U.cf[p % 3][w][lane], a.coef + NCOEF * row + lane);
         }
       }
     }
@@ -254,7 +258,7 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
       for (int k = 0; k < 3; ++k) enew[k] = e[k];
       e_apply<float, CEPS, 7, !CEPS, UPML>(a, (own && z <= z1) ? A.d_new : nullptr, cxx, cyy, cz, c, enew,
                                            CEPS ? 0.f : epsh[z & 1][w][lane], UPML ? U.d[z & 1][w][lane] : nullptr,
-                                           UPML ? U.cf[z & 1][0] : nullptr);
+                                           UPML ? U.cf[z % 3][0] : nullptr);
       if (ximg || yimg) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) enew[k] = cmul(ph, enew[k]);
@@ -276,7 +280,7 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
 #pragma unroll
         for (int k = 0; k < 3; ++k) hn[k] = hp[k];
         h_update<float, UPML>(a, x, y, z - 1, ep, xp, yp, zp, hn, UPML ? U.b[z & 1][w][lane] : nullptr,
-                              UPML ? U.cf[z & 1][1] : nullptr);
+                              UPML ? U.cf[z % 3][1] : nullptr);
         const long i = g.at(x, y, z - 1);
 #pragma unroll
         for (int k = 0; k < 3; ++k) st<float>(A.h_new + k * g.comp + i, hn[k]);
