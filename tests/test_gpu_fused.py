@@ -100,6 +100,19 @@ def test_fused_two_boxes(iris, oracle, tmp_path):
         assert np.array_equal(ef.get_fdata(1, j), es.get_fdata(1, j))
 
 
+@pytest.mark.parametrize("pmlzf", [8, 9])
+def test_fused_without_interior_range(iris, oracle, tmp_path, pmlzf):
+    """pmlzf <= pmlzi + 2 leaves no planes for the launch without UPML code:
+    every plane goes through the slab launch, still bitwise the split passes."""
+    w, op = make_case(oracle, tmp_path, (16, 8, 20, 6, pmlzf, 7, 1, 4.0, 7, (1, 16, 1, 8, 3, 17)), 2)
+    op.texit = 60
+    es, Js = run(iris, op, 1, (0.2 + 0j, 0j, 0j), None)
+    ef, Jf = run(iris, op, 2, (0.2 + 0j, 0j, 0j), None)
+    for which in (iris.E, iris.H):
+        assert np.array_equal(interior(ef.get_field(which), op), interior(es.get_field(which), op)), which
+    assert np.array_equal(Jf, Js)
+
+
 def test_fused_rejected_in_fp64(iris, oracle, tmp_path):
     w, op = make_case(oracle, tmp_path, (8, 6, 40, 6, 35, 15, 10, 4.0, 10, (1, 8, 1, 6, 8, 32)), 2)
     with pytest.raises(iris.IrisError) as e:
