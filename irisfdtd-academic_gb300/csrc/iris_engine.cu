@@ -5,12 +5,13 @@
 // Data layout in HBM
 //   * E and H: three component arrays each, complex (double2 in FP64 mode,
 //     float2 in FP32 mode), x fastest, ghost planes 0 and n+1 on every axis,
-//     rows padded so that x = 1 starts on a 128-byte boundary.  Updated in
-//     place: the leapfrog update of a cell reads only its own old value, so
-//     the reference's cur/prev pointer swap (code/driver.f90:358-384) needs no
-//     second copy.
-//   * UPML auxiliaries D and B exist for the two z slabs only, also updated
-//     in place.
+//     rows padded so that x = 1 starts on a 128-byte boundary.  The split
+//     passes update them in place: the leapfrog update of a cell reads only
+//     its own old value, so the reference's cur/prev pointer swap
+//     (code/driver.f90:358-384) needs no second copy.  The fused pass (the
+//     FP32 default) writes a second set and the two swap every step.
+//   * UPML auxiliaries D and B exist for the two z slabs only, updated in
+//     place (D double-buffered under the fused pass).
 //   * Structure inverse permittivity over z in [hi, hf] (real when the
 //     material is lossless, complex otherwise).
 //   * DFT: a ring of K sample slots [K][P] gathered from the box faces after
@@ -18,7 +19,8 @@
 //     one block of samples at a time.
 //
 // The batched form lives in iris_batch.cu, the adjoint form in
-// iris_adjoint.cu; the per-cell operators they share are in iris_device.cuh.
+// iris_adjoint.cu; the per-cell operators they share are in iris_device.cuh,
+// the fused pass's tile column in iris_fused.cuh.
 
 #include <cuda_runtime.h>
 
