@@ -268,6 +268,29 @@ int batch_upload_args(iris_batch* B) {
   return IRIS_OK;
 }
 
+// Frees the members' second buffer sets (tuning only: every set holds the
+// zero state then, so the first one can be made current without a copy).
+int batch_drop_second(iris_batch* B) {
+  CK(cudaStreamSynchronize(B->master->st));
+  if (B->parity) {
+    for (iris_engine* E : B->cells) swap_sets(E);
+    B->parity = 0;
+  }
+  bool any = B->second;
+  for (iris_engine* E : B->cells) {
+    void* ptrs[] = {E->e2, E->h2, E->pml_d2[0], E->pml_d2[1]};
+    for (void* q : ptrs)
+      if (q) {
+        cudaFree(q);
+        any = true;
+      }
+    E->e2 = E->h2 = nullptr;
+    E->pml_d2[0] = E->pml_d2[1] = nullptr;
+  }
+  B->second = false;
+  return any ? batch_upload_args(B) : IRIS_OK;
+}
+
 // The members' second field buffers and D (zero), for the FUSED work list.
 int batch_second_buffers(iris_batch* B) {
   if (B->second) return IRIS_OK;
@@ -702,6 +725,15 @@ int iris_batch_tune(iris_batch* B, int reps, int* best, double* ms) {
     for (int t = ntry; t < NTILES; ++t) ms[t] = -1.0;
   for (int t = 0; t < ntry; ++t) {
     int rc = batch_build_items(B, t);
+    if (rc == IRIS_ENOMEM && t == FUSED) {
+      // no room for the second buffer sets: not a candidate on this batch
+      cudaGetLastError();
+      clear_error();
+      rc = batch_drop_second(B);
+      if (rc) return rc;
+      if (ms) ms[t] = -1.0;
+      continue;
+    }
     if (rc) return rc;
     // fields are still zero (both buffer sets), so the passes leave the state unchanged
     for (int r = 0; r < 2; ++r) pass();
@@ -720,25 +752,8 @@ int iris_batch_tune(iris_batch* B, int reps, int* best, double* ms) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (best) *best = arg;
-  if (arg != FUSED && B->second) {
-    // the second buffer sets are not needed; every set still holds the zero
-    // state, so the first one can be made current without a copy
-    CK(cudaStreamSynchronize(M->st));
-    if (B->parity) {
-      for (iris_engine* E : B->cells) swap_sets(E);
-      B->parity = 0;
-    }
-    for (iris_engine* E : B->cells) {
-      cudaFree(E->e2);
-      cudaFree(E->h2);
-      E->e2 = E->h2 = nullptr;
-      for (int s = 0; s < 2; ++s) {
-        cudaFree(E->pml_d2[s]);
-        E->pml_d2[s] = nullptr;
-      }
-    }
-    B->second = false;
-    int rc = batch_upload_args(B);
+  if (arg != FUSED) {
+    int rc = batch_drop_second(B);
     if (rc) return rc;
   }
   return batch_build_items(B, arg);

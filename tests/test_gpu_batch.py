@@ -115,3 +115,17 @@ def test_batch_rejects_mixed_timesteps(iris, oracle, tmp_path):
     with pytest.raises(iris.IrisError) as e:
         iris.Batch(params, cells[0][1].fw)
     assert e.value.code == -1
+
+
+def test_batch_tune_fp32_matches_single_engines(iris, oracle, tmp_path):
+    """FP32 tuning times every work list, the fused one included (its second
+    buffer sets are dropped again when another list wins), and stepping after
+    it still matches the single engines bit for bit."""
+    cells = make_cells(oracle, tmp_path)
+    b, singles = batch_and_singles(iris, cells, 1, tune=True)
+    assert b.info()["tile"] in iris.TILES
+    for c, (e, _) in enumerate(singles):
+        for which in (iris.E, iris.H):
+            fb = interior(b.get_field(c, which), cells[c][1])
+            fs = interior(e.get_field(which), cells[c][1])
+            assert np.array_equal(fb, fs), (c, which)
