@@ -353,7 +353,10 @@ int iris_batch_info(const iris_batch* b, long* info);
  * transposed DFT as its source, accumulated against the forward curl of H
  * over the design cells.  Forward states are checkpointed every
  * checkpoint_every steps and each segment is recomputed from its checkpoint
- * during the backward sweep.
+ * during the backward sweep; the last segment's curls are recorded during the
+ * forward solve itself, so checkpoint_every >= nsteps (one segment, curls of
+ * every step kept: nsteps x 3 x design cells complex values) needs no
+ * recompute.
  *
  * design: {x0, x1, y0, y1, z0, z1}, 1-based and inclusive, inside
  * [1,nx] x [1,ny] x [hi,hf].  weights: [2][nof] (w5 then w6), or NULL for
