@@ -63,3 +63,51 @@ def test_invalid_parameters_rejected(iris):
     with pytest.raises(iris.IrisError) as e:
         iris.Engine(q, fw)
     assert e.value.code == -1
+
+
+C_CLIENT = r"""
+#include <stdio.h>
+#include <string.h>
+#include "iris_fdtd.h"
+
+int main(int argc, char** argv) {
+  iris_params p;
+  double fw[1024];
+  char desc[256];
+  int rc = iris_setparam(argv[1], 1, &p, fw, 1024, desc, sizeof desc);
+  if (rc != IRIS_OK) { printf("setparam %d %s\n", rc, iris_last_error()); return 1; }
+  printf("grid %d %d %d nof %d texit %d\n", p.nx, p.ny, p.nz, p.nof, p.texit);
+  iris_engine* e = NULL;
+  rc = iris_create(&p, fw, &e);
+  printf("create %d %s\n", rc, rc == IRIS_OK ? "ok" : iris_strerror(rc));
+  if (rc == IRIS_OK) iris_destroy(e);
+  return 0;
+}
+"""
+
+
+def test_c_client_links_and_fails_loudly_without_gpu(iris, tmp_path):
+    """The header is plain C99: a C host (as a Fortran iso_c_binding host
+    would) compiles against it, links the library, parses a reference deck,
+    and gets a status code, not a crash or a CPU fallback, when no GPU is
+    there (IRIS_OK when one is)."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    lib = iris.build()
+    src = tmp_path / "client.c"
+    src.write_text(C_CLIENT)
+    exe = tmp_path / "client"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe), lib, "-Wl,-rpath," + os.path.dirname(lib)], check=True)
+    out = subprocess.run([str(exe), golden("example_1.inputFDTD.dat")], capture_output=True, text=True, check=True)
+    lines = out.stdout.splitlines()
+    assert lines[0] == "grid 1 1 400 nof 500 texit 25962", lines
+    code = int(lines[1].split()[1])
+    try:
+        import torch
+        gpu = torch.cuda.is_available()
+    except ImportError:
+        gpu = False
+    assert code == 0 if gpu else code in (-8, -3), lines
