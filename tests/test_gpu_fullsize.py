@@ -7,9 +7,11 @@ pi/dx), where the FP64 oracle cannot follow:
   doubles every field value and quadruples the flux.  In FP64 this holds bit
   for bit (scaling by 2 is exact in binary floating point; checked on the
   cell resized to 160 planes, where FP64 steps are quick).  In FP32 it holds
-  to a few ulps (normwise 1e-5 of the field's scale asserted, ~3e-8 seen):
-  the Gaussian pulse rises at the source through the FP32 subnormal range,
-  whose fixed absolute quantum does not scale with the amplitude;
+  to a few ulps (normwise 1e-5 of the field's scale asserted): the FP32
+  stencil alone is exactly homogeneous, but the Gaussian pulse rises at the
+  source through the FP32 subnormal range, whose fixed absolute quantum does
+  not scale with the amplitude; once the two runs differ anywhere, their
+  later roundings differ too, and the difference settles at FP32 rounding;
 * the fluxes are finite, and the x/y faces carry the flux scattered sideways
   by the spheres.
 """
