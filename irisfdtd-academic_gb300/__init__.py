@@ -314,7 +314,10 @@ class Batch:
         return (re + 1j * im).reshape(shape)
 
     def tune(self, reps: int = 3):
-        """Autotune the E/H tile shape on this batch (before the first step)."""
+        """Time every work list (split-pass tiles, flat runs and, in FP32, the
+        fused pass) on this batch and keep the fastest; call before the first
+        step.  Returns (the chosen entry of TILES, {entry: ms per E+H pass},
+        -1 for a list the precision or memory does not allow)."""
         best = ctypes.c_int(0)
         ms = np.zeros(len(TILES))
         check(self.L.iris_batch_tune(self.h, reps, ctypes.byref(best), _dp(ms)), "iris_batch_tune")
