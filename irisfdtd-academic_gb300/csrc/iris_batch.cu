@@ -138,7 +138,9 @@ __global__ void __launch_bounds__(256, MINB) k_batch_flat(const FieldArgs<T>* __
 // The fused E+H pass over FUSED items: one tile column of one cell per
 // item, the cell's FusedArgs (for the current buffer parity) copied to
 // shared memory when the item's cell changes.  UPML as in k_fused: items
-// outside the slabs with the kernel compiled without slab code.
+// outside the slabs with the kernel compiled without slab code.  CEPS: the
+// batch holds a complex material somewhere; each item still picks the
+// column for its own cell's material (a real one has no complex table).
 template <bool CEPS, bool UPML>
 __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_batch_fused(const FusedArgs* __restrict__ args,
                                                              const FItem* __restrict__ items, long nitems) {
@@ -158,7 +160,10 @@ __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_batch_fused(const FusedArgs* 
       __syncthreads();
       if (tid == 0) scell = it.cell;
     }
-    fused_column<CEPS, UPML>(sa, S, U, it.bx, it.by, it.z0, it.z1);
+    // CEPS: some cell of the batch has a complex material; cells with a real
+    // one (eps_c null) still take the real-material column
+    if (CEPS && sa.f.eps_c) fused_column<true, UPML>(sa, S, U, it.bx, it.by, it.z0, it.z1);
+    else fused_column<false, UPML>(sa, S, U, it.bx, it.by, it.z0, it.z1);
   }
 }
 

@@ -129,3 +129,20 @@ def test_batch_tune_fp32_matches_single_engines(iris, oracle, tmp_path):
             fb = interior(b.get_field(c, which), cells[c][1])
             fs = interior(e.get_field(which), cells[c][1])
             assert np.array_equal(fb, fs), (c, which)
+
+
+def test_batch_fused_complex_material(iris, oracle, tmp_path):
+    """The fused work list with a lossy (complex) material in one cell runs
+    the complex-material kernel for the whole batch, still bitwise the single
+    engines."""
+    cells = make_cells(oracle, tmp_path)[:3]
+    r = np.random.default_rng(9)
+    w, op, ak, eps = cells[1]
+    eps = eps.astype(complex) + 1j * r.uniform(-0.05, 0.0, eps.shape)
+    cells[1] = (w, op, ak, eps)
+    b, singles = batch_and_singles(iris, cells, 1, tile=7)
+    for c, (e, _) in enumerate(singles):
+        for which in (iris.E, iris.H):
+            fb = interior(b.get_field(c, which), cells[c][1])
+            fs = interior(e.get_field(which), cells[c][1])
+            assert np.array_equal(fb, fs), (c, which)
