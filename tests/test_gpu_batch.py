@@ -146,3 +146,19 @@ def test_batch_fused_complex_material(iris, oracle, tmp_path):
             fb = interior(b.get_field(c, which), cells[c][1])
             fs = interior(e.get_field(which), cells[c][1])
             assert np.array_equal(fb, fs), (c, which)
+
+
+def test_batch_fused_cell_without_interior_range(iris, oracle, tmp_path):
+    """A cell whose UPML slabs leave no planes for the launch without slab
+    code (pmlzf = pmlzi + 2) rides in the slab launch of the fused list."""
+    cells = make_cells(oracle, tmp_path)[:2]
+    w = cfg.Workload("thin", 10, 6, 20, 6, 8, 7, 1, 4.0, 0, 7, (1, 10, 1, 6, 3, 17), 9, STEPS,
+                     structure="pattern", extra=dict(seed=77, fill=0.5))
+    op = oracle.setparam(cfg.write_input(str(tmp_path / "thin.dat"), w, no_downloads=3))
+    cells.append((w, op, (0.2 + 0j, 0j, 0j), cfg.binary_pattern_material(w)))
+    b, singles = batch_and_singles(iris, cells, 1, tile=7)
+    for c, (e, _) in enumerate(singles):
+        for which in (iris.E, iris.H):
+            fb = interior(b.get_field(c, which), cells[c][1])
+            fs = interior(e.get_field(which), cells[c][1])
+            assert np.array_equal(fb, fs), (c, which)

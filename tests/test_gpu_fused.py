@@ -113,6 +113,17 @@ def test_fused_without_interior_range(iris, oracle, tmp_path, pmlzf):
     assert np.array_equal(Jf, Js)
 
 
+def test_fused_without_structure_layer(iris, oracle, tmp_path):
+    """A deck whose structure layer is empty (hf < hi: no eps table at all)."""
+    w, op = make_case(oracle, tmp_path, (24, 10, 48, 6, 43, 20, 0, 4.0, 10, (1, 24, 1, 10, 8, 40)), 2)
+    op.texit = 80
+    es, Js = run(iris, op, 1, (0.3 + 0j, 0j, 0j), None)
+    ef, Jf = run(iris, op, 2, (0.3 + 0j, 0j, 0j), None)
+    for which in (iris.E, iris.H):
+        assert np.array_equal(interior(ef.get_field(which), op), interior(es.get_field(which), op)), which
+    assert np.array_equal(Jf, Js)
+
+
 def test_fused_rejected_in_fp64(iris, oracle, tmp_path):
     w, op = make_case(oracle, tmp_path, (8, 6, 40, 6, 35, 15, 10, 4.0, 10, (1, 8, 1, 6, 8, 32)), 2)
     with pytest.raises(iris.IrisError) as e:
