@@ -42,6 +42,7 @@ OP_E, OP_H, OP_TFSF, OP_DFT, OP_WAIT_CHECK = 1, 2, 3, 4, 5
 __all__ = [
     "FP64", "FP32", "E", "H", "IrisError", "IrisParams", "Engine", "build", "lib", "setparam",
     "set_emconstants", "run_input", "tr_normalise", "wavelength_axis", "frequencies", "physconsts",
+    "write_scatt", "read_scatt",
 ]
 
 
@@ -363,6 +364,16 @@ def tr_normalise(j5: np.ndarray, j6: np.ndarray):
 def wavelength_axis(lno: float, dlamda: float, nof: int) -> np.ndarray:
     """The plotting axis of IrisFDTD_scattering.py:111,143."""
     return np.linspace(lno, lno + dlamda * nof, nof)
+
+
+def write_scatt(directory: str, box: int, it: int, J: np.ndarray):
+    """Append one output block (step it, J[6, nof] as returned by Engine.flux)
+    to <box+1>_scatt1..6.dat and <box+1>_scatt.dat in directory, in the
+    records scattering_fourier_out writes (code/dataprocess.f90:279-299)."""
+    J = np.ascontiguousarray(J, dtype=np.float64)
+    if J.ndim != 2 or J.shape[0] != 6:
+        raise ValueError("J must be [6, nof]")
+    check(lib().iris_write_scatt(os.fsencode(directory), box, it, J.shape[1], _dp(J)), "iris_write_scatt")
 
 
 def read_scatt(path: str, nof: int) -> np.ndarray:
