@@ -615,7 +615,7 @@ def cpu_sample(w, side, threads, steps, warm=1):
     return tr / (ws.cells * steps), td / (npts * op.nof * steps), ws
 
 
-def cpu_baseline(w, full_points, steps=12, side=24):
+def cpu_baseline(w, full_points, steps=192, side=32):
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     t_cell, t_pf, ws = cpu_sample(w, side, threads, steps)
@@ -684,7 +684,7 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-steps", type=int, default=12)
+    ap.add_argument("--cpu-sample-steps", type=int, default=192)
     ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="run the workload resized to this grid (profiling cases)")
     ap.add_argument("--nof", type=int, default=None, help="number of DFT frequencies with --grid")
