@@ -115,7 +115,10 @@ typedef struct iris_params {
   int system_model;   /* never assigned by the reference: 0                */
   /* engine options (not part of the reference) */
   int precision;      /* IRIS_FP64 or IRIS_FP32                            */
-  int dft_block;      /* samples buffered per DFT accumulation; 0: default */
+  int dft_block;      /* samples buffered per DFT accumulation; 0: default
+                       * (FP32 512, FP64 32; at most 512 / 256, halved
+                       * while the ring would exceed half the memory left
+                       * after the accumulators)                          */
   int device;         /* CUDA device ordinal                               */
   int stencil;        /* IRIS_STENCIL_*: how E and H are stepped           */
   int dft_faces;      /* IRIS_DFT_ALL or IRIS_DFT_Z                        */

@@ -1102,20 +1102,34 @@ void fused_chunks(std::vector<int>& r, int za, int zb, long tiles) {
 // it, or *itp + it when itp is given.
 void fused_one(iris_engine* E, int it, const int* itp, bool sampled) {
   {
-    // the planes outside the UPML slabs with a kernel without slab code, then the slabs
+    // the planes outside the UPML slabs with a kernel without slab code and,
+    // concurrently on the second stream, the slabs: the two launches write
+    // disjoint planes and read only the old state, so the slab launch fills
+    // the SMs the interior launch's last wave leaves idle.  One timer spans
+    // the pass.
+    const bool both = !E->fzr[0].empty() && !E->fzr[1].empty();
+    KTimer tm(E, IRIS_KC_FUSED);
+    if (both) {
+      cudaEventRecord(E->fz_fork, E->st);
+      cudaStreamWaitEvent(E->st2, E->fz_fork, 0);
+    }
     for (int part = 0; part < 2; ++part) {
       const std::vector<int>& r = E->fzr[part];
       if (r.empty()) continue;
-      KTimer tm(E, IRIS_KC_FUSED);
       const FusedArgs a = fused_args(E, part);
       const dim3 grd(E->fgrd.x, E->fgrd.y, (unsigned)(r[3] + (r.size() > 4 ? r[7] : 0)));
       if (part == 0) {
         if (E->eps_complex) k_fused<true, false><<<grd, E->fblk, 0, E->st>>>(a);
         else k_fused<false, false><<<grd, E->fblk, 0, E->st>>>(a);
       } else {
-        if (E->eps_complex) k_fused<true, true><<<grd, E->fblk, FZ_UPML_SMEM, E->st>>>(a);
-        else k_fused<false, true><<<grd, E->fblk, FZ_UPML_SMEM, E->st>>>(a);
+        cudaStream_t s = both ? E->st2 : E->st;
+        if (E->eps_complex) k_fused<true, true><<<grd, E->fblk, FZ_UPML_SMEM, s>>>(a);
+        else k_fused<false, true><<<grd, E->fblk, FZ_UPML_SMEM, s>>>(a);
       }
+    }
+    if (both) {
+      cudaEventRecord(E->fz_join, E->st2);
+      cudaStreamWaitEvent(E->st, E->fz_join, 0);
     }
   }
   std::swap(E->e, E->e2);
@@ -1384,11 +1398,15 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
   CK(cudaMemGetInfo(&freeb, &totb));
   const size_t fd_bytes = (size_t)P * p.nof * sizeof(double2);
   if (fd_bytes > freeb) return fail(IRIS_ENOMEM, "DFT accumulators exceed free device memory");
-  // at most 256 slots (the FP64 block kernel stages K x 8 twiddles in 32 KB of
-  // shared memory); FP32 defaults to 256 so the FP64 epilogue is amortised
-  int K = std::min(256, p.dft_block > 0 ? p.dft_block : (E->prec == IRIS_FP64 ? 32 : 256));
+  // FP64: at most 256 slots (its block kernel stages K x 8 twiddles in 32 KB
+  // of shared memory), 32 by default.  FP32: up to 512, the default: a block
+  // reads and writes the FP64 accumulators once, so a longer block moves
+  // fewer accumulator bytes per sample.  The ring takes at most half of the
+  // memory left after the accumulators.
+  const int kmax = E->prec == IRIS_FP64 ? 256 : 512;
+  int K = std::min(kmax, p.dft_block > 0 ? p.dft_block : (E->prec == IRIS_FP64 ? 32 : 512));
   const size_t slot_bytes = std::max<size_t>(1, (size_t)P * E->esz);
-  const size_t budget = (freeb - fd_bytes) / 4;
+  const size_t budget = (freeb - fd_bytes) / 2;
   while (K > 1 && (size_t)K * slot_bytes > budget) K /= 2;
   E->K = std::max(1, K);
   E->nslot = 0;
@@ -1432,6 +1450,9 @@ void free_engine(iris_engine* E) {
     }
   if (E->t0) cudaEventDestroy(E->t0);
   if (E->t1) cudaEventDestroy(E->t1);
+  if (E->fz_fork) cudaEventDestroy(E->fz_fork);
+  if (E->fz_join) cudaEventDestroy(E->fz_join);
+  if (E->st2) cudaStreamDestroy(E->st2);
   if (E->st) cudaStreamDestroy(E->st);
 }
 
@@ -1567,6 +1588,10 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
       fused_chunks(E->fzr[1], 1, p.nz, tiles);
     }
     E->fblk = dim3(FZ_X, FZ_Y, 1);
+    if (cudaStreamCreateWithFlags(&E->st2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->fz_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->fz_join, cudaEventDisableTiming) != cudaSuccess)
+      return bail(fail(IRIS_ECUDA, "fused pass: stream creation failed"));
     for (const void* kf : {(const void*)k_fused<false, true>, (const void*)k_fused<true, true>})
       if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FZ_UPML_SMEM) != cudaSuccess)
         return bail(fail(IRIS_ECUDA, "fused pass: shared memory configuration failed"));

@@ -88,6 +88,10 @@ struct iris_engine {
   // the UPML slabs, [1] the slabs
   std::vector<int> fzr[2];
   dim3 fblk, fgrd;
+  // the slab launch runs on st2, concurrently with the interior launch (they
+  // write disjoint planes and read only the old state): fork / join events
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t fz_fork = nullptr, fz_join = nullptr;
   // CUDA graph of one DFT block of steps (iris_params.graph): d_it holds the
   // step base the captured kernels add to their offsets, dev_it its value
   cudaGraphExec_t gexec = nullptr;
@@ -106,7 +110,8 @@ struct iris_engine {
 
 namespace iris {
 
-// Brackets one kernel launch with a pair of events when timing is on.
+// Brackets one kernel launch (or the fused pass's two concurrent launches)
+// with a pair of events when timing is on.
 struct KTimer {
   iris_engine* E;
   int k;

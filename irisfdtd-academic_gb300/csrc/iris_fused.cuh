@@ -40,7 +40,8 @@ namespace iris {
 // the old state of its planes and the plane below and above it): the planes
 // pmlzi+1 .. pmlzf-2 by the kernel compiled without UPML code (UPML =
 // false), and the two slabs, each with the one plane next to it, by the
-// kernel with it.  The interior range stops at pmlzf-2 because a chunk also
+// kernel with it, the two on separate streams so that they run
+// concurrently (they write disjoint planes).  The interior range stops at pmlzf-2 because a chunk also
 // computes E' one plane past its end (its last H' needs it), and that plane
 // must not lie in a slab.
 

@@ -133,8 +133,8 @@ def test_fused_rejected_in_fp64(iris, oracle, tmp_path):
 
 def test_stencil_selection(iris, oracle, tmp_path):
     """The per-kernel timers show which pass ran: fused by default in FP32
-    (two launches a step: the planes outside the UPML slabs, then the slabs),
-    split on request."""
+    (one timer a step over its two concurrent launches: the planes outside
+    the UPML slabs and the slabs), split on request."""
     w, op = make_case(oracle, tmp_path, (16, 8, 40, 6, 35, 15, 10, 4.0, 10, (1, 16, 1, 8, 8, 32)), 2)
     for stencil, fused in ((0, True), (1, False), (2, True)):
         eng = iris.Engine(engine_params_from_oracle(iris, op, precision=1), op.fw, stencil=stencil)
@@ -142,7 +142,7 @@ def test_stencil_selection(iris, oracle, tmp_path):
         eng.step(1, 5)
         _, ms, n = eng.timing_read()
         if fused:
-            assert n["fused_eh"] == 10 and n["update_e"] == 0 and n["update_h"] == 0
+            assert n["fused_eh"] == 5 and n["update_e"] == 0 and n["update_h"] == 0
         else:
             assert n["fused_eh"] == 0 and n["update_e"] == 5 and n["update_h"] == 5
         eng.close()
