@@ -1,0 +1,86 @@
+"""Size-independent properties of the CPU oracle itself, on the CPU.
+
+The reference can be pinned to the numbers it states (test_oracle_pins.py);
+these check the oracle's wrap and source handling where no reference number
+exists:
+
+* Bloch wrap with ak = 0 (code/boundary.f90:163-348): a cell repeated twice
+  along x or y (material tiled, DFT box over the whole supercell) holds, in
+  each copy, the small cell's fields; the flux through the faces normal to
+  the repeat axis is the small cell's, through the other faces twice it.
+  The deck is read with double-precision literals, so that the normal
+  incidence source does not depend on x (with the reference's REAL(4) pi,
+  cos(pi/2) is -4.4e-8 and the incident field varies with x at 1e-8).
+* Linearity in the source amplitude: doubling Epump doubles every field
+  value and quadruples every flux value, bit for bit (scaling by 2 is exact
+  in binary floating point).
+"""
+import importlib
+
+import numpy as np
+import pytest
+
+cfg = importlib.import_module("irisfdtd-academic_gb300.configs")
+NX, NY, NZ, STEPS = 5, 3, 48, 140
+
+
+def workload(nx, ny):
+    return cfg.Workload("periodic", nx, ny, NZ, 6, 43, 18, 10, 4.0, 0, 10, (1, nx, 1, ny, 8, 38), 9, STEPS,
+                        structure="spheres", extra=dict(nspheres=3, rmin=1, rmax=3, emin=1.5, emax=6.0))
+
+
+def tile(a, reps, axis):
+    """Repeat the interior of a ghost-padded [z, y, x] array along axis
+    (2: x, 1: y) and refill that axis's ghosts by the periodic wrap."""
+    inner = np.take(a, range(1, a.shape[axis] - 1), axis=axis)
+    t = np.concatenate([inner] * reps, axis=axis)
+    n = t.shape[axis]
+    return np.concatenate([np.take(t, [n - 1], axis=axis), t, np.take(t, [0], axis=axis)], axis=axis)
+
+
+def run(oracle, tmp_path, w, eps, epump=1.0, name="in.dat"):
+    p = oracle.setparam(cfg.write_input(str(tmp_path / name), w, epump=epump), single_literals=False)
+    o = oracle.Oracle(p)
+    try:
+        o.set_eps_inv(eps)
+        o.run(1, p.texit)
+        return o.get_field(o.E_CUR), o.get_field(o.H_CUR), o.flux(0)
+    finally:
+        o.close()
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.parametrize("axis", ["x", "y"])
+def test_supercell_of_a_periodic_cell(oracle, tmp_path, axis):
+    small = workload(NX, NY)
+    eps = cfg.spheres_material(small, seed=11)
+    reps = 2
+    big = workload(NX * reps, NY) if axis == "x" else workload(NX, NY * reps)
+    ax = 2 if axis == "x" else 1
+    e1, h1, J1 = run(oracle, tmp_path, small, eps, name="small.dat")
+    e2, h2, J2 = run(oracle, tmp_path, big, tile(eps, reps, ax), name="big.dat")
+    assert np.any(e1[1:-1, 1:-1, 1:-1] != 0)
+    n = NX if axis == "x" else NY
+    for f1, f2 in ((e1, e2), (h1, h2)):
+        want = f1[1:-1, 1:-1, 1:-1]
+        for r in range(reps):
+            sl = slice(1 + r * n, 1 + (r + 1) * n)
+            got = f2[1:-1, 1:-1, sl] if axis == "x" else f2[1:-1, sl, 1:-1]
+            assert rel(got, want) <= 1e-12, (axis, r)
+    # faces 1, 2 (x), 3, 4 (y), 5, 6 (z): the repeat axis's faces keep their area
+    factor = np.array([1, 1, reps, reps, reps, reps] if axis == "x" else [reps, reps, 1, 1, reps, reps])
+    for j in range(6):
+        assert rel(J2[j], factor[j] * J1[j]) <= 1e-12, j
+
+
+def test_linear_in_the_source_bitwise(oracle, tmp_path):
+    w = workload(NX, NY)
+    eps = cfg.spheres_material(w, seed=11)
+    e1, h1, J1 = run(oracle, tmp_path, w, eps, 1.0, "a.dat")
+    e2, h2, J2 = run(oracle, tmp_path, w, eps, 2.0, "b.dat")
+    assert np.any(J1 != 0)
+    assert np.array_equal(e2, 2.0 * e1) and np.array_equal(h2, 2.0 * h1)
+    assert np.array_equal(J2, 4.0 * J1)
