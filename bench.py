@@ -176,6 +176,25 @@ def algorithmic_bytes(w, p, sc, sm):
     return e, h
 
 
+def dft_accounting(P, nof, kblock, sc, ms_block, ms_gather):
+    """The DFT's own work per sampled step, apart from the stencil's: P x nof
+    complex multiply-adds, the sample ring written by the gather and read by
+    the block (P x sc bytes each way), and the FP64 accumulators read and
+    written once per block of kblock samples (2 x P x nof x 16 / kblock bytes
+    a step).  The gather also reads its P samples from the fields."""
+    acc = 2.0 * P * nof * 16 / max(kblock, 1)
+    ring = P * sc
+    out = {"points": P, "frequencies": nof, "block_samples": kblock, "complex_macs_per_step": P * nof,
+           "accumulator_bytes_per_step": int(round(acc)), "ring_bytes_per_step": ring,
+           "block_ms_per_step": round(ms_block, 4), "gather_ms_per_step": round(ms_gather, 4)}
+    if ms_block > 0:
+        out["block_gbs"] = round((acc + ring) / (ms_block * 1e-3) / 1e9, 1)
+        out["block_gmacs"] = round(P * nof / (ms_block * 1e-3) / 1e9, 1)
+    if ms_gather > 0:
+        out["gather_gbs"] = round(2.0 * ring / (ms_gather * 1e-3) / 1e9, 1)
+    return out
+
+
 def run_engine(args, rank, world, local):
     iris = importlib.import_module(PKG)
     D = Dist(world)
@@ -312,6 +331,8 @@ def run_engine(args, rank, world, local):
                      "min_bytes_per_pass": min_bytes,
                      "frac_of_min_bytes": round(min_bytes / dt_ / 1e9 / hbm, 4)},
         "stencil_gcells": round(cells / ((t_e + t_h)) / 1e9, 3),
+        "dft": dft_accounting(info["dft_points"], w.nof, info["dft_block"], sc, kms["dft_block"] / K,
+                              kms["dft_gather"] / K),
         "clocks": clocks,
         "material_setup_s": round(t_mat, 2),
     }
@@ -625,18 +646,50 @@ def cpu_sample(w, side, threads, steps, warm=1):
     return tr / (ws.cells * steps), td / (npts * op.nof * steps), ws
 
 
-def cpu_baseline(w, full_points, steps=192, side=32):
+def host_cpu():
+    """The host CPU as /proc/cpuinfo names it (x86: model name; Arm: implementer and part)."""
+    import platform
+    name, arm = None, {}
+    try:
+        for line in open("/proc/cpuinfo"):
+            k, _, v = line.partition(":")
+            k, v = k.strip(), v.strip()
+            if k == "model name" and name is None:
+                name = v
+            elif k in ("CPU implementer", "CPU part") and k not in arm:
+                arm[k] = v
+    except OSError:
+        pass
+    if name is None and arm:
+        name = "Arm implementer %s part %s" % (arm.get("CPU implementer", "?"), arm.get("CPU part", "?"))
+    return {"cpu": name or platform.processor() or "unknown", "machine": platform.machine(),
+            "nproc": os.cpu_count() or 1}
+
+
+def cpu_baseline(w, full_points, steps=192, side=32, single_steps=8, single_side=16):
+    """The oracle on all host cores (the reported value) and, like the
+    reference (which has no threading), on one core over a smaller sample."""
     threads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    t_cell, t_pf, ws = cpu_sample(w, side, threads, steps)
-    wall = time.perf_counter() - t0
     cells = w.nx * w.ny * w.nz
-    t_step = t_cell * cells + t_pf * full_points * w.nof
-    return {"value": round(cells / t_step / 1e9, 6), "unit": "Gcell/s", "cores": threads, "kind": "port",
+
+    def sample(thr, sd, st):
+        t0 = time.perf_counter()
+        t_cell, t_pf, _ = cpu_sample(w, sd, thr, st)
+        wall = time.perf_counter() - t0
+        return t_cell, t_pf, cells / (t_cell * cells + t_pf * full_points * w.nof) / 1e9, wall
+
+    t_cell, t_pf, v, wall = sample(threads, side, steps)
+    t_cell1, t_pf1, v1, wall1 = sample(1, single_side, single_steps)
+    return {"value": round(v, 6), "unit": "Gcell/s", "cores": threads, "kind": "port",
             "sample": (f"oracle (C++ FP64 restatement, OpenMP {threads} threads) on a {side}x{side}x{w.nz} column of "
                        f"the workload for {steps} steps ({wall:.1f} s); per-cell ({t_cell * 1e9:.2f} ns) and per-DFT-"
                        f"point-frequency ({t_pf * 1e9:.3f} ns) costs scaled to the full grid and its {full_points} "
-                       f"DFT points x {w.nof} frequencies")}
+                       f"DFT points x {w.nof} frequencies"),
+            "single_thread": {"value": round(v1, 6), "unit": "Gcell/s", "cores": 1,
+                              "sample": (f"the same on one thread, a {single_side}x{single_side}x{w.nz} column for "
+                                         f"{single_steps} steps ({wall1:.1f} s); per-cell {t_cell1 * 1e9:.2f} ns, "
+                                         f"per-DFT-point-frequency {t_pf1 * 1e9:.3f} ns")},
+            "host": host_cpu()}
 
 
 def run_reference(args, rank, world):

@@ -42,3 +42,31 @@ def test_reference_arm_other_ranks_exit_quietly():
 def test_warmup_below_three_is_refused():
     r = run_bench("--impl", "reference", "--steps", "1", "--warmup", "1")
     assert r.returncode != 0 and "warmup" in r.stderr
+
+
+def bench_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_under_test", os.path.join(ROOT, "bench.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def test_dft_accounting():
+    b = bench_module()
+    d = b.dft_accounting(1000, 300, 512, 8, 0.5, 0.25)
+    assert d["complex_macs_per_step"] == 300000 and d["ring_bytes_per_step"] == 8000
+    assert d["accumulator_bytes_per_step"] == round(2 * 1000 * 300 * 16 / 512)
+    assert abs(d["block_gbs"] - (d["accumulator_bytes_per_step"] + 8000) / 0.5e-3 / 1e9) < 0.1
+    assert abs(d["gather_gbs"] - 2 * 8000 / 0.25e-3 / 1e9) < 0.1
+    assert "block_gbs" not in b.dft_accounting(0, 300, 512, 8, 0.0, 0.0)
+
+
+def test_cpu_baseline_keys():
+    b = bench_module()
+    cfg = __import__("importlib").import_module("irisfdtd-academic_gb300.configs")
+    w = cfg.workload(3)
+    d = b.cpu_baseline(w, 14856192, steps=1, side=8, single_steps=1, single_side=8)
+    assert d["kind"] == "port" and d["unit"] == "Gcell/s" and d["value"] > 0 and d["cores"] >= 1
+    assert d["single_thread"]["cores"] == 1 and d["single_thread"]["value"] > 0
+    assert d["host"]["nproc"] >= 1 and d["host"]["cpu"]
