@@ -528,12 +528,15 @@ int get_planes(iris_engine* eng, int which, const std::vector<SdlPlane>& pls, st
   return IRIS_OK;
 }
 
-// main() + driver(), code/main.f90:43-213 and code/driver.f90:66-555
-int run_main(const std::string& dir, int precision) {
+// main() + driver(), code/main.f90:43-213 and code/driver.f90:66-555; loop:
+// called from the <<LOOP>> mode, whose main(i) logs an empty description
+// (code/main.f90:108-113)
+int run_main(const std::string& dir, int precision, bool loop = false) {
   iris_params p;
   char desc[128] = {0};
   int rc = iris_setparam((dir + "/inputFDTD.dat").c_str(), 1, &p, nullptr, 0, desc, sizeof(desc));
   if (rc) return rc;
+  if (loop) desc[0] = 0;
   p.precision = precision;
   std::vector<double> fw(p.nof);
   iris_frequencies(&p, fw.data(), p.nof);
@@ -631,9 +634,9 @@ extern "C" int iris_run_input(const char* dir, int precision) {
     return fail(IRIS_EPARSE, "invalid <<LOOP>> header");
   int rc = IRIS_OK;
   if (io != ifm) {
-    for (int i = io; i <= ifm && rc == IRIS_OK; ++i) rc = run_main(d, precision);
+    for (int i = io; i <= ifm && rc == IRIS_OK; ++i) rc = run_main(d, precision, true);
   } else {
-    rc = run_main(d, precision);
+    rc = run_main(d, precision, true);
   }
   return rc;
 }

@@ -95,3 +95,29 @@ def test_list_directed_details(iris, oracle, tmp_path):
     bad = tmp_path / "inputFDTD.dat"
     bad.write_text("\n".join(src))
     _compare(iris, oracle, str(bad))
+
+
+def _loop_deck(tmp_path, name, header):
+    body = open(golden("example_1.inputFDTD.dat")).read().split("\n", 1)[1]  # without the description line
+    d = tmp_path / name
+    d.mkdir()
+    (d / "inputFDTD.dat").write_text("<<LOOP>>\n" + header + body)
+    return d
+
+
+def test_loop_mode_header(iris, tmp_path):
+    """program.f90:36-57: after <<LOOP>> come io_main, if_main and delta_x/y/z;
+    do i = io_main, if_main runs no iteration when io_main > if_main (no
+    engine, no files), and a header that is not numbers is a parse error."""
+    d = _loop_deck(tmp_path, "empty", "3\n2\n0.0\n0.0\n0.0\n")
+    iris.run_input(str(d), iris.FP64)
+    assert not (d / "log.dat").exists()
+    bad = _loop_deck(tmp_path, "bad", "three\n2\n")
+    with pytest.raises(iris.IrisError) as e:
+        iris.run_input(str(bad), iris.FP64)
+    assert e.value.code == -4
+    # setparam's section scan still finds every section after the loop header
+    ok = _loop_deck(tmp_path, "one", "1\n1\n0.0\n0.0\n0.0\n")
+    p, fw, desc = iris.setparam(str(ok / "inputFDTD.dat"))
+    q, _, _ = iris.setparam(golden("example_1.inputFDTD.dat"))
+    assert (p.nx, p.ny, p.nz, p.texit, p.nof) == (q.nx, q.ny, q.nz, q.texit, q.nof)
