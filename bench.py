@@ -7,13 +7,16 @@ on-the-fly DFT at 300 frequencies on all six faces of the box, as the
 reference accumulates them in 3D), FP32 fields with FP64 incident field and
 FP64 DFT accumulation.  One bench step is one full time step of the hot path:
 E update, UPML-E, Bloch, H update, UPML-H, Bloch, TF/SF, DFT sample, plus the
-DFT block accumulation amortised over its K samples.
+DFT block accumulation amortised over its K samples (the sample ring is empty
+when the clock starts, and every timed sample is accumulated inside the
+clock: a flux read ends the timed steps).
 
 Metric: Gcell/s = cells * steps / time.  `value` is device-timed (CUDA events
 on the engine's stream) with the state resident in HBM; `e2e` goes through the
 public API from host buffers (engine creation, material upload, the steps and
-the flux read back).  `roofline` is for the dominant kernel (the H update),
-algorithmic bytes per launch over its event-timed duration.
+the flux read back).  `roofline` is for the dominant pass (the fused E+H pass
+in FP32, the slower split pass otherwise): algorithmic bytes per pass over
+its event-timed duration; `dft` reports the DFT's own work apart from it.
 
 --impl reference times the CPU restatement of the reference (the oracle; the
 Fortran reference has no compiler here) on the host cores, on a bounded
