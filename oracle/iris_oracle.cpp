@@ -21,9 +21,10 @@
 // Parity of this restatement is pinned in tests/test_oracle_pins.py against
 // the reference's own numbers (dt and step count of example_1 quoted in
 // irisfdtd_movie.py:25) and the analytic film spectrum the reference writes
-// (code/common.f90:104-131).  The reference itself cannot be compiled here
-// (no Fortran compiler), so bit-level pinning against a reference run is not
-// possible.
+// (code/common.f90:104-131); tests/test_oracle_properties.py checks its Bloch
+// wrap (periodic supercells) and its linearity in the source.  The reference
+// itself cannot be compiled here (no Fortran compiler), so bit-level pinning
+// against a reference run is not possible.
 
 #include <chrono>
 #include <cmath>

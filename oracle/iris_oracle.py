@@ -13,6 +13,9 @@ Python half of the CPU FP64 restatement of IrisFDTD-Academic's hot path:
 * ``struct_limit`` — code/files.f90:385-409.
 * ``Oracle`` — ctypes wrapper of ``iris_oracle.cpp`` (the numerics: Yee E/H,
   UPML, Bloch, TF/SF, on-the-fly DFT, flux).
+* ``tr_normalise``, ``wavelength_axis`` — irisfdtd_scatt.py:37-42 and
+  IrisFDTD_scattering.py:111,143, checked bit for bit against fixtures the
+  reference's own reader produced (tests/test_scatt_files.py).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 this module, as the checker or as the timed CPU baseline.  The product never

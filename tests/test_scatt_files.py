@@ -55,6 +55,17 @@ def test_tr_and_wavelength_axis_match_the_reference_reader(iris):
         assert np.array_equal(R, g["R"][it]) and np.array_equal(T, g["T"][it])
 
 
+def test_oracle_tr_matches_the_reference_reader(iris, oracle):
+    g = fixture()
+    nof = int(g["nof"])
+    r5 = iris.read_scatt(golden(os.path.join("scatt", "1_scatt5.dat")), nof)
+    r6 = iris.read_scatt(golden(os.path.join("scatt", "1_scatt6.dat")), nof)
+    for it in range(len(g["its"])):
+        R, T = oracle.tr_normalise(r5[it], r6[it])
+        assert np.array_equal(R, g["R"][it]) and np.array_equal(T, g["T"][it])
+    assert np.array_equal(oracle.wavelength_axis(float(g["lno"]), float(g["dlamda"]), nof), g["x"][0])
+
+
 def test_writer_rejects_bad_arguments(iris, tmp_path):
     import pytest
     with pytest.raises(ValueError):
