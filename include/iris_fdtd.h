@@ -279,7 +279,10 @@ int iris_run_input(const char* dir, int precision);
 #define IRIS_KC_GATHER 3 /* DFT face sample gather                        */
 #define IRIS_KC_DFT 4    /* DFT block accumulation (and its twiddles)     */
 #define IRIS_KC_FLUX 5   /* flux reduction                                */
-#define IRIS_KC_FUSED 6  /* fused E+H pass (TF/SF and DFT samples inside) */
+#define IRIS_KC_FUSED 6  /* fused E+H pass: one entry a step spanning its  */
+                         /* two concurrent launches (outside the UPML     */
+                         /* slabs, the slabs); TF/SF and the DFT sample   */
+                         /* follow as their own kernels                   */
 #define IRIS_NKC 7
 
 /*
@@ -289,7 +292,9 @@ int iris_run_input(const char* dir, int precision);
  */
 int iris_timing(iris_engine* eng, int enable);
 /* End the region: its device time, and per kernel class the summed device
- * time (ms) and launch count (arrays of IRIS_NKC, either may be NULL). */
+ * time (ms) and the number of timed entries (arrays of IRIS_NKC, either may
+ * be NULL): one per launch, except IRIS_KC_FUSED (one per step) and the
+ * batch's persistent work lists (one per pass). */
 int iris_timing_read(iris_engine* eng, double* region_ms, double* kernel_ms, long* launches);
 /* Sizes: info[0] DFT sample points, [1] DFT block length K, [2] bytes per
  * stored complex value, [3] elements per field component, [4] complex
