@@ -293,8 +293,9 @@ int iris_run_input(const char* dir, int precision);
 int iris_timing(iris_engine* eng, int enable);
 /* End the region: its device time, and per kernel class the summed device
  * time (ms) and the number of timed entries (arrays of IRIS_NKC, either may
- * be NULL): one per launch, except IRIS_KC_FUSED (one per step) and the
- * batch's persistent work lists (one per pass). */
+ * be NULL): one per launch, except the plain engine's IRIS_KC_FUSED (one
+ * per step) and the batch's flat work lists (one per E or H pass of two
+ * launches). */
 int iris_timing_read(iris_engine* eng, double* region_ms, double* kernel_ms, long* launches);
 /* Sizes: info[0] DFT sample points, [1] DFT block length K, [2] bytes per
  * stored complex value, [3] elements per field component, [4] complex
