@@ -279,10 +279,8 @@ int iris_run_input(const char* dir, int precision);
 #define IRIS_KC_GATHER 3 /* DFT face sample gather                        */
 #define IRIS_KC_DFT 4    /* DFT block accumulation (and its twiddles)     */
 #define IRIS_KC_FLUX 5   /* flux reduction                                */
-#define IRIS_KC_FUSED 6  /* fused E+H pass: one entry a step spanning its  */
-                         /* two concurrent launches (outside the UPML     */
-                         /* slabs, the slabs); TF/SF and the DFT sample   */
-                         /* follow as their own kernels                   */
+#define IRIS_KC_FUSED 6  /* fused E+H pass (TF/SF and the DFT sample      */
+                         /* follow as their own kernels)                  */
 #define IRIS_NKC 7
 
 /*
