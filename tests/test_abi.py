@@ -49,6 +49,13 @@ def test_no_gpu_means_error_not_fallback(iris):
     with pytest.raises(iris.IrisError) as e:
         iris.Engine(p, fw)
     assert e.value.code in (-8, -3)
+    # the batched and gradient forms refuse the same way
+    with pytest.raises(iris.IrisError) as e:
+        iris.Batch([p, p.copy()], fw, dft_faces=iris.DFT_Z)
+    assert e.value.code in (-8, -3)
+    with pytest.raises(iris.IrisError) as e:
+        iris.Adjoint(p, fw, (1, 1, 1, 1, p.hi, p.hi + 2))
+    assert e.value.code in (-8, -3)
 
 
 def test_invalid_parameters_rejected(iris):
