@@ -14,6 +14,8 @@ exists:
 * Linearity in the source amplitude: doubling Epump doubles every field
   value and quadruples every flux value, bit for bit (scaling by 2 is exact
   in binary floating point).
+* The e_fdtd and h_fdtd operators against an independent vectorised numpy
+  restatement of code/fdtd.f90:57-248, bit for bit, regions included.
 """
 import importlib
 
@@ -84,3 +86,75 @@ def test_linear_in_the_source_bitwise(oracle, tmp_path):
     assert np.any(J1 != 0)
     assert np.array_equal(e2, 2.0 * e1) and np.array_equal(h2, 2.0 * h1)
     assert np.array_equal(J2, 4.0 * J1)
+
+
+# ---------------------------------------------------------------------------
+# e_fdtd / h_fdtd of the oracle against an independent, vectorised numpy
+# restatement of code/fdtd.f90:57-248 (same operation order, no FMA on either
+# side, real eps_inv): equal to the last bit in every region, and nothing
+# written outside the regions.
+
+def _vec_case(oracle, tmp_path):
+    w = cfg.Workload("ops", 7, 5, 40, 6, 35, 15, 9, 4.0, 0, 10, (1, 7, 1, 5, 8, 32), 5, 10)
+    p = oracle.setparam(cfg.write_input(str(tmp_path / "ops.dat"), w))
+    o = oracle.Oracle(p)
+    rng = np.random.default_rng(21)
+    eps = 1.0 / rng.uniform(1.0, 6.0, (p.hf - p.hi + 3, p.ny + 2, p.nx + 2)) + 0j
+    o.set_eps_inv(eps)
+    shp = o.field_shape
+    fields = [rng.standard_normal(shp) + 1j * rng.standard_normal(shp) for _ in range(4)]
+    return p, o, eps, fields
+
+
+def _sh(a, dz=0, dy=0, dx=0):
+    """a[z+dz, y+dy, x+dx] over the interior x, y and all z (z shifted later)."""
+    return a[:, 1 + dy:a.shape[1] - 1 + dy, 1 + dx:a.shape[2] - 1 + dx]
+
+
+def test_e_fdtd_against_numpy(oracle, tmp_path):
+    p, o, eps, (e_prev, h_prev, e_cur0, _) = _vec_case(oracle, tmp_path)
+    o.set_field(o.E_PREV, e_prev)
+    o.set_field(o.H_PREV, h_prev)
+    o.set_field(o.E_CUR, e_cur0)
+    o.op("e_fdtd")
+    got = o.get_field(o.E_CUR)
+    H = [h_prev[..., k] for k in range(3)]
+    want = e_cur0.copy()
+    for z in range(p.pmlzi + 1, p.pmlzf):
+        def at(k, dz=0, dy=0, dx=0):
+            return _sh(H[k], dy=dy, dx=dx)[z + dz]
+        c = [((at(2) - at(2, dy=-1)) - at(1)) + at(1, dz=-1),
+             ((at(0) - at(0, dz=-1)) - at(2)) + at(2, dx=-1),
+             ((at(1) - at(1, dx=-1)) - at(0)) + at(0, dy=-1)]
+        if z < p.hi:
+            m = 1.0 / p.eps1
+        elif z > p.hf:
+            m = 1.0 / p.eps3
+        else:
+            m = eps[z - p.hi + 1, 1:-1, 1:-1].real
+        for k in range(3):
+            want[z, 1:-1, 1:-1, k] = e_prev[z, 1:-1, 1:-1, k] + m * c[k]
+    assert np.array_equal(got, want)
+
+
+def test_h_fdtd_against_numpy(oracle, tmp_path):
+    p, o, eps, (e_cur, h_prev, _, h_cur0) = _vec_case(oracle, tmp_path)
+    o.set_field(o.E_CUR, e_cur)
+    o.set_field(o.H_PREV, h_prev)
+    o.set_field(o.H_CUR, h_cur0)
+    o.op("h_fdtd")
+    got = o.get_field(o.H_CUR)
+    c0, Q, dt = p.consts["c0"], p.Q, p.dt
+    coef = (dt * c0 / Q) * (dt * c0 / Q)
+    E = [e_cur[..., k] for k in range(3)]
+    want = h_cur0.copy()
+    zmx = p.hf if p.pmlzf < p.hf else p.pmlzf - 1
+    for z in range(p.pmlzi, zmx + 1):
+        def at(k, dz=0, dy=0, dx=0):
+            return _sh(E[k], dy=dy, dx=dx)[z + dz]
+        c = [((at(2, dy=1) - at(2)) - at(1, dz=1)) + at(1),
+             ((at(0, dz=1) - at(0)) - at(2, dx=1)) + at(2),
+             ((at(1, dx=1) - at(1)) - at(0, dy=1)) + at(0)]
+        for k in range(3):
+            want[z, 1:-1, 1:-1, k] = h_prev[z, 1:-1, 1:-1, k] - coef * c[k]
+    assert np.array_equal(got, want)
