@@ -15,7 +15,8 @@ exists:
   value and quadruples every flux value, bit for bit (scaling by 2 is exact
   in binary floating point).
 * The e_fdtd and h_fdtd operators against an independent vectorised numpy
-  restatement of code/fdtd.f90:57-248, bit for bit, regions included.
+  restatement of code/fdtd.f90:57-248, bit for bit, regions included; the
+  Bloch wrap with complex ak on all three axes against numpy.
 """
 import importlib
 
@@ -158,3 +159,35 @@ def test_h_fdtd_against_numpy(oracle, tmp_path):
         for k in range(3):
             want[z, 1:-1, 1:-1, k] = h_prev[z, 1:-1, 1:-1, k] - coef * c[k]
     assert np.array_equal(got, want)
+
+
+def test_bloch_wrap_against_numpy(oracle, tmp_path):
+    """bc_{x,y,z}max_bloch / bc_{x,y,z}min_bloch (code/boundary.f90:163-348):
+    the max ghosts of E and H take exp(+i ak) times the first interior plane,
+    the min ghosts exp(-i ak) times the last, axis by axis over the interior
+    of the other two axes (edges and corners untouched)."""
+    w = cfg.Workload("bloch", 6, 4, 12, 3, 10, 5, 2, 4.0, 0, 4, (1, 6, 1, 4, 4, 8), 3, 10)
+    p = oracle.setparam(cfg.write_input(str(tmp_path / "bloch.dat"), w))
+    ak = (0.7 - 0.05j, -1.3 + 0.02j, 0.4 + 0j)
+    o = oracle.Oracle(p, ak=ak)
+    rng = np.random.default_rng(8)
+    shp = o.field_shape
+    for op, sign in (("bloch_max", +1), ("bloch_min", -1)):
+        e0 = rng.standard_normal(shp) + 1j * rng.standard_normal(shp)
+        h0 = rng.standard_normal(shp) + 1j * rng.standard_normal(shp)
+        o.set_field(o.E_CUR, e0)
+        o.set_field(o.H_CUR, h0)
+        o.op(op)
+        for f0, got in ((e0, o.get_field(o.E_CUR)), (h0, o.get_field(o.H_CUR))):
+            want = f0.copy()
+            fx, fy, fz = (np.exp(sign * 1j * a) for a in ak)
+            if sign > 0:
+                want[1:-1, 1:-1, -1] = fx * want[1:-1, 1:-1, 1]
+                want[1:-1, -1, 1:-1] = fy * want[1:-1, 1, 1:-1]
+                want[-1, 1:-1, 1:-1] = fz * want[1, 1:-1, 1:-1]
+            else:
+                want[1:-1, 1:-1, 0] = fx * want[1:-1, 1:-1, -2]
+                want[1:-1, 0, 1:-1] = fy * want[1:-1, -2, 1:-1]
+                want[0, 1:-1, 1:-1] = fz * want[-2, 1:-1, 1:-1]
+            assert np.max(np.abs(got - want)) <= 1e-14 * np.max(np.abs(want)), op
+            assert np.array_equal(got[1:-1, 1:-1, 1:-1], f0[1:-1, 1:-1, 1:-1])
