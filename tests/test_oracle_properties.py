@@ -16,7 +16,8 @@ exists:
   in binary floating point).
 * The e_fdtd and h_fdtd operators against an independent vectorised numpy
   restatement of code/fdtd.f90:57-248, bit for bit, regions included; the
-  Bloch wrap with complex ak on all three axes against numpy.
+  Bloch wrap with complex ak on all three axes against numpy; the flux of
+  the z faces recomputed in numpy from the oracle's own accumulators.
 """
 import importlib
 
@@ -191,3 +192,29 @@ def test_bloch_wrap_against_numpy(oracle, tmp_path):
                 want[0, 1:-1, 1:-1] = fz * want[-2, 1:-1, 1:-1]
             assert np.max(np.abs(got - want)) <= 1e-14 * np.max(np.abs(want)), op
             assert np.array_equal(got[1:-1, 1:-1, 1:-1], f0[1:-1, 1:-1, 1:-1])
+
+
+def test_flux_from_the_accumulated_samples(oracle, tmp_path):
+    """scattering_fourier_out (code/dataprocess.f90:246-277) restated in numpy
+    on the oracle's own accumulators and sample list: J5 = -sum Re(Ex Hy* -
+    Ey Hx*) over the z = szi face, J6 = +sum over z = szf, both times
+    eps0 Q / (2 dt)."""
+    w = workload(NX, NY)
+    p = oracle.setparam(cfg.write_input(str(tmp_path / "flux.dat"), w), single_literals=False)
+    o = oracle.Oracle(p)
+    o.set_eps_inv(cfg.spheres_material(w, seed=11))
+    o.run(1, 90)
+    J = o.flux(0)
+    fd = o.fdata(0, 3)             # [iw, point]
+    pto = o.pto(0, 3)              # (component 1..6, ix, iy, iz) per point
+    scale = p.consts["eps0"] * p.Q / (2.0 * p.dt)
+    szi, szf = p.box1[4], p.box1[5]
+    for j, z, sign in ((4, szi, -1.0), (5, szf, 1.0)):
+        def comp(c):
+            sel = (pto[:, 0] == c) & (pto[:, 3] == z)
+            order = np.lexsort((pto[sel, 1], pto[sel, 2]))
+            return fd[:, sel][:, order]
+        ex, ey, hx, hy = comp(1), comp(2), comp(4), comp(5)
+        want = sign * np.sum((ex * np.conj(hy) - ey * np.conj(hx)).real, axis=1) * scale
+        assert np.any(want != 0)
+        assert np.max(np.abs(J[j] - want)) <= 1e-12 * np.max(np.abs(want)), j
