@@ -17,9 +17,12 @@ exists:
 * The e_fdtd and h_fdtd operators against an independent vectorised numpy
   restatement of code/fdtd.f90:57-248, bit for bit, regions included; the
   Bloch wrap with complex ak on all three axes against numpy; the flux of
-  the z faces recomputed in numpy from the oracle's own accumulators.
+  the z faces recomputed in numpy from the oracle's own accumulators;
+  UPML_Array_e (with its component-to-profile permutation read from
+  code/boundary_II.f90:86-99) and set_sz against numpy.
 """
 import importlib
+import math
 
 import numpy as np
 import pytest
@@ -218,3 +221,68 @@ def test_flux_from_the_accumulated_samples(oracle, tmp_path):
         want = sign * np.sum((ex * np.conj(hy) - ey * np.conj(hx)).real, axis=1) * scale
         assert np.any(want != 0)
         assert np.max(np.abs(J[j] - want)) <= 1e-12 * np.max(np.abs(want)), j
+
+
+def test_upml_e_against_numpy(oracle, tmp_path):
+    """UPML_Array_e (code/boundary_II.f90:60-138) restated in numpy: per slab
+    curl * eps0^2, D_k decays with profile (2, 3, 1)[k] and E_k with profile
+    (3, 1, 2)[k] (1-based, as in the reference), bit for bit."""
+    p, o, eps, (e_prev, h_prev, e_cur0, _) = _vec_case(oracle, tmp_path)
+    rng = np.random.default_rng(5)
+    dprev = [rng.standard_normal(o.pml_shape(s)) + 1j * rng.standard_normal(o.pml_shape(s)) for s in (0, 1)]
+    o.set_field(o.E_PREV, e_prev)
+    o.set_field(o.H_PREV, h_prev)
+    o.set_field(o.E_CUR, e_cur0)
+    for s in (0, 1):
+        o.set_pml(0, 0, s, dprev[s])
+    o.op("upml_e")
+    got_e = o.get_field(o.E_CUR)
+    fpn, fmn, fpx, fmx = o.get_sz()
+    eps0 = p.consts["eps0"]
+    H = [h_prev[..., k] for k in range(3)]
+    want_e = e_cur0.copy()
+    pd, pe = (1, 2, 0), (2, 0, 1)
+    for s, (z0, z1, fp, fm, eb) in enumerate(((1, p.pmlzi, fpn, fmn, p.eps1), (p.pmlzf, p.nz, fpx, fmx, p.eps3))):
+        want_d = np.empty_like(dprev[s])
+        for z in range(z0, z1 + 1):
+            zr = z - z0
+
+            def at(k, dz=0, dy=0, dx=0):
+                return _sh(H[k], dy=dy, dx=dx)[z + dz]
+            c = [((at(2) - at(2, dy=-1)) - at(1)) + at(1, dz=-1),
+                 ((at(0) - at(0, dz=-1)) - at(2)) + at(2, dx=-1),
+                 ((at(1) - at(1, dx=-1)) - at(0)) + at(0, dy=-1)]
+            c = [(eps0 * eps0) * ck for ck in c]
+            for k in range(3):
+                dold = dprev[s][zr, :, :, k]
+                dn = (fm[zr, pd[k]] / fp[zr, pd[k]]) * dold + ((2 * eb) / fp[zr, pd[k]]) * c[k]
+                want_d[zr, :, :, k] = dn
+                v = (fm[zr, pe[k]] / fp[zr, pe[k]]) * e_prev[z, 1:-1, 1:-1, k]
+                wv = fp[zr, k] * dn - fm[zr, k] * dold
+                want_e[z, 1:-1, 1:-1, k] = v + (1 / (eps0 * eb * fp[zr, pe[k]])) * wv
+        assert np.array_equal(o.get_pml(0, 1, s), want_d), s
+    assert np.array_equal(got_e, want_e)
+
+
+def test_set_sz_against_numpy(oracle, tmp_path):
+    """set_sz (code/boundary_II.f90:224-276) restated in numpy: only the third
+    profile is graded, sigma and kappa - 1 grow as ((pmlzi - i)/(pmlzi - 1))^n
+    into the bottom slab and ((i - pmlzf)/(nz - pmlzf))^n into the top one,
+    with the REAL(4) literal 1.8 for kappa."""
+    p, o, _, _ = _vec_case(oracle, tmp_path)
+    k = p.consts
+    got = o.get_sz()
+    n = p.npml
+    want = []
+    for eb, r in ((p.eps1, np.array([(p.pmlzi - i) ** n / float(p.pmlzi - 1) ** n for i in range(1, p.pmlzi + 1)])),
+                  (p.eps3, np.array([(i - p.pmlzf) ** n / float(p.nz - p.pmlzf) ** n
+                                     for i in range(p.pmlzf, p.nz + 1)]))):
+        sg = np.zeros((r.size, 3))
+        kap = np.ones((r.size, 3))
+        sg[:, 2] = math.sqrt(eb) * p.wzpml * r
+        kap[:, 2] = 1 + math.sqrt(eb) * k["pmlalfa"] * r
+        want += [2 * k["eps0"] * eb * kap + p.dt * sg, 2 * k["eps0"] * eb * kap - p.dt * sg]
+    for g, wv in zip(got, want):
+        assert g.shape == wv.shape
+        assert np.max(np.abs(g - wv)) <= 1e-14 * np.max(np.abs(wv))
+    assert k["pmlalfa"] == 1.7999999523162842
