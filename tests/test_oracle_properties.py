@@ -18,8 +18,8 @@ exists:
   restatement of code/fdtd.f90:57-248, bit for bit, regions included; the
   Bloch wrap with complex ak on all three axes against numpy; the flux of
   the z faces recomputed in numpy from the oracle's own accumulators;
-  UPML_Array_e (with its component-to-profile permutation read from
-  code/boundary_II.f90:86-99) and set_sz against numpy.
+  UPML_Array_e and UPML_Array_h (with the component-to-profile permutation
+  read from code/boundary_II.f90:86-99,170-183) and set_sz against numpy.
 """
 import importlib
 import math
@@ -286,3 +286,44 @@ def test_set_sz_against_numpy(oracle, tmp_path):
         assert g.shape == wv.shape
         assert np.max(np.abs(g - wv)) <= 1e-14 * np.max(np.abs(wv))
     assert k["pmlalfa"] == 1.7999999523162842
+
+
+def test_upml_h_against_numpy(oracle, tmp_path):
+    """UPML_Array_h (code/boundary_II.f90:142-220) restated in numpy, bit for
+    bit: B_k = (fm/fp)[(2, 3, 1)[k]] B_prev - ((2 eps / fp) dtq2) curl E,
+    H_k decays with profile (3, 1, 2)[k], mu0 in the B-to-H step."""
+    p, o, eps, (e_cur, h_prev, _, h_cur0) = _vec_case(oracle, tmp_path)
+    rng = np.random.default_rng(6)
+    bprev = [rng.standard_normal(o.pml_shape(s)) + 1j * rng.standard_normal(o.pml_shape(s)) for s in (0, 1)]
+    o.set_field(o.E_CUR, e_cur)
+    o.set_field(o.H_PREV, h_prev)
+    o.set_field(o.H_CUR, h_cur0)
+    for s in (0, 1):
+        o.set_pml(1, 0, s, bprev[s])
+    o.op("upml_h")
+    got_h = o.get_field(o.H_CUR)
+    fpn, fmn, fpx, fmx = o.get_sz()
+    mu0 = p.consts["mu0"]
+    dtq2 = (p.dt / p.Q) * (p.dt / p.Q)
+    E = [e_cur[..., k] for k in range(3)]
+    want_h = h_cur0.copy()
+    pd, pe = (1, 2, 0), (2, 0, 1)
+    for s, (z0, z1, fp, fm, eb) in enumerate(((1, p.pmlzi, fpn, fmn, p.eps1), (p.pmlzf, p.nz, fpx, fmx, p.eps3))):
+        want_b = np.empty_like(bprev[s])
+        for z in range(z0, z1 + 1):
+            zr = z - z0
+
+            def at(k, dz=0, dy=0, dx=0):
+                return _sh(E[k], dy=dy, dx=dx)[z + dz]
+            c = [((at(2, dy=1) - at(2)) - at(1, dz=1)) + at(1),
+                 ((at(0, dz=1) - at(0)) - at(2, dx=1)) + at(2),
+                 ((at(1, dx=1) - at(1)) - at(0, dy=1)) + at(0)]
+            for k in range(3):
+                bold = bprev[s][zr, :, :, k]
+                bn = (fm[zr, pd[k]] / fp[zr, pd[k]]) * bold - (((2 * eb) / fp[zr, pd[k]]) * dtq2) * c[k]
+                want_b[zr, :, :, k] = bn
+                v = (fm[zr, pe[k]] / fp[zr, pe[k]]) * h_prev[z, 1:-1, 1:-1, k]
+                wv = fp[zr, k] * bn - fm[zr, k] * bold
+                want_h[z, 1:-1, 1:-1, k] = v + (1 / (mu0 * fp[zr, pe[k]])) * wv
+        assert np.array_equal(o.get_pml(1, 1, s), want_b), s
+    assert np.array_equal(got_h, want_h)
