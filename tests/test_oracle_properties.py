@@ -19,7 +19,8 @@ exists:
   Bloch wrap with complex ak on all three axes against numpy; the flux of
   the z faces recomputed in numpy from the oracle's own accumulators;
   UPML_Array_e and UPML_Array_h (with the component-to-profile permutation
-  read from code/boundary_II.f90:86-99,170-183) and set_sz against numpy.
+  read from code/boundary_II.f90:86-99,170-183) and set_sz against numpy;
+  the on-the-fly DFT of two samples over every face pair's sample list.
 """
 import importlib
 import math
@@ -327,3 +328,26 @@ def test_upml_h_against_numpy(oracle, tmp_path):
                 want_h[z, 1:-1, 1:-1, k] = v + (1 / (mu0 * fp[zr, pe[k]])) * wv
         assert np.array_equal(o.get_pml(1, 1, s), want_b), s
     assert np.array_equal(got_h, want_h)
+
+
+def test_dft_samples_against_numpy(oracle, tmp_path):
+    """scattering_fourier (code/dataprocess.f90:109-209) with the sample list
+    of init_store_pts_fourier (:793-903): after two samples at steps t1, t2
+    every accumulator is dt * (F(t1) e^{i w t1} + F(t2) e^{i w t2}) of its
+    point's field component (E for components 1-3, H for 4-6)."""
+    p, o, eps, (e1, h1, e2, h2) = _vec_case(oracle, tmp_path)
+    fw = np.asarray(p.fw, dtype=np.float64)
+    want = {}
+    for (e, h), t in (((e1, h1), 7), ((e2, h2), 12)):
+        o.set_field(o.E_CUR, e)
+        o.set_field(o.H_CUR, h)
+        o.op("dft", t)
+        for j in (1, 2, 3):
+            pto = o.pto(0, j)
+            comp, x, y, z = pto[:, 0], pto[:, 1], pto[:, 2], pto[:, 3]
+            f = np.where(comp <= 3, e[z, y, x, np.minimum(comp, 3) - 1], h[z, y, x, np.maximum(comp, 4) - 4])
+            want[j] = want.get(j, 0) + (p.dt * f)[None, :] * np.exp(1j * fw[:, None] * t)
+    for j in (1, 2, 3):
+        got = o.fdata(0, j)
+        assert got.shape == want[j].shape and got.shape[1] > 0
+        assert np.max(np.abs(got - want[j])) <= 1e-14 * np.max(np.abs(want[j])), j
