@@ -7,9 +7,11 @@ on-the-fly DFT at 300 frequencies on all six faces of the box, as the
 reference accumulates them in 3D), FP32 fields with FP64 incident field and
 FP64 DFT accumulation.  One bench step is one full time step of the hot path:
 E update, UPML-E, Bloch, H update, UPML-H, Bloch, TF/SF, DFT sample, plus the
-DFT block accumulation amortised over its K samples (the sample ring is empty
-when the clock starts, and every timed sample is accumulated inside the
-clock: a flux read ends the timed steps).
+DFT accumulation.  The DFT buffer is empty when the clock starts and a flux
+read ends the timed steps; on the FP32 tensor-core path that read adds the
+samples still buffered on the fly and leaves them buffered, so the timed
+time also carries their share of the commit they wait for (a full block's
+commit is timed after the timed steps; its share is buffered / block).
 
 Metric: Gcell/s = cells * steps / time.  `value` is device-timed (CUDA events
 on the engine's stream) with the state resident in HBM; `e2e` goes through the
@@ -17,11 +19,12 @@ public API from host buffers (engine creation, material upload, the steps and
 the flux read back).  `roofline` is for the dominant pass (the fused E+H pass
 in FP32, the slower split pass otherwise): algorithmic bytes per pass over
 its event-timed duration; `dft` reports the DFT's own work apart from it.
+The default line also carries the batched form (256 uneven cells) as `batch`.
 
 --impl reference times the CPU restatement of the reference (the oracle; the
 Fortran reference has no compiler here) on the host cores, on a bounded
 column of the same workload, and scales its per-cell and per-DFT-point costs
-to the full workload.
+to the full workload (marked "extrapolated").
 """
 import argparse
 import glob
@@ -179,23 +182,62 @@ def algorithmic_bytes(w, p, sc, sm):
     return e, h
 
 
-def dft_accounting(P, nof, kblock, sc, ms_block, ms_gather):
-    """The DFT's own work per sampled step, apart from the stencil's: P x nof
-    complex multiply-adds, the sample ring written by the gather and read by
-    the block (P x sc bytes each way), and the FP64 accumulators read and
-    written once per block of kblock samples (2 x P x nof x 16 / kblock bytes
-    a step).  The gather also reads its P samples from the fields."""
-    acc = 2.0 * P * nof * 16 / max(kblock, 1)
-    ring = P * sc
-    out = {"points": P, "frequencies": nof, "block_samples": kblock, "complex_macs_per_step": P * nof,
-           "accumulator_bytes_per_step": int(round(acc)), "ring_bytes_per_step": ring,
-           "block_ms_per_step": round(ms_block, 4), "gather_ms_per_step": round(ms_gather, 4)}
-    if ms_block > 0:
-        out["block_gbs"] = round((acc + ring) / (ms_block * 1e-3) / 1e9, 1)
-        out["block_gmacs"] = round(P * nof / (ms_block * 1e-3) / 1e9, 1)
-    if ms_gather > 0:
-        out["gather_gbs"] = round(2.0 * ring / (ms_gather * 1e-3) / 1e9, 1)
+def dft_accounting(P, nof, kblock, sc, K, kms, kn, buffered, flux_points, commit_ms):
+    """The DFT's own work over the K timed steps, apart from the stencil's.
+
+    Every step gathers its P face samples into the ring (P x sc bytes
+    written).  A commit accumulates the ring into the FP64 accumulators: it
+    reads and writes all of them (2 x P x nof x 16 bytes) and reads the ring.
+    The flux read that ends the timed steps reads the four flux components'
+    accumulators (flux_points x nof x 16 bytes) and, on the tensor-core path,
+    adds the `buffered` samples not yet committed on the fly.  The bytes
+    below are those of the commits and flux reads that ran inside the timed
+    region; `commit` is one full block's commit measured after it, whose
+    share for the buffered samples (buffered / kblock of it) the timed
+    region's value includes."""
+    ncommit, nflux = kn["dft_block"], kn["flux"]
+    acc_commit = ncommit * 2.0 * P * nof * 16
+    ring_commit = (K - buffered) * P * sc  # every committed sample was gathered inside the window
+    acc_flux = nflux * flux_points * nof * 16.0
+    ring_flux = nflux * buffered * flux_points * sc
+    out = {"points": P, "frequencies": nof, "block_samples": kblock, "timed_steps": K,
+           "complex_macs_per_step": P * nof, "commits_in_window": ncommit, "flux_reads_in_window": nflux,
+           "samples_left_buffered": buffered,
+           "accumulator_bytes_per_step": int(round((acc_commit + acc_flux) / K)),
+           "ring_bytes_per_step": P * sc,
+           "block_ms_per_step": round(kms["dft_block"] / K, 4), "flux_ms_per_step": round(kms["flux"] / K, 4),
+           "gather_ms_per_step": round(kms["dft_gather"] / K, 4)}
+    if kms["dft_block"] > 0 and ncommit:
+        out["block_gbs"] = round((acc_commit + ring_commit) / (kms["dft_block"] * 1e-3) / 1e9, 1)
+    if kms["flux"] > 0 and nflux:
+        out["flux_gbs"] = round((acc_flux + ring_flux) / (kms["flux"] * 1e-3) / 1e9, 1)
+    if kms["dft_gather"] > 0:
+        out["gather_gbs"] = round(2.0 * K * P * sc / (kms["dft_gather"] * 1e-3) / 1e9, 1)
+    if commit_ms:
+        full = 2.0 * P * nof * 16 + kblock * P * sc
+        out["commit"] = {"block_samples": kblock, "ms": round(commit_ms, 3),
+                         "gbs": round(full / (commit_ms * 1e-3) / 1e9, 1),
+                         "share_ms_in_value": round(commit_ms * buffered / kblock, 4),
+                         "what": ("one commit of a full block of samples, timed by CUDA events after the timed "
+                                  "steps; the value's time includes its share for the samples the timed steps "
+                                  "left buffered")}
     return out
+
+
+def full_block_commit(eng, it, kb, buffered):
+    """Steps on from it until the DFT buffer (buffered samples in it) is full and
+    commits: the device time of that one commit of kb samples (ms)."""
+    eng.timing_start(per_kernel=True)
+    eng.step(it, kb - buffered)
+    _, kc, nc = eng.timing_read()
+    assert nc["dft_block"] == 1 and eng.info()["dft_buffered"] == 0, (nc, eng.info())
+    return kc["dft_block"], it + kb - buffered
+
+
+def flux_points(info):
+    """Sample points one flux read touches: the four flux components of every
+    face location of one box (P counts six components per location)."""
+    return info["dft_points"] * 4 // 6 // max(1, info["boxes"])
 
 
 def run_engine(args, rank, world, local):
@@ -233,32 +275,39 @@ def run_engine(args, rank, world, local):
     eng.step(1, K)
     J = eng.flux(0)
     t_e2e = time.perf_counter() - t0
-    t_e2e = D.max(t_e2e)
     info = eng.info()
+    buffered_e2e = info["dft_buffered"]
     h2d = eps.size * eps.itemsize + fw.size * 8
     d2h = J.size * 8
 
-    # --- device-timed steady state: the DFT sample ring is empty when the
-    # clock starts (the flux read flushes it), and the samples of the timed
-    # steps are all accumulated inside the clock (a block that fills during
-    # the steps, the rest by the flux read that ends them)
+    # --- device-timed steady state: the DFT buffer is empty when the clock
+    # starts; the flux read that ends the timed steps accumulates every timed
+    # sample (on the tensor-core path it adds the samples still buffered on
+    # the fly and leaves them buffered, so the share of their later commit is
+    # measured below and added to the timed region)
     it = K + 1
     eng.step(it, W)
     it += W
-    eng.flux(0)
+    eng.dft_commit()
     eng.sync()
     D.barrier()
     pr, cpath = start_clocks(local)
     eng.timing_start(per_kernel=True)
     eng.step(it, K)
     eng.flux(0)
-    reg_ms, kms, kn = eng.timing_read()
+    win_ms, kms, kn = eng.timing_read()
     clocks = stop_clocks(pr, cpath)
     it += K
-    reg_ms = D.max(reg_ms)
+    buffered = eng.info()["dft_buffered"]
+    commit_ms = 0.0
+    if buffered or buffered_e2e:
+        commit_ms, it = full_block_commit(eng, it, info["dft_block"], buffered)
+    reg_ms = D.max(win_ms + commit_ms * buffered / info["dft_block"])
+    t_e2e = D.max(t_e2e + commit_ms * 1e-3 * buffered_e2e / info["dft_block"])
     graph_line = None
     if args.graph:
         # the same steps replayed from captured graphs (per-kernel events off)
+        eng.dft_commit()
         eng.timing_start(per_kernel=False)
         eng.step(it, K)
         reg_g, _, _ = eng.timing_read()
@@ -292,10 +341,14 @@ def run_engine(args, rank, world, local):
     wl_name = w.name
     traffic, tsrc = ncu_traffic(dom, w.name + "_" + args.precision)
     # one fused timer per step spans its launches: the planes outside the UPML
-    # slabs and, concurrently, the slabs (one launch when no plane lies outside)
+    # slabs and, concurrently, the slabs (one launch when no plane lies outside);
+    # a commit is two launches (twiddles, block); a flux read on the tensor-core
+    # path three (twiddles of the buffered samples, the tile partials, their sum)
     fused_launches = 2 if p.pmlzf - 2 >= p.pmlzi + 1 else 1
-    launches = kn["update_e"] + kn["update_h"] + kn["tfsf"] + kn["dft_gather"] + kn["flux"] + \
-        kn["fused_eh"] * fused_launches + kn["dft_block"] * (2 if prec == iris.FP32 else 1)
+    dft_tc = prec == iris.FP32 and args.dft_kernel != iris.DFT_KERNEL_CUDA
+    flux_launches = (3 if buffered else 2) if dft_tc else 1
+    launches = kn["update_e"] + kn["update_h"] + kn["tfsf"] + kn["dft_gather"] + kn["flux"] * flux_launches + \
+        kn["fused_eh"] * fused_launches + kn["dft_block"] * 2
     value = world * cells * K / (reg_ms * 1e-3) / 1e9
     out = {
         "metric": METRIC,
@@ -333,9 +386,10 @@ def run_engine(args, rank, world, local):
                      "algorithmic_bytes_per_pass": db,
                      "min_bytes_per_pass": min_bytes,
                      "frac_of_min_bytes": round(min_bytes / dt_ / 1e9 / hbm, 4)},
+        "window_ms_per_step": round(win_ms / K, 4),
         "stencil_gcells": round(cells / ((t_e + t_h)) / 1e9, 3),
-        "dft": dft_accounting(info["dft_points"], w.nof, info["dft_block"], sc, kms["dft_block"] / K,
-                              kms["dft_gather"] / K),
+        "dft": dft_accounting(info["dft_points"], w.nof, info["dft_block"], sc, K, kms, kn, buffered,
+                              flux_points(info), commit_ms),
         "clocks": clocks,
         "material_setup_s": round(t_mat, 2),
     }
@@ -347,17 +401,39 @@ def run_engine(args, rank, world, local):
         out["fp64_plain"] = fp64_compare(iris, p, fw, eps, cells, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(w, info["dft_points"], args.cpu_sample_steps)
+    if args.workload == 3 and not args.grid and not args.no_batch and prec == iris.FP32:
+        # the batched form (256 uneven cells) on the same GPU(s), same steps and warm-up
+        bt = guarded(measure_batch, iris, args, rank, world, local, K, W, D)
+        keys = ("value", "unit", "ms_per_step", "steps", "config", "e2e", "gpu_launches", "kernels_ms_per_step",
+                "window_ms_per_step", "dft_commit", "roofline", "stencil_gcells", "clocks", "error")
+        out["batch"] = {k: bt[k] for k in keys if k in bt}
+    if args.workload == 3 and not args.grid and not args.no_configs and world == 1:
+        # the other named workloads, each through the public API on this GPU
+        out["configs0_tiny"] = guarded(measure_tiny, iris, local)
+        out["configs1_slit"] = guarded(measure_slit, iris, local)
+        out["configs4_adjoint"] = guarded(measure_adjoint, iris, local, args.adjoint_fd_voxels)
     D.close()
     return out
 
 
 def run_batch(args, rank, world, local):
+    """The batched workload as its own bench line (--workload 4)."""
+    iris = importlib.import_module(PKG)
+    D = Dist(world)
+    out = measure_batch(iris, args, rank, world, local, args.steps, args.warmup, D,
+                        loop_sample=args.loop_sample if rank == 0 and world == 1 else 0)
+    D.close()
+    return out
+
+
+def measure_batch(iris, args, rank, world, local, K, W, D, loop_sample=0):
     """The batched workload: 256 independent Bloch cells of uneven size (seed+i per cell),
     FP32 fields, FP64 DFT at 128 frequencies on the reflection and transmission
-    planes, all cells stepped by one launch per operator."""
-    iris = importlib.import_module(PKG)
+    planes, all cells stepped by one launch per operator.  Timing as for the
+    single engine: the DFT buffer empty when the clock starts, K steps and a
+    flux read, plus the share of the buffered samples' later commit (one full
+    block's commit, measured after the timed steps)."""
     cfg = importlib.import_module(PKG + ".configs")
-    D = Dist(world)
     ncells = args.cells
     ws = cfg.batch_cells(ncells, seed=1000 * rank, nof=128)
     d = tempfile.mkdtemp(prefix="iris_batch_")
@@ -370,7 +446,6 @@ def run_batch(args, rank, world, local):
         mats.append(cfg.binary_pattern_material(w))
     t_mat = time.perf_counter() - t
     cells = sum(w.cells for w in ws)
-    K, W = args.steps, args.warmup
     D.barrier()
     t0 = time.perf_counter()
     b = iris.Batch(params, fw, precision=iris.FP32, dft_faces=iris.DFT_Z, device=local)
@@ -383,18 +458,32 @@ def run_batch(args, rank, world, local):
         tile, tune_ms = b.tune(reps=2)
     b.step(1, K)
     J = [b.flux(i) for i in range(ncells)]
-    t_e2e = D.max(time.perf_counter() - t0)
+    t_e2e = time.perf_counter() - t0
     info = b.info()
-    b.step(K + 1, W)
-    b.flux(0)  # the sample ring empty when the clock starts, every timed sample accumulated inside it
+    buffered_e2e = info["dft_buffered"]
+    kb = info["dft_block"]
+    it = K + 1
+    b.step(it, W)
+    it += W
+    b.dft_commit()
     D.barrier()
     pr, cpath = start_clocks(local)
     b.timing_start(per_kernel=True)
-    b.step(K + W + 1, K)
+    b.step(it, K)
     b.flux(0)
-    reg_ms, kms, kn = b.timing_read()
+    win_ms, kms, kn = b.timing_read()
     clocks = stop_clocks(pr, cpath)
-    reg_ms = D.max(reg_ms)
+    it += K
+    buffered = b.info()["dft_buffered"]
+    commit_ms = 0.0
+    if buffered or buffered_e2e:
+        b.timing_start(per_kernel=True)
+        b.step(it, kb - buffered)
+        _, kc, nc = b.timing_read()
+        assert nc["dft_block"] == 1 and b.info()["dft_buffered"] == 0, nc
+        commit_ms = kc["dft_block"]
+    reg_ms = D.max(win_ms + commit_ms * buffered / kb)
+    t_e2e = D.max(t_e2e + commit_ms * 1e-3 * buffered_e2e / kb)
     b.close()
     hbm, src = peaks()
     # algorithmic bytes of one E and one H pass over every cell (as for one engine)
@@ -413,8 +502,9 @@ def run_batch(args, rank, world, local):
         t_h = kms["update_h"] / kn["update_h"] * 1e-3
         dom, db, dt_ = ("update_h", hb, t_h) if t_h >= t_e else ("update_e", eb, t_e)
     achieved = db / dt_ / 1e9
+    flux_launches = 3 if buffered else 2
     launches = info["launches_per_pass"] * (kn["update_e"] + kn["update_h"]) + kn["fused_eh"] + \
-        sum(kn[k] for k in ("tfsf", "dft_gather", "flux")) + 2 * kn["dft_block"]
+        kn["tfsf"] + kn["dft_gather"] + kn["flux"] * flux_launches + 2 * kn["dft_block"]
     value = world * cells * K / (reg_ms * 1e-3) / 1e9
     h2d = sum(m.size * 16 for m in mats)
     out = {
@@ -423,7 +513,7 @@ def run_batch(args, rank, world, local):
         "dtype": "c64 fields (fp32), fp64 incident field and DFT accumulation",
         "data": "synthetic (seeded binary eps patterns, numpy PCG64 seed+i per cell)",
         "config": {"workload": f"batch of {ncells} uneven Bloch cells", "grid_cells": cells,
-                   "nof": 128, "dft_points": info["dft_points"], "dft_block": info["dft_block"],
+                   "nof": 128, "dft_points": info["dft_points"], "dft_block": kb,
                    "dft_faces": "z planes (reflection, transmission)", "tile": list(tile),
                    "tune_ms_per_eh_pass": {"_".join(map(str, k)) if isinstance(k[0], str) else "x".join(map(str, k)):
                                            round(v, 3) for k, v in tune_ms.items()},
@@ -435,15 +525,17 @@ def run_batch(args, rank, world, local):
                     ncells, K)},
         "gpu_launches": int(launches),
         "kernels_ms_per_step": {k: round(v / K, 4) for k, v in kms.items()},
+        "window_ms_per_step": round(win_ms / K, 4),
+        "dft_commit": {"block_samples": kb, "ms": round(commit_ms, 3), "samples_left_buffered": buffered,
+                       "share_ms_in_value": round(commit_ms * buffered / kb, 4)},
         "roofline": {"kernel": "batch_" + dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
                      "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_source": src, "traffic": None,
                      "algorithmic_bytes_per_pass": db},
         "stencil_gcells": round(cells / (t_e + t_h) / 1e9, 3),
         "clocks": clocks, "material_setup_s": round(t_mat, 2),
     }
-    if rank == 0 and world == 1 and args.loop_sample:
-        out["loop_plain"] = loop_plain(iris, ws, params, mats, fw, local, args.loop_sample, steps=16)
-    D.close()
+    if loop_sample:
+        out["loop_plain"] = loop_plain(iris, ws, params, mats, fw, local, loop_sample, steps=16)
     return out
 
 
@@ -587,27 +679,162 @@ def loop_plain(iris, ws, params, mats, fw, local, nsample, steps):
 def tr_error(iris, p, fw, eps, local):
     """FP32 against FP64 over the whole run (texit steps): R = J5/(J5+J6) and
     T = J6/(J5+J6) of box 1 per wavelength, their largest absolute
-    differences.  The FP64 engine stands for the FP64 oracle (the parity
-    tests hold it within 1e-12 of the oracle); z-plane DFTs only."""
-    out = {}
+    differences, and each precision's device time.  The FP64 engine stands
+    for the FP64 oracle (tests/test_gpu_slit.py holds it within 1e-12 of the
+    oracle on this grid); z-plane DFTs only (all T/R needs)."""
+    out, cells = {}, p.nx * p.ny * p.nz
     for prec in (iris.FP64, iris.FP32):
         q = p.copy()
         q.dft_faces = iris.DFT_Z
         e = iris.Engine(q, fw, precision=prec, device=local)
         e.set_material(eps)
         t0 = time.perf_counter()
+        e.timing_start(per_kernel=False)
         e.step(1, p.texit)
         J = e.flux(0)
-        out[prec] = (iris.tr_normalise(J[4], J[5]), time.perf_counter() - t0)
+        ms, _, _ = e.timing_read()
+        out[prec] = (iris.tr_normalise(J[4], J[5]), time.perf_counter() - t0, ms)
         e.close()
-    (r64, t64), s64 = out[iris.FP64]
-    (r32, t32), s32 = out[iris.FP32]
-    return {"steps": p.texit, "nof": p.nof, "R_max_abs_err": float(np.max(np.abs(r32 - r64))),
+    (r64, t64), s64, ms64 = out[iris.FP64]
+    (r32, t32), s32, ms32 = out[iris.FP32]
+    return {"grid": [p.nx, p.ny, p.nz], "steps": p.texit, "nof": p.nof,
+            "R_max_abs_err": float(np.max(np.abs(r32 - r64))),
             "T_max_abs_err": float(np.max(np.abs(t32 - t64))),
             "R_rel_err": float(np.max(np.abs(r32 - r64)) / np.max(np.abs(r64))),
             "T_rel_err": float(np.max(np.abs(t32 - t64)) / np.max(np.abs(t64))),
+            "fp64_gcells": round(cells * p.texit / (ms64 * 1e-3) / 1e9, 3),
+            "fp32_gcells": round(cells * p.texit / (ms32 * 1e-3) / 1e9, 3),
+            "device_ms": {"fp64": round(ms64, 1), "fp32": round(ms32, 1)},
             "wall_s": {"fp64": round(s64, 2), "fp32": round(s32, 2)},
-            "note": "FP32 (fused pass, tensor-core DFT) against FP64 over the full run, per spectrum"}
+            "note": ("FP32 (fused pass, tensor-core DFT) against FP64 over the full run, per spectrum; its state "
+                     "(75 MB) lives in the 129 MB L2, so no HBM roofline applies")}
+
+
+def guarded(fn, *a, **k):
+    """A sub-measurement of the default line: its result, or its error (the
+    main line stands either way)."""
+    try:
+        return fn(*a, **k)
+    except Exception as e:  # noqa: BLE001
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def measure_slit(iris, local):
+    """configs[1]: the 256x4x768 slit array, FP32 against FP64 over its 8000 steps."""
+    cfg = importlib.import_module(PKG + ".configs")
+    w = cfg.workload(2)
+    path = cfg.write_input(os.path.join(tempfile.mkdtemp(prefix="iris_slit_"), "inputFDTD.dat"), w)
+    p, fw, _ = iris.setparam(path)
+    p.device = local
+    return tr_error(iris, p, fw, cfg.slit_material(w), local)
+
+
+def measure_tiny(iris, local):
+    """configs[0]: the 4x4x512 FP64 slab, DFT of the z = 30 and z = 480 planes at
+    200 frequencies, 4000 steps, stepped by the persistent kernel (one
+    cooperative launch per span of steps); the same run through the split
+    passes replayed from CUDA graphs, which must give the same spectra bit
+    for bit; and the reference's 3D DFT over every face pair for scale."""
+    cfg = importlib.import_module(PKG + ".configs")
+    w = cfg.workload(1)
+    path = cfg.write_input(os.path.join(tempfile.mkdtemp(prefix="iris_tiny_"), "inputFDTD.dat"), w)
+    p, fw, _ = iris.setparam(path)
+    p.device = local
+    cells, N = w.cells, p.texit
+    res = {}
+    for name, stencil, graph, faces in (("persistent", iris.STENCIL_PERSISTENT, False, iris.DFT_Z),
+                                        ("split_graphs", iris.STENCIL_SPLIT, True, iris.DFT_Z),
+                                        ("persistent_all_faces", iris.STENCIL_PERSISTENT, False, iris.DFT_ALL)):
+        q = p.copy()
+        q.dft_faces = faces
+        e = iris.Engine(q, fw, precision=iris.FP64, device=local, stencil=stencil, graph=graph)
+        e.step(1, 8)  # modules loaded, graphs captured before the clock
+        e.flux(0)
+        e.close()
+        t0 = time.perf_counter()
+        e = iris.Engine(q, fw, precision=iris.FP64, device=local, stencil=stencil, graph=graph)
+        e.timing_start(per_kernel=False)
+        e.step(1, N)
+        J = e.flux(0)
+        ms, _, _ = e.timing_read()
+        wall = time.perf_counter() - t0
+        e.close()
+        res[name] = (J, ms, wall)
+    J0, ms0, wall0 = res["persistent"]
+    Jg, msg, _ = res["split_graphs"]
+    Ja, msa, _ = res["persistent_all_faces"]
+    R, T = iris.tr_normalise(J0[4], J0[5])
+    return {"workload": "slab_4x4x512_fp64", "grid": [w.nx, w.ny, w.nz], "steps": N, "nof": p.nof,
+            "dft_faces": "z planes 30 and 480", "value": round(cells * N / (ms0 * 1e-3) / 1e9, 4),
+            "unit": "Gcell/s", "ms_per_step": round(ms0 / N, 5), "dtype": "c128 (fp64)",
+            "e2e": {"value": round(cells * N / wall0 / 1e9, 4), "unit": "Gcell/s",
+                    "what": "iris_create + %d steps + iris_flux to host" % N},
+            "split_graphs_ms_per_step": round(msg / N, 5),
+            "speedup_vs_split_graphs": round(msg / ms0, 2),
+            "spectra_bitwise_equal_to_split": bool(np.array_equal(J0, Jg)),
+            "all_faces_ms_per_step": round(msa / N, 5),
+            "T_at_first_and_last_frequency": [float(T[0]), float(T[-1])],
+            "note": ("launch-bound: 8192 cells a step; the reference's 3D DFT over every face pair "
+                     "(43488 points x 200 frequencies) is FP64-ALU-bound instead")}
+
+
+def measure_adjoint(iris, local, fd_voxels=64):
+    """configs[4]: dL/d eps over the 128x128x32 design region of the 160x160x512
+    cell, FP32 forward and adjoint over 6000 steps with checkpoints every 256;
+    the gradient against the FP64 adjoint, and against central differences
+    (h = 1e-3) of the FP64 forward along a seeded +-1 direction over
+    fd_voxels seeded voxels (one directional derivative: two FP64 solves)."""
+    cfg = importlib.import_module(PKG + ".configs")
+    w = cfg.workload(5)
+    ex = w.extra
+    design = (ex["x0"], ex["x1"], ex["y0"], ex["y1"], w.hi, w.hi + w.dh - 1)
+    eps_inv = cfg.design_region_material(w, seed=0).real
+    path = cfg.write_input(os.path.join(tempfile.mkdtemp(prefix="iris_adj_"), "inputFDTD.dat"), w)
+    p, fw, _ = iris.setparam(path)
+    p.device = local
+    N, cells = w.nsteps, w.cells
+    eta = eps_inv[1:-1, design[2]:design[3] + 1, design[0]:design[1] + 1].copy()
+
+    def solve(precision):
+        adj = iris.Adjoint(p, fw, design, checkpoint_every=256, precision=precision, device=local)
+        adj.set_material(eps_inv)
+        t0 = time.perf_counter()
+        L, _ = adj.forward(N)
+        g = adj.backward()
+        return adj, L, -g * eta ** 2, adj.timing(), time.perf_counter() - t0
+
+    a32, L32, g32, tm32, wall32 = solve(iris.FP32)
+    a32.close()
+    a64, L64, g64, tm64, _ = solve(iris.FP64)
+    fwd, bwd = tm32["forward_ms"], tm32["recompute_ms"] + tm32["adjoint_ms"]
+    r = np.random.default_rng(0)
+    idx = r.choice(eta.size, fd_voxels, replace=False)
+    v = np.zeros(eta.size)
+    v[idx] = r.choice([-1.0, 1.0], fd_voxels)
+    v = v.reshape(eta.shape)
+    h = 1e-3
+    Ls = []
+    for sgn in (1, -1):
+        a64.set_design(1.0 / (1.0 / eta + sgn * h * v))
+        Ls.append(a64.forward(N)[0])
+    a64.close()
+    fd = (Ls[0] - Ls[1]) / (2 * h)
+    d32, d64 = float(np.sum(g32 * v)), float(np.sum(g64 * v))
+    return {"workload": f"{w.name} gradient", "grid": [w.nx, w.ny, w.nz], "design_region": list(design),
+            "steps": N, "nof": w.nof, "checkpoint_every": 256,
+            "value": round(cells * N / ((fwd + bwd) * 1e-3) / 1e9, 3), "unit": "Gcell/s",
+            "value_is": "grid cell-updates of the forward solve / device time of forward + backward (FP32)",
+            "forward_gcells": round(cells * N / (fwd * 1e-3) / 1e9, 3),
+            "forward_ms": round(fwd, 1), "backward_ms": round(bwd, 1),
+            "gradient_cost_vs_forward": round(bwd / fwd, 3),
+            "e2e_wall_s": round(wall32, 2),
+            "grad_rel_err_fp32_vs_fp64": float(np.max(np.abs(g32 - g64)) / np.max(np.abs(g64))),
+            "L_rel_err_fp32_vs_fp64": abs(L32 - L64) / abs(L64),
+            "fd_check": {"voxels": fd_voxels, "h": h, "direction": "seeded +-1 on the voxels, 0 elsewhere",
+                         "fd_fp64": fd, "adjoint_fp64": d64, "adjoint_fp32": d32,
+                         "rel_err_fp64": abs(d64 - fd) / abs(fd), "rel_err_fp32": abs(d32 - fd) / abs(fd)},
+            "fp64_forward_ms": round(tm64["forward_ms"], 1),
+            "fp64_backward_ms": round(tm64["recompute_ms"] + tm64["adjoint_ms"], 1)}
 
 
 def fp64_compare(iris, p, fw, eps, cells, local, K=32, W=3):
@@ -628,21 +855,41 @@ def fp64_compare(iris, p, fw, eps, cells, local, K=32, W=3):
             "note": "same workload, FP64 fields and DFT (parity mode), per step incl. one DFT block of 32"}
 
 
+def column(w, side):
+    """A side x side column of workload w: all of z (the same UPML, source,
+    structure layer, DFT planes and frequencies), the DFT box across the
+    column, the Bloch phase per period scaled to the column's width.  w
+    itself when it is no wider."""
+    cfg = importlib.import_module(PKG + ".configs")
+    nx, ny = min(side, w.nx), min(side, w.ny)
+    if (nx, ny) == (w.nx, w.ny):
+        return w
+    extra = dict(w.extra)
+    structure = w.structure
+    if structure == "spheres":
+        extra["nspheres"] = 4
+    elif structure == "design":
+        structure = "slab"
+    dx = int(round(w.dx * nx / w.nx)) if w.dx else 0
+    return cfg.Workload(f"{w.name}_column_{nx}x{ny}", nx, ny, w.nz, w.pmlzi, w.pmlzf, w.hi, w.dh, w.eps_bbox, dx,
+                        w.tfsf_zi, (1, nx, 1, ny, w.box[4], w.box[5]), w.nof, w.nsteps, w.eps1, w.eps3,
+                        w.akx * nx / w.nx, w.aky * ny / w.ny, structure, extra)
+
+
 def cpu_sample(w, side, threads, steps, warm=1):
-    """Oracle on a side x side column of the workload (all z, same source, UPML
-    and DFT frequencies): seconds per cell-step (everything but the DFT) and
-    per DFT point-frequency-step."""
+    """Oracle on a side x side column of workload w (see column()): seconds per
+    cell-step (everything but the DFT) and per DFT point-frequency-step."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import iris_oracle as O
     cfg = importlib.import_module(PKG + ".configs")
-    ws = cfg.workload(3, nx=side, ny=side, box=(1, side, 1, side, w.box[4], w.box[5]))
-    ws.extra = dict(ws.extra, nspheres=4)
+    ws = column(w, side)
     d = tempfile.mkdtemp(prefix="iris_cpu_")
     path = cfg.write_input(os.path.join(d, "inputFDTD.dat"), ws)
     op = O.setparam(path)
-    o = O.Oracle(op, ak=(complex(0.3 * math.pi * side), 0j, 0j), threads=threads)
-    o.set_eps_inv(cfg.spheres_material(ws))
-    o.run_timed(1, warm)
+    o = O.Oracle(op, ak=(complex(ws.akx), complex(ws.aky), 0j), threads=threads)
+    o.set_eps_inv(cfg.material(ws))
+    if warm:
+        o.run_timed(1, warm)
     td, tr = o.run_timed(1 + warm, steps)
     npts = o.total_points()
     o.close()
@@ -723,9 +970,15 @@ def run_reference(args, rank, world):
     wall = time.perf_counter() - t0
     t_step = t_cell * cells + t_pf * full_points * w.nof
     v = cells / t_step / 1e9
-    sample = (f"oracle (C++ FP64 restatement of the Fortran path, OpenMP {threads} threads) on a {side}x{side}x{w.nz} "
-              f"column for {args.steps} steps ({wall:.1f} s), per-cell and per-DFT-point costs scaled to the "
-              f"{w.nx}x{w.ny}x{w.nz} grid with {full_points} DFT points x {w.nof} frequencies")
+    extrapolated = ws is not w or cells_all is not None
+    if extrapolated:
+        sample = (f"oracle (C++ FP64 restatement of the Fortran path, OpenMP {threads} threads) run on a "
+                  f"{ws.nx}x{ws.ny}x{ws.nz} column of {w.name} for {args.steps} steps ({wall:.1f} s); its measured "
+                  f"cost per cell-step and per DFT point-frequency-step scaled to the {cells} cells and "
+                  f"{full_points} DFT points x {w.nof} frequencies of the workload (a model, not a run of it)")
+    else:
+        sample = (f"oracle (C++ FP64 restatement of the Fortran path, OpenMP {threads} threads) run on the whole "
+                  f"{w.nx}x{w.ny}x{w.nz} workload for {args.steps} steps ({wall:.1f} s)")
     return {
         "metric": METRIC, "impl": "reference", "value": round(v, 6), "unit": "Gcell/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 1),
@@ -735,7 +988,11 @@ def run_reference(args, rank, world):
                                 if args.workload == 4 else w.name),
                    "grid": [w.nx, w.ny, w.nz], "grid_cells": cells, "nof": w.nof},
         "cpu_baseline": {"value": round(v, 6), "unit": "Gcell/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "extrapolated": extrapolated,
+                         "column": [ws.nx, ws.ny, ws.nz],
+                         "seconds_per_cell_step": t_cell, "seconds_per_point_frequency_step": t_pf,
+                         "timed_seconds": round(wall, 3)},
+        "extrapolated": extrapolated,
         "e2e": {"value": round(v, 6), "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -750,6 +1007,11 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="default workload: skip the batched-form sub-measurement")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="default workload: skip the configs[0], [1] and [4] sub-measurements")
+    ap.add_argument("--adjoint-fd-voxels", type=int, default=64,
+                    help="default line: voxels of the adjoint's directional finite-difference check")
     ap.add_argument("--cpu-sample-steps", type=int, default=192)
     ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="run the workload resized to this grid (profiling cases)")

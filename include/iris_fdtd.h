@@ -58,6 +58,12 @@ extern "C" {
  * CUDA context stay usable.  No memory is touched but the engine's
  * error word.                                                          */
 #define IRIS_OP_WAIT_CHECK 5
+/* The same for the persistent kernel's grid barrier: a cooperative launch of
+ * two CTAs in which one never arrives; the other waits with the persistent
+ * kernel's limit divided by 2^arg (arg 0..30), gives up and records it.
+ * IRIS_ETIMEOUT; the engine stays usable.  Engines stepping with the
+ * persistent kernel only.                                              */
+#define IRIS_OP_BARRIER_CHECK 6
 
 /* ---- field selectors (iris_get_field / iris_set_field) --------------- */
 #define IRIS_E 0
@@ -142,8 +148,9 @@ typedef struct iris_params {
 #define IRIS_DFT_Z 1
 
 /* ---- stencil variants (iris_params.stencil) -------------------------- */
-/* default: the fused pass in IRIS_FP32 (the faster variant on GB300), the
- * split passes in IRIS_FP64                                               */
+/* default: the persistent kernel on small grids, else the fused pass in
+ * IRIS_FP32 (the faster variant on GB300) and the split passes in
+ * IRIS_FP64                                                               */
 #define IRIS_STENCIL_DEFAULT 0
 /* separate in-place E and H passes (18 complex values per cell per step)  */
 #define IRIS_STENCIL_SPLIT 1
@@ -154,6 +161,12 @@ typedef struct iris_params {
  * copies, z-marching tiles; IRIS_FP32 with a real material (a complex
  * material steps with the split passes)                                   */
 #define IRIS_STENCIL_STREAM 3
+/* small grids: one cooperative launch runs a span of whole steps (E, H,
+ * TF/SF, DFT sample) with grid-wide barriers between the passes; the split
+ * passes' arithmetic, so the same results bit for bit.  The default for
+ * grids of at most IRIS_PERSISTENT_MAX_CELLS cells in both precisions     */
+#define IRIS_STENCIL_PERSISTENT 4
+#define IRIS_PERSISTENT_MAX_CELLS 65536
 
 typedef struct iris_engine iris_engine;
 
@@ -215,9 +228,19 @@ int iris_sync(iris_engine* eng);
  * Poynting flux per face of box 1 or 2 (box = 0 or 1), J[6][nof], face-
  * major: the Jabs array of scattering_fourier_out
  * (code/dataprocess.f90:243-277), eps0*Q/(2 dt) included.  Returns
- * IRIS_ENAN if any value is not finite.
+ * IRIS_ENAN if any value is not finite.  Every sample taken so far counts;
+ * in IRIS_FP32 mode (tensor-core DFT) the samples still buffered are added
+ * on the fly and stay buffered, so a flux read changes no state.
  */
 int iris_flux(iris_engine* eng, int box, double* J);
+
+/*
+ * Accumulate the DFT samples still buffered into fdata now (the engine
+ * otherwise does so when its buffer of dft_block samples is full, and
+ * before iris_get_fdata).  The running sum of scattering_fourier
+ * (code/dataprocess.f90:143-147) is the same either way.
+ */
+int iris_dft_commit(iris_engine* eng);
 
 /*
  * Append one output block to <box>_scatt1..6.dat and <box>_scatt.dat in
@@ -230,12 +253,29 @@ int iris_get_field(iris_engine* eng, int which, double* re, double* im);
 int iris_set_field(iris_engine* eng, int which, const double* re, const double* im);
 
 /*
+ * The same in the reference's own storage: c is the complex(8) array
+ * e(3, 0:nx+1, 0:ny+1, 0:nz+1) or h(...) of code/main.f90:166-167 (and of
+ * driver()'s e_cur, h_cur, code/driver.f90:301-302) as interleaved
+ * (re, im) doubles (C99 double _Complex, Fortran complex(c_double_complex)),
+ * 6*(nx+2)*(ny+2)*(nz+2) doubles.  A Fortran host passes its arrays
+ * directly: the engine converts on the device, a few z planes at a time
+ * through a staging buffer of at most 64 MB (or one plane), so no host copy
+ * of the field is made.
+ */
+int iris_get_field_c(iris_engine* eng, int which, double* c);
+int iris_set_field_c(iris_engine* eng, int which, const double* c);
+
+/*
  * UPML auxiliaries d (which = 0) or b (which = 1) of slab 0 (z in
  * [1,pmlzi]) or slab 1 (z in [pmlzf,nz]) in the reference layout
  * (3,1:nx,1:ny,slab) (code/driver.f90:177-188), re/im arrays.
  */
 int iris_get_pml(iris_engine* eng, int which, int slab, double* re, double* im);
 int iris_set_pml(iris_engine* eng, int which, int slab, const double* re, const double* im);
+/* The same as complex(8) arrays (3,1:nx,1:ny,slab planes), interleaved
+ * (re, im) doubles, converted on the device like iris_get_field_c. */
+int iris_get_pml_c(iris_engine* eng, int which, int slab, double* c);
+int iris_set_pml_c(iris_engine* eng, int which, int slab, const double* c);
 
 /*
  * One plane of E or H extracted on the device, for the SDL snapshots of
@@ -281,7 +321,8 @@ int iris_run_input(const char* dir, int precision);
 #define IRIS_KC_FLUX 5   /* flux reduction                                */
 #define IRIS_KC_FUSED 6  /* fused E+H pass (TF/SF and the DFT sample      */
                          /* follow as their own kernels)                  */
-#define IRIS_NKC 7
+#define IRIS_KC_PERSIST 7 /* persistent kernel: a span of whole steps     */
+#define IRIS_NKC 8
 
 /*
  * Start a timed region on the engine's stream: records a start event and,
@@ -297,7 +338,8 @@ int iris_timing(iris_engine* eng, int enable);
 int iris_timing_read(iris_engine* eng, double* region_ms, double* kernel_ms, long* launches);
 /* Sizes: info[0] DFT sample points, [1] DFT block length K, [2] bytes per
  * stored complex value, [3] elements per field component, [4] complex
- * material flag, [5] number of DFT boxes. */
+ * material flag, [5] number of DFT boxes, [6] DFT samples buffered and not
+ * yet accumulated into fdata (info: 7 entries). */
 int iris_info(const iris_engine* eng, long* info);
 
 /* ---- batched form ------------------------------------------------------ */
@@ -319,6 +361,8 @@ int iris_batch_set_material(iris_batch* b, int cell, const double* eps_inv_re, c
 int iris_batch_step(iris_batch* b, int it0, int nsteps);
 /* iris_flux (box 1) of one cell. */
 int iris_batch_flux(iris_batch* b, int cell, double* J);
+/* iris_dft_commit for every cell (they share one sample buffer). */
+int iris_batch_dft_commit(iris_batch* b);
 /* iris_get_field of one cell. */
 int iris_batch_get_field(iris_batch* b, int cell, int which, double* re, double* im);
 /*
@@ -342,7 +386,8 @@ int iris_batch_timing(iris_batch* b, int enable);
 int iris_batch_timing_read(iris_batch* b, double* region_ms, double* kernel_ms, long* launches);
 /* info[0] cells, [1] total grid cells, [2] DFT points, [3] DFT block K,
  * [4] tile index, [5] work items per pass, [6] kernel launches per E or H
- * pass, or per fused pass (info: 7 entries). */
+ * pass, or per fused pass, [7] DFT samples buffered and not yet accumulated
+ * (info: 8 entries). */
 int iris_batch_info(const iris_batch* b, long* info);
 
 /* ---- adjoint (gradient) form ------------------------------------------- */
@@ -420,11 +465,18 @@ int iris_adjoint_timing(const iris_adjoint* a, double* ms);
  * nk*nof above that are rejected with IRIS_EINVAL (split the block).  The
  * first call on each device looks up that array's device address (a
  * one-time set-up per device, made with the caller's current device); make
- * that first call before any stream capture.  Every call reuses the same
- * array and overwrites the entries it uses, so nothing needs clearing, but
- * calls whose kernels overlap on the GPU (different streams, no ordering)
- * race on it.  Returns before the kernels finish; errors of the launches
- * are reported, errors of their execution surface at the next sync.
+ * that first call before any stream capture.  The address is kept for the
+ * life of the process: it does not survive cudaDeviceReset or the teardown
+ * of the device's primary context, after which this entry point must not be
+ * called again in that process.  Every call reuses the same array and
+ * overwrites the entries it uses, so nothing needs clearing, but calls whose
+ * kernels overlap on the GPU (different streams, no ordering) race on it.
+ * samples and fw must be 8-byte aligned and fdata 16-byte aligned.  Every
+ * argument is checked before any CUDA call, so a refused call touches no
+ * device.  A CUDA error still pending from earlier work on the calling
+ * thread is returned as IRIS_ECUDA (with its text) and nothing is launched.
+ * Returns before the kernels finish; errors of the launches are reported,
+ * errors of their execution surface at the next sync.
  */
 #define IRIS_NOALLOC_MAX_TWIDDLES 65536
 int iris_dft_block_noalloc(const void* samples, int nk, long npts, int t0, int t_step,

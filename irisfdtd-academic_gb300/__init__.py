@@ -34,10 +34,11 @@ from . import native
 from .native import IrisError, IrisParams, build, check, lib
 
 FP64, FP32 = 0, 1
-STENCIL_DEFAULT, STENCIL_SPLIT, STENCIL_FUSED, STENCIL_STREAM = 0, 1, 2, 3
+STENCIL_DEFAULT, STENCIL_SPLIT, STENCIL_FUSED, STENCIL_STREAM, STENCIL_PERSISTENT = 0, 1, 2, 3, 4
+PERSISTENT_MAX_CELLS = 65536
 DFT_KERNEL_AUTO, DFT_KERNEL_CUDA, DFT_KERNEL_TENSOR = 0, 1, 2
 E, H = 0, 1
-OP_E, OP_H, OP_TFSF, OP_DFT, OP_WAIT_CHECK = 1, 2, 3, 4, 5
+OP_E, OP_H, OP_TFSF, OP_DFT, OP_WAIT_CHECK, OP_BARRIER_CHECK = 1, 2, 3, 4, 5, 6
 
 __all__ = [
     "FP64", "FP32", "E", "H", "IrisError", "IrisParams", "Engine", "build", "lib", "setparam",
@@ -202,6 +203,31 @@ class Engine:
         re, im = np.ascontiguousarray(a.real), np.ascontiguousarray(a.imag)
         check(self.L.iris_set_field(self.h, which, _dp(re), _dp(im)), "iris_set_field")
 
+    def get_field_c(self, which: int) -> np.ndarray:
+        """The field as the reference stores it, complex(8) (3, 0:nx+1, 0:ny+1,
+        0:nz+1) in Fortran order, i.e. a C-order complex128 array [z, y, x, c]
+        filled in place by the device (iris_get_field_c)."""
+        a = np.empty(self.field_shape, dtype=np.complex128)
+        check(self.L.iris_get_field_c(self.h, which, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+              "iris_get_field_c")
+        return a
+
+    def set_field_c(self, which: int, f: np.ndarray):
+        a = np.ascontiguousarray(np.asarray(f, dtype=np.complex128).reshape(self.field_shape))
+        check(self.L.iris_set_field_c(self.h, which, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+              "iris_set_field_c")
+
+    def get_pml_c(self, which: int, slab: int) -> np.ndarray:
+        a = np.empty(self.pml_shape(slab), dtype=np.complex128)
+        check(self.L.iris_get_pml_c(self.h, which, slab, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+              "iris_get_pml_c")
+        return a
+
+    def set_pml_c(self, which: int, slab: int, v: np.ndarray):
+        a = np.ascontiguousarray(np.asarray(v, dtype=np.complex128).reshape(self.pml_shape(slab)))
+        check(self.L.iris_set_pml_c(self.h, which, slab, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+              "iris_set_pml_c")
+
     def get_pml(self, which: int, slab: int) -> np.ndarray:
         n = int(np.prod(self.pml_shape(slab)))
         re, im = np.empty(n), np.empty(n)
@@ -223,7 +249,7 @@ class Engine:
         return (re + 1j * im).reshape(n2, n1, 3)
 
     # -- instrumentation
-    KERNELS = ("update_e", "update_h", "tfsf", "dft_gather", "dft_block", "flux", "fused_eh")
+    KERNELS = ("update_e", "update_h", "tfsf", "dft_gather", "dft_block", "flux", "fused_eh", "persistent")
 
     def timing_start(self, per_kernel: bool = True):
         check(self.L.iris_timing(self.h, 1 if per_kernel else 0), "iris_timing")
@@ -237,10 +263,14 @@ class Engine:
         return reg.value, dict(zip(self.KERNELS, ms.tolist())), dict(zip(self.KERNELS, list(n)))
 
     def info(self) -> dict:
-        a = (ctypes.c_long * 6)()
+        a = (ctypes.c_long * 7)()
         check(self.L.iris_info(self.h, a), "iris_info")
         return dict(dft_points=a[0], dft_block=a[1], bytes_per_complex=a[2], comp_elems=a[3],
-                    complex_material=bool(a[4]), boxes=a[5])
+                    complex_material=bool(a[4]), boxes=a[5], dft_buffered=a[6])
+
+    def dft_commit(self):
+        """Accumulate the buffered DFT samples into fdata now (iris_dft_commit)."""
+        check(self.L.iris_dft_commit(self.h), "iris_dft_commit")
 
     def get_fdata(self, box: int, j: int) -> np.ndarray:
         """emg(j)%fdata in the reference order as complex [iw, i_pts]."""
@@ -338,10 +368,14 @@ class Batch:
         return reg.value, dict(zip(Engine.KERNELS, ms.tolist())), dict(zip(Engine.KERNELS, list(n)))
 
     def info(self) -> dict:
-        a = (ctypes.c_long * 7)()
+        a = (ctypes.c_long * 8)()
         check(self.L.iris_batch_info(self.h, a), "iris_batch_info")
         return dict(cells=a[0], grid_cells=a[1], dft_points=a[2], dft_block=a[3], tile=TILES[a[4]], items=a[5],
-                    launches_per_pass=a[6])
+                    launches_per_pass=a[6], dft_buffered=a[7])
+
+    def dft_commit(self):
+        """Accumulate the buffered DFT samples of every cell (iris_batch_dft_commit)."""
+        check(self.L.iris_batch_dft_commit(self.h), "iris_batch_dft_commit")
 
 
 from .adjoint import Adjoint, design_objective  # noqa: E402

@@ -785,6 +785,16 @@ int iris_batch_info(const iris_batch* B, long* info) {
   info[4] = B->tile;
   info[5] = B->nitems;
   info[6] = B->tile >= FLAT ? (B->nitems_in > 0) + (B->nitems > B->nitems_in) : 1;  // per E, H or fused pass
+  info[7] = B->master->nslot;
+  return IRIS_OK;
+}
+
+int iris_batch_dft_commit(iris_batch* B) {
+  clear_error();
+  if (!B) return fail(IRIS_EINVAL, "null batch");
+  CK(cudaSetDevice(B->device));
+  dft_flush(B->master);
+  CK(cudaGetLastError());
   return IRIS_OK;
 }
 

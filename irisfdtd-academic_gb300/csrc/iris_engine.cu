@@ -805,6 +805,446 @@ __global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict_
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_NMAX) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Flux read without committing the sample ring (FP32 mode, tensor cores).
+//
+// For face f and frequency iw, the Jabs of scattering_fourier_out
+// (code/dataprocess.f90:246-277) over the accumulators as they would stand
+// after a commit of the nk samples still in the ring:
+//   J = sign * scale * sum_L Re(A_a conj A_b) - Re(A_c conj A_d),
+//   A_x(L, iw) = fdata[iw][p_x + L] + sum_k F_k(p_x + L) Wt_k(iw).
+// The pending sum is k_dft_tc's block GEMM (the same MMAs on the same
+// operands, so each A_x is the value a commit would store), but nothing is
+// written back: a flux read costs one read of the four flux components'
+// accumulators, and the ring is committed when it is full, as before.
+//
+// A CTA owns one tile of FL_LOC = 32 locations of one face and one frequency
+// group.  Its 128 A rows (the TMEM lanes) are the four flux components of the
+// 32 locations: row 32 c + l is component c (a, b, c, d) at location L0 + l.
+// The components' runs start at any point index, so samples come by plain
+// loads, one chunk ahead into registers; the B operands are bulk-copied per
+// chunk as in k_dft_tc.  The accumulators stream into registers one
+// 8-frequency chunk ahead, the first chunk before the MMAs are issued.
+// Epilogue: half w / 4 of the CTA takes the chunks w / 4, w / 4 + 2, ...;
+// warp w % 4 holds component w % 4 of the 32 locations, adds its TMEM
+// partials, and the four components meet in shared memory (over the dead
+// operand stages); warp c then forms the products of frequencies 2c and
+// 2c + 1 and sums its 32 locations with shuffles.  One partial per
+// (frequency, tile) goes to part[iw][tile]; k_flux_sum adds a face's tiles
+// in a fixed order, so the result does not depend on scheduling.
+constexpr int FL_LOC = 32;
+constexpr size_t FL_SMEM = 2 * TC_STAGE;
+static_assert((size_t)2 * 4 * 8 * FL_LOC * sizeof(double2) <= FL_SMEM, "epilogue exchange fits the stages");
+
+struct FluxTiles {
+  int start[7];  // first tile of face f; start[6]: tiles of the set
+};
+
+__device__ __forceinline__ long face_comp(const FluxFace& F, int c) {
+  return c == 0 ? F.pa : c == 1 ? F.pb : c == 2 ? F.pc : F.pd;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 2) k_flux_tc(const float2* __restrict__ S, long P, int nk,
+                                                           const float* __restrict__ Bt,
+                                                           const double2* __restrict__ fd, int nof, int ngroups,
+                                                           const FluxFace* __restrict__ faces, FluxTiles ft,
+                                                           double* __restrict__ part, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint64_t bar_in[2], bar_mma[2];
+  __shared__ uint32_t taddr_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = blockIdx.x % ngroups;
+  const int tile = blockIdx.x / ngroups;
+  int f = 0, fs = 0;  // the face holding this tile (start indices never decrease)
+#pragma unroll
+  for (int i = 1; i < 6; ++i)
+    if (tile >= ft.start[i]) {
+      f = i;
+      fs = ft.start[i];
+    }
+  const FluxFace F = faces[f];
+  const long L0 = (long)(tile - fs) * FL_LOC;
+  const int nl = (int)min((long)FL_LOC, F.n - L0);
+  const int nw = min(TC_NW, nof - g * TC_NW);
+  const int ncol = ((2 * nw + 15) / 16) * 16;
+  const int nch = (2 * nk + TC_KC - 1) / TC_KC;
+  const int nchk = (nw + 7) / 8;
+  const long per = (long)TC_BROWS * TC_KC;
+  const int ntiles = ft.start[6];
+  // split row of this thread (component rc at location rl) and its epilogue
+  // point (component q4 at location lane); -1 past the face's last location
+  const int row = tid & (TC_M - 1), half = tid >> 7;
+  const int rc = row >> 5, rl = row & 31;
+  const long rp = rl < nl ? face_comp(F, rc) + L0 + rl : -1;
+  const int q4 = warp & 3, hw = warp >> 2;
+  const long ep = lane < nl ? face_comp(F, q4) + L0 + lane : -1;
+  const double2* fdg = fd + (long)g * TC_NW * P;
+
+  auto load_fd = [&](int ch, double2* dst) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      dst[j] = (ep >= 0 && 8 * ch + j < nw) ? fdg[(long)(8 * ch + j) * P + ep] : make_double2(0.0, 0.0);
+  };
+  double2 fa[8], fb[8];
+  if (hw < nchk) load_fd(hw, fa);
+
+  bool bad = false;
+  uint32_t tmem = 0;
+  if (nk > 0) {
+    if (tid == 0) {
+      for (int s = 0; s < 2; ++s) {
+        mbar_init(&bar_in[s], 1);
+        mbar_init(&bar_mma[s], 1);
+      }
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&taddr_s)),
+                   "r"(TC_NMAX)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem = taddr_s;
+    const uint32_t idesc = tc_idesc(ncol);
+    const unsigned nb = (unsigned)(ncol * TC_KC * 4);
+    auto issue_b = [&](int c, int s) {
+      unsigned char* st = smem + s * TC_STAGE;
+      const float* src = Bt + ((long)(g * nch + c) * 2) * per;
+      mbar_expect_tx(&bar_in[s], 2 * nb);
+      fence_proxy_async();
+      bulk_g2s(st + 2 * TC_A_BYTES, src, nb, &bar_in[s]);
+      bulk_g2s(st + 2 * TC_A_BYTES + TC_B_BYTES, src + per, nb, &bar_in[s]);
+    };
+    // samples 4 half .. 4 half + 3 of chunk c at this thread's split row
+    auto load_s = [&](int c, float2* dst) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = c * (TC_KC / 2) + 4 * half + q;
+        dst[q] = (rp >= 0 && k < nk) ? S[(long)k * P + rp] : make_float2(0.f, 0.f);
+      }
+    };
+    float2 sv[4], sn[4] = {};
+    load_s(0, sv);
+    unsigned par_in = 0, par_mma = 0;
+    if (tid == 0) issue_b(0, 0);
+    for (int c = 0; c < nch; ++c) {
+      const int s = c & 1;
+      unsigned char* st = smem + s * TC_STAGE;
+      float* Ah = (float*)st;
+      float* Al = (float*)(st + TC_A_BYTES);
+      const float* Bh = (const float*)(st + 2 * TC_A_BYTES);
+      const float* Bl = (const float*)(st + 2 * TC_A_BYTES + TC_B_BYTES);
+      if (c + 1 < nch) {
+        // stage s^1 was last read by the MMAs of chunk c-1
+        if (c >= 1) {
+          bad |= !mbar_wait(&bar_mma[s ^ 1], (par_mma >> (s ^ 1)) & 1u, STREAM_WAIT_CYCLES);
+          par_mma ^= 1u << (s ^ 1);
+        }
+        if (tid == 0) issue_b(c + 1, s ^ 1);
+        load_s(c + 1, sn);
+      }
+      bad |= !mbar_wait(&bar_in[s], (par_in >> s) & 1u, STREAM_WAIT_CYCLES);
+      par_in ^= 1u << s;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int kq = 4 * half + 2 * q;
+        const float4 v = make_float4(sv[2 * q].x, sv[2 * q].y, sv[2 * q + 1].x, sv[2 * q + 1].y);
+        const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+        *(float4*)(Ah + tc_off(row, 2 * kq)) = h;
+        *(float4*)(Al + tc_off(row, 2 * kq)) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      }
+      fence_proxy_async();
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+        for (int ks = 0; ks < TC_KC / 8; ++ks) {
+          const uint64_t ah = tc_desc(Ah + 64 * ks), al = tc_desc(Al + 64 * ks);
+          const uint64_t bh = tc_desc(Bh + 64 * ks), bl = tc_desc(Bl + 64 * ks);
+          tc_mma(tmem, ah, bh, idesc, (c > 0 || ks > 0) ? 1 : 0);
+          tc_mma(tmem, ah, bl, idesc, 1);
+          tc_mma(tmem, al, bh, idesc, 1);
+        }
+        tc_commit(&bar_mma[s]);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) sv[q] = sn[q];
+    }
+    for (int c = max(0, nch - 2); c < nch; ++c) {
+      const int s = c & 1;
+      bad |= !mbar_wait(&bar_mma[s], (par_mma >> s) & 1u, STREAM_WAIT_CYCLES);
+      par_mma ^= 1u << s;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  // every MMA has completed: the operand stages hold the exchange now
+  const bool give_up = __syncthreads_or(bad);
+  if (give_up) {
+    if (tid == 0) atomicExch(err, 5);
+  } else {
+    double2* X = (double2*)smem + hw * (4 * 8 * FL_LOC);  // [component][frequency][location]
+    for (int ch = hw; ch < nchk; ch += 2) {
+      if (ch + 2 < nchk) load_fd(ch + 2, fb);
+      if (nk > 0) {
+        uint32_t r[16];
+        const uint32_t ta = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(16 * ch);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(ta)
+            : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          fa[j].x += (double)__uint_as_float(r[2 * j]);
+          fa[j].y += (double)__uint_as_float(r[2 * j + 1]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) X[(q4 * 8 + j) * FL_LOC + lane] = fa[j];
+      asm volatile("bar.sync %0, %1;" ::"r"(1 + hw), "r"(128) : "memory");
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj) {
+        const int j = 2 * q4 + jj;
+        double v = 0.0;
+        if (lane < nl) {
+          const double2 a = X[(0 * 8 + j) * FL_LOC + lane], b = X[(1 * 8 + j) * FL_LOC + lane];
+          const double2 c = X[(2 * 8 + j) * FL_LOC + lane], d = X[(3 * 8 + j) * FL_LOC + lane];
+          v = (a.x * b.x + a.y * b.y) - (c.x * d.x + c.y * d.y);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && 8 * ch + j < nw) part[(long)(g * TC_NW + 8 * ch + j) * ntiles + tile] = v;
+      }
+      asm volatile("bar.sync %0, %1;" ::"r"(1 + hw), "r"(128) : "memory");
+#pragma unroll
+      for (int j = 0; j < 8; ++j) fa[j] = fb[j];
+    }
+  }
+  if (nk > 0) {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_NMAX) : "memory");
+  }
+}
+
+// J[f][iw] = scale * sign * (sum of face f's tile partials, in tile order
+// within each thread, then a fixed tree).
+__global__ void __launch_bounds__(256) k_flux_sum(const double* __restrict__ part, FluxTiles ft,
+                                                  const FluxFace* __restrict__ faces, int nof, double scale,
+                                                  double* __restrict__ J) {
+  __shared__ double red[256];
+  const int iw = blockIdx.x, f = blockIdx.y;
+  const long ntiles = ft.start[6];
+  int t0 = 0, t1 = 0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+    if (i == f) {
+      t0 = ft.start[i];
+      t1 = ft.start[i + 1];
+    }
+  double s = 0.0;
+  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) s += part[(long)iw * ntiles + t];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) J[f * nof + iw] = scale * (faces[f].sign > 0 ? red[0] : -red[0]);
+}
+
+// Tiles of FL_LOC locations per face of one set of six flux faces.
+FluxTiles flux_tiles(const FluxFace* f6) {
+  FluxTiles ft{};
+  for (int f = 0; f < 6; ++f)
+    ft.start[f + 1] = ft.start[f] + (f6[f].active ? (int)((f6[f].n + FL_LOC - 1) / FL_LOC) : 0);
+  return ft;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent whole-step kernel for small grids (IRIS_STENCIL_PERSISTENT).
+//
+// On a grid of a few thousand cells each operator launch of a step costs a
+// few microseconds of launch latency for well under a microsecond of work.
+// k_tiny runs a span of steps in one cooperative launch (every CTA resident
+// at once): per step the E pass, the H pass, the TF/SF corrections and the
+// DFT sample, each a grid-stride loop over its cells with the split passes'
+// per-cell functions, separated by grid-wide barriers.  The arithmetic and
+// every value stored are the split passes', so the results are theirs bit
+// for bit.  The barrier is a counter and a generation word in global
+// memory; every wait is bounded (about a second): a CTA that gives up
+// records it (code 6) and returns, and so do the others at their next wait.
+
+struct GridBar {
+  unsigned count, gen;
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// All CTAs of the launch reach this point before any passes it; false when
+// the wait gave up.  gen: the generation this CTA waits to see advance
+// (thread 0's copy is the one used).
+__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned& gen, unsigned nblk, int* err,
+                                             long long limit = STREAM_WAIT_CYCLES) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    if (atomicAdd(&b->count, 1u) == nblk - 1) {
+      atomicExch(&b->count, 0u);
+      __threadfence();
+      atomicAdd(&b->gen, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (ld_acquire_u32(&b->gen) == gen)
+        if (clock64() - t0 > limit) {
+          ok = 0;
+          break;
+        }
+    }
+    __threadfence();
+    gen += 1;
+    if (!ok) atomicExch(err, 6);
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <typename T> struct TinyArgs {
+  FieldArgs<T> a;
+  SrcArgs s;
+  const Seg* segs;
+  int nsegs;
+  typename V2<T>::t* S;  // the DFT ring
+  long P;
+  int* tk;
+  int slot0;             // first free ring slot
+  int it0, n;            // steps it0 .. it0 + n - 1
+  int to_fourier, sample_fourier, dft;
+  GridBar* bar;
+  int* err;
+};
+
+constexpr int TINY_THREADS = 128;
+
+// IRIS_OP_BARRIER_CHECK: a cooperative launch of two CTAs in which the second
+// returns without arriving, so the first waits at the grid barrier with the
+// persistent kernel's limit divided by 2^shift, gives up and records it.
+__global__ void k_barrier_check(GridBar* bar, int* err, int shift) {
+  unsigned gen = 0;
+  if (blockIdx.x != 0) return;
+  if (threadIdx.x == 0) gen = ld_acquire_u32(&bar->gen);
+  grid_barrier(bar, gen, 2, err, STREAM_WAIT_CYCLES >> shift);
+}
+
+template <typename T, bool CEPS> __global__ void __launch_bounds__(TINY_THREADS) k_tiny(TinyArgs<T> A) {
+  using V = typename V2<T>::t;
+  const Geo g = A.a.g;
+  const long nxy = (long)g.nx * g.ny, ncell = nxy * g.nz;
+  const long gt = (long)blockIdx.x * blockDim.x + threadIdx.x, gs = (long)gridDim.x * blockDim.x;
+  const long tf_items = (long)(g.nx + 2) * ((g.ny + 2 + TFSF_YCH - 1) / TFSF_YCH);
+  unsigned gen = 0;
+  if (threadIdx.x == 0) gen = ld_acquire_u32(&A.bar->gen);
+  int slot = A.slot0;
+  for (int i = 0; i < A.n; ++i) {
+    const int it = A.it0 + i;
+    for (long c = gt; c < ncell; c += gs) {
+      const int z = (int)(c / nxy) + 1, r = (int)(c % nxy);
+      e_split_cell<T, CEPS>(A.a, r % g.nx + 1, r / g.nx + 1, z);
+    }
+    if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
+    for (long c = gt; c < ncell; c += gs) {
+      const int z = (int)(c / nxy) + 1, r = (int)(c % nxy);
+      h_split_cell<T>(A.a, r % g.nx + 1, r / g.nx + 1, z);
+    }
+    if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
+    if (A.s.variant != 0) {
+      // the columns k_tfsf covers: ix in [0, nx+1], rows in chunks of TFSF_YCH
+      for (long w = gt; w < tf_items; w += gs) {
+        const int ix = (int)(w % (g.nx + 2)), y0 = (int)(w / (g.nx + 2)) * TFSF_YCH;
+        tfsf_column<T>(A.a.e, A.a.h, g, A.s, it, ix, y0, min(y0 + TFSF_YCH - 1, g.ny + 1));
+      }
+      if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
+    }
+    if (A.dft && it >= A.to_fourier && it % A.sample_fourier == 0) {
+      V* dst = A.S + (long)slot * A.P;
+      for (int k = 0; k < A.nsegs; ++k) {
+        const Seg sg = A.segs[k];
+        const V* src = sg.field < 3 ? A.a.e + sg.field * g.comp : A.a.h + (sg.field - 3) * g.comp;
+        const long n = (long)sg.nu * sg.nv;
+        for (long L = gt; L < n; L += gs) {
+          const long v = L / sg.nu, u = L - v * sg.nu;
+          dst[sg.p0 + L] = src[sg.src + u * sg.su + v * sg.sv];
+        }
+      }
+      if (gt == 0) A.tk[slot] = it + 1 - A.to_fourier;
+      ++slot;
+      // the next step's E pass overwrites what was just sampled
+      if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Field transfer in the reference's own layout, complex(8) (3, 0:nx+1,
+// 0:ny+1, 0:nz+1) (UPML: (3, 1:nx, 1:ny, planes)), a chunk of z planes at a
+// time through a device staging buffer: the host array is read or written
+// in place, with no host copy of the field.  Element t of a chunk is
+// component t % 3 of location t / 3, x fastest.  pc: component stride of
+// the device arrays; ox, oy: the first x and y (0 for fields with ghosts, 1
+// for the UPML slabs); at(x, y, z): storage index.
+struct XferMap {
+  Geo g;       // fields: the engine geometry
+  long pc;     // component stride
+  int nx, ny;  // extents of x and y in the host layout
+  int ox, oy;  // first x, y of the host layout
+  int pml;     // 1: UPML slab indexing ((z ny + y-1) nx + x-1)
+  __device__ __forceinline__ long at(int x, int y, int z) const {
+    return pml ? ((long)z * (ny) + (y - 1)) * (long)nx + (x - 1) : g.at(x, y, z);
+  }
+};
+
+template <typename T>
+__global__ void k_pack(const typename V2<T>::t* __restrict__ f, XferMap m, int z0, long n, double2* __restrict__ out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int c = (int)(t % 3);
+  long r = t / 3;
+  const int x = (int)(r % m.nx) + m.ox;
+  r /= m.nx;
+  const int y = (int)(r % m.ny) + m.oy, z = z0 + (int)(r / m.ny);
+  const typename V2<T>::t v = f[c * m.pc + m.at(x, y, z)];
+  out[t] = make_double2((double)v.x, (double)v.y);
+}
+
+template <typename T>
+__global__ void k_unpack(typename V2<T>::t* __restrict__ f, XferMap m, int z0, long n, const double2* __restrict__ in) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int c = (int)(t % 3);
+  long r = t / 3;
+  const int x = (int)(r % m.nx) + m.ox;
+  r /= m.nx;
+  const int y = (int)(r % m.ny) + m.oy, z = z0 + (int)(r / m.ny);
+  const double2 v = in[t];
+  typename V2<T>::t w;
+  w.x = (T)v.x;
+  w.y = (T)v.y;
+  f[c * m.pc + m.at(x, y, z)] = w;
+}
+
 // One plane of a field (SDL snapshots): out[(i2 * n1 + i1) * 3 + k].
 template <typename T>
 __global__ void k_plane(const typename V2<T>::t* __restrict__ f, Geo g, int axis, int index, int lo1, int n1, int lo2,
@@ -1022,7 +1462,7 @@ int validate(const iris_params& p) {
       if (lo < 1 || hi > n[a] || lo > hi) return bad("DFT box planes must satisfy 1 <= lo <= hi <= n on every axis");
     }
   if (p.precision != IRIS_FP64 && p.precision != IRIS_FP32) return bad("precision must be IRIS_FP64 or IRIS_FP32");
-  if (p.stencil < IRIS_STENCIL_DEFAULT || p.stencil > IRIS_STENCIL_STREAM) return bad("unknown stencil variant");
+  if (p.stencil < IRIS_STENCIL_DEFAULT || p.stencil > IRIS_STENCIL_PERSISTENT) return bad("unknown stencil variant");
   if (p.stencil == IRIS_STENCIL_FUSED && p.precision != IRIS_FP32) return bad("the fused stencil is FP32 only");
   if (p.stencil == IRIS_STENCIL_STREAM && p.precision != IRIS_FP32) return bad("the streamed stencil is FP32 only");
   if (p.dft_faces != IRIS_DFT_ALL && p.dft_faces != IRIS_DFT_Z) return bad("dft_faces must be IRIS_DFT_ALL or IRIS_DFT_Z");
@@ -1180,6 +1620,49 @@ template <typename T> int step_t(iris_engine* E, int it0, int n) {
     launch_tfsf<T>(E, it);
     if (it >= p.to_fourier && it % p.sample_fourier == 0) dft_sample<T>(E, it + 1 - p.to_fourier);
     ++it;
+  }
+  CK(cudaGetLastError());
+  return IRIS_OK;
+}
+
+// Steps it0 .. it0+n-1 with the persistent kernel: spans that end where the
+// DFT ring fills (its commit runs between launches) or after 1024 steps.
+template <typename T> int step_persist(iris_engine* E, int it0, int n) {
+  const iris_params& p = E->p;
+  int it = it0;
+  while (it < it0 + n) {
+    int span = 0, samples = 0;
+    while (it + span < it0 + n && span < 1024) {
+      const int t = it + span;
+      ++span;
+      if (E->P > 0 && t >= p.to_fourier && t % p.sample_fourier == 0 && ++samples + E->nslot == E->K) break;
+    }
+    TinyArgs<T> A{};
+    A.a = field_args<T>(E);
+    A.s = E->src;
+    A.segs = E->d_segs;
+    A.nsegs = (int)E->segs.size();
+    A.S = (typename V2<T>::t*)E->S;
+    A.P = E->P;
+    A.tk = E->d_tk;
+    A.slot0 = E->nslot;
+    A.it0 = it;
+    A.n = span;
+    A.to_fourier = p.to_fourier;
+    A.sample_fourier = p.sample_fourier;
+    A.dft = E->P > 0 ? 1 : 0;
+    A.bar = (GridBar*)E->d_bar;
+    A.err = E->d_err;
+    void* args[] = {&A};
+    {
+      KTimer tm(E, IRIS_KC_PERSIST);
+      CK(cudaMemsetAsync(E->d_bar, 0, sizeof(GridBar), E->st));
+      const void* k = E->eps_complex ? (const void*)k_tiny<T, true> : (const void*)k_tiny<T, false>;
+      CK(cudaLaunchCooperativeKernel(k, dim3(E->persist_blocks), dim3(TINY_THREADS), args, 0, E->st));
+    }
+    E->nslot += samples;
+    if (E->nslot == E->K) dft_flush(E);
+    it += span;
   }
   CK(cudaGetLastError());
   return IRIS_OK;
@@ -1419,10 +1902,15 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
   if (E->prec == IRIS_FP32) CK(cudaMalloc(&E->d_wt, sizeof(float2) * (size_t)E->K * p.nof));
   if (E->prec == IRIS_FP64) CK(cudaMalloc(&E->d_wt64, sizeof(double2) * (size_t)E->K * p.nof));
   E->dft_tc = E->prec == IRIS_FP32 && p.dft_kernel != IRIS_DFT_KERNEL_CUDA;
+  E->flux_faces.assign(faces, faces + nfaces);
   if (E->dft_tc) {
     const int ng = (p.nof + TC_NW - 1) / TC_NW, nch = (2 * E->K + TC_KC - 1) / TC_KC;
     CK(cudaMalloc(&E->d_wtc, sizeof(float) * (size_t)ng * nch * 2 * TC_BROWS * TC_KC));
     CK(cudaFuncSetAttribute(k_dft_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+    CK(cudaFuncSetAttribute(k_flux_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FL_SMEM));
+    long maxt = 1;
+    for (int s = 0; s + 6 <= nfaces; s += 6) maxt = std::max(maxt, (long)flux_tiles(faces + s).start[6]);
+    CK(cudaMalloc(&E->d_part, sizeof(double) * (size_t)maxt * p.nof));
   }
   if (!E->segs.empty()) {
     CK(cudaMalloc(&E->d_segs, sizeof(Seg) * E->segs.size()));
@@ -1438,7 +1926,7 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
 void free_engine(iris_engine* E) {
   void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
                   E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J, E->e2, E->h2, E->pml_d2[0],
-                  E->pml_d2[1], E->d_err, E->d_it, E->d_wtc, E->d_wt64};
+                  E->pml_d2[1], E->d_err, E->d_it, E->d_wtc, E->d_wt64, E->d_part, E->d_bar, E->d_stage};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (E->h_J) cudaFreeHost(E->h_J);
@@ -1561,9 +2049,36 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
   E->src = make_src(p);
   E->tf_blk = dim3(64);
   E->tf_grd = dim3((p.nx + 2 + 63) / 64, (p.ny + 2 + TFSF_YCH - 1) / TFSF_YCH);
-  // FP32 steps with the fused E+H pass unless the split or streamed passes
-  // are asked for (FP64 always steps with the split passes)
-  E->fused = E->prec == IRIS_FP32 && (p.stencil == IRIS_STENCIL_FUSED || p.stencil == IRIS_STENCIL_DEFAULT);
+  // Small grids step with the persistent kernel (asked for, or by default up
+  // to IRIS_PERSISTENT_MAX_CELLS cells when the device runs cooperative
+  // launches); otherwise FP32 steps with the fused E+H pass unless the split
+  // or streamed passes are asked for (FP64 with the split passes).
+  {
+    int coop = 0, nsm = 0, occ = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, E->device);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E->device);
+    const long cells = (long)p.nx * p.ny * p.nz;
+    const bool want = !member && (p.stencil == IRIS_STENCIL_PERSISTENT ||
+                                  (p.stencil == IRIS_STENCIL_DEFAULT && cells <= IRIS_PERSISTENT_MAX_CELLS));
+    if (want && coop) {
+      const void* k = E->prec == IRIS_FP64 ? (const void*)k_tiny<double, false> : (const void*)k_tiny<float, false>;
+      const void* kc = E->prec == IRIS_FP64 ? (const void*)k_tiny<double, true> : (const void*)k_tiny<float, true>;
+      int o1 = 0, o2 = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k, TINY_THREADS, 0) == cudaSuccess &&
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, kc, TINY_THREADS, 0) == cudaSuccess)
+        occ = std::min(o1, o2);
+      // one CTA per SM at most (the FP64 pipes are per SM), no more than the cells need
+      const long need = (cells + TINY_THREADS - 1) / TINY_THREADS;
+      E->persist_blocks = (int)std::max(1L, std::min<long>(need, (long)nsm * std::min(occ, 1)));
+      E->persist = occ >= 1;
+    }
+    if (p.stencil == IRIS_STENCIL_PERSISTENT && !E->persist)
+      return bail(fail(IRIS_EINVAL, "the persistent stencil needs cooperative launches on this device"));
+    if (E->persist && cudaMalloc(&E->d_bar, 64) != cudaSuccess)
+      return bail(fail(IRIS_ENOMEM, "barrier allocation failed"));
+  }
+  E->fused = !E->persist && E->prec == IRIS_FP32 &&
+             (p.stencil == IRIS_STENCIL_FUSED || p.stencil == IRIS_STENCIL_DEFAULT);
   if (E->fused) {
     if (cudaMalloc(&E->e2, fbytes) != cudaSuccess || cudaMalloc(&E->h2, fbytes) != cudaSuccess)
       return bail(fail(IRIS_ENOMEM, "second field buffers: allocation failed"));
@@ -1639,15 +2154,37 @@ static int stream_status(iris_engine* E) {
   const char* what = h == 1   ? "a streamed E pass gave up waiting for its staged plane"
                      : h == 2 ? "a streamed H pass gave up waiting for its staged plane"
                      : h == 3 ? "the tensor-core DFT block gave up waiting"
+                     : h == 5 ? "the tensor-core flux read gave up waiting"
+                     : h == 6 ? "the persistent step kernel gave up at a grid barrier"
                               : "the wait check gave up (as it must)";
   return fail(IRIS_ETIMEOUT, what);
 }
 
+// The flux of one face set.  FP32 mode on the tensor cores: over the
+// accumulators plus the samples still in the ring, which stay there
+// (k_twiddle_tc for the pending samples, k_flux_tc, k_flux_sum).  Otherwise
+// the ring is committed first and k_flux reads the accumulators.
 int iris::read_flux(iris_engine* E, int set, double* J) {
   const iris_params& p = E->p;
-  dft_flush(E);
   const double scale = p.eps0 * p.Q / (2.0 * p.dt);
-  {
+  const FluxFace* f6 = E->flux_faces.data() + 6 * set;
+  const FluxTiles ft = flux_tiles(f6);
+  const int ng = (p.nof + TC_NW - 1) / TC_NW;
+  if (E->dft_tc && (long)ft.start[6] * ng <= 0x7fffffffL) {
+    KTimer tm(E, IRIS_KC_FLUX);
+    const int nk = E->nslot;
+    if (nk > 0) {
+      const int nch = (2 * nk + TC_KC - 1) / TC_KC;
+      const long nt = (long)ng * nch * TC_BROWS * TC_KC;
+      k_twiddle_tc<<<(unsigned)((nt + 255) / 256), 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, p.nof, p.dt, ng, nch,
+                                                                     E->d_wtc);
+    }
+    if (ft.start[6] > 0)
+      k_flux_tc<<<(unsigned)((long)ft.start[6] * ng), TC_THREADS, FL_SMEM, E->st>>>(
+          (const float2*)E->S, E->P, nk, E->d_wtc, E->fd, p.nof, ng, E->d_faces + 6 * set, ft, E->d_part, E->d_err);
+    k_flux_sum<<<dim3(p.nof, 6), 256, 0, E->st>>>(E->d_part, ft, E->d_faces + 6 * set, p.nof, scale, E->d_J);
+  } else {
+    dft_flush(E);
     KTimer tm(E, IRIS_KC_FLUX);
     k_flux<<<dim3(p.nof, 6), 256, 0, E->st>>>(E->fd, E->P, E->d_faces + 6 * set, p.nof, scale, E->d_J);
   }
@@ -1690,6 +2227,8 @@ int iris_step(iris_engine* E, int it0, int nsteps) {
   clear_error();
   if (!E || nsteps < 0) return fail(IRIS_EINVAL, "bad argument");
   CK(cudaSetDevice(E->device));
+  if (E->persist)
+    return E->prec == IRIS_FP64 ? step_persist<double>(E, it0, nsteps) : step_persist<float>(E, it0, nsteps);
   if (E->fused) return step_fused(E, it0, nsteps);
   return E->prec == IRIS_FP64 ? step_t<double>(E, it0, nsteps) : step_t<float>(E, it0, nsteps);
 }
@@ -1795,6 +2334,86 @@ static int pml_io(iris_engine* E, int which, int slab, double* re, double* im, c
     CK(cudaStreamSynchronize(E->st));
   }
   return IRIS_OK;
+}
+
+// Chunked transfer between the host array c (interleaved re, im doubles in
+// the host layout of m, planes z_first .. z_first + nplanes - 1) and the
+// device arrays dev (get: device to host; else host to device).
+static int xfer_c(iris_engine* E, void* dev, const XferMap& m, int z_first, int nplanes, double* c, bool get) {
+  const size_t per_plane = (size_t)3 * m.nx * m.ny * sizeof(double2);
+  const size_t cap = std::max<size_t>(per_plane, (size_t)64 << 20);
+  if (E->stage_bytes < std::min(cap, per_plane * nplanes)) {
+    if (E->d_stage) CK(cudaFree(E->d_stage));
+    E->d_stage = nullptr;
+    E->stage_bytes = std::min(cap, per_plane * nplanes);
+    CK(cudaMalloc(&E->d_stage, E->stage_bytes));
+  }
+  const int chunk = (int)std::max<size_t>(1, E->stage_bytes / per_plane);
+  for (int z0 = 0; z0 < nplanes; z0 += chunk) {
+    const int nz = std::min(chunk, nplanes - z0);
+    const long n = 3L * m.nx * m.ny * nz;
+    double* host = c + 2 * (size_t)3 * m.nx * m.ny * z0;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (get) {
+      if (E->prec == IRIS_FP64)
+        k_pack<double><<<blocks, 256, 0, E->st>>>((const double2*)dev, m, z_first + z0, n, (double2*)E->d_stage);
+      else
+        k_pack<float><<<blocks, 256, 0, E->st>>>((const float2*)dev, m, z_first + z0, n, (double2*)E->d_stage);
+      CK(cudaMemcpyAsync(host, E->d_stage, n * sizeof(double2), cudaMemcpyDeviceToHost, E->st));
+    } else {
+      CK(cudaMemcpyAsync(E->d_stage, host, n * sizeof(double2), cudaMemcpyHostToDevice, E->st));
+      if (E->prec == IRIS_FP64)
+        k_unpack<double><<<blocks, 256, 0, E->st>>>((double2*)dev, m, z_first + z0, n, (const double2*)E->d_stage);
+      else
+        k_unpack<float><<<blocks, 256, 0, E->st>>>((float2*)dev, m, z_first + z0, n, (const double2*)E->d_stage);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(E->st));
+  }
+  return IRIS_OK;
+}
+
+static int field_c(iris_engine* E, int which, double* c, bool get) {
+  if (!E || !c || (which != IRIS_E && which != IRIS_H)) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  XferMap m{};
+  m.g = E->g;
+  m.pc = E->g.comp;
+  m.nx = E->p.nx + 2;
+  m.ny = E->p.ny + 2;
+  return xfer_c(E, which == IRIS_E ? E->e : E->h, m, 0, E->p.nz + 2, c, get);
+}
+
+static int pml_c(iris_engine* E, int which, int slab, double* c, bool get) {
+  if (!E || !c || (which != 0 && which != 1) || (slab != 0 && slab != 1)) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  XferMap m{};
+  m.pc = E->pcomp[slab];
+  m.nx = E->p.nx;
+  m.ny = E->p.ny;
+  m.ox = m.oy = 1;
+  m.pml = 1;
+  return xfer_c(E, which == 0 ? E->pml_d[slab] : E->pml_b[slab], m, 0, slab == 0 ? E->nbot : E->ntop, c, get);
+}
+
+int iris_get_field_c(iris_engine* E, int which, double* c) {
+  clear_error();
+  return field_c(E, which, c, true);
+}
+
+int iris_set_field_c(iris_engine* E, int which, const double* c) {
+  clear_error();
+  return field_c(E, which, const_cast<double*>(c), false);
+}
+
+int iris_get_pml_c(iris_engine* E, int which, int slab, double* c) {
+  clear_error();
+  return pml_c(E, which, slab, c, true);
+}
+
+int iris_set_pml_c(iris_engine* E, int which, int slab, const double* c) {
+  clear_error();
+  return pml_c(E, which, slab, const_cast<double*>(c), false);
 }
 
 int iris_get_pml(iris_engine* E, int which, int slab, double* re, double* im) {
@@ -1915,6 +2534,16 @@ int iris_info(const iris_engine* E, long* info) {
   info[3] = E->g.comp;
   info[4] = E->eps_complex ? 1 : 0;
   info[5] = E->nboxes;
+  info[6] = E->nslot;
+  return IRIS_OK;
+}
+
+int iris_dft_commit(iris_engine* E) {
+  clear_error();
+  if (!E) return fail(IRIS_EINVAL, "null engine");
+  CK(cudaSetDevice(E->device));
+  dft_flush(E);
+  CK(cudaGetLastError());
   return IRIS_OK;
 }
 
@@ -1936,6 +2565,16 @@ int iris_apply(iris_engine* E, int op, int arg) {
       if (arg < 0 || arg > 30) return fail(IRIS_EINVAL, "wait check: arg must be 0..30");
       k_wait_check<<<1, 32, 0, E->st>>>(E->d_err, arg);
       break;
+    case IRIS_OP_BARRIER_CHECK: {
+      if (arg < 0 || arg > 30) return fail(IRIS_EINVAL, "barrier check: arg must be 0..30");
+      if (!E->persist) return fail(IRIS_EINVAL, "barrier check: the engine does not step with the persistent kernel");
+      CK(cudaMemsetAsync(E->d_bar, 0, sizeof(GridBar), E->st));
+      GridBar* bar = (GridBar*)E->d_bar;
+      int* err = E->d_err;
+      void* args[] = {&bar, &err, &arg};
+      CK(cudaLaunchCooperativeKernel((const void*)k_barrier_check, dim3(2), dim3(32), args, 0, E->st));
+      break;
+    }
     default: return fail(IRIS_EINVAL, "unknown operator");
   }
   CK(cudaGetLastError());
@@ -1969,8 +2608,13 @@ void* g_noalloc_addr[kNoallocMaxDevices] = {};
 extern "C" int iris_dft_block_noalloc(const void* samples, int nk, long npts, int t0, int t_step, const double* fw,
                                       int nof, double dt, void* fdata, void* stream) {
   clear_error();
+  // every argument check comes before the first CUDA call: a refused call
+  // touches no device
   if (!samples || !fw || !fdata) return fail(IRIS_EINVAL, "iris_dft_block_noalloc: null device pointer");
   if (nk < 1 || npts < 1 || nof < 1) return fail(IRIS_EINVAL, "iris_dft_block_noalloc: nk, npts and nof must be >= 1");
+  if ((uintptr_t)samples % 8 || (uintptr_t)fw % 8 || (uintptr_t)fdata % 16)
+    return fail(IRIS_EINVAL,
+                "iris_dft_block_noalloc: samples and fw must be 8-byte aligned, fdata 16-byte aligned");
   if ((long)nk * nof > IRIS_NOALLOC_MAX_TWIDDLES)
     return fail(IRIS_EINVAL, "iris_dft_block_noalloc: nk*nof = " + std::to_string((long)nk * nof) +
                                  " exceeds the static scratch of " + std::to_string(IRIS_NOALLOC_MAX_TWIDDLES) +
@@ -1981,6 +2625,12 @@ extern "C" int iris_dft_block_noalloc(const void* samples, int nk, long npts, in
   int dev = 0;
   CK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kNoallocMaxDevices) return fail(IRIS_EINVAL, "iris_dft_block_noalloc: device ordinal >= 64");
+  // an error left by earlier work on this thread is reported as such, not
+  // taken for this call's, and nothing is launched
+  const cudaError_t prior = cudaGetLastError();
+  if (prior != cudaSuccess)
+    return fail(IRIS_ECUDA, std::string("iris_dft_block_noalloc: a CUDA error from before this call was pending: ") +
+                                cudaGetErrorString(prior));
   void* wt = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);

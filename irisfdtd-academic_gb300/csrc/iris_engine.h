@@ -72,6 +72,10 @@ struct iris_engine {
   double2* d_wt64 = nullptr;  // FP64 mode twiddles of one block
   bool dft_tc = false;     // FP32 block accumulation on the tensor cores
   float* d_wtc = nullptr;  // its B operands (k_twiddle_tc)
+  // flux faces as uploaded to d_faces (6 per set), and the per-tile flux
+  // partials of the tensor-core flux read (tile count of the largest set x nof)
+  std::vector<iris::FluxFace> flux_faces;
+  double* d_part = nullptr;
   iris::FluxFace* d_faces = nullptr;
   double* d_J = nullptr;
   double* h_J = nullptr;
@@ -97,6 +101,14 @@ struct iris_engine {
   cudaGraphExec_t gexec = nullptr;
   int* d_it = nullptr;
   int dev_it = -1;
+  // persistent whole-step kernel (small grids): CTAs of its cooperative
+  // launch and its grid-barrier words
+  bool persist = false;
+  int persist_blocks = 0;
+  void* d_bar = nullptr;
+  // staging buffer of the complex(8) field transfers (allocated on first use)
+  void* d_stage = nullptr;
+  size_t stage_bytes = 0;
   // streamed split passes (FP32, real material); d_err: a kernel's give-up record
   bool stream = false;
   dim3 sgrd;

@@ -475,7 +475,9 @@ int sdl_output(const std::string& dir, const iris_params& p, const SdlParams& q,
           default: v = 0.0;
         }
       }
-      out[c] = v / norm;
+      // output = real(output)/SDLnorm (code/sdl.f90:363): rounded to REAL(4),
+      // divided in REAL(8), written as REAL(4) (:449-456)
+      out[c] = (double)(float)v / norm;
     }
   std::vector<float> rec;
   if (q.copy_flag) {
@@ -499,7 +501,11 @@ int sdl_output(const std::string& dir, const iris_params& p, const SdlParams& q,
 }
 
 // setSDL_FILE (code/sdl.f90:404-448) for one plane: E quantities from e (the
-// current E), H quantities from h (the H of the step before).
+// current E), H quantities from h (the H of the step before).  SDLField(4:6)
+// switch the H components on, but SDL_output takes the mode (and the name's
+// suffix) of component k from SDLField(k), the E entry (:140-153, :202-212);
+// with no mode there the name has no suffix and the values are left
+// unassigned by the reference (0 here).
 int sdl_files(const std::string& dir, const iris_params& p, const SdlParams& q, const SdlPlane& pl, int nos,
               const std::vector<double>& ere, const std::vector<double>& eim, const std::vector<double>& hre,
               const std::vector<double>& him) {
@@ -509,7 +515,7 @@ int sdl_files(const std::string& dir, const iris_params& p, const SdlParams& q, 
   for (int k = 0; k < 3 && !rc; ++k)
     if (q.field[k] >= 1) rc = sdl_output(dir, p, q, pl, nos, 1, k, q.field[k], false, ere, eim);
   for (int k = 0; k < 3 && !rc; ++k)
-    if (q.field[3 + k] >= 1) rc = sdl_output(dir, p, q, pl, nos, 2, k, q.field[3 + k], false, hre, him);
+    if (q.field[3 + k] >= 1) rc = sdl_output(dir, p, q, pl, nos, 2, k, q.field[k], false, hre, him);
   return rc;
 }
 
@@ -591,8 +597,10 @@ int run_main(const std::string& dir, int precision, bool loop = false) {
     it = next;
     if (output && sdl_on) {
       rc = get_planes(eng, IRIS_E, planes, ere, eim);
+      // the driver numbers the snapshot files nos + 1 (code/driver.f90:473-491)
       for (size_t i = 0; i < planes.size() && !rc; ++i)
-        rc = sdl_files(dir, p, sdl, planes[i], nos, ere[i], eim[i], sdl_h ? hre[i] : ere[i], sdl_h ? him[i] : eim[i]);
+        rc = sdl_files(dir, p, sdl, planes[i], nos + 1, ere[i], eim[i], sdl_h ? hre[i] : ere[i],
+                       sdl_h ? him[i] : eim[i]);
       if (rc) break;
     }
     if (it >= p.to_fourier && (it == p.to_fourier + p.no_downloads * nos || it == p.texit)) {

@@ -100,10 +100,11 @@ class IrisParams(ctypes.Structure):
 EXPORTS = [
     "iris_strerror", "iris_last_error", "iris_setparam", "iris_physconsts", "iris_frequencies",
     "iris_create", "iris_destroy", "iris_set_material", "iris_step", "iris_sync", "iris_flux",
-    "iris_write_scatt", "iris_get_field", "iris_set_field", "iris_get_pml", "iris_set_pml",
+    "iris_dft_commit", "iris_write_scatt", "iris_get_field", "iris_set_field", "iris_get_pml", "iris_set_pml",
+    "iris_get_field_c", "iris_set_field_c", "iris_get_pml_c", "iris_set_pml_c",
     "iris_get_fdata", "iris_get_plane", "iris_apply", "iris_run_input", "iris_timing", "iris_timing_read", "iris_info",
     "iris_dft_block_noalloc", "iris_batch_create", "iris_batch_destroy", "iris_batch_set_material",
-    "iris_batch_step", "iris_batch_flux", "iris_batch_get_field", "iris_batch_tune", "iris_batch_set_tile",
+    "iris_batch_step", "iris_batch_flux", "iris_batch_dft_commit", "iris_batch_get_field", "iris_batch_tune", "iris_batch_set_tile",
     "iris_batch_timing", "iris_batch_timing_read", "iris_batch_info",
     "iris_adjoint_create", "iris_adjoint_destroy", "iris_adjoint_set_material", "iris_adjoint_set_design",
     "iris_adjoint_forward", "iris_adjoint_backward", "iris_adjoint_engine", "iris_adjoint_apply",
@@ -138,11 +139,16 @@ def lib():
     L.iris_step.argtypes = [vp, ip, ip]
     L.iris_sync.argtypes = [vp]
     L.iris_flux.argtypes = [vp, ip, dp]
+    L.iris_dft_commit.argtypes = [vp]
     L.iris_write_scatt.argtypes = [cp, ip, ip, ip, dp]
     L.iris_get_field.argtypes = [vp, ip, dp, dp]
     L.iris_set_field.argtypes = [vp, ip, dp, dp]
     L.iris_get_pml.argtypes = [vp, ip, ip, dp, dp]
     L.iris_set_pml.argtypes = [vp, ip, ip, dp, dp]
+    L.iris_get_field_c.argtypes = [vp, ip, dp]
+    L.iris_set_field_c.argtypes = [vp, ip, dp]
+    L.iris_get_pml_c.argtypes = [vp, ip, ip, dp]
+    L.iris_set_pml_c.argtypes = [vp, ip, ip, dp]
     L.iris_get_fdata.argtypes = [vp, ip, ip, dp, dp, ctypes.POINTER(ctypes.c_long)]
     L.iris_get_plane.argtypes = [vp, ip, ip, ip, ip, ip, ip, ip, dp, dp]
     L.iris_apply.argtypes = [vp, ip, ip]
@@ -158,6 +164,7 @@ def lib():
     L.iris_batch_set_material.argtypes = [vp, ip, dp, dp]
     L.iris_batch_step.argtypes = [vp, ip, ip]
     L.iris_batch_flux.argtypes = [vp, ip, dp]
+    L.iris_batch_dft_commit.argtypes = [vp]
     L.iris_batch_get_field.argtypes = [vp, ip, ip, dp, dp]
     L.iris_batch_tune.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int), dp]
     L.iris_batch_set_tile.argtypes = [vp, ip]

@@ -16,6 +16,12 @@ Python half of the CPU FP64 restatement of IrisFDTD-Academic's hot path:
 * ``tr_normalise``, ``wavelength_axis`` — irisfdtd_scatt.py:37-42 and
   IrisFDTD_scattering.py:111,143, checked bit for bit against fixtures the
   reference's own reader produced (tests/test_scatt_files.py).
+* ``setparam_sdl``, ``sdl_output``, ``sdl_snapshot`` — the field snapshots:
+  setparam_SDL (code/sdl.f90:365-400) with the SDLextended layers
+  (code/files.f90:291-320), SDL_output (code/sdl.f90:68-483) and the driver's
+  calls (code/driver.f90:468-494), from the oracle's own field arrays; the
+  files it writes are read back by the reference's reader in
+  tests/test_sdl_oracle.py.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 this module, as the checker or as the timed CPU baseline.  The product never
@@ -595,3 +601,179 @@ def tr_normalise(j5: np.ndarray, j6: np.ndarray):
 def wavelength_axis(lno: float, dlamda: float, nof: int) -> np.ndarray:
     """IrisFDTD_scattering.py:111,143: linspace(iwav, iwav + dlambda*nof, nof)."""
     return np.linspace(lno, lno + dlamda * nof, nof)
+
+
+# ---------------------------------------------------------------------------
+# SDL field snapshots (code/sdl.f90)
+
+@dataclass
+class SdlParams:
+    copy_flag: int = 0
+    copy_no: int = 1
+    xi: tuple = (0, 0, 0)
+    xf: tuple = (0, 0, 0)
+    yi: tuple = (0, 0, 0)
+    yf: tuple = (0, 0, 0)
+    zi: tuple = (0, 0, 0)
+    zf: tuple = (0, 0, 0)
+    module_e: int = 0     # SDLModuleE: 1 |E|, 2 |H|
+    field: tuple = (0, 0, 0, 0, 0, 0)  # SDLField(1:6): Ex Ey Ez Hx Hy Hz
+    delta: tuple = ((0,), (0,), (0,))  # SDL_deltaX/Y/Z (code/files.f90:291-320)
+
+
+def setparam_sdl(path: str) -> SdlParams:
+    """setparam_SDL (code/sdl.f90:365-400): after the "Time evolution options"
+    header, SDL_copy_flag and SDL_copy_no, the six rows xi, xf, yi, yf, zi, zf
+    (one value per plane orientation), SDLModuleE and SDLField(1:6); then the
+    optional "Extra parameters-SDLextended" section (code/files.f90:291-320)."""
+    with open(path, "r", encoding="latin-1") as fh:
+        lines = fh.read().splitlines()
+    R = _Records(lines)
+
+    def seek(header):
+        R.rewind()
+        while not R.eof():
+            if _as_str(R.read(1)[0]) == header:
+                return True
+        return False
+
+    if not seek("Time evolution options"):
+        raise ValueError("no Time evolution options")
+    q = SdlParams()
+    a, b = R.read(2)
+    q.copy_flag, q.copy_no = _as_int(a), _as_int(b)
+    rows = [tuple(_as_int(t) for t in R.read(3)) for _ in range(6)]
+    q.xi, q.xf, q.yi, q.yf, q.zi, q.zf = rows
+    q.module_e = _as_int(R.read(1)[0])
+    q.field = tuple(_as_int(R.read(1)[0]) for _ in range(6))
+    if seek("Extra parameters-SDLextended"):
+        n = [_as_int(t) for t in R.read(3)]
+        q.delta = tuple(tuple(_as_int(R.read(1)[0]) for _ in range(n[a])) for a in range(3))
+    return q
+
+
+def inttoascii(n: int) -> str:
+    """inttoASCII (code/common.f90:40-101): the decimal digits of 0 <= n < 100000."""
+    if not 0 <= n < 100000:
+        raise ValueError("inttoASCII covers 0..99999")
+    return str(n)
+
+
+def _f4(x):
+    """REAL(4) rounding of a REAL(8) value (Fortran real() without a kind)."""
+    return np.asarray(x, dtype=np.float64).astype(np.float32)
+
+
+def sdl_output(ino: int, comp: int, em: int, f: np.ndarray, q: SdlParams, layer: int, ranges, norm: float):
+    """SDL_output (code/sdl.f90:68-483) for one plane: returns the file name
+    and the record's REAL(4) values in file order (first index fastest).
+
+    f: the field (e or h) as complex [z, y, x, component] over 0..n+1.
+    comp: NoComponente (1..3, 0 for the modulus), em: 1 E, 2 H, 0 modulus.
+    layer: 1, 2, 3 (x, y, z = const); ranges: (index, lo1, hi1, lo2, hi2) with
+    the plane index and the two in-plane ranges (y, z / x, z / x, y).
+    norm: SDLnorm = q*Epump with the TF/SF source on (:358-362), 1 if 0.
+    The files of the "cluster" path are the ones this version writes
+    (RUTA_SDL = 'cluster', :373), named './X_SDL...' (:178-193, :207-215)."""
+    index, lo1, hi1, lo2, hi2 = ranges
+    # EXT and EXT2 (:115-156)
+    if em == 0:
+        ext = ".e"
+        ext2 = "_E" if q.module_e == 1 else "_H"
+    else:
+        ext = (".e" if em == 1 else ".h") + str(comp)
+        # select case(SDLField(NoComponente)) (:140-153, :202-212): the mode of
+        # an H component is read from the E entries SDLField(1:3) too; with no
+        # matching case the name has no suffix and Output stays unassigned
+        # (0 here)
+        mode = q.field[comp - 1]
+        ext2 = {1: "_R", 2: "_I", 3: "_MC", 4: "_MR", 5: "_MI"}.get(mode, "")
+    axis = "XYZ"[layer - 1]
+    one_layer = all(len(d) == 1 for d in q.delta)
+    if one_layer:
+        name = f"./{axis}_SDL{ext2}{inttoascii(ino)}{ext}"
+    else:
+        name = f"./{axis}_SDL{inttoascii(index)}layer{ext2}{inttoascii(ino)}{ext}"
+    # Output(i1, i2) over the plane (:195-330)
+    n1, n2 = hi1 - lo1 + 1, hi2 - lo2 + 1
+    out = np.zeros((n2, n1))  # [i2, i1]
+    for b in range(n2):
+        for a in range(n1):
+            u, v = lo1 + a, lo2 + b
+            x, y, z = (index, u, v) if layer == 1 else (u, index, v) if layer == 2 else (u, v, index)
+            if em == 0:
+                g = 0.0
+                for k in range(3):
+                    c = f[z, y, x, k]
+                    g = g + (c.conjugate() * c).real
+                out[b, a] = np.sqrt(abs(g)) if layer == 2 else np.sqrt(g)
+            else:
+                c = f[z, y, x, comp - 1]
+                if mode == 1:
+                    out[b, a] = c.real
+                elif mode == 2:
+                    out[b, a] = c.imag
+                elif mode == 3:
+                    out[b, a] = np.sqrt((c.conjugate() * c).real)
+                elif mode == 4:
+                    out[b, a] = np.sqrt(c.real * c.real)
+                elif mode == 5:
+                    out[b, a] = np.sqrt(c.imag * c.imag)
+    if norm == 0.0:
+        norm = 1.0
+    # output = real(output)/SDLnorm (:363): REAL(4) first, then the REAL(8)
+    # quotient, written as REAL(4) again (:449-456)
+    out = _f4(_f4(out).astype(np.float64) / norm)
+    if not q.copy_flag:
+        return name, out.reshape(-1)
+    # the copies (:391-421): output_aux(ixo : SDL_copy_no*(ixf+1-ixo), iyo : ...)
+    # (both axes for z planes); this restatement covers lo1 = 1 (and lo2 = 1 for
+    # z planes), where every cell of output_aux is written
+    c2 = q.copy_no if layer == 3 else 1
+    if lo1 != 1 or (layer == 3 and lo2 != 1):
+        raise ValueError("copies are restated for planes starting at index 1")
+    aux = np.tile(out, (c2, q.copy_no))
+    return name, aux.reshape(-1)
+
+
+def sdl_snapshot(ino: int, e: np.ndarray, h_prev: np.ndarray, q: SdlParams, planes_on, norm: float) -> dict:
+    """The driver's snapshot at one output step (code/driver.f90:468-494): for
+    each plane orientation switched on and each extra layer, setSDL_FILE
+    (code/sdl.f90:404-448) with e_cur and h_prev; ino is the file number the
+    driver passes (nos + 1).  Returns {file name: REAL(4) values}."""
+    out = {}
+    for layer in (1, 2, 3):
+        if not planes_on[layer - 1]:
+            continue
+        j = layer - 1
+        for d in q.delta[j]:
+            if layer == 1:
+                r = (q.xi[j] + d, q.yi[j], q.yf[j], q.zi[j], q.zf[j])
+            elif layer == 2:
+                r = (q.yi[j] + d, q.xi[j], q.xf[j], q.zi[j], q.zf[j])
+            else:
+                r = (q.zi[j] + d, q.xi[j], q.xf[j], q.yi[j], q.yf[j])
+            if q.module_e == 1:
+                k, v = sdl_output(ino, 0, 0, e, q, layer, r, norm)
+                out[k] = v
+            if q.module_e == 2:
+                k, v = sdl_output(ino, 0, 0, h_prev, q, layer, r, norm)
+                out[k] = v
+            for c in (1, 2, 3):
+                if q.field[c - 1] >= 1:
+                    k, v = sdl_output(ino, c, 1, e, q, layer, r, norm)
+                    out[k] = v
+            for c in (1, 2, 3):
+                if q.field[c + 2] >= 1:
+                    k, v = sdl_output(ino, c, 2, h_prev, q, layer, r, norm)
+                    out[k] = v
+    return out
+
+
+def write_sdl_record(path: str, values: np.ndarray):
+    """One Fortran unformatted sequential record: a 4-byte length, the REAL(4)
+    values, the length again."""
+    v = np.asarray(values, dtype="<f4")
+    n = np.asarray([v.size * 4], dtype="<i4").tobytes()
+    with open(path, "wb") as fh:
+        fh.write(n + v.tobytes() + n)

@@ -73,4 +73,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_fixtures.py <path of the IrisFDTD-Academic checkout>")
+    main(sys.argv[1])

@@ -118,3 +118,22 @@ def test_c_client_links_and_fails_loudly_without_gpu(iris, tmp_path):
     except ImportError:
         gpu = False
     assert code == 0 if gpu else code in (-8, -3), lines
+
+
+def test_noalloc_refusals_touch_no_device(iris):
+    """iris_dft_block_noalloc checks every argument before any CUDA call:
+    null or misaligned pointers and blocks beyond the fixed scratch are
+    refused with IRIS_EINVAL (the addresses below are never dereferenced)."""
+    L = iris.lib()
+    a8, a16 = 0x10000, 0x20000
+    call = L.iris_dft_block_noalloc
+    assert call(None, 1, 1, 0, 1, a8, 1, 1.0, a16, None) == -1
+    assert b"null" in L.iris_last_error()
+    assert call(a8, 0, 1, 0, 1, a8, 1, 1.0, a16, None) == -1
+    assert call(a8 + 4, 1, 1, 0, 1, a8, 1, 1.0, a16, None) == -1
+    assert b"aligned" in L.iris_last_error()
+    assert call(a8, 1, 1, 0, 1, a8 + 2, 1, 1.0, a16, None) == -1
+    assert call(a8, 1, 1, 0, 1, a8, 1, 1.0, a16 + 8, None) == -1
+    assert b"aligned" in L.iris_last_error()
+    assert call(a8, 65537, 1, 0, 1, a8, 1, 1.0, a16, None) == -1
+    assert b"exceeds" in L.iris_last_error()

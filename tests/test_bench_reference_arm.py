@@ -53,13 +53,29 @@ def bench_module():
 
 
 def test_dft_accounting():
+    """The accumulator bytes charged are those of the commits and flux reads that
+    ran inside the timed steps, not a per-block average."""
     b = bench_module()
-    d = b.dft_accounting(1000, 300, 512, 8, 0.5, 0.25)
-    assert d["complex_macs_per_step"] == 300000 and d["ring_bytes_per_step"] == 8000
-    assert d["accumulator_bytes_per_step"] == round(2 * 1000 * 300 * 16 / 512)
-    assert abs(d["block_gbs"] - (d["accumulator_bytes_per_step"] + 8000) / 0.5e-3 / 1e9) < 0.1
-    assert abs(d["gather_gbs"] - 2 * 8000 / 0.25e-3 / 1e9) < 0.1
-    assert "block_gbs" not in b.dft_accounting(0, 300, 512, 8, 0.0, 0.0)
+    P, nof, kb, sc = 1200, 300, 512, 8
+    fp = P * 4 // 6
+    kn = {"dft_block": 0, "flux": 1, "dft_gather": 20}
+    kms = {"dft_block": 0.0, "flux": 2.0, "dft_gather": 0.5}
+    # 20 steps, no commit inside the window, one flux read over 20 buffered samples
+    d = b.dft_accounting(P, nof, kb, sc, 20, kms, kn, 20, fp, 40.0)
+    assert d["complex_macs_per_step"] == P * nof and d["ring_bytes_per_step"] == P * sc
+    assert d["commits_in_window"] == 0 and d["samples_left_buffered"] == 20
+    assert d["accumulator_bytes_per_step"] == round(fp * nof * 16 / 20)
+    assert "block_gbs" not in d
+    assert abs(d["flux_gbs"] - (fp * nof * 16 + 20 * fp * sc) / 2.0e-3 / 1e9) < 0.1
+    assert abs(d["gather_gbs"] - 2 * 20 * P * sc / 0.5e-3 / 1e9) < 0.1
+    assert d["commit"]["share_ms_in_value"] == round(40.0 * 20 / kb, 4)
+    # 512 steps: one commit of the whole block inside the window, nothing left buffered
+    kn = {"dft_block": 1, "flux": 1, "dft_gather": 512}
+    kms = {"dft_block": 30.0, "flux": 2.0, "dft_gather": 10.0}
+    d = b.dft_accounting(P, nof, kb, sc, 512, kms, kn, 0, fp, 0.0)
+    assert d["accumulator_bytes_per_step"] == round((2 * P * nof * 16 + fp * nof * 16) / 512)
+    assert abs(d["block_gbs"] - (2 * P * nof * 16 + 512 * P * sc) / 30.0e-3 / 1e9) < 0.1
+    assert "commit" not in d
 
 
 def test_cpu_baseline_keys():

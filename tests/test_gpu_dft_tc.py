@@ -10,6 +10,11 @@ FP64 oracle the tolerance is the FP32 mode's 1e-4.  Cases: every face pair in
 3D with 300 frequencies (three frequency groups, the last one partial), DFT
 blocks of 32 and 256 samples with a partial block flushed at the flux read,
 and a 2-D grid.
+
+The FP32 flux read on the tensor cores (k_flux_tc) adds the samples still
+buffered on the fly and leaves them buffered: it changes no state, and
+committing the buffer first gives the same spectra bit for bit (the pending
+sums are the same MMAs on the same operands).
 """
 import importlib
 import os
@@ -68,3 +73,34 @@ def test_tensor_dft_against_oracle(iris, oracle, tmp_path):
     Jo, _ = o.run(1, op.texit, max_out=len(output_steps(op)))
     assert rel_err(J, Jo) <= 1e-4
     assert rel_err(interior(e.get_field(iris.E), op), interior(o.get_field(o.E_CUR), op)) <= 1e-4
+
+
+@pytest.mark.parametrize("steps,block", [(1, 256), (13, 256), (90, 32), (64, 32)])
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_flux_read_leaves_buffer_and_equals_commit(iris, oracle, tmp_path, case, steps, block):
+    name, spec, nof, _ = case
+    w, op = make(oracle, tmp_path, spec, nof, steps + 10)
+    eps = cfg.spheres_material(w, seed=2)
+    p = engine_params_from_oracle(iris, op, precision=1, ak=(0.3 + 0j, 0j, 0j))
+    e = iris.Engine(p, op.fw, dft_block=block, dft_kernel=iris.DFT_KERNEL_TENSOR)
+    e.set_material(eps)
+    e.step(1, steps)
+    sampled = sum(1 for it in range(1, steps + 1) if it >= op.to_fourier and it % op.sample_fourier == 0)
+    n0 = e.info()["dft_buffered"]
+    assert n0 == sampled % block
+    J1 = e.flux(0)
+    assert e.info()["dft_buffered"] == n0
+    assert np.array_equal(e.flux(0), J1)  # a second read: same state, same bits
+    e.dft_commit()
+    assert e.info()["dft_buffered"] == 0
+    J2 = e.flux(0)
+    assert np.array_equal(J1, J2)
+    # the CUDA-core path commits before it reads: same spectra to FP32's partial-sum rounding
+    c = iris.Engine(p, op.fw, dft_block=block, dft_kernel=iris.DFT_KERNEL_CUDA)
+    c.set_material(eps)
+    c.step(1, steps)
+    assert rel_err(J1, c.flux(0)) <= 1e-5
+    # stepping on after a flux read: the buffer keeps filling and commits when full
+    e.step(steps + 1, 10)
+    c.step(steps + 1, 10)
+    assert rel_err(e.flux(0), c.flux(0)) <= 1e-5

@@ -133,16 +133,23 @@ def test_fused_rejected_in_fp64(iris, oracle, tmp_path):
 
 def test_stencil_selection(iris, oracle, tmp_path):
     """The per-kernel timers show which pass ran: fused by default in FP32
-    (one timer a step over its two concurrent launches: the planes outside
-    the UPML slabs and the slabs), split on request."""
-    w, op = make_case(oracle, tmp_path, (16, 8, 40, 6, 35, 15, 10, 4.0, 10, (1, 16, 1, 8, 8, 32)), 2)
-    for stencil, fused in ((0, True), (1, False), (2, True)):
+    above PERSISTENT_MAX_CELLS cells (one timer a step over its two
+    concurrent launches: the planes outside the UPML slabs and the slabs),
+    the persistent kernel by default at or below it (one launch for the five
+    steps), split, fused or persistent on request."""
+    small = make_case(oracle, tmp_path, (16, 8, 40, 6, 35, 15, 10, 4.0, 10, (1, 16, 1, 8, 8, 32)), 2)[1]
+    large = make_case(oracle, tmp_path, (48, 40, 40, 6, 35, 15, 10, 4.0, 10, (1, 48, 1, 40, 8, 32)), 2)[1]
+    assert 48 * 40 * 40 > iris.PERSISTENT_MAX_CELLS
+    for op, stencil, kind in ((large, 0, "fused"), (small, 0, "persistent"), (small, 1, "split"),
+                              (small, 2, "fused"), (small, 4, "persistent")):
         eng = iris.Engine(engine_params_from_oracle(iris, op, precision=1), op.fw, stencil=stencil)
         eng.timing_start()
         eng.step(1, 5)
         _, ms, n = eng.timing_read()
-        if fused:
-            assert n["fused_eh"] == 5 and n["update_e"] == 0 and n["update_h"] == 0
+        if kind == "fused":
+            assert n["fused_eh"] == 5 and n["update_e"] == 0 and n["update_h"] == 0 and n["persistent"] == 0
+        elif kind == "split":
+            assert n["fused_eh"] == 0 and n["update_e"] == 5 and n["update_h"] == 5 and n["persistent"] == 0
         else:
-            assert n["fused_eh"] == 0 and n["update_e"] == 5 and n["update_h"] == 5
+            assert n["persistent"] == 1 and n["fused_eh"] == 0 and n["update_e"] == 0 and n["update_h"] == 0
         eng.close()
