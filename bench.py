@@ -154,6 +154,10 @@ def ncu_traffic(kernel, workload):
     return None, None
 
 
+def cfg_mod():
+    return importlib.import_module(PKG + ".configs")
+
+
 def setup_workload(n, rank=0, grid=None, nof=None):
     cfg = importlib.import_module(PKG + ".configs")
     w = cfg.workload(n)
@@ -271,13 +275,21 @@ def run_engine(args, rank, world, local):
     t0 = time.perf_counter()
     eng = iris.Engine(p, fw, precision=prec, dft_block=args.dft_block, device=local, stencil=args.stencil,
                       graph=args.graph, dft_kernel=args.dft_kernel)
-    eng.set_material(eps)
+    if w.structure == "spheres":
+        # the geometry crosses the API as the spheres' parameters; the engine voxelises them
+        sph = cfg_mod().sphere_params(w)
+        eng.material_spheres(sph)
+        h2d = sph.nbytes + fw.size * 8
+        mat_what = "iris_material_spheres (%d spheres, voxelised on the device)" % sph.shape[0]
+    else:
+        eng.set_material(eps)
+        h2d = eps.size * eps.itemsize + fw.size * 8
+        mat_what = "iris_set_material (host eps)"
     eng.step(1, K)
     J = eng.flux(0)
     t_e2e = time.perf_counter() - t0
     info = eng.info()
     buffered_e2e = info["dft_buffered"]
-    h2d = eps.size * eps.itemsize + fw.size * 8
     d2h = J.size * 8
 
     # --- device-timed steady state: the DFT buffer is empty when the clock
@@ -376,8 +388,8 @@ def run_engine(args, rank, world, local):
         },
         "e2e": {"value": round(world * cells * K / t_e2e / 1e9, 3), "unit": "Gcell/s",
                 "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(d2h / K, 1),
-                "what": ("iris_create + iris_set_material (host eps) + %d steps + iris_flux to host, in a process "
-                         "whose CUDA context was started by a small engine before the clock" % K)},
+                "what": ("iris_create + %s + %d steps + iris_flux to host, in a process whose CUDA context was "
+                         "started by a small engine before the clock" % (mat_what, K))},
         "gpu_launches": int(launches),
         "kernels_ms_per_step": {k: round(v / K, 4) for k, v in kms.items()},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
@@ -437,20 +449,18 @@ def measure_batch(iris, args, rank, world, local, K, W, D, loop_sample=0):
     ncells = args.cells
     ws = cfg.batch_cells(ncells, seed=1000 * rank, nof=128)
     d = tempfile.mkdtemp(prefix="iris_batch_")
-    params, mats = [], []
-    t = time.perf_counter()
+    params = []
     for i, w in enumerate(ws):
         p, fw, _ = iris.setparam(cfg.write_input(os.path.join(d, f"c{i}.dat"), w))
         p.device = local
         params.append(p)
-        mats.append(cfg.binary_pattern_material(w))
-    t_mat = time.perf_counter() - t
     cells = sum(w.cells for w in ws)
     D.barrier()
     t0 = time.perf_counter()
     b = iris.Batch(params, fw, precision=iris.FP32, dft_faces=iris.DFT_Z, device=local)
-    for i, m in enumerate(mats):
-        b.set_material(i, m)
+    for i, w in enumerate(ws):
+        # each cell's binary pattern generated on the device from its seed and fill
+        b.material_pattern(i, cfg.pattern_seed(w), w.extra["fill"], 4.0, 1.0)
     if args.tile is not None:
         b.set_tile(args.tile)
         tile, tune_ms = iris.TILES[args.tile], {}
@@ -506,7 +516,7 @@ def measure_batch(iris, args, rank, world, local, K, W, D, loop_sample=0):
     launches = info["launches_per_pass"] * (kn["update_e"] + kn["update_h"]) + kn["fused_eh"] + \
         kn["tfsf"] + kn["dft_gather"] + kn["flux"] * flux_launches + 2 * kn["dft_block"]
     value = world * cells * K / (reg_ms * 1e-3) / 1e9
-    h2d = sum(m.size * 16 for m in mats)
+    h2d = 0  # the patterns are generated on the device
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": round(reg_ms / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -521,8 +531,8 @@ def measure_batch(iris, args, rank, world, local, K, W, D, loop_sample=0):
                    "parallelism": f"replicas x{world} (independent batches, one per GPU)"},
         "e2e": {"value": round(world * cells * K / t_e2e / 1e9, 3), "unit": "Gcell/s",
                 "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(sum(j.size for j in J) * 8 / K, 1),
-                "what": "iris_batch_create + set_material x%d (host eps) + tune + %d steps + flux of every cell" % (
-                    ncells, K)},
+                "what": ("iris_batch_create + iris_batch_material_pattern x%d (generated on the device) + tune + "
+                         "%d steps + flux of every cell" % (ncells, K))},
         "gpu_launches": int(launches),
         "kernels_ms_per_step": {k: round(v / K, 4) for k, v in kms.items()},
         "window_ms_per_step": round(win_ms / K, 4),
@@ -532,10 +542,10 @@ def measure_batch(iris, args, rank, world, local, K, W, D, loop_sample=0):
                      "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_source": src, "traffic": None,
                      "algorithmic_bytes_per_pass": db},
         "stencil_gcells": round(cells / (t_e + t_h) / 1e9, 3),
-        "clocks": clocks, "material_setup_s": round(t_mat, 2),
+        "clocks": clocks,
     }
     if loop_sample:
-        out["loop_plain"] = loop_plain(iris, ws, params, mats, fw, local, loop_sample, steps=16)
+        out["loop_plain"] = loop_plain(iris, ws, params, fw, local, loop_sample, steps=16)
     return out
 
 
@@ -654,7 +664,7 @@ def run_adjoint(args, rank, world, local):
     return out
 
 
-def loop_plain(iris, ws, params, mats, fw, local, nsample, steps):
+def loop_plain(iris, ws, params, fw, local, nsample, steps):
     """The same cells stepped one after another, each on its own engine (the plain
     solver in a loop), on a sample of the batch: aggregate Gcell/s."""
     tot_cells, tot_ms = 0, 0.0
@@ -663,7 +673,7 @@ def loop_plain(iris, ws, params, mats, fw, local, nsample, steps):
         q = params[i].copy()
         q.dft_faces = iris.DFT_Z
         e = iris.Engine(q, fw, precision=iris.FP32, device=local)
-        e.set_material(mats[i])
+        e.material_pattern(cfg_mod().pattern_seed(ws[i]), ws[i].extra["fill"], 4.0, 1.0)
         e.step(1, 3)
         e.sync()
         e.timing_start(per_kernel=False)

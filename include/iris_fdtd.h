@@ -213,6 +213,33 @@ void iris_destroy(iris_engine* eng);
 int iris_set_material(iris_engine* eng, const double* eps_inv_re, const double* eps_inv_im);
 
 /*
+ * Material generators: the structure's eps_inv over planes hi..hf built on
+ * the device instead of uploaded (the geometry front-end; slit(),
+ * code/mesh.f90:57-69, is the reference's only generator).  Each replaces
+ * the whole structure material like iris_set_material, as a real material
+ * over the background 1/eps_bbox (eps_bbox must be real).
+ *   spheres: n rows (cx, cy, cz, r, eps), in order, later rows win; a cell
+ *     takes 1/eps where ((z-cz)^2 + (y-cy)^2) + (x-cx)^2 <= r^2, over the
+ *     sphere's bounding box clipped to [hi, hf] in z and to nx, ny cells from
+ *     floor(c - r) in x, y, taken modulo the period; ghost rows and columns
+ *     hold their periodic images.
+ *   pattern: 1/eps_in where the i-th draw of a SplitMix64 stream started at
+ *     seed is below fill, else 1/eps_out; i = ((z-hi)*ny + y-1)*nx + x-1;
+ *     ghosts as above.
+ *   design: 1/(emin + (emax-emin)*u_i) over region {x0, x1, y0, y1} (all
+ *     planes hi..hf), u_i the i-th draw, i in the region's own (z, y, x)
+ *     order; 1/eps_bbox elsewhere, ghosts included.
+ * The draws: state = seed + (i+1)*0x9E3779B97F4A7C15, SplitMix64's
+ * finaliser, top 53 bits times 2^-53.
+ */
+int iris_material_spheres(iris_engine* eng, int n, const double* spheres);
+int iris_material_pattern(iris_engine* eng, unsigned long long seed, double fill, double eps_in, double eps_out);
+int iris_material_design(iris_engine* eng, unsigned long long seed, const int region[4], double emin, double emax);
+/* The stored material, planes hi..hf: re/im arrays of (hf-hi+1)*(ny+2)*(nx+2)
+ * values, x fastest (im is 0 for a real material). */
+int iris_get_material(iris_engine* eng, double* re, double* im);
+
+/*
  * Advance the fields by nsteps steps, it = it0 .. it0+nsteps-1: the body of
  * the time loop, code/driver.f90:356-451, in the reference's order:
  * E (all regions), UPML-E, Bloch max ghosts, H, UPML-H, Bloch min ghosts,
@@ -357,6 +384,9 @@ int iris_batch_create(int ncells, const iris_params* params, const double* fw, i
 void iris_batch_destroy(iris_batch* b);
 /* iris_set_material for one cell of the batch. */
 int iris_batch_set_material(iris_batch* b, int cell, const double* eps_inv_re, const double* eps_inv_im);
+/* iris_material_pattern for one cell of the batch. */
+int iris_batch_material_pattern(iris_batch* b, int cell, unsigned long long seed, double fill, double eps_in,
+                                double eps_out);
 /* iris_step for every cell: steps it0 .. it0+nsteps-1. */
 int iris_batch_step(iris_batch* b, int it0, int nsteps);
 /* iris_flux (box 1) of one cell. */

@@ -164,6 +164,28 @@ class Engine:
         re, im = _split_material(eps_inv)
         check(self.L.iris_set_material(self.h, _dp(re), _dp(im) if im is not None else None), "iris_set_material")
 
+    # -- material generated on the device (the same values as the host voxelisers in configs.py)
+    def material_spheres(self, spheres: np.ndarray):
+        """Rows (cx, cy, cz, r, eps) over 1/eps_bbox, later rows win (iris_material_spheres)."""
+        a = np.ascontiguousarray(np.asarray(spheres, dtype=np.float64).reshape(-1, 5))
+        check(self.L.iris_material_spheres(self.h, a.shape[0], _dp(a)), "iris_material_spheres")
+
+    def material_pattern(self, seed: int, fill: float, eps_in: float = 4.0, eps_out: float = 1.0):
+        check(self.L.iris_material_pattern(self.h, seed, fill, eps_in, eps_out), "iris_material_pattern")
+
+    def material_design(self, seed: int, region, emin: float, emax: float):
+        r = (ctypes.c_int * 4)(*[int(v) for v in region])
+        check(self.L.iris_material_design(self.h, seed, r, emin, emax), "iris_material_design")
+
+    def get_material(self) -> np.ndarray:
+        """The stored eps_inv, planes hi..hf, as complex [z, y, x] over 0..n+1."""
+        p = self.p
+        shape = (max(0, p.hf - p.hi + 1), p.ny + 2, p.nx + 2)
+        n = int(np.prod(shape))
+        re, im = np.zeros(max(n, 1)), np.zeros(max(n, 1))
+        check(self.L.iris_get_material(self.h, _dp(re), _dp(im)), "iris_get_material")
+        return (re[:n] + 1j * im[:n]).reshape(shape)
+
     # -- stepping
     def step(self, it0: int, n: int):
         check(self.L.iris_step(self.h, it0, n), "iris_step")
@@ -327,6 +349,10 @@ class Batch:
         re, im = _split_material(eps_inv)
         check(self.L.iris_batch_set_material(self.h, cell, _dp(re), _dp(im) if im is not None else None),
               "iris_batch_set_material")
+
+    def material_pattern(self, cell: int, seed: int, fill: float, eps_in: float = 4.0, eps_out: float = 1.0):
+        check(self.L.iris_batch_material_pattern(self.h, cell, seed, fill, eps_in, eps_out),
+              "iris_batch_material_pattern")
 
     def step(self, it0: int, n: int):
         check(self.L.iris_batch_step(self.h, it0, n), "iris_batch_step")

@@ -14,7 +14,13 @@
   steps (code/files.f90:142).
 * ``spheres_material``, ``binary_pattern_material``, ``design_region_material``:
   seeded voxelisers that build eps_inv over (hi-1:hf+1, 0:ny+1, 0:nx+1), the
-  array slit() fills in the reference (code/mesh.f90:57-69).
+  array slit() fills in the reference (code/mesh.f90:57-69).  The engine
+  builds the same arrays on the device (iris_material_spheres,
+  iris_material_pattern, iris_material_design), value for value: the
+  spheres' parameters are drawn here (``sphere_params``) and passed, the
+  per-voxel draws of the patterns and design regions are the i-th outputs of
+  a SplitMix64 stream started at the seed (``splitmix_uniform``), which both
+  sides compute from the voxel's index.
 """
 from __future__ import annotations
 
@@ -208,19 +214,45 @@ def slit_material(w: Workload) -> np.ndarray:
     return a
 
 
-def spheres_material(w: Workload, seed: int = 0) -> np.ndarray:
-    """nspheres seeded spheres (radius ~U[rmin,rmax] cells, eps ~U[emin,emax],
-    centres in the layer), periodic in x and y, later spheres win."""
+SPLITMIX_GAMMA = 0x9E3779B97F4A7C15
+
+
+def splitmix_uniform(seed: int, idx) -> np.ndarray:
+    """The idx-th outputs (idx >= 0) of a SplitMix64 generator started at seed,
+    as doubles in [0, 1): state = seed + (idx + 1) * 0x9E3779B97F4A7C15, mixed
+    by SplitMix64's finaliser, top 53 bits scaled by 2^-53."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + (np.asarray(idx, dtype=np.uint64) + np.uint64(1)) * \
+            np.uint64(SPLITMIX_GAMMA)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def sphere_params(w: Workload, seed: int = 0) -> np.ndarray:
+    """The nspheres seeded spheres as rows (cx, cy, cz, radius, eps): radius
+    ~U[rmin,rmax] cells, eps ~U[emin,emax], centres in the layer."""
     ex = w.extra
-    a = _base(w)
     hf = w.hi + w.dh - 1
     r = np.random.default_rng(seed)
-    for _ in range(int(ex["nspheres"])):
-        cx = r.uniform(1, w.nx)
-        cy = r.uniform(1, w.ny)
-        cz = r.uniform(w.hi, hf)
-        rad = r.uniform(ex["rmin"], ex["rmax"])
-        eps = r.uniform(ex["emin"], ex["emax"])
+    out = np.empty((int(ex["nspheres"]), 5))
+    for i in range(out.shape[0]):
+        out[i, 0] = r.uniform(1, w.nx)
+        out[i, 1] = r.uniform(1, w.ny)
+        out[i, 2] = r.uniform(w.hi, hf)
+        out[i, 3] = r.uniform(ex["rmin"], ex["rmax"])
+        out[i, 4] = r.uniform(ex["emin"], ex["emax"])
+    return out
+
+
+def spheres_material(w: Workload, seed: int = 0) -> np.ndarray:
+    """nspheres seeded spheres (sphere_params), periodic in x and y, later
+    spheres win: a cell takes 1/eps of the last sphere whose closed ball,
+    over the sphere's bounding box of at most nx by ny cells, holds it."""
+    a = _base(w)
+    hf = w.hi + w.dh - 1
+    for cx, cy, cz, rad, eps in sphere_params(w, seed):
         z = np.arange(max(w.hi, math.floor(cz - rad)), min(hf, math.ceil(cz + rad)) + 1)
         if z.size == 0:
             continue
@@ -240,23 +272,34 @@ def spheres_material(w: Workload, seed: int = 0) -> np.ndarray:
     return a
 
 
+PATTERN_SEED_OFFSET = 1_000_003
+
+
+def pattern_seed(w: Workload) -> int:
+    return int(w.extra["seed"]) + PATTERN_SEED_OFFSET
+
+
 def binary_pattern_material(w: Workload) -> np.ndarray:
-    """Voxelwise Bernoulli(fill) eps in {1, 4} over the layer."""
+    """Voxelwise Bernoulli(fill) eps in {1, 4} over the layer: voxel (z, y, x) of
+    the layer, flat index i = ((z - hi) * ny + y - 1) * nx + x - 1, is eps 4
+    when the i-th SplitMix64 draw of pattern_seed(w) is below fill."""
     ex = w.extra
     a = _base(w)
-    r = np.random.default_rng(ex["seed"] + 1_000_003)
-    m = r.random((w.dh, w.ny, w.nx)) < ex["fill"]
-    a[1:-1, 1:-1, 1:-1] = np.where(m, 1.0 / 4.0, 1.0)
+    u = splitmix_uniform(pattern_seed(w), np.arange(w.dh * w.ny * w.nx)).reshape(w.dh, w.ny, w.nx)
+    a[1:-1, 1:-1, 1:-1] = np.where(u < ex["fill"], 1.0 / 4.0, 1.0)
     _wrap_ghosts(a)
     return a
 
 
 def design_region_material(w: Workload, seed: int = 0) -> np.ndarray:
-    """Continuous eps ~U[emin,emax] over the design region, 1 elsewhere."""
+    """Continuous eps ~U[emin,emax] over the design region, 1 elsewhere: voxel
+    (z, y, x) of the region, flat index i in its own (z, y, x) order, has
+    eps = emin + (emax - emin) * the i-th SplitMix64 draw of seed."""
     ex = w.extra
     a = _base(w)
-    r = np.random.default_rng(seed)
-    eps = r.uniform(ex["emin"], ex["emax"], size=(w.dh, ex["y1"] - ex["y0"] + 1, ex["x1"] - ex["x0"] + 1))
+    shape = (w.dh, ex["y1"] - ex["y0"] + 1, ex["x1"] - ex["x0"] + 1)
+    u = splitmix_uniform(seed, np.arange(int(np.prod(shape)))).reshape(shape)
+    eps = ex["emin"] + (ex["emax"] - ex["emin"]) * u
     a[1:-1, ex["y0"]:ex["y1"] + 1, ex["x0"]:ex["x1"] + 1] = 1.0 / eps
     return a
 

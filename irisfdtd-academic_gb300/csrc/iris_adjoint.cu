@@ -233,9 +233,17 @@ __global__ void __launch_bounds__(256) k_adj_record(FieldArgs<T> a, Design d, ty
 // Adjoint DFT source of one sampled step on one z face:
 //   Ebar_x += c Y_Hy, Ebar_y -= c Y_Hx, Hbar_x -= c Y_Ey, Hbar_y += c Y_Ex
 // summed over frequencies, c = w * exp(-i fw t), Y the final DFT values.
+// The DFT values in FP64: FP64-mode accumulators, or FP32 mode's
+// double-float pairs (re_hi, im_hi, re_lo, im_lo).
+__device__ __forceinline__ double2 adj_acc(const void* fd, long i, bool df) {
+  if (!df) return ((const double2*)fd)[i];
+  const float4 a = ((const float4*)fd)[i];
+  return make_double2((double)a.x + (double)a.z, (double)a.y + (double)a.w);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_adj_source(typename V2<T>::t* __restrict__ ae, typename V2<T>::t* __restrict__ ah,
-                                                    Geo g, const double2* __restrict__ fd, long P, AdjFace f,
+                                                    Geo g, const void* __restrict__ fd, long P, AdjFace f,
                                                     const double* __restrict__ w, const double* __restrict__ fw,
                                                     int nof, int t) {
   extern __shared__ double2 tw[];
@@ -248,9 +256,11 @@ __global__ void __launch_bounds__(256) k_adj_source(typename V2<T>::t* __restric
   const long L = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= f.n) return;
   double2 gex = {0, 0}, gey = {0, 0}, ghx = {0, 0}, ghy = {0, 0};
+  const bool df = sizeof(T) == 4;  // FP32 mode: double-float accumulators
   for (int iw = 0; iw < nof; ++iw) {
-    const double2* row = fd + (long)iw * P;
-    const double2 xe = row[f.b[0] + L], ye = row[f.b[1] + L], xh = row[f.b[3] + L], yh = row[f.b[4] + L];
+    const long row = (long)iw * P;
+    const double2 xe = adj_acc(fd, row + f.b[0] + L, df), ye = adj_acc(fd, row + f.b[1] + L, df);
+    const double2 xh = adj_acc(fd, row + f.b[3] + L, df), yh = adj_acc(fd, row + f.b[4] + L, df);
     const double2 c = tw[iw];
     gex.x += c.x * yh.x - c.y * yh.y; gex.y += c.x * yh.y + c.y * yh.x;
     ghy.x += c.x * xe.x - c.y * xe.y; ghy.y += c.x * xe.y + c.y * xe.x;
@@ -440,7 +450,7 @@ template <typename T> int adj_forward(iris_adjoint* J, int nsteps) {
   }
   int rc = zero_state(F, J->fbytes, J->sbytes);
   if (rc) return rc;
-  CK(cudaMemsetAsync(F->fd, 0, (size_t)F->P * F->p.nof * sizeof(double2), F->st));
+  CK(cudaMemsetAsync(F->fd, 0, (size_t)F->P * F->p.nof * 16, F->st));
   F->nslot = 0;
   CK(cudaEventRecord(J->ev[0], F->st));
   for (int it = 1; it <= nsteps; ++it) {

@@ -673,6 +673,17 @@ int iris_batch_set_material(iris_batch* B, int cell, const double* re, const dou
   return batch_upload_args(B);  // the material pointer may have changed
 }
 
+int iris_batch_material_pattern(iris_batch* B, int cell, unsigned long long seed, double fill, double eps_in,
+                                double eps_out) {
+  clear_error();
+  if (!B || cell < 0 || cell >= B->n) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(B->device));
+  CK(cudaStreamSynchronize(B->master->st));
+  int rc = iris_material_pattern(B->cells[cell], seed, fill, eps_in, eps_out);
+  if (rc) return rc;
+  return batch_upload_args(B);  // the material pointer has changed
+}
+
 int iris_batch_step(iris_batch* B, int it0, int nsteps) {
   clear_error();
   if (!B || nsteps < 0) return fail(IRIS_EINVAL, "bad argument");

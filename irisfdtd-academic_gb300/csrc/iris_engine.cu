@@ -462,6 +462,39 @@ __global__ void __launch_bounds__(128) k_dft_fp64(const double2* __restrict__ S,
     if (j < nw) fd[(long)(w0 + j) * P + p] = acc[j];
 }
 
+// FP32 mode accumulators: each complex value of fdata is a compensated
+// (double-float) pair per part, float4 (re_hi, im_hi, re_lo, im_lo), 16 bytes
+// like a double2.  GB300 runs FP64 arithmetic at a small fraction of its FP32
+// rate, and the block accumulation and the flux read add to every stored
+// value: in FP64 those adds and the float-to-double conversions bound both
+// kernels, in FP32 they cost nothing next to the memory traffic.  A partial
+// sum p is added exactly (TwoSum twice): hi + lo carries about 48 bits, the
+// error of the sum is that of rounding lo + e once.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float p) {
+  const float s = __fadd_rn(hi, p);
+  const float bp = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+  const float t = __fadd_rn(lo, e);
+  const float h = __fadd_rn(s, t);
+  const float bt = __fsub_rn(h, s);
+  lo = __fadd_rn(__fsub_rn(s, __fsub_rn(h, bt)), __fsub_rn(t, bt));
+  hi = h;
+}
+// The accumulator types: double2 (FP64 accumulation) and float4 (double-float).
+__device__ __forceinline__ void acc_add(double2& a, float re, float im) {
+  a.x += (double)re;
+  a.y += (double)im;
+}
+__device__ __forceinline__ void acc_add(float4& a, float re, float im) {
+  df_add(a.x, a.z, re);
+  df_add(a.y, a.w, im);
+}
+// Value of an accumulator in FP64.
+__device__ __forceinline__ double2 acc_value(const double2& a) { return a; }
+__device__ __forceinline__ double2 acc_value(const float4& a) {
+  return make_double2((double)a.x + (double)a.z, (double)a.y + (double)a.w);
+}
+
 // FP32 mode twiddles: Wt[k][iw] = dt*exp(i*fw(iw)*t_k), phase formed in FP64
 // (it reaches ~1e4 rad), rounded to FP32 once.
 // Time index of sample k: tk[k], or t0 + k*tstep when tk is null.
@@ -477,7 +510,8 @@ __global__ void k_twiddle(const int* __restrict__ tk, int t0, int tstep, int nk,
 }
 
 // FP32 mode: partial[p][iw] = sum_k F_k(p)*Wt[k][iw] in FP32 registers over
-// the block of nk samples, then one FP64 add per (p, iw) into fdata.
+// the block of nk samples, then one add per (p, iw) into fdata (double-float
+// in the engine, FP64 accumulators for iris_dft_block_noalloc's callers).
 // CTA tile: 128 points x 32 frequencies, 128 threads (three CTAs per SM, so one
 // CTA's staging overlaps the others' FMAs).  Lane l owns points l + 32 i
 // (i < 4), warp w owns frequencies 8 w + j (j < 8), so each thread keeps a
@@ -486,9 +520,10 @@ __global__ void k_twiddle(const int* __restrict__ tk, int t0, int tstep, int nk,
 // 1-D grid runs the frequency chunks of one point tile back to back so the
 // tile's samples are read from HBM once and from L2 after that.
 constexpr int DFT_TP = 128, DFT_TW = 32, DFT_KC = 32, DFT_THREADS = 128;
+template <typename ACC>
 __global__ void __launch_bounds__(DFT_THREADS) k_dft_fp32(const float2* __restrict__ S, long P, int nk,
                                                   const float2* __restrict__ Wt, int nof, int nwc,
-                                                  double2* __restrict__ fd) {
+                                                  ACC* __restrict__ fd) {
   __shared__ float2 Ss[DFT_KC][DFT_TP];
   __shared__ float4 Ws[DFT_KC][DFT_TW / 2];
   const int wc = blockIdx.x % nwc;
@@ -545,10 +580,9 @@ __global__ void __launch_bounds__(DFT_THREADS) k_dft_fp32(const float2* __restri
     for (int j = 0; j < 8; ++j) {
       const int w = wc * DFT_TW + warp * 8 + j;
       if (w >= nof) continue;
-      double2* q = fd + (long)w * P + p;
-      double2 f = *q;
-      f.x += (double)ar[i][j];
-      f.y += (double)ai[i][j];
+      ACC* q = fd + (long)w * P + p;
+      ACC f = *q;
+      acc_add(f, ar[i][j], ai[i][j]);
       *q = f;
     }
   }
@@ -565,27 +599,20 @@ __global__ void __launch_bounds__(DFT_THREADS) k_dft_fp32(const float2* __restri
 // FP32 accuracy from TF32 operands: with X = Xh + Xl, Xh = X rounded to TF32,
 // A B ~ Ah Bh + Ah Bl + Al Bh (the Al Bl term is below FP32 rounding).
 //
-// A CTA owns TC_M = 128 points (the 128 TMEM lanes) and a group of up to
-// TC_NW = 128 frequencies (256 FP32 TMEM columns).  K is walked in chunks of
-// TC_KC = 16 (8 samples) through two shared-memory stages: the CTA's four
-// warps split the chunk's samples into the hi/lo A operands (K-major core
-// matrices, no swizzle) while the previous chunk's twelve MMAs run; the B
-// operands, identical for every CTA, are prepared once per block in global
-// memory in the same layout by k_twiddle_tc and bulk-copied (TMA) per chunk.
-// One elected thread issues the MMAs and commits them to an mbarrier; the
-// epilogue reads the accumulators back with tcgen05.ld and adds them to
-// fdata in FP64, one coalesced double2 row per frequency.  Every wait is
-// bounded; a CTA that gives up records it in err, still waits (bounded) for
-// its MMAs, frees its TMEM and exits.
+// A work item is a row tile of TC_M = 128 sample points (the 128 TMEM lanes)
+// and a group of up to TC_NW = 128 frequencies (256 FP32 TMEM columns).  K
+// is walked in chunks of TC_KC = 16 (8 samples): the A operands split into
+// hi/lo (K-major core matrices, no swizzle) in shared memory, the B
+// operands, identical for every item of a group, prepared once per block in
+// global memory in the same layout by k_twiddle_tc and bulk-copied (TMA) per
+// chunk.  The kernel is k_dft_ws below.
 
-constexpr int TC_M = 128, TC_NW = 128, TC_KC = 16, TC_THREADS = 256;
+constexpr int TC_M = 128, TC_NW = 128, TC_KC = 16;
 constexpr int TC_NMAX = 2 * TC_NW;                       // TMEM columns per CTA
 constexpr int TC_BROWS = TC_NMAX;                        // B rows per chunk buffer
 constexpr size_t TC_A_BYTES = (size_t)TC_M * TC_KC * 4;  // one of A hi / A lo
 constexpr size_t TC_B_BYTES = (size_t)TC_BROWS * TC_KC * 4;
-constexpr size_t TC_R_BYTES = (size_t)(TC_KC / 2) * TC_M * 8;  // raw samples of one chunk
 constexpr size_t TC_STAGE = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
-constexpr size_t TC_SMEM = 2 * TC_STAGE + 2 * TC_R_BYTES;
 
 // Offset (in floats) of element (row r, k) of a K-major, unswizzled operand
 // of TC_KC columns: 8-row x 16-byte core matrices, the K-neighbour core
@@ -650,161 +677,6 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
                : "memory");
 }
 
-// CTA (point tile, frequency group), the groups of one tile adjacent in
-// blockIdx.x so the tile's samples are read from HBM once.  Eight warps: all
-// split samples into A; warp w reads TMEM lanes 32 (w % 4) .. +31 and the
-// w / 4 half of the columns in the epilogue.  The samples of a chunk (8 rows
-// of 128 points, 1 KB each; P is even, so every row starts 16-byte aligned)
-// and its B operands are bulk-copied one chunk ahead.
-__global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict__ S, long P, int nk,
-                                                       const float* __restrict__ Bt, int nof, int ngroups,
-                                                       double2* __restrict__ fd, int* err) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint64_t bar_in[2], bar_mma[2];
-  __shared__ uint32_t taddr_s;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int g = blockIdx.x % ngroups;
-  const long p0 = (long)(blockIdx.x / ngroups) * TC_M;
-  const int np = (int)min((long)TC_M, P - p0);  // points of this tile (even)
-  const int nw = min(TC_NW, nof - g * TC_NW);   // frequencies of this group
-  const int ncol = ((2 * nw + 15) / 16) * 16;   // MMA N: a multiple of 16
-  const int nch = (2 * nk + TC_KC - 1) / TC_KC;
-  const long per = (long)TC_BROWS * TC_KC;
-  unsigned char* raw = smem + 2 * TC_STAGE;
-  if (tid == 0) {
-    for (int s = 0; s < 2; ++s) {
-      mbar_init(&bar_in[s], 1);
-      mbar_init(&bar_mma[s], 1);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&taddr_s)),
-                 "r"(TC_NMAX)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = taddr_s;
-  const uint32_t idesc = tc_idesc(ncol);
-  const unsigned nb = (unsigned)(ncol * TC_KC * 4);
-  // chunk c's inputs (its raw samples and B operands) into slot s
-  auto issue = [&](int c, int s) {
-    const int k0 = c * (TC_KC / 2), nr = min(TC_KC / 2, nk - k0);
-    unsigned char* st = smem + s * TC_STAGE;
-    const float* src = Bt + ((long)(g * nch + c) * 2) * per;
-    mbar_expect_tx(&bar_in[s], 2 * nb + (unsigned)(nr * np * 8));
-    fence_proxy_async();
-    bulk_g2s(st + 2 * TC_A_BYTES, src, nb, &bar_in[s]);
-    bulk_g2s(st + 2 * TC_A_BYTES + TC_B_BYTES, src + per, nb, &bar_in[s]);
-    for (int r = 0; r < nr; ++r)
-      bulk_g2s(raw + s * TC_R_BYTES + (size_t)r * TC_M * 8, S + (long)(k0 + r) * P + p0, (unsigned)(np * 8),
-               &bar_in[s]);
-  };
-  unsigned par_in = 0, par_mma = 0;
-  bool bad = false;
-  if (tid == 0) issue(0, 0);
-  for (int c = 0; c < nch; ++c) {
-    const int s = c & 1;
-    unsigned char* st = smem + s * TC_STAGE;
-    float* Ah = (float*)st;
-    float* Al = (float*)(st + TC_A_BYTES);
-    const float* Bh = (const float*)(st + 2 * TC_A_BYTES);
-    const float* Bl = (const float*)(st + 2 * TC_A_BYTES + TC_B_BYTES);
-    if (c + 1 < nch) {
-      // slot s^1 was last read by the MMAs of chunk c-1 (its raw samples by
-      // this CTA's split of chunk c-1, finished at that iteration's barrier)
-      if (c >= 1) {
-        bad |= !mbar_wait(&bar_mma[s ^ 1], (par_mma >> (s ^ 1)) & 1u, STREAM_WAIT_CYCLES);
-        par_mma ^= 1u << (s ^ 1);
-      }
-      if (tid == 0) issue(c + 1, s ^ 1);
-    }
-    bad |= !mbar_wait(&bar_in[s], (par_in >> s) & 1u, STREAM_WAIT_CYCLES);
-    par_in ^= 1u << s;
-    // split: thread (row, half) takes samples 4 half .. 4 half + 3 of the chunk
-    {
-      const int row = tid & (TC_M - 1), half = tid >> 7;
-      const int k0 = c * (TC_KC / 2);
-      const float2* rw = (const float2*)(raw + s * TC_R_BYTES);
-#pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        const int kq = 4 * half + 2 * q;  // sample pair kq, kq+1 of the chunk
-        float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-        if (row < np) {
-          if (k0 + kq < nk) a = rw[kq * TC_M + row];
-          if (k0 + kq + 1 < nk) b = rw[(kq + 1) * TC_M + row];
-        }
-        const float4 v = make_float4(a.x, a.y, b.x, b.y);
-        const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-        *(float4*)(Ah + tc_off(row, 2 * kq)) = h;
-        *(float4*)(Al + tc_off(row, 2 * kq)) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
-      }
-    }
-    fence_proxy_async();  // generic-proxy writes of A before the tensor core reads them
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-      for (int ks = 0; ks < TC_KC / 8; ++ks) {
-        const uint64_t ah = tc_desc(Ah + 64 * ks), al = tc_desc(Al + 64 * ks);
-        const uint64_t bh = tc_desc(Bh + 64 * ks), bl = tc_desc(Bl + 64 * ks);
-        tc_mma(tmem, ah, bh, idesc, (c > 0 || ks > 0) ? 1 : 0);
-        tc_mma(tmem, ah, bl, idesc, 1);
-        tc_mma(tmem, al, bh, idesc, 1);
-      }
-      tc_commit(&bar_mma[s]);
-    }
-  }
-  // the commits of the last two chunks (each covers every earlier MMA)
-  for (int c = max(0, nch - 2); c < nch; ++c) {
-    const int s = c & 1;
-    bad |= !mbar_wait(&bar_mma[s], (par_mma >> s) & 1u, STREAM_WAIT_CYCLES);
-    par_mma ^= 1u << s;
-  }
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (__syncthreads_or(bad)) {
-    if (tid == 0) atomicExch(err, 3);
-  } else {
-    // epilogue: lanes 32 (w % 4) + lane = points, columns of half w / 4
-    const int q4 = warp & 3, hw = warp >> 2;
-    const int row = 32 * q4 + lane;
-    const long pp = p0 + row;
-    const int cbeg = hw * (ncol / 2), cend = cbeg + ncol / 2;  // ncol / 2 is a multiple of 8
-    for (int c0 = cbeg; c0 < cend; c0 += 16) {
-      uint32_t r[16];
-      const uint32_t ta = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)c0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-          : "r"(ta)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < np) {
-        const int j0 = c0 / 2, jn = min(8, min(nw, cend / 2) - j0);
-        double2 f[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          if (j < jn) f[j] = fd[(long)(g * TC_NW + j0 + j) * P + pp];
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          if (j < jn) {
-            f[j].x += (double)__uint_as_float(r[2 * j]);
-            f[j].y += (double)__uint_as_float(r[2 * j + 1]);
-            fd[(long)(g * TC_NW + j0 + j) * P + pp] = f[j];
-          }
-      }
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_NMAX) : "memory");
-}
-
 // ---------------------------------------------------------------------------
 // Flux read without committing the sample ring (FP32 mode, tensor cores).
 //
@@ -813,28 +685,14 @@ __global__ void __launch_bounds__(TC_THREADS) k_dft_tc(const float2* __restrict_
 // after a commit of the nk samples still in the ring:
 //   J = sign * scale * sum_L Re(A_a conj A_b) - Re(A_c conj A_d),
 //   A_x(L, iw) = fdata[iw][p_x + L] + sum_k F_k(p_x + L) Wt_k(iw).
-// The pending sum is k_dft_tc's block GEMM (the same MMAs on the same
+// The pending sum is the commit's block GEMM (the same MMAs on the same
 // operands, so each A_x is the value a commit would store), but nothing is
 // written back: a flux read costs one read of the four flux components'
-// accumulators, and the ring is committed when it is full, as before.
-//
-// A CTA owns one tile of FL_LOC = 32 locations of one face and one frequency
-// group.  Its 128 A rows (the TMEM lanes) are the four flux components of the
-// 32 locations: row 32 c + l is component c (a, b, c, d) at location L0 + l.
-// The components' runs start at any point index, so samples come by plain
-// loads, one chunk ahead into registers; the B operands are bulk-copied per
-// chunk as in k_dft_tc.  The accumulators stream into registers one
-// 8-frequency chunk ahead, the first chunk before the MMAs are issued.
-// Epilogue: half w / 4 of the CTA takes the chunks w / 4, w / 4 + 2, ...;
-// warp w % 4 holds component w % 4 of the 32 locations, adds its TMEM
-// partials, and the four components meet in shared memory (over the dead
-// operand stages); warp c then forms the products of frequencies 2c and
-// 2c + 1 and sums its 32 locations with shuffles.  One partial per
-// (frequency, tile) goes to part[iw][tile]; k_flux_sum adds a face's tiles
-// in a fixed order, so the result does not depend on scheduling.
+// accumulators, and the ring is committed when it is full, as before.  Its
+// work items are tiles of FL_LOC = 32 locations of one face (k_dft_ws in
+// flux mode); k_flux_sum adds the partials of a face in a fixed order, so
+// the result does not depend on scheduling.
 constexpr int FL_LOC = 32;
-constexpr size_t FL_SMEM = 2 * TC_STAGE;
-static_assert((size_t)2 * 4 * 8 * FL_LOC * sizeof(double2) <= FL_SMEM, "epilogue exchange fits the stages");
 
 struct FluxTiles {
   int start[7];  // first tile of face f; start[6]: tiles of the set
@@ -844,212 +702,381 @@ __device__ __forceinline__ long face_comp(const FluxFace& F, int c) {
   return c == 0 ? F.pa : c == 1 ? F.pb : c == 2 ? F.pc : F.pd;
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 2) k_flux_tc(const float2* __restrict__ S, long P, int nk,
-                                                           const float* __restrict__ Bt,
-                                                           const double2* __restrict__ fd, int nof, int ngroups,
-                                                           const FluxFace* __restrict__ faces, FluxTiles ft,
-                                                           double* __restrict__ part, int* err) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint64_t bar_in[2], bar_mma[2];
-  __shared__ uint32_t taddr_s;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int g = blockIdx.x % ngroups;
-  const int tile = blockIdx.x / ngroups;
-  int f = 0, fs = 0;  // the face holding this tile (start indices never decrease)
-#pragma unroll
-  for (int i = 1; i < 6; ++i)
-    if (tile >= ft.start[i]) {
-      f = i;
-      fs = ft.start[i];
-    }
-  const FluxFace F = faces[f];
-  const long L0 = (long)(tile - fs) * FL_LOC;
-  const int nl = (int)min((long)FL_LOC, F.n - L0);
-  const int nw = min(TC_NW, nof - g * TC_NW);
-  const int ncol = ((2 * nw + 15) / 16) * 16;
-  const int nch = (2 * nk + TC_KC - 1) / TC_KC;
-  const int nchk = (nw + 7) / 8;
-  const long per = (long)TC_BROWS * TC_KC;
-  const int ntiles = ft.start[6];
-  // split row of this thread (component rc at location rl) and its epilogue
-  // point (component q4 at location lane); -1 past the face's last location
-  const int row = tid & (TC_M - 1), half = tid >> 7;
-  const int rc = row >> 5, rl = row & 31;
-  const long rp = rl < nl ? face_comp(F, rc) + L0 + rl : -1;
-  const int q4 = warp & 3, hw = warp >> 2;
-  const long ep = lane < nl ? face_comp(F, q4) + L0 + lane : -1;
-  const double2* fdg = fd + (long)g * TC_NW * P;
+// ---------------------------------------------------------------------------
+// Warp-specialised persistent DFT block kernel (FP32 mode, tensor cores).
+//
+// One CTA per SM walks work items (a row tile and a frequency group) with
+// three roles that overlap each other through mbarriers:
+//   * producers (warps 0-3, one thread per A row): the samples of a chunk of
+//     8 samples into the TF32 hi/lo A operands of a stage (plain loads, one
+//     chunk ahead in registers), and one thread bulk-copies the chunk's B
+//     operands into the same stage; WS_STAGES stages in a ring;
+//   * the MMA thread (warp 12): three tcgen05.mma kind::tf32 per 8 K columns
+//     into one of two TMEM accumulators (256 columns each), each stage freed
+//     by a commit when its MMAs are done, each finished item signalled by a
+//     commit on that accumulator;
+//   * epilogue warps (4-11; warp w reads TMEM lanes 32 (w % 4)): drain an
+//     accumulator while the MMAs of the next item fill the other, streaming
+//     the FP64 accumulators one 8-frequency chunk ahead in registers.
+// Commit mode: rows are 128 consecutive sample points; the epilogue adds the
+// partial sums into fdata (read once, written once).
+// Flux mode: rows are the four flux components of 32 locations of one face,
+// row 32 q + 4 l + c = component c of location 8 q + l, so that the warp
+// reading TMEM lane quarter q holds all four components of its 8 locations;
+// the epilogue adds the partial sums to the accumulators it reads, forms the
+// face's products with shuffles inside the warp and writes one partial per
+// (frequency, tile, quarter); fdata is not written.  No barrier spans
+// warps, so a warp that gives up leaves no other waiting for it.
+// Every wait is bounded: a role that gives up records it (code 3 in commit
+// mode, 5 in flux mode) and stops; the others stop at their next wait; the
+// CTA waits (bounded) for its copies and MMAs before it frees its TMEM.
 
-  auto load_fd = [&](int ch, double2* dst) {
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-      dst[j] = (ep >= 0 && 8 * ch + j < nw) ? fdg[(long)(8 * ch + j) * P + ep] : make_double2(0.0, 0.0);
-  };
-  double2 fa[8], fb[8];
-  if (hw < nchk) load_fd(hw, fa);
+constexpr int WS_STAGES = 3, WS_PROD = 128, WS_EPI = 256;
+constexpr int WS_THREADS = WS_PROD + WS_EPI + 32;  // + the MMA warp
+constexpr size_t WS_SMEM = WS_STAGES * TC_STAGE;
 
-  bool bad = false;
-  uint32_t tmem = 0;
-  if (nk > 0) {
-    if (tid == 0) {
-      for (int s = 0; s < 2; ++s) {
-        mbar_init(&bar_in[s], 1);
-        mbar_init(&bar_mma[s], 1);
-      }
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (warp == 0) {
-      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&taddr_s)),
-                   "r"(TC_NMAX)
-                   : "memory");
-      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    tmem = taddr_s;
-    const uint32_t idesc = tc_idesc(ncol);
-    const unsigned nb = (unsigned)(ncol * TC_KC * 4);
-    auto issue_b = [&](int c, int s) {
-      unsigned char* st = smem + s * TC_STAGE;
-      const float* src = Bt + ((long)(g * nch + c) * 2) * per;
-      mbar_expect_tx(&bar_in[s], 2 * nb);
-      fence_proxy_async();
-      bulk_g2s(st + 2 * TC_A_BYTES, src, nb, &bar_in[s]);
-      bulk_g2s(st + 2 * TC_A_BYTES + TC_B_BYTES, src + per, nb, &bar_in[s]);
-    };
-    // samples 4 half .. 4 half + 3 of chunk c at this thread's split row
-    auto load_s = [&](int c, float2* dst) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int k = c * (TC_KC / 2) + 4 * half + q;
-        dst[q] = (rp >= 0 && k < nk) ? S[(long)k * P + rp] : make_float2(0.f, 0.f);
-      }
-    };
-    float2 sv[4], sn[4] = {};
-    load_s(0, sv);
-    unsigned par_in = 0, par_mma = 0;
-    if (tid == 0) issue_b(0, 0);
-    for (int c = 0; c < nch; ++c) {
-      const int s = c & 1;
-      unsigned char* st = smem + s * TC_STAGE;
-      float* Ah = (float*)st;
-      float* Al = (float*)(st + TC_A_BYTES);
-      const float* Bh = (const float*)(st + 2 * TC_A_BYTES);
-      const float* Bl = (const float*)(st + 2 * TC_A_BYTES + TC_B_BYTES);
-      if (c + 1 < nch) {
-        // stage s^1 was last read by the MMAs of chunk c-1
-        if (c >= 1) {
-          bad |= !mbar_wait(&bar_mma[s ^ 1], (par_mma >> (s ^ 1)) & 1u, STREAM_WAIT_CYCLES);
-          par_mma ^= 1u << (s ^ 1);
-        }
-        if (tid == 0) issue_b(c + 1, s ^ 1);
-        load_s(c + 1, sn);
-      }
-      bad |= !mbar_wait(&bar_in[s], (par_in >> s) & 1u, STREAM_WAIT_CYCLES);
-      par_in ^= 1u << s;
-#pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        const int kq = 4 * half + 2 * q;
-        const float4 v = make_float4(sv[2 * q].x, sv[2 * q].y, sv[2 * q + 1].x, sv[2 * q + 1].y);
-        const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-        *(float4*)(Ah + tc_off(row, 2 * kq)) = h;
-        *(float4*)(Al + tc_off(row, 2 * kq)) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
-      }
-      fence_proxy_async();
-      __syncthreads();
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-        for (int ks = 0; ks < TC_KC / 8; ++ks) {
-          const uint64_t ah = tc_desc(Ah + 64 * ks), al = tc_desc(Al + 64 * ks);
-          const uint64_t bh = tc_desc(Bh + 64 * ks), bl = tc_desc(Bl + 64 * ks);
-          tc_mma(tmem, ah, bh, idesc, (c > 0 || ks > 0) ? 1 : 0);
-          tc_mma(tmem, ah, bl, idesc, 1);
-          tc_mma(tmem, al, bh, idesc, 1);
-        }
-        tc_commit(&bar_mma[s]);
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) sv[q] = sn[q];
-    }
-    for (int c = max(0, nch - 2); c < nch; ++c) {
-      const int s = c & 1;
-      bad |= !mbar_wait(&bar_mma[s], (par_mma >> s) & 1u, STREAM_WAIT_CYCLES);
-      par_mma ^= 1u << s;
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  }
-  // every MMA has completed: the operand stages hold the exchange now
-  const bool give_up = __syncthreads_or(bad);
-  if (give_up) {
-    if (tid == 0) atomicExch(err, 5);
-  } else {
-    double2* X = (double2*)smem + hw * (4 * 8 * FL_LOC);  // [component][frequency][location]
-    for (int ch = hw; ch < nchk; ch += 2) {
-      if (ch + 2 < nchk) load_fd(ch + 2, fb);
-      if (nk > 0) {
-        uint32_t r[16];
-        const uint32_t ta = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(16 * ch);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-            : "r"(ta)
-            : "memory");
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          fa[j].x += (double)__uint_as_float(r[2 * j]);
-          fa[j].y += (double)__uint_as_float(r[2 * j + 1]);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 8; ++j) X[(q4 * 8 + j) * FL_LOC + lane] = fa[j];
-      asm volatile("bar.sync %0, %1;" ::"r"(1 + hw), "r"(128) : "memory");
-#pragma unroll
-      for (int jj = 0; jj < 2; ++jj) {
-        const int j = 2 * q4 + jj;
-        double v = 0.0;
-        if (lane < nl) {
-          const double2 a = X[(0 * 8 + j) * FL_LOC + lane], b = X[(1 * 8 + j) * FL_LOC + lane];
-          const double2 c = X[(2 * 8 + j) * FL_LOC + lane], d = X[(3 * 8 + j) * FL_LOC + lane];
-          v = (a.x * b.x + a.y * b.y) - (c.x * d.x + c.y * d.y);
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0 && 8 * ch + j < nw) part[(long)(g * TC_NW + 8 * ch + j) * ntiles + tile] = v;
-      }
-      asm volatile("bar.sync %0, %1;" ::"r"(1 + hw), "r"(128) : "memory");
-#pragma unroll
-      for (int j = 0; j < 8; ++j) fa[j] = fb[j];
-    }
-  }
-  if (nk > 0) {
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (warp == 0)
-      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_NMAX) : "memory");
-  }
+struct WsArgs {
+  const float2* S;  // the sample ring [nk][P]
+  long P;
+  int nk;
+  const float* Bt;  // B operands of the nk samples (k_twiddle_tc)
+  float4* fd;       // double-float accumulators [nof][P]
+  int nof, ngroups;
+  long nitems;      // row tiles x frequency groups
+  // flux mode
+  const FluxFace* faces;
+  FluxTiles ft;
+  double* part;
+  int* err;
+};
+
+__device__ __forceinline__ void mbar_expect_tx_only(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// J[f][iw] = scale * sign * (sum of face f's tile partials, in tile order
-// within each thread, then a fixed tree).
+template <bool FLUX> struct WsRow {
+  long p0;  // commit: first point of the tile
+  int np;   // commit: points of the tile
+  FluxFace F;
+  long L0;
+  int nl, tile;
+};
+
+template <bool FLUX> __device__ __forceinline__ WsRow<FLUX> ws_item(const WsArgs& A, long item, int& g) {
+  WsRow<FLUX> r{};
+  g = (int)(item % A.ngroups);
+  const long t = item / A.ngroups;
+  r.tile = (int)t;
+  if (FLUX) {
+    int f = 0, fs = 0;
+#pragma unroll
+    for (int i = 1; i < 6; ++i)
+      if (t >= A.ft.start[i]) {
+        f = i;
+        fs = A.ft.start[i];
+      }
+    r.F = A.faces[f];
+    r.L0 = (t - fs) * FL_LOC;
+    r.nl = (int)min((long)FL_LOC, r.F.n - r.L0);
+  } else {
+    r.p0 = t * TC_M;
+    r.np = (int)min((long)TC_M, A.P - r.p0);
+  }
+  return r;
+}
+
+// Sample point of A row `row` (-1: none).
+template <bool FLUX> __device__ __forceinline__ long ws_point(const WsRow<FLUX>& r, int row) {
+  if (FLUX) {
+    const int c = row & 3, l = ((row >> 5) << 3) + ((row & 31) >> 2);
+    return l < r.nl ? face_comp(r.F, c) + r.L0 + l : -1;
+  }
+  return row < r.np ? r.p0 + row : -1;
+}
+
+template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint64_t full[WS_STAGES], empty[WS_STAGES], accf[2], acce[2], fin;
+  __shared__ uint32_t taddr_s;
+  __shared__ int stop_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int code = FLUX ? 5 : 3;
+  const int nch = (2 * A.nk + TC_KC - 1) / TC_KC;
+  const long per = (long)TC_BROWS * TC_KC;
+  const bool mma = A.nk > 0;
+  if (tid == 0) {
+    for (int s = 0; s < WS_STAGES; ++s) {
+      mbar_init(&full[s], WS_PROD);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], WS_EPI);
+    }
+    mbar_init(&fin, 1);
+    stop_s = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 12 && mma) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&taddr_s)),
+                 "r"(2 * TC_NMAX)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = mma ? taddr_s : 0u;
+  auto give_up = [&]() {
+    atomicExch(A.err, code);
+    *(volatile int*)&stop_s = 1;
+  };
+  auto stopped = [&]() { return *(volatile int*)&stop_s != 0; };
+
+  if (tid < WS_PROD) {
+    // ---- producers: one flat sequence of (item, chunk) pairs, the samples of
+    // the next two chunks in registers while a chunk is split into its stage
+    if (mma) {
+      const int row = tid;
+      int armed[WS_STAGES] = {};  // fills issued per stage (thread 0: the last one is drained at exit)
+      struct Cur {
+        long j;
+        int c, g;
+        long rp;
+        bool ok;
+      };
+      auto at = [&](long j, int c) {
+        Cur x{j, c, 0, -1, false};
+        const long item = blockIdx.x + j * gridDim.x;
+        if (item < A.nitems) {
+          const WsRow<FLUX> r = ws_item<FLUX>(A, item, x.g);
+          x.rp = ws_point<FLUX>(r, row);
+          x.ok = true;
+        }
+        return x;
+      };
+      auto next = [&](const Cur& x) { return x.c + 1 < nch ? Cur{x.j, x.c + 1, x.g, x.rp, x.ok} : at(x.j + 1, 0); };
+      auto load = [&](const Cur& x, float2* dst) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int k = x.c * (TC_KC / 2) + q;
+          dst[q] = (x.ok && x.rp >= 0 && k < A.nk) ? A.S[(long)k * A.P + x.rp] : make_float2(0.f, 0.f);
+        }
+      };
+      Cur c0 = at(0, 0), c1 = next(c0), c2 = next(c1);
+      float2 v0[8], v1[8], v2[8];
+      load(c0, v0);
+      load(c1, v1);
+      for (long n = 0; c0.ok && !stopped(); ++n) {
+        load(c2, v2);
+        const int s = (int)(n % WS_STAGES);
+        const long u = n / WS_STAGES;
+        if (u > 0 && !mbar_wait(&empty[s], (unsigned)((u - 1) & 1), STREAM_WAIT_CYCLES)) {
+          give_up();
+          break;
+        }
+        unsigned char* st = smem + s * TC_STAGE;
+        if (tid == 0) {
+          const int ncol = ((2 * min(TC_NW, A.nof - c0.g * TC_NW) + 15) / 16) * 16;
+          const unsigned nb = (unsigned)(ncol * TC_KC * 4);
+          const float* src = A.Bt + ((long)(c0.g * nch + c0.c) * 2) * per;
+          mbar_expect_tx_only(&full[s], 2 * nb);
+          fence_proxy_async();
+          bulk_g2s(st + 2 * TC_A_BYTES, src, nb, &full[s]);
+          bulk_g2s(st + 2 * TC_A_BYTES + TC_B_BYTES, src + per, nb, &full[s]);
+          ++armed[s];
+        }
+        float* Ah = (float*)st;
+        float* Al = (float*)(st + TC_A_BYTES);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const float4 x = make_float4(v0[2 * m].x, v0[2 * m].y, v0[2 * m + 1].x, v0[2 * m + 1].y);
+          const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+          *(float4*)(Ah + tc_off(row, 4 * m)) = h;
+          *(float4*)(Al + tc_off(row, 4 * m)) = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+        }
+        fence_proxy_async();  // the generic-proxy writes of A before the tensor core reads them
+        mbar_arrive(&full[s]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          v0[q] = v1[q];
+          v1[q] = v2[q];
+        }
+        c0 = c1;
+        c1 = c2;
+        c2 = next(c2);
+      }
+      if (tid == 0)
+        // copies issued into a stage whose MMAs never ran must land before the CTA exits
+        for (int s = 0; s < WS_STAGES; ++s)
+          if (armed[s] && stopped()) mbar_wait(&full[s], (unsigned)((armed[s] - 1) & 1), STREAM_WAIT_CYCLES);
+    }
+  } else if (warp == 12) {
+    // ---- the MMA thread
+    if (mma && lane == 0) {
+      long n = 0, j = 0;
+      for (long item = blockIdx.x; item < A.nitems && !stopped(); item += gridDim.x, ++j) {
+        const int b = (int)(j & 1);
+        const long vv = j >> 1;
+        if (j >= 2 && !mbar_wait(&acce[b], (unsigned)((vv - 1) & 1), STREAM_WAIT_CYCLES)) {
+          give_up();
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int g = (int)(item % A.ngroups);
+        const int ncol = ((2 * min(TC_NW, A.nof - g * TC_NW) + 15) / 16) * 16;
+        const uint32_t idesc = tc_idesc(ncol), acc = tmem + (uint32_t)(b * TC_NMAX);
+        bool ok = true;
+        for (int c = 0; c < nch; ++c, ++n) {
+          const int s = (int)(n % WS_STAGES);
+          const long u = n / WS_STAGES;
+          if (!mbar_wait(&full[s], (unsigned)(u & 1), STREAM_WAIT_CYCLES)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          unsigned char* st = smem + s * TC_STAGE;
+          const float* Ah = (const float*)st;
+          const float* Al = (const float*)(st + TC_A_BYTES);
+          const float* Bh = (const float*)(st + 2 * TC_A_BYTES);
+          const float* Bl = (const float*)(st + 2 * TC_A_BYTES + TC_B_BYTES);
+#pragma unroll
+          for (int ks = 0; ks < TC_KC / 8; ++ks) {
+            const uint64_t ah = tc_desc(Ah + 64 * ks), al = tc_desc(Al + 64 * ks);
+            const uint64_t bh = tc_desc(Bh + 64 * ks), bl = tc_desc(Bl + 64 * ks);
+            tc_mma(acc, ah, bh, idesc, (c > 0 || ks > 0) ? 1 : 0);
+            tc_mma(acc, ah, bl, idesc, 1);
+            tc_mma(acc, al, bh, idesc, 1);
+          }
+          tc_commit(&empty[s]);
+        }
+        if (!ok) {
+          give_up();
+          break;
+        }
+        tc_commit(&accf[b]);
+      }
+      // every MMA issued has completed before the TMEM is freed
+      tc_commit(&fin);
+      mbar_wait(&fin, 0, STREAM_WAIT_CYCLES);
+    }
+  } else {
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4); the two warps of a
+    // quarter take alternate 8-frequency chunks
+    const int q4 = warp & 3, hw = (warp - 4) >> 2;
+    long j = 0;
+    for (long item = blockIdx.x; item < A.nitems; item += gridDim.x, ++j) {
+      if (__any_sync(0xffffffffu, stopped())) break;
+      const int b = (int)(j & 1);
+      const long vv = j >> 1;
+      int g;
+      const WsRow<FLUX> r = ws_item<FLUX>(A, item, g);
+      const long ep = ws_point<FLUX>(r, 32 * q4 + lane);
+      const int nw = min(TC_NW, A.nof - g * TC_NW), nchk = (nw + 7) / 8;
+      float4* fdg = A.fd + (long)g * TC_NW * A.P;
+      auto load_fd = [&](int ch, float4* dst) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          dst[q] = (ep >= 0 && 8 * ch + q < nw) ? fdg[(long)(8 * ch + q) * A.P + ep] : make_float4(0.f, 0.f, 0.f, 0.f);
+      };
+      // this half's chunks hw, hw + 2, ...: the accumulators of the next two
+      // in registers while one is added and written (or reduced)
+      float4 fa[8], fb[8], fc[8];
+      if (hw < nchk) load_fd(hw, fa);
+      if (hw + 2 < nchk) load_fd(hw + 2, fb);
+      if (mma) {
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&accf[b], (unsigned)(vv & 1), STREAM_WAIT_CYCLES));
+        if (!ok) {
+          if (lane == 0) give_up();
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      }
+      for (int ch = hw; ch < nchk; ch += 2) {
+        if (ch + 4 < nchk) load_fd(ch + 4, fc);
+        if (mma) {
+          uint32_t t[16];
+          const uint32_t ta = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(b * TC_NMAX + 16 * ch);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+              "[%16];\n"
+              : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7]),
+                "=r"(t[8]), "=r"(t[9]), "=r"(t[10]), "=r"(t[11]), "=r"(t[12]), "=r"(t[13]), "=r"(t[14]), "=r"(t[15])
+              : "r"(ta)
+              : "memory");
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int q = 0; q < 8; ++q) acc_add(fa[q], __uint_as_float(t[2 * q]), __uint_as_float(t[2 * q + 1]));
+        }
+        if (FLUX) {
+          // lane 4 l + c holds component c of location 8 q4 + l: the lane of
+          // component 0 forms Re(a conj b) - Re(c conj d) from the leading
+          // parts of its three neighbours' values, the 8 locations are summed
+          // in a fixed order, and the sum goes out in FP64.  The products are
+          // FP32 on values scaled by a power of two that brings the warp's
+          // largest to [1, 2) (undone exactly in FP64), so that fields far
+          // below 1 (the pulse's leading tail) neither underflow nor lose
+          // precision; values far below the warp's largest do not count.
+          const bool has = ep >= 0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const unsigned ex = max(__float_as_uint(fa[q].x) >> 23 & 0xffu, __float_as_uint(fa[q].y) >> 23 & 0xffu);
+            const int sc = min(126, max(-126, 127 - (int)__reduce_max_sync(0xffffffffu, ex)));
+            const float f = __uint_as_float((unsigned)(127 + sc) << 23);
+            const float ax = fa[q].x * f, ay = fa[q].y * f;
+            const float bx = __shfl_down_sync(0xffffffffu, ax, 1), by = __shfl_down_sync(0xffffffffu, ay, 1);
+            const float cx2 = __shfl_down_sync(0xffffffffu, ax, 2), cy = __shfl_down_sync(0xffffffffu, ay, 2);
+            const float dx = __shfl_down_sync(0xffffffffu, ax, 3), dy = __shfl_down_sync(0xffffffffu, ay, 3);
+            float v = ((lane & 3) == 0 && has) ? (ax * bx + ay * by) - (cx2 * dx + cy * dy) : 0.f;
+#pragma unroll
+            for (int o = 16; o >= 4; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && 8 * ch + q < nw)
+              A.part[(long)(g * TC_NW + 8 * ch + q) * (4L * A.ft.start[6]) + 4L * r.tile + q4] =
+                  (double)v * __longlong_as_double((long long)(1023 - 2 * sc) << 52);
+          }
+        } else if (ep >= 0) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            if (8 * ch + q < nw) fdg[(long)(8 * ch + q) * A.P + ep] = fa[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          fa[q] = fb[q];
+          fb[q] = fc[q];
+        }
+      }
+      if (mma) {
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(&acce[b]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 12 && mma)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_NMAX) : "memory");
+}
+
+// J[f][iw] = scale * sign * (sum of face f's partials, four per tile, in
+// order within each thread, then a fixed tree).
 __global__ void __launch_bounds__(256) k_flux_sum(const double* __restrict__ part, FluxTiles ft,
                                                   const FluxFace* __restrict__ faces, int nof, double scale,
                                                   double* __restrict__ J) {
   __shared__ double red[256];
   const int iw = blockIdx.x, f = blockIdx.y;
-  const long ntiles = ft.start[6];
-  int t0 = 0, t1 = 0;
+  const long nparts = 4L * ft.start[6];  // one partial per tile and TMEM lane quarter
+  long t0 = 0, t1 = 0;
 #pragma unroll
   for (int i = 0; i < 6; ++i)
     if (i == f) {
-      t0 = ft.start[i];
-      t1 = ft.start[i + 1];
+      t0 = 4L * ft.start[i];
+      t1 = 4L * ft.start[i + 1];
     }
   double s = 0.0;
-  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) s += part[(long)iw * ntiles + t];
+  for (long t = t0 + threadIdx.x; t < t1; t += blockDim.x) s += part[(long)iw * nparts + t];
   red[threadIdx.x] = s;
   __syncthreads();
   for (int w = 128; w > 0; w >>= 1) {
@@ -1198,6 +1225,100 @@ template <typename T, bool CEPS> __global__ void __launch_bounds__(TINY_THREADS)
 }
 
 // ---------------------------------------------------------------------------
+// Material generators: the structure's eps_inv over planes hi..hf (ghost
+// rows and columns included) built on the device, the voxelisers of the
+// geometry front-end (slit() of code/mesh.f90:57-69 generalised), value for
+// value what the host voxelisers compute:
+//   kind 1 (spheres): 1/eps_bbox, then for each sphere (cx, cy, cz, r, eps)
+//     in order, 1/eps where ((z-cz)^2 + (y-cy)^2) + (x-cx)^2 <= r^2 over the
+//     sphere's bounding box (z clipped to [hi, hf], x and y at most nx and
+//     ny cells from floor(c - r), taken modulo the period); later spheres
+//     win;
+//   kind 2 (pattern): 1/eps_in where the i-th SplitMix64 draw of the seed is
+//     below fill, else 1/eps_out, i = ((z-hi) ny + y-1) nx + x-1;
+//   kind 3 (design region): 1/(emin + (emax-emin) u_i) over [x0,x1] x [y0,y1],
+//     i in the region's own (z, y, x) order, 1/eps_bbox elsewhere.
+// Kinds 1 and 2 fill the ghost rows and columns with their periodic images;
+// kind 3 leaves them at 1/eps_bbox.  FP64 operations are the host's, one
+// rounding each.
+struct GenArgs {
+  int kind, hi, hf;
+  double base;
+  const double* sph;
+  int nsph;
+  unsigned long long seed;
+  double fill, v_in, v_out;
+  int x0, x1, y0, y1;
+  double emin, emax;
+};
+
+__device__ __forceinline__ double splitmix_u(unsigned long long seed, unsigned long long i) {
+  unsigned long long z = seed + (i + 1ull) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+template <typename T> __global__ void k_material_gen(GenArgs G, Geo g, T* __restrict__ out) {
+  const long nx2 = g.nx + 2, nxy = nx2 * (g.ny + 2);
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nzs = G.hf - G.hi + 1;
+  if (t >= nxy * nzs) return;
+  const int zz = (int)(t / nxy);
+  const long rr = t % nxy;
+  const int y = (int)(rr / nx2), x = (int)(rr % nx2), z = G.hi + zz;
+  double v = G.base;
+  if (G.kind == 3) {
+    if (x >= G.x0 && x <= G.x1 && y >= G.y0 && y <= G.y1) {
+      const unsigned long long nxr = G.x1 - G.x0 + 1, nyr = G.y1 - G.y0 + 1;
+      const unsigned long long i = ((unsigned long long)zz * nyr + (unsigned long long)(y - G.y0)) * nxr + (x - G.x0);
+      v = __ddiv_rn(1.0, __dadd_rn(G.emin, __dmul_rn(__dsub_rn(G.emax, G.emin), splitmix_u(G.seed, i))));
+    }
+  } else {
+    const int xs = x == 0 ? g.nx : x == g.nx + 1 ? 1 : x;
+    const int ys = y == 0 ? g.ny : y == g.ny + 1 ? 1 : y;
+    if (G.kind == 2) {
+      const unsigned long long i =
+          ((unsigned long long)zz * g.ny + (unsigned long long)(ys - 1)) * (unsigned long long)g.nx + (xs - 1);
+      v = splitmix_u(G.seed, i) < G.fill ? G.v_in : G.v_out;
+    } else {
+      for (int k = 0; k < G.nsph; ++k) {
+        const double cx = G.sph[5 * k], cy = G.sph[5 * k + 1], cz = G.sph[5 * k + 2], r = G.sph[5 * k + 3];
+        const int zlo = max(G.hi, (int)floor(__dsub_rn(cz, r))), zhi = min(G.hf, (int)ceil(__dadd_rn(cz, r)));
+        if (z < zlo || z > zhi) continue;
+        const int xlo = (int)floor(__dsub_rn(cx, r)), ylo = (int)floor(__dsub_rn(cy, r));
+        const int lx = min(g.nx, (int)ceil(__dadd_rn(cx, r)) - xlo + 1);
+        const int ly = min(g.ny, (int)ceil(__dadd_rn(cy, r)) - ylo + 1);
+        const int xu = xlo + ((xs - xlo) % g.nx + g.nx) % g.nx, yu = ylo + ((ys - ylo) % g.ny + g.ny) % g.ny;
+        if (xu > xlo + lx - 1 || yu > ylo + ly - 1) continue;
+        const double dz = __dsub_rn((double)z, cz), dy = __dsub_rn((double)yu, cy), dx = __dsub_rn((double)xu, cx);
+        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dz, dz), __dmul_rn(dy, dy)), __dmul_rn(dx, dx));
+        if (d2 <= __dmul_rn(r, r)) v = __ddiv_rn(1.0, G.sph[5 * k + 4]);
+      }
+    }
+  }
+  out[(long)zz * g.plane + (long)y * g.pitch + (x + g.xo)] = (T)v;
+}
+
+// Stored material planes hi..hf out to the host (real and imaginary parts).
+template <typename T> __global__ void k_material_get(const void* __restrict__ eps, bool cplx, Geo g, int nzs,
+                                                     double* __restrict__ re, double* __restrict__ im) {
+  const long nx2 = g.nx + 2, nxy = nx2 * (g.ny + 2);
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nxy * nzs) return;
+  const long src = (t / nxy) * g.plane + ((t % nxy) / nx2) * g.pitch + (t % nx2) + g.xo;
+  if (cplx) {
+    const typename V2<T>::t v = ((const typename V2<T>::t*)eps)[src];
+    re[t] = (double)v.x;
+    im[t] = (double)v.y;
+  } else {
+    re[t] = (double)((const T*)eps)[src];
+    im[t] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Field transfer in the reference's own layout, complex(8) (3, 0:nx+1,
 // 0:ny+1, 0:nz+1) (UPML: (3, 1:nx, 1:ny, planes)), a chunk of z planes at a
 // time through a device staging buffer: the host array is read or written
@@ -1291,16 +1412,18 @@ __global__ void k_material(const double* __restrict__ re, const double* __restri
 }
 
 
-__global__ void __launch_bounds__(256) k_flux(const double2* __restrict__ fd, long P, const FluxFace* __restrict__ faces,
+template <typename ACC>
+__global__ void __launch_bounds__(256) k_flux(const ACC* __restrict__ fd, long P, const FluxFace* __restrict__ faces,
                                               int nof, double scale, double* __restrict__ J) {
   __shared__ double red[256];
   const int iw = blockIdx.x, f = blockIdx.y;
   const FluxFace F = faces[f];
   double s = 0.0;
   if (F.active) {
-    const double2* row = fd + (long)iw * P;
+    const ACC* row = fd + (long)iw * P;
     for (long L = threadIdx.x; L < F.n; L += blockDim.x) {
-      const double2 a = row[F.pa + L], b = row[F.pb + L], c = row[F.pc + L], d = row[F.pd + L];
+      const double2 a = acc_value(row[F.pa + L]), b = acc_value(row[F.pb + L]), c = acc_value(row[F.pc + L]),
+                    d = acc_value(row[F.pd + L]);
       s += (a.x * b.x + a.y * b.y) - (c.x * d.x + c.y * d.y);
     }
   }
@@ -1728,6 +1851,44 @@ int upload_material(iris_engine* E, const double* re, const double* im) {
   return IRIS_OK;
 }
 
+// Builds the structure material on the device (k_material_gen); a real
+// material, so eps_bbox must be real.
+int generate_material(iris_engine* E, GenArgs G, const double* host_spheres) {
+  const iris_params& p = E->p;
+  if (p.eps_bbox_im != 0.0) return fail(IRIS_EINVAL, "material generators need a real eps_bbox");
+  const int nzs = p.hf - p.hi + 1;
+  if (nzs <= 0) return fail(IRIS_EINVAL, "no structure planes (hf < hi)");
+  graph_reset(E);  // captured launches hold the old material pointer
+  G.hi = p.hi;
+  G.hf = p.hf;
+  G.base = 1.0 / p.eps_bbox_re;
+  if (E->eps) {
+    CK(cudaStreamSynchronize(E->st));
+    cudaFree(E->eps);
+    E->eps = nullptr;
+  }
+  const Geo& g = E->g;
+  const size_t rsz = E->prec == IRIS_FP64 ? 8 : 4;
+  CK(cudaMalloc(&E->eps, (size_t)nzs * g.plane * rsz));
+  CK(cudaMemsetAsync(E->eps, 0, (size_t)nzs * g.plane * rsz, E->st));
+  double* dsph = nullptr;
+  if (G.kind == 1 && G.nsph > 0) {
+    CK(cudaMalloc(&dsph, sizeof(double) * 5 * G.nsph));
+    CK(cudaMemcpyAsync(dsph, host_spheres, sizeof(double) * 5 * G.nsph, cudaMemcpyHostToDevice, E->st));
+  }
+  G.sph = dsph;
+  const long n = (long)(p.nx + 2) * (p.ny + 2) * nzs;
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  if (E->prec == IRIS_FP64) k_material_gen<double><<<nb, 256, 0, E->st>>>(G, g, (double*)E->eps);
+  else k_material_gen<float><<<nb, 256, 0, E->st>>>(G, g, (float*)E->eps);
+  const cudaError_t e1 = cudaGetLastError();
+  const cudaError_t e2 = cudaStreamSynchronize(E->st);
+  if (dsph) cudaFree(dsph);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) return fail(IRIS_ECUDA, "material generation failed");
+  E->eps_complex = false;
+  return IRIS_OK;
+}
+
 int build_dft(iris_engine* E) {
   const iris_params& p = E->p;
   bool single = true;
@@ -1808,22 +1969,30 @@ void dft_flush(iris_engine* E) {
     const long nblk = (E->P + 127) / 128;
     k_twiddle64<<<(nk * E->p.nof + 255) / 256, 256, 0, E->st>>>(E->d_tk, nk, E->d_fw, E->p.nof, E->d_wt64);
     k_dft_fp64<<<(unsigned)(nblk * nwc), 128, (size_t)nk * DFT64_WC * sizeof(double2), E->st>>>(
-        (const double2*)E->S, E->P, nk, E->d_wt64, E->p.nof, nwc, E->p.dt, E->fd);
+        (const double2*)E->S, E->P, nk, E->d_wt64, E->p.nof, nwc, E->p.dt, (double2*)E->fd);
   } else if (E->dft_tc) {
     const int ng = (E->p.nof + TC_NW - 1) / TC_NW, nch = (2 * nk + TC_KC - 1) / TC_KC;
     const long nt = (long)ng * nch * TC_BROWS * TC_KC;
     k_twiddle_tc<<<(unsigned)((nt + 255) / 256), 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, ng,
                                                                    nch, E->d_wtc);
-    const long ntiles = (E->P + TC_M - 1) / TC_M;
-    k_dft_tc<<<(unsigned)(ntiles * ng), TC_THREADS, TC_SMEM, E->st>>>((const float2*)E->S, E->P, nk, E->d_wtc,
-                                                                       E->p.nof, ng, E->fd, E->d_err);
+    WsArgs A{};
+    A.S = (const float2*)E->S;
+    A.P = E->P;
+    A.nk = nk;
+    A.Bt = E->d_wtc;
+    A.fd = (float4*)E->fd;
+    A.nof = E->p.nof;
+    A.ngroups = ng;
+    A.nitems = (E->P + TC_M - 1) / TC_M * ng;
+    A.err = E->d_err;
+    k_dft_ws<false><<<(unsigned)std::min<long>(A.nitems, E->ws_blocks), WS_THREADS, WS_SMEM, E->st>>>(A);
   } else {
     const int nt = nk * E->p.nof;
     k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
     const int nwc = (E->p.nof + DFT_TW - 1) / DFT_TW;
     const long nblk = (E->P + DFT_TP - 1) / DFT_TP;
-    k_dft_fp32<<<(unsigned)(nblk * nwc), DFT_THREADS, 0, E->st>>>((const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, nwc,
-                                                        E->fd);
+    k_dft_fp32<float4><<<(unsigned)(nblk * nwc), DFT_THREADS, 0, E->st>>>((const float2*)E->S, E->P, nk, E->d_wt, E->p.nof, nwc,
+                                                        (float4*)E->fd);
   }
   E->nslot = 0;
 }
@@ -1906,11 +2075,14 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
   if (E->dft_tc) {
     const int ng = (p.nof + TC_NW - 1) / TC_NW, nch = (2 * E->K + TC_KC - 1) / TC_KC;
     CK(cudaMalloc(&E->d_wtc, sizeof(float) * (size_t)ng * nch * 2 * TC_BROWS * TC_KC));
-    CK(cudaFuncSetAttribute(k_dft_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
-    CK(cudaFuncSetAttribute(k_flux_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FL_SMEM));
+    CK(cudaFuncSetAttribute(k_dft_ws<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WS_SMEM));
+    CK(cudaFuncSetAttribute(k_dft_ws<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WS_SMEM));
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E->device));
+    E->ws_blocks = std::max(1, nsm);  // one persistent CTA per SM (its TMEM takes all 512 columns)
     long maxt = 1;
     for (int s = 0; s + 6 <= nfaces; s += 6) maxt = std::max(maxt, (long)flux_tiles(faces + s).start[6]);
-    CK(cudaMalloc(&E->d_part, sizeof(double) * (size_t)maxt * p.nof));
+    CK(cudaMalloc(&E->d_part, sizeof(double) * 4 * (size_t)maxt * p.nof));
   }
   if (!E->segs.empty()) {
     CK(cudaMalloc(&E->d_segs, sizeof(Seg) * E->segs.size()));
@@ -2162,7 +2334,7 @@ static int stream_status(iris_engine* E) {
 
 // The flux of one face set.  FP32 mode on the tensor cores: over the
 // accumulators plus the samples still in the ring, which stay there
-// (k_twiddle_tc for the pending samples, k_flux_tc, k_flux_sum).  Otherwise
+// (k_twiddle_tc for the pending samples, k_dft_ws in flux mode, k_flux_sum).  Otherwise
 // the ring is committed first and k_flux reads the accumulators.
 int iris::read_flux(iris_engine* E, int set, double* J) {
   const iris_params& p = E->p;
@@ -2170,7 +2342,7 @@ int iris::read_flux(iris_engine* E, int set, double* J) {
   const FluxFace* f6 = E->flux_faces.data() + 6 * set;
   const FluxTiles ft = flux_tiles(f6);
   const int ng = (p.nof + TC_NW - 1) / TC_NW;
-  if (E->dft_tc && (long)ft.start[6] * ng <= 0x7fffffffL) {
+  if (E->dft_tc) {
     KTimer tm(E, IRIS_KC_FLUX);
     const int nk = E->nslot;
     if (nk > 0) {
@@ -2179,14 +2351,32 @@ int iris::read_flux(iris_engine* E, int set, double* J) {
       k_twiddle_tc<<<(unsigned)((nt + 255) / 256), 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, p.nof, p.dt, ng, nch,
                                                                      E->d_wtc);
     }
-    if (ft.start[6] > 0)
-      k_flux_tc<<<(unsigned)((long)ft.start[6] * ng), TC_THREADS, FL_SMEM, E->st>>>(
-          (const float2*)E->S, E->P, nk, E->d_wtc, E->fd, p.nof, ng, E->d_faces + 6 * set, ft, E->d_part, E->d_err);
+    if (ft.start[6] > 0) {
+      WsArgs A{};
+      A.S = (const float2*)E->S;
+      A.P = E->P;
+      A.nk = nk;
+      A.Bt = E->d_wtc;
+      A.fd = (float4*)E->fd;
+      A.nof = p.nof;
+      A.ngroups = ng;
+      A.nitems = (long)ft.start[6] * ng;
+      A.faces = E->d_faces + 6 * set;
+      A.ft = ft;
+      A.part = E->d_part;
+      A.err = E->d_err;
+      k_dft_ws<true><<<(unsigned)std::min<long>(A.nitems, E->ws_blocks), WS_THREADS, WS_SMEM, E->st>>>(A);
+    }
     k_flux_sum<<<dim3(p.nof, 6), 256, 0, E->st>>>(E->d_part, ft, E->d_faces + 6 * set, p.nof, scale, E->d_J);
   } else {
     dft_flush(E);
     KTimer tm(E, IRIS_KC_FLUX);
-    k_flux<<<dim3(p.nof, 6), 256, 0, E->st>>>(E->fd, E->P, E->d_faces + 6 * set, p.nof, scale, E->d_J);
+    if (E->prec == IRIS_FP64)
+      k_flux<double2><<<dim3(p.nof, 6), 256, 0, E->st>>>((const double2*)E->fd, E->P, E->d_faces + 6 * set, p.nof,
+                                                          scale, E->d_J);
+    else
+      k_flux<float4><<<dim3(p.nof, 6), 256, 0, E->st>>>((const float4*)E->fd, E->P, E->d_faces + 6 * set, p.nof, scale,
+                                                         E->d_J);
   }
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(E->h_J, E->d_J, sizeof(double) * 6 * p.nof, cudaMemcpyDeviceToHost, E->st));
@@ -2221,6 +2411,76 @@ int iris_set_material(iris_engine* E, const double* re, const double* im) {
   CK(cudaSetDevice(E->device));
   CK(cudaStreamSynchronize(E->st));
   return upload_material(E, re, im);
+}
+
+int iris_material_spheres(iris_engine* E, int n, const double* spheres) {
+  clear_error();
+  if (!E || n < 0 || (n > 0 && !spheres)) return fail(IRIS_EINVAL, "bad argument");
+  for (int k = 0; k < n; ++k)
+    if (!(spheres[5 * k + 3] >= 0.0) || !(spheres[5 * k + 4] != 0.0) || !std::isfinite(spheres[5 * k]) ||
+        !std::isfinite(spheres[5 * k + 1]) || !std::isfinite(spheres[5 * k + 2]) ||
+        !std::isfinite(spheres[5 * k + 3]) || spheres[5 * k + 3] > 1e6)
+      return fail(IRIS_EINVAL, "sphere " + std::to_string(k) + ": centre, radius (0..1e6) or eps invalid");
+  CK(cudaSetDevice(E->device));
+  GenArgs G{};
+  G.kind = 1;
+  G.nsph = n;
+  return generate_material(E, G, spheres);
+}
+
+int iris_material_pattern(iris_engine* E, unsigned long long seed, double fill, double eps_in, double eps_out) {
+  clear_error();
+  if (!E || eps_in == 0.0 || eps_out == 0.0) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  GenArgs G{};
+  G.kind = 2;
+  G.seed = seed;
+  G.fill = fill;
+  G.v_in = 1.0 / eps_in;
+  G.v_out = 1.0 / eps_out;
+  return generate_material(E, G, nullptr);
+}
+
+int iris_material_design(iris_engine* E, unsigned long long seed, const int region[4], double emin, double emax) {
+  clear_error();
+  if (!E || !region) return fail(IRIS_EINVAL, "bad argument");
+  const iris_params& p = E->p;
+  if (region[0] < 1 || region[1] > p.nx || region[0] > region[1] || region[2] < 1 || region[3] > p.ny ||
+      region[2] > region[3])
+    return fail(IRIS_EINVAL, "design region must lie in [1,nx] x [1,ny]");
+  CK(cudaSetDevice(E->device));
+  GenArgs G{};
+  G.kind = 3;
+  G.seed = seed;
+  G.x0 = region[0];
+  G.x1 = region[1];
+  G.y0 = region[2];
+  G.y1 = region[3];
+  G.emin = emin;
+  G.emax = emax;
+  return generate_material(E, G, nullptr);
+}
+
+int iris_get_material(iris_engine* E, double* re, double* im) {
+  clear_error();
+  if (!E || !re || !im) return fail(IRIS_EINVAL, "bad argument");
+  CK(cudaSetDevice(E->device));
+  const iris_params& p = E->p;
+  const int nzs = p.hf - p.hi + 1;
+  if (nzs <= 0 || !E->eps) return IRIS_OK;
+  const long n = (long)(p.nx + 2) * (p.ny + 2) * nzs;
+  double* d = nullptr;
+  CK(cudaMalloc(&d, sizeof(double) * 2 * n));
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  if (E->prec == IRIS_FP64) k_material_get<double><<<nb, 256, 0, E->st>>>(E->eps, E->eps_complex, E->g, nzs, d, d + n);
+  else k_material_get<float><<<nb, 256, 0, E->st>>>(E->eps, E->eps_complex, E->g, nzs, d, d + n);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(re, d, sizeof(double) * n, cudaMemcpyDeviceToHost, E->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(im, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, E->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(E->st);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(IRIS_ECUDA, std::string("iris_get_material: ") + cudaGetErrorString(e));
+  return IRIS_OK;
 }
 
 int iris_step(iris_engine* E, int it0, int nsteps) {
@@ -2473,17 +2733,28 @@ int iris_get_fdata(iris_engine* E, int box, int j, double* re, double* im, long*
   if (!im) return fail(IRIS_EINVAL, "null buffer");
   dft_flush(E);
   const int nof = E->p.nof;
+  // 16 bytes per value: a double2, or in FP32 mode the double-float pairs
+  // (re_hi, im_hi, re_lo, im_lo) whose sums are exact in FP64
+  const bool df = E->prec != IRIS_FP64;
   std::vector<double2> row((size_t)E->P);
   for (int iw = 0; iw < nof; ++iw) {
-    CK(cudaMemcpyAsync(row.data(), E->fd + (size_t)iw * E->P, sizeof(double2) * E->P, cudaMemcpyDeviceToHost, E->st));
+    CK(cudaMemcpyAsync(row.data(), (const char*)E->fd + (size_t)iw * E->P * 16, 16 * (size_t)E->P,
+                       cudaMemcpyDeviceToHost, E->st));
     CK(cudaStreamSynchronize(E->st));
     for (int side = 0; side < 2; ++side)
       for (int ip = 0; ip < 6; ++ip)
         for (long L = 0; L < F.nloc; ++L) {
           const long q = side * 6 * F.nloc + ip + 6 * L;
           const double2 v = row[F.base[side][ip] + L];
-          re[(size_t)iw * n + q] = v.x;
-          im[(size_t)iw * n + q] = v.y;
+          if (df) {
+            float f[4];
+            std::memcpy(f, &v, sizeof f);
+            re[(size_t)iw * n + q] = (double)f[0] + (double)f[2];
+            im[(size_t)iw * n + q] = (double)f[1] + (double)f[3];
+          } else {
+            re[(size_t)iw * n + q] = v.x;
+            im[(size_t)iw * n + q] = v.y;
+          }
         }
   }
   return IRIS_OK;
@@ -2646,7 +2917,7 @@ extern "C" int iris_dft_block_noalloc(const void* samples, int nk, long npts, in
   cudaStream_t st = (cudaStream_t)stream;
   const int nt = nk * nof;
   k_twiddle<<<(nt + 255) / 256, 256, 0, st>>>(nullptr, t0, t_step, nk, fw, nof, dt, (float2*)wt);
-  k_dft_fp32<<<(unsigned)(nblk * nwc), DFT_THREADS, 0, st>>>((const float2*)samples, npts, nk, (const float2*)wt, nof,
+  k_dft_fp32<double2><<<(unsigned)(nblk * nwc), DFT_THREADS, 0, st>>>((const float2*)samples, npts, nk, (const float2*)wt, nof,
                                                            nwc, (double2*)fdata);
   CK(cudaGetLastError());
   return IRIS_OK;

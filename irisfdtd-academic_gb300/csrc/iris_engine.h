@@ -67,13 +67,16 @@ struct iris_engine {
   void* S = nullptr;
   int* d_tk = nullptr;
   double* d_fw = nullptr;
-  double2* fd = nullptr;
+  // accumulators [nof][P], 16 bytes a value: double2 in FP64 mode, the
+  // double-float float4 (re_hi, im_hi, re_lo, im_lo) in FP32 mode
+  void* fd = nullptr;
   float2* d_wt = nullptr;
   double2* d_wt64 = nullptr;  // FP64 mode twiddles of one block
   bool dft_tc = false;     // FP32 block accumulation on the tensor cores
   float* d_wtc = nullptr;  // its B operands (k_twiddle_tc)
-  // flux faces as uploaded to d_faces (6 per set), and the per-tile flux
-  // partials of the tensor-core flux read (tile count of the largest set x nof)
+  int ws_blocks = 0;       // CTAs of its persistent launches (one per SM)
+  // flux faces as uploaded to d_faces (6 per set), and the flux partials of
+  // the tensor-core flux read (4 per tile of the largest set, x nof)
   std::vector<iris::FluxFace> flux_faces;
   double* d_part = nullptr;
   iris::FluxFace* d_faces = nullptr;

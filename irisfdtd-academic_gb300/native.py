@@ -100,7 +100,8 @@ class IrisParams(ctypes.Structure):
 EXPORTS = [
     "iris_strerror", "iris_last_error", "iris_setparam", "iris_physconsts", "iris_frequencies",
     "iris_create", "iris_destroy", "iris_set_material", "iris_step", "iris_sync", "iris_flux",
-    "iris_dft_commit", "iris_write_scatt", "iris_get_field", "iris_set_field", "iris_get_pml", "iris_set_pml",
+    "iris_dft_commit", "iris_material_spheres", "iris_material_pattern", "iris_material_design",
+    "iris_get_material", "iris_batch_material_pattern", "iris_write_scatt", "iris_get_field", "iris_set_field", "iris_get_pml", "iris_set_pml",
     "iris_get_field_c", "iris_set_field_c", "iris_get_pml_c", "iris_set_pml_c",
     "iris_get_fdata", "iris_get_plane", "iris_apply", "iris_run_input", "iris_timing", "iris_timing_read", "iris_info",
     "iris_dft_block_noalloc", "iris_batch_create", "iris_batch_destroy", "iris_batch_set_material",
@@ -140,6 +141,12 @@ def lib():
     L.iris_sync.argtypes = [vp]
     L.iris_flux.argtypes = [vp, ip, dp]
     L.iris_dft_commit.argtypes = [vp]
+    u64 = ctypes.c_ulonglong
+    L.iris_material_spheres.argtypes = [vp, ip, dp]
+    L.iris_material_pattern.argtypes = [vp, u64, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    L.iris_material_design.argtypes = [vp, u64, ctypes.POINTER(ctypes.c_int), ctypes.c_double, ctypes.c_double]
+    L.iris_get_material.argtypes = [vp, dp, dp]
+    L.iris_batch_material_pattern.argtypes = [vp, ip, u64, ctypes.c_double, ctypes.c_double, ctypes.c_double]
     L.iris_write_scatt.argtypes = [cp, ip, ip, ip, dp]
     L.iris_get_field.argtypes = [vp, ip, dp, dp]
     L.iris_set_field.argtypes = [vp, ip, dp, dp]

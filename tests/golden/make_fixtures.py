@@ -7,7 +7,8 @@ Writes:
 * example_1.inputFDTD.dat, example_2.inputFDTD.dat — the two reference input
   decks (example_{1,2}/inputFDTD.dat) re-emitted value for value through this
   project's own writer: the same section headers and the same leading values
-  on every line setparam() reads, without the reference's comments.
+  on every line setparam() and setparam_SDL() read, without the reference's
+  comments.
 * example_1_oracle.npz — three of the CPU oracle's flux blocks for example_1
   at full length (25962 steps): a regression anchor for the oracle itself.
 * pins.json — numbers the reference states outright: dt and step count of
@@ -39,7 +40,18 @@ def raw_values(path):
         ("Fourier transformation options", [[b1[i], b2[i]] for i in range(6)] +
          [[p.nof], [p.dlamda], [p.lno], [p.to_fourier, p.sample_fourier]]),
         ("Slit Array", [[p.dh], [p.dx]]),
-    ]
+    ] + sdl_values(path, p)
+
+
+def sdl_values(path, p):
+    """The snapshot section setparam_SDL reads (code/sdl.f90:365-400), when the
+    deck turns a snapshot plane on."""
+    if not any(p.sdl_plane_on):
+        return []
+    q = O.setparam_sdl(path)
+    rows = [[q.copy_flag, q.copy_no], list(q.xi), list(q.xf), list(q.yi), list(q.yf), list(q.zi), list(q.zf),
+            [q.module_e]] + [[v] for v in q.field]
+    return [("Time evolution options", rows)]
 
 
 def emit(values, description, out):

@@ -2,8 +2,8 @@
 spectra for the 256x4x768 slit-array workload (eps 4.0, 80 cells thick,
 one 64-cell air slit per period, 16-cell UPML, TF/SF at z = 40, DFT planes
 z = 30 and z = 738) over its full 8000 steps, with 24 of its 300
-frequencies (every 12th wavelength of the workload's grid) to keep the
-oracle's run to about a minute on a few cores.  tests/test_gpu_slit.py
+frequencies (every 12th wavelength of the workload's grid); the oracle's
+run takes about eleven minutes on 8 cores.  tests/test_gpu_slit.py
 compares the GPU engine's FP32 and FP64 spectra with it per spectrum.
 
 Usage: make_slit_fixture.py [threads]

@@ -11,7 +11,7 @@ FP64 oracle the tolerance is the FP32 mode's 1e-4.  Cases: every face pair in
 blocks of 32 and 256 samples with a partial block flushed at the flux read,
 and a 2-D grid.
 
-The FP32 flux read on the tensor cores (k_flux_tc) adds the samples still
+The FP32 flux read on the tensor cores (k_dft_ws in flux mode) adds the samples still
 buffered on the fly and leaves them buffered: it changes no state, and
 committing the buffer first gives the same spectra bit for bit (the pending
 sums are the same MMAs on the same operands).

@@ -10,7 +10,8 @@ spectrum dielectric_layer_spectra.dat (code/common.f90:104-131).  The blocks
 are read back from the files (17 significant digits: the doubles round-trip
 exactly) and compared with the oracle's flux blocks at the same steps within
 1e-12 in FP64; log.dat's step size and step count with the numbers the
-reference quotes for example_1 (irisfdtd_movie.py:25).
+reference quotes for example_1 (irisfdtd_movie.py:25); the deck's snapshot
+plane gives one file per output step, numbered as the movie script expects.
 
 <<LOOP>> mode (code/program.f90:36-57) runs main() once per index with the
 same input; the scatt files are opened for appending, so a two-index deck
@@ -90,6 +91,12 @@ def test_run_input_example1_against_oracle(iris, example1_oracle, tmp_path):
     assert abs(float(dt[0].split("=")[1]) - pins["example_1"]["dt_fs"]) < 5e-9
     assert int(nit[0].split("=")[1].split()[0]) == pins["example_1"]["itmax_steps"]
     assert log[-1].strip() == "...done! status=0"
+    # example_1's snapshot plane (y = 1, z = 75..325, copied 300 times, |E|): one
+    # file per output step, numbered from 2 as the movie script reads them
+    # (irisfdtd_movie.py:21-31); their values are checked in tests/test_gpu_sdl.py
+    snaps = sorted(int(n[len("Y_SDL_E"):-2]) for n in os.listdir(tmp_path) if n.startswith("Y_SDL_E"))
+    assert snaps == list(range(2, len(its) + 2))
+    assert os.path.getsize(tmp_path / "Y_SDL_E2.e") == 300 * 251 * 4 + 8
     # the analytic film spectrum written next to every run
     f = np.loadtxt(tmp_path / "dielectric_layer_spectra.dat")
     assert f.shape == (op.nof, 3)
@@ -121,7 +128,7 @@ def test_run_input_example2_fp32_tr(iris, oracle, tmp_path):
     # the step count enters through itmax (fs): (steps + 0.5) dt, as the workload decks set it
     lines = src.split("\n")
     k = lines.index('"Job options"')
-    lines[k + 2] = repr((steps + 0.5) * op.dt * op.consts["uat"])
+    lines[k + 2] = repr(float((steps + 0.5) * op.dt * op.consts["uat"]))
     (d / "inputFDTD.dat").write_text("\n".join(lines))
     op = oracle.setparam(str(d / "inputFDTD.dat"))
     assert op.texit == steps

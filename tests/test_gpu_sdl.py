@@ -7,7 +7,8 @@ Every snapshot file the engine writes must be one the oracle writes (same
 names: orientation, layer, mode suffix, file number nos + 1, extension)
 with the same REAL(4) record, from the oracle's own run of the same deck: E
 of the output step and H of the step before it, over q*Epump.  Tolerance:
-one REAL(4) rounding step (the FP64 fields agree to ~1e-15 and can straddle
+one REAL(4) rounding step of the file's largest value plus 1e-12 of the
+incident amplitude (the FP64 fields agree to ~1e-15 of it and can straddle
 a rounding boundary).  Cases: example_1's slab with its y plane copied three
 times (E modulus, Ex real, Ey imaginary, Hy with the mode of Ey's entry), and
 a 3D cell with x, y and z planes, two extra z layers, copies on both axes of
@@ -133,10 +134,13 @@ def test_sdl_files_against_oracle(iris, oracle, tmp_path, deck):
     got = sorted(n for n in os.listdir(d) if "_SDL" in n)
     assert got == sorted(want), (got, sorted(want))
     for n, v in want.items():
-        g = read_record(d / n)
+        g = read_record(d / n).astype(np.float64)
         assert g.shape == v.shape, n
-        # at most one REAL(4) rounding step apart
-        np.testing.assert_allclose(g, v, rtol=2.0 ** -22, atol=1e-30, err_msg=n)
+        # the values are over q*Epump, so the incident field is O(1): one REAL(4)
+        # rounding step of the file's largest value, plus the FP64 modes' 1e-12
+        # (components at the roundoff floor, such as Ez here, differ there)
+        err = np.max(np.abs(g - v))
+        assert err <= 2.0 ** -22 * np.max(np.abs(v)) + 1e-12, (n, err)
     # the 3D deck reaches every plane orientation, both z layers and the copies on both axes
     if deck == "3d_planes":
         assert any(n.startswith("X_SDL3layer") for n in got) and any(n.startswith("Y_SDL2layer") for n in got)
