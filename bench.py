@@ -258,9 +258,11 @@ def run_engine(args, rank, world, local):
         eps = np.ascontiguousarray(eps.real)  # a lossless material crosses the API as a real array
 
     # the process's CUDA context and the kernels' modules come up once, on a
-    # small engine of the same configuration, before the end-to-end clock
+    # small engine of the same configuration, before the end-to-end clock;
+    # 16 x 16 columns keep it above the persistent kernel's cell limit, so it
+    # steps with the kernels the full grid uses
     warm_p = p.copy()
-    warm_p.nx, warm_p.ny = min(p.nx, 8), min(p.ny, 8)
+    warm_p.nx, warm_p.ny = min(p.nx, 16), min(p.ny, 16)
     for box in (warm_p.box1, warm_p.box2):  # x and y bounds of the DFT box inside the small grid
         box[0], box[1], box[2], box[3] = 1, warm_p.nx, 1, warm_p.ny
     warm_p.aix, warm_p.afx = 1, 0  # no slit

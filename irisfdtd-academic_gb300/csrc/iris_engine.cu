@@ -468,16 +468,16 @@ __global__ void __launch_bounds__(128) k_dft_fp64(const double2* __restrict__ S,
 // rate, and the block accumulation and the flux read add to every stored
 // value: in FP64 those adds and the float-to-double conversions bound both
 // kernels, in FP32 they cost nothing next to the memory traffic.  A partial
-// sum p is added exactly (TwoSum twice): hi + lo carries about 48 bits, the
-// error of the sum is that of rounding lo + e once.
+// sum p is added by TwoSum (hi + p exactly as s + e), the error term joins
+// lo, and the pair is renormalised (Fast2Sum): hi + lo carries about 48
+// bits.
 __device__ __forceinline__ void df_add(float& hi, float& lo, float p) {
   const float s = __fadd_rn(hi, p);
   const float bp = __fsub_rn(s, hi);
   const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
   const float t = __fadd_rn(lo, e);
   const float h = __fadd_rn(s, t);
-  const float bt = __fsub_rn(h, s);
-  lo = __fadd_rn(__fsub_rn(s, __fsub_rn(h, bt)), __fsub_rn(t, bt));
+  lo = __fsub_rn(t, __fsub_rn(h, s));
   hi = h;
 }
 // The accumulator types: double2 (FP64 accumulation) and float4 (double-float).
@@ -489,6 +489,23 @@ __device__ __forceinline__ void acc_add(float4& a, float re, float im) {
   df_add(a.x, a.z, re);
   df_add(a.y, a.w, im);
 }
+// v * 2^e2 as a double, formed from the float's bits with integer operations
+// (exact; GB300's FP64 pipe is kept out of the flux epilogue).  A zero stays
+// a signed zero, Inf and NaN stay Inf and NaN; subnormal v goes through the
+// FP64 pipe (rare: v is a sum of values scaled to about 1).
+__device__ __forceinline__ double scaled_double(float v, int e2) {
+  const unsigned u = __float_as_uint(v);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const unsigned ef = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  if (ef == 0u) {
+    if (m == 0u) return __longlong_as_double((long long)sign);
+    return (double)v * __longlong_as_double((long long)(1023 + e2) << 52);
+  }
+  if (ef == 0xffu) return __longlong_as_double((long long)(sign | (0x7ffull << 52) | ((unsigned long long)m << 29)));
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)((int)ef - 127 + 1023 + e2) << 52) | ((unsigned long long)m << 29)));
+}
+
 // Value of an accumulator in FP64.
 __device__ __forceinline__ double2 acc_value(const double2& a) { return a; }
 __device__ __forceinline__ double2 acc_value(const float4& a) {
@@ -707,17 +724,23 @@ __device__ __forceinline__ long face_comp(const FluxFace& F, int c) {
 //
 // One CTA per SM walks work items (a row tile and a frequency group) with
 // three roles that overlap each other through mbarriers:
-//   * producers (warps 0-3, one thread per A row): the samples of a chunk of
+//   * producers (warps 0-1, two A rows a thread): the samples of a chunk of
 //     8 samples into the TF32 hi/lo A operands of a stage (plain loads, one
 //     chunk ahead in registers), and one thread bulk-copies the chunk's B
 //     operands into the same stage; WS_STAGES stages in a ring;
-//   * the MMA thread (warp 12): three tcgen05.mma kind::tf32 per 8 K columns
+//   * the MMA thread (warp 18): three tcgen05.mma kind::tf32 per 8 K columns
 //     into one of two TMEM accumulators (256 columns each), each stage freed
 //     by a commit when its MMAs are done, each finished item signalled by a
 //     commit on that accumulator;
-//   * epilogue warps (4-11; warp w reads TMEM lanes 32 (w % 4)): drain an
-//     accumulator while the MMAs of the next item fill the other, streaming
-//     the FP64 accumulators one 8-frequency chunk ahead in registers.
+//   * epilogue warps (2-17; warp w reads TMEM lanes 32 (w % 4), the four
+//     warps of a group cover the four lane quarters, group k takes the
+//     4-frequency chunks k, k + 4, ...): drain an accumulator while the MMAs
+//     of the next item fill the other, streaming the accumulators one chunk
+//     ahead in registers.  Sixteen warps, because the epilogue's work per
+//     value (the double-float update, the products and their shuffles) needs
+//     more warps in flight than its memory stream alone would.  Registers
+//     are handed out to whole groups of four warps: the 19 warps take 96 a
+//     thread.
 // Commit mode: rows are 128 consecutive sample points; the epilogue adds the
 // partial sums into fdata (read once, written once).
 // Flux mode: rows are the four flux components of 32 locations of one face,
@@ -731,8 +754,9 @@ __device__ __forceinline__ long face_comp(const FluxFace& F, int c) {
 // mode, 5 in flux mode) and stops; the others stop at their next wait; the
 // CTA waits (bounded) for its copies and MMAs before it frees its TMEM.
 
-constexpr int WS_STAGES = 3, WS_PROD = 128, WS_EPI = 256;
-constexpr int WS_THREADS = WS_PROD + WS_EPI + 32;  // + the MMA warp
+constexpr int WS_STAGES = 3, WS_PROD = 64, WS_EPI = 512, WS_FCH = 4;
+constexpr int WS_THREADS = WS_PROD + WS_EPI + 32;  // + the MMA warp: 19 warps
+constexpr int WS_MMA_WARP = (WS_PROD + WS_EPI) / 32;
 constexpr size_t WS_SMEM = WS_STAGES * TC_STAGE;
 
 struct WsArgs {
@@ -797,7 +821,7 @@ template <bool FLUX> __device__ __forceinline__ long ws_point(const WsRow<FLUX>&
   return row < r.np ? r.p0 + row : -1;
 }
 
-template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
+template <bool FLUX> __global__ void __launch_bounds__(WS_THREADS, 1) k_dft_ws(WsArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint64_t full[WS_STAGES], empty[WS_STAGES], accf[2], acce[2], fin;
   __shared__ uint32_t taddr_s;
@@ -820,7 +844,7 @@ template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
     stop_s = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 12 && mma) {
+  if (warp == WS_MMA_WARP && mma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&taddr_s)),
                  "r"(2 * TC_NMAX)
                  : "memory");
@@ -837,41 +861,45 @@ template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
   auto stopped = [&]() { return *(volatile int*)&stop_s != 0; };
 
   if (tid < WS_PROD) {
-    // ---- producers: one flat sequence of (item, chunk) pairs, the samples of
-    // the next two chunks in registers while a chunk is split into its stage
+    // ---- producers: one flat sequence of (item, chunk) pairs; a thread takes
+    // rows tid and tid + 64, the samples of the next chunk in registers while
+    // a chunk is split into its stage
     if (mma) {
-      const int row = tid;
       int armed[WS_STAGES] = {};  // fills issued per stage (thread 0: the last one is drained at exit)
       struct Cur {
         long j;
         int c, g;
-        long rp;
+        long rp0, rp1;
         bool ok;
       };
       auto at = [&](long j, int c) {
-        Cur x{j, c, 0, -1, false};
+        Cur x{j, c, 0, -1, -1, false};
         const long item = blockIdx.x + j * gridDim.x;
         if (item < A.nitems) {
           const WsRow<FLUX> r = ws_item<FLUX>(A, item, x.g);
-          x.rp = ws_point<FLUX>(r, row);
+          x.rp0 = ws_point<FLUX>(r, tid);
+          x.rp1 = ws_point<FLUX>(r, tid + WS_PROD);
           x.ok = true;
         }
         return x;
       };
-      auto next = [&](const Cur& x) { return x.c + 1 < nch ? Cur{x.j, x.c + 1, x.g, x.rp, x.ok} : at(x.j + 1, 0); };
+      auto next = [&](const Cur& x) {
+        return x.c + 1 < nch ? Cur{x.j, x.c + 1, x.g, x.rp0, x.rp1, x.ok} : at(x.j + 1, 0);
+      };
       auto load = [&](const Cur& x, float2* dst) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           const int k = x.c * (TC_KC / 2) + q;
-          dst[q] = (x.ok && x.rp >= 0 && k < A.nk) ? A.S[(long)k * A.P + x.rp] : make_float2(0.f, 0.f);
+          const bool kk = x.ok && k < A.nk;
+          dst[q] = (kk && x.rp0 >= 0) ? A.S[(long)k * A.P + x.rp0] : make_float2(0.f, 0.f);
+          dst[8 + q] = (kk && x.rp1 >= 0) ? A.S[(long)k * A.P + x.rp1] : make_float2(0.f, 0.f);
         }
       };
-      Cur c0 = at(0, 0), c1 = next(c0), c2 = next(c1);
-      float2 v0[8], v1[8], v2[8];
+      Cur c0 = at(0, 0), c1 = next(c0);
+      float2 v0[16], v1[16];
       load(c0, v0);
-      load(c1, v1);
       for (long n = 0; c0.ok && !stopped(); ++n) {
-        load(c2, v2);
+        load(c1, v1);
         const int s = (int)(n % WS_STAGES);
         const long u = n / WS_STAGES;
         if (u > 0 && !mbar_wait(&empty[s], (unsigned)((u - 1) & 1), STREAM_WAIT_CYCLES)) {
@@ -892,29 +920,30 @@ template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
         float* Ah = (float*)st;
         float* Al = (float*)(st + TC_A_BYTES);
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const float4 x = make_float4(v0[2 * m].x, v0[2 * m].y, v0[2 * m + 1].x, v0[2 * m + 1].y);
-          const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
-          *(float4*)(Ah + tc_off(row, 4 * m)) = h;
-          *(float4*)(Al + tc_off(row, 4 * m)) = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const int row = tid + h2 * WS_PROD;
+#pragma unroll
+          for (int m = 0; m < 4; ++m) {
+            const float2 a = v0[8 * h2 + 2 * m], bq = v0[8 * h2 + 2 * m + 1];
+            const float4 x = make_float4(a.x, a.y, bq.x, bq.y);
+            const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+            *(float4*)(Ah + tc_off(row, 4 * m)) = h;
+            *(float4*)(Al + tc_off(row, 4 * m)) = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+          }
         }
         fence_proxy_async();  // the generic-proxy writes of A before the tensor core reads them
         mbar_arrive(&full[s]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          v0[q] = v1[q];
-          v1[q] = v2[q];
-        }
+        for (int q = 0; q < 16; ++q) v0[q] = v1[q];
         c0 = c1;
-        c1 = c2;
-        c2 = next(c2);
+        c1 = next(c1);
       }
       if (tid == 0)
         // copies issued into a stage whose MMAs never ran must land before the CTA exits
         for (int s = 0; s < WS_STAGES; ++s)
           if (armed[s] && stopped()) mbar_wait(&full[s], (unsigned)((armed[s] - 1) & 1), STREAM_WAIT_CYCLES);
     }
-  } else if (warp == 12) {
+  } else if (warp == WS_MMA_WARP) {
     // ---- the MMA thread
     if (mma && lane == 0) {
       long n = 0, j = 0;
@@ -964,9 +993,9 @@ template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
       mbar_wait(&fin, 0, STREAM_WAIT_CYCLES);
     }
   } else {
-    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4); the two warps of a
-    // quarter take alternate 8-frequency chunks
-    const int q4 = warp & 3, hw = (warp - 4) >> 2;
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4); group (w - 2) / 4
+    // takes the 4-frequency chunks of its index mod 4
+    const int q4 = warp & 3, grp = (warp - WS_PROD / 32) >> 2;
     long j = 0;
     for (long item = blockIdx.x; item < A.nitems; item += gridDim.x, ++j) {
       if (__any_sync(0xffffffffu, stopped())) break;
@@ -975,18 +1004,16 @@ template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
       int g;
       const WsRow<FLUX> r = ws_item<FLUX>(A, item, g);
       const long ep = ws_point<FLUX>(r, 32 * q4 + lane);
-      const int nw = min(TC_NW, A.nof - g * TC_NW), nchk = (nw + 7) / 8;
+      const int nw = min(TC_NW, A.nof - g * TC_NW), nchk = (nw + WS_FCH - 1) / WS_FCH;
       float4* fdg = A.fd + (long)g * TC_NW * A.P;
       auto load_fd = [&](int ch, float4* dst) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
-          dst[q] = (ep >= 0 && 8 * ch + q < nw) ? fdg[(long)(8 * ch + q) * A.P + ep] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int q = 0; q < WS_FCH; ++q)
+          dst[q] = (ep >= 0 && WS_FCH * ch + q < nw) ? fdg[(long)(WS_FCH * ch + q) * A.P + ep]
+                                                     : make_float4(0.f, 0.f, 0.f, 0.f);
       };
-      // this half's chunks hw, hw + 2, ...: the accumulators of the next two
-      // in registers while one is added and written (or reduced)
-      float4 fa[8], fb[8], fc[8];
-      if (hw < nchk) load_fd(hw, fa);
-      if (hw + 2 < nchk) load_fd(hw + 2, fb);
+      float4 fa[WS_FCH], fb[WS_FCH];
+      if (grp < nchk) load_fd(grp, fa);
       if (mma) {
         const bool ok = __all_sync(0xffffffffu, mbar_wait(&accf[b], (unsigned)(vv & 1), STREAM_WAIT_CYCLES));
         if (!ok) {
@@ -995,21 +1022,18 @@ template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       }
-      for (int ch = hw; ch < nchk; ch += 2) {
-        if (ch + 4 < nchk) load_fd(ch + 4, fc);
+      for (int ch = grp; ch < nchk; ch += 4) {
+        if (ch + 4 < nchk) load_fd(ch + 4, fb);
         if (mma) {
-          uint32_t t[16];
-          const uint32_t ta = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(b * TC_NMAX + 16 * ch);
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-              "[%16];\n"
-              : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7]),
-                "=r"(t[8]), "=r"(t[9]), "=r"(t[10]), "=r"(t[11]), "=r"(t[12]), "=r"(t[13]), "=r"(t[14]), "=r"(t[15])
-              : "r"(ta)
-              : "memory");
+          uint32_t t[2 * WS_FCH];
+          const uint32_t ta = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(b * TC_NMAX + 2 * WS_FCH * ch);
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                       : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7])
+                       : "r"(ta)
+                       : "memory");
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-          for (int q = 0; q < 8; ++q) acc_add(fa[q], __uint_as_float(t[2 * q]), __uint_as_float(t[2 * q + 1]));
+          for (int q = 0; q < WS_FCH; ++q) acc_add(fa[q], __uint_as_float(t[2 * q]), __uint_as_float(t[2 * q + 1]));
         }
         if (FLUX) {
           // lane 4 l + c holds component c of location 8 q4 + l: the lane of
@@ -1017,12 +1041,13 @@ template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
           // parts of its three neighbours' values, the 8 locations are summed
           // in a fixed order, and the sum goes out in FP64.  The products are
           // FP32 on values scaled by a power of two that brings the warp's
-          // largest to [1, 2) (undone exactly in FP64), so that fields far
-          // below 1 (the pulse's leading tail) neither underflow nor lose
-          // precision; values far below the warp's largest do not count.
+          // largest to [1, 2) (undone exactly when the sum is widened), so
+          // that fields far below 1 (the pulse's leading tail) neither
+          // underflow nor lose precision; values far below the warp's largest
+          // do not count.
           const bool has = ep >= 0;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
+          for (int q = 0; q < WS_FCH; ++q) {
             const unsigned ex = max(__float_as_uint(fa[q].x) >> 23 & 0xffu, __float_as_uint(fa[q].y) >> 23 & 0xffu);
             const int sc = min(126, max(-126, 127 - (int)__reduce_max_sync(0xffffffffu, ex)));
             const float f = __uint_as_float((unsigned)(127 + sc) << 23);
@@ -1033,20 +1058,17 @@ template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
             float v = ((lane & 3) == 0 && has) ? (ax * bx + ay * by) - (cx2 * dx + cy * dy) : 0.f;
 #pragma unroll
             for (int o = 16; o >= 4; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0 && 8 * ch + q < nw)
-              A.part[(long)(g * TC_NW + 8 * ch + q) * (4L * A.ft.start[6]) + 4L * r.tile + q4] =
-                  (double)v * __longlong_as_double((long long)(1023 - 2 * sc) << 52);
+            if (lane == 0 && WS_FCH * ch + q < nw)
+              A.part[(long)(g * TC_NW + WS_FCH * ch + q) * (4L * A.ft.start[6]) + 4L * r.tile + q4] =
+                  scaled_double(v, -2 * sc);
           }
         } else if (ep >= 0) {
 #pragma unroll
-          for (int q = 0; q < 8; ++q)
-            if (8 * ch + q < nw) fdg[(long)(8 * ch + q) * A.P + ep] = fa[q];
+          for (int q = 0; q < WS_FCH; ++q)
+            if (WS_FCH * ch + q < nw) fdg[(long)(WS_FCH * ch + q) * A.P + ep] = fa[q];
         }
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          fa[q] = fb[q];
-          fb[q] = fc[q];
-        }
+        for (int q = 0; q < WS_FCH; ++q) fa[q] = fb[q];
       }
       if (mma) {
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -1056,7 +1078,7 @@ template <bool FLUX> __global__ void __maxnreg__(152) k_dft_ws(WsArgs A) {
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 12 && mma)
+  if (warp == WS_MMA_WARP && mma)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_NMAX) : "memory");
 }
 
@@ -1117,6 +1139,17 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned x) {
+  unsigned v;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "r"(x) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u32(unsigned* p, unsigned x) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
+}
+__device__ __forceinline__ void red_add_release(unsigned* p, unsigned x) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
+}
 
 // All CTAs of the launch reach this point before any passes it; false when
 // the wait gave up.  gen: the generation this CTA waits to see advance
@@ -1127,11 +1160,13 @@ __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned& gen, unsigned
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    __threadfence();
-    if (atomicAdd(&b->count, 1u) == nblk - 1) {
-      atomicExch(&b->count, 0u);
-      __threadfence();
-      atomicAdd(&b->gen, 1u);
+    // the arrival releases this CTA's writes (ordered before it by the
+    // __syncthreads) and acquires the earlier arrivals'; the last arriver
+    // resets the count and releases the new generation, which the others
+    // acquire
+    if (atom_add_acq_rel(&b->count, 1u) == nblk - 1) {
+      st_relaxed_u32(&b->count, 0u);
+      red_add_release(&b->gen, 1u);
     } else {
       const long long t0 = clock64();
       while (ld_acquire_u32(&b->gen) == gen)
@@ -1140,7 +1175,6 @@ __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned& gen, unsigned
           break;
         }
     }
-    __threadfence();
     gen += 1;
     if (!ok) atomicExch(err, 6);
     ok_s = ok;
@@ -1241,10 +1275,19 @@ template <typename T, bool CEPS> __global__ void __launch_bounds__(TINY_THREADS)
 // Kinds 1 and 2 fill the ghost rows and columns with their periodic images;
 // kind 3 leaves them at 1/eps_bbox.  FP64 operations are the host's, one
 // rounding each.
+// A sphere as the generator reads it: centre, r^2 and 1/eps, and its
+// bounding box, the z planes [zlo, zhi] and the x and y ranges xlo .. xlo +
+// lx - 1, ylo .. ylo + ly - 1 (periodic in x and y); built on the host, with
+// the same IEEE operations, once per sphere rather than once per cell.
+struct SphereBox {
+  double cx, cy, cz, r2, inv;
+  int zlo, zhi, xlo, lx, ylo, ly;
+};
+
 struct GenArgs {
   int kind, hi, hf;
   double base;
-  const double* sph;
+  const SphereBox* sph;
   int nsph;
   unsigned long long seed;
   double fill, v_in, v_out;
@@ -1284,17 +1327,13 @@ template <typename T> __global__ void k_material_gen(GenArgs G, Geo g, T* __rest
       v = splitmix_u(G.seed, i) < G.fill ? G.v_in : G.v_out;
     } else {
       for (int k = 0; k < G.nsph; ++k) {
-        const double cx = G.sph[5 * k], cy = G.sph[5 * k + 1], cz = G.sph[5 * k + 2], r = G.sph[5 * k + 3];
-        const int zlo = max(G.hi, (int)floor(__dsub_rn(cz, r))), zhi = min(G.hf, (int)ceil(__dadd_rn(cz, r)));
-        if (z < zlo || z > zhi) continue;
-        const int xlo = (int)floor(__dsub_rn(cx, r)), ylo = (int)floor(__dsub_rn(cy, r));
-        const int lx = min(g.nx, (int)ceil(__dadd_rn(cx, r)) - xlo + 1);
-        const int ly = min(g.ny, (int)ceil(__dadd_rn(cy, r)) - ylo + 1);
-        const int xu = xlo + ((xs - xlo) % g.nx + g.nx) % g.nx, yu = ylo + ((ys - ylo) % g.ny + g.ny) % g.ny;
-        if (xu > xlo + lx - 1 || yu > ylo + ly - 1) continue;
-        const double dz = __dsub_rn((double)z, cz), dy = __dsub_rn((double)yu, cy), dx = __dsub_rn((double)xu, cx);
+        const SphereBox b = G.sph[k];
+        if (z < b.zlo || z > b.zhi) continue;
+        const int xu = b.xlo + ((xs - b.xlo) % g.nx + g.nx) % g.nx, yu = b.ylo + ((ys - b.ylo) % g.ny + g.ny) % g.ny;
+        if (xu > b.xlo + b.lx - 1 || yu > b.ylo + b.ly - 1) continue;
+        const double dz = __dsub_rn((double)z, b.cz), dy = __dsub_rn((double)yu, b.cy), dx = __dsub_rn((double)xu, b.cx);
         const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dz, dz), __dmul_rn(dy, dy)), __dmul_rn(dx, dx));
-        if (d2 <= __dmul_rn(r, r)) v = __ddiv_rn(1.0, G.sph[5 * k + 4]);
+        if (d2 <= b.r2) v = b.inv;
       }
     }
   }
@@ -1871,10 +1910,28 @@ int generate_material(iris_engine* E, GenArgs G, const double* host_spheres) {
   const size_t rsz = E->prec == IRIS_FP64 ? 8 : 4;
   CK(cudaMalloc(&E->eps, (size_t)nzs * g.plane * rsz));
   CK(cudaMemsetAsync(E->eps, 0, (size_t)nzs * g.plane * rsz, E->st));
-  double* dsph = nullptr;
+  SphereBox* dsph = nullptr;
+  std::vector<SphereBox> boxes;
   if (G.kind == 1 && G.nsph > 0) {
-    CK(cudaMalloc(&dsph, sizeof(double) * 5 * G.nsph));
-    CK(cudaMemcpyAsync(dsph, host_spheres, sizeof(double) * 5 * G.nsph, cudaMemcpyHostToDevice, E->st));
+    boxes.resize(G.nsph);
+    for (int k = 0; k < G.nsph; ++k) {
+      const double* q = host_spheres + 5 * k;
+      const double cx = q[0], cy = q[1], cz = q[2], r = q[3];
+      SphereBox& b = boxes[k];
+      b.cx = cx;
+      b.cy = cy;
+      b.cz = cz;
+      b.r2 = r * r;
+      b.inv = 1.0 / q[4];
+      b.zlo = std::max(p.hi, (int)std::floor(cz - r));
+      b.zhi = std::min(p.hf, (int)std::ceil(cz + r));
+      b.xlo = (int)std::floor(cx - r);
+      b.lx = std::min(p.nx, (int)std::ceil(cx + r) - b.xlo + 1);
+      b.ylo = (int)std::floor(cy - r);
+      b.ly = std::min(p.ny, (int)std::ceil(cy + r) - b.ylo + 1);
+    }
+    CK(cudaMalloc(&dsph, sizeof(SphereBox) * G.nsph));
+    CK(cudaMemcpyAsync(dsph, boxes.data(), sizeof(SphereBox) * G.nsph, cudaMemcpyHostToDevice, E->st));
   }
   G.sph = dsph;
   const long n = (long)(p.nx + 2) * (p.ny + 2) * nzs;
