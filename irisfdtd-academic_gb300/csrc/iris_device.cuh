@@ -184,17 +184,18 @@ __device__ __forceinline__ void e_cell(const FieldArgs<T>& a, typename V2<T>::t*
 // and of its +x, +y, +z neighbours (xp: components 2,3; yp: 1,3; zp: 1,2),
 // the old H read from a.h, the UPML auxiliary B updated in place.  UPML =
 // false: the cell lies outside the UPML slabs.  bv / cfv: the cell's old B and
-// the plane's coefficient row when the caller has copied them ahead.
-template <typename T, bool UPML = true>
+// the plane's coefficient row when the caller has copied them ahead.  MASK
+// selects the components computed (bit k: H_{k+1}).
+template <typename T, bool UPML = true, int MASK = 7>
 __device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, int z, const cx<T> ev[3],
                                          const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3],
                                          const cx<T>* bv = nullptr, const T* cfv = nullptr) {
   using V = typename V2<T>::t;
   const Geo& g = a.g;
   cx<T> c[3];
-  c[0] = cadd(csub(csub(yp[2], ev[2]), zp[1]), ev[1]);
-  c[1] = cadd(csub(csub(zp[0], ev[0]), xp[2]), ev[2]);
-  c[2] = cadd(csub(csub(xp[1], ev[1]), yp[0]), ev[0]);
+  if (MASK & 1) c[0] = cadd(csub(csub(yp[2], ev[2]), zp[1]), ev[1]);
+  if (MASK & 2) c[1] = cadd(csub(csub(zp[0], ev[0]), xp[2]), ev[2]);
+  if (MASK & 4) c[2] = cadd(csub(csub(xp[1], ev[1]), yp[0]), ev[0]);
   if (UPML && (z <= a.pmlzi || z >= a.pmlzf)) {
     const int slab = z <= a.pmlzi ? 0 : 1;
     const int zr = slab == 0 ? z - 1 : z - a.pmlzf;
@@ -205,6 +206,7 @@ __device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, in
     const long pc = a.pcomp[slab];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
+      if (!(MASK & (1 << k))) continue;
       const cx<T> bold = bv ? bv[k] : ld<T>(B + k * pc + pi);
       const cx<T> bn = csub(rmul(cf[CD_A + k], bold), rmul(cf[CB_B + k], c[k]));
       st<T>(B + k * pc + pi, bn);
@@ -212,46 +214,54 @@ __device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, in
     }
   } else {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) h[k] = csub(h[k], rmul(a.dtcq2, c[k]));
+    for (int k = 0; k < 3; ++k)
+      if (MASK & (1 << k)) h[k] = csub(h[k], rmul(a.dtcq2, c[k]));
   }
 }
 
 // h_update with the old H of the cell loaded from a.h.
-template <typename T, bool UPML = true>
+template <typename T, bool UPML = true, int MASK = 7>
 __device__ __forceinline__ void h_cell(const FieldArgs<T>& a, int x, int y, int z, const cx<T> ev[3],
                                        const cx<T> xp[3], const cx<T> yp[3], const cx<T> zp[3], cx<T> h[3]) {
   const long i = a.g.at(x, y, z);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) h[k] = ld<T>(a.h + k * a.g.comp + i);
-  h_update<T, UPML>(a, x, y, z, ev, xp, yp, zp, h);
+  for (int k = 0; k < 3; ++k)
+    if (MASK & (1 << k)) h[k] = ld<T>(a.h + k * a.g.comp + i);
+  h_update<T, UPML, MASK>(a, x, y, z, ev, xp, yp, zp, h);
 }
 
 // Split E pass of one cell: e_cell in place + bc_{x,y,z}max_bloch
-// (code/boundary.f90:193-216,257-284,321-348) for the E ghosts.
-template <typename T, bool CEPS, bool UPML = true>
+// (code/boundary.f90:193-216,257-284,321-348) for the E ghosts.  MASK: the
+// components computed and stored (bit k: E_{k+1}); the components of a cell
+// are independent, so a cell may be split over threads.
+template <typename T, bool CEPS, bool UPML = true, int MASK = 7>
 __device__ __forceinline__ void e_split_cell(const FieldArgs<T>& a, int x, int y, int z) {
   using V = typename V2<T>::t;
   const Geo& g = a.g;
   const long i = g.at(x, y, z);
   V* E[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
   cx<T> e[3];
-  e_cell<T, CEPS, 7, UPML>(a, a.pml_d, x, y, z, e);
+  e_cell<T, CEPS, MASK, UPML>(a, a.pml_d, x, y, z, e);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) st<T>(E[k] + i, e[k]);
+  for (int k = 0; k < 3; ++k)
+    if (MASK & (1 << k)) st<T>(E[k] + i, e[k]);
   if (x == 1) {
     const long j = g.at(g.nx + 1, y, z);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pxp, e[k]));
+    for (int k = 0; k < 3; ++k)
+      if (MASK & (1 << k)) st<T>(E[k] + j, cmul(a.pxp, e[k]));
   }
   if (y == 1) {
     const long j = g.at(x, g.ny + 1, z);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pyp, e[k]));
+    for (int k = 0; k < 3; ++k)
+      if (MASK & (1 << k)) st<T>(E[k] + j, cmul(a.pyp, e[k]));
   }
   if (z == 1) {
     const long j = g.at(x, y, g.nz + 1);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) st<T>(E[k] + j, cmul(a.pzp, e[k]));
+    for (int k = 0; k < 3; ++k)
+      if (MASK & (1 << k)) st<T>(E[k] + j, cmul(a.pzp, e[k]));
   }
 }
 
@@ -259,7 +269,7 @@ __device__ __forceinline__ void e_split_cell(const FieldArgs<T>& a, int x, int y
 // (code/boundary.f90:163-187,224-251,288-315) for the H ghosts and the E
 // ghosts at 0.  The ghosts at nx+1/ny+1/nz+1 of H are never read by any
 // operator and are not maintained.
-template <typename T, bool UPML = true>
+template <typename T, bool UPML = true, int MASK = 7>
 __device__ __forceinline__ void h_split_cell(const FieldArgs<T>& a, int x, int y, int z) {
   using V = typename V2<T>::t;
   const Geo& g = a.g;
@@ -275,32 +285,36 @@ __device__ __forceinline__ void h_split_cell(const FieldArgs<T>& a, int x, int y
   yp[2] = ld<T>(Ec[2] + i + g.pitch);
   zp[0] = ld<T>(Ec[0] + i + g.plane);
   zp[1] = ld<T>(Ec[1] + i + g.plane);
-  h_cell<T, UPML>(a, x, y, z, ev, xp, yp, zp, h);
+  h_cell<T, UPML, MASK>(a, x, y, z, ev, xp, yp, zp, h);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) st<T>(H[k] + i, h[k]);
+  for (int k = 0; k < 3; ++k)
+    if (MASK & (1 << k)) st<T>(H[k] + i, h[k]);
   if (x == g.nx) {
     const long j = g.at(0, y, z);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      st<T>(Ec[k] + j, cmul(a.pxm, ev[k]));
-      st<T>(H[k] + j, cmul(a.pxm, h[k]));
-    }
+    for (int k = 0; k < 3; ++k)
+      if (MASK & (1 << k)) {
+        st<T>(Ec[k] + j, cmul(a.pxm, ev[k]));
+        st<T>(H[k] + j, cmul(a.pxm, h[k]));
+      }
   }
   if (y == g.ny) {
     const long j = g.at(x, 0, z);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      st<T>(Ec[k] + j, cmul(a.pym, ev[k]));
-      st<T>(H[k] + j, cmul(a.pym, h[k]));
-    }
+    for (int k = 0; k < 3; ++k)
+      if (MASK & (1 << k)) {
+        st<T>(Ec[k] + j, cmul(a.pym, ev[k]));
+        st<T>(H[k] + j, cmul(a.pym, h[k]));
+      }
   }
   if (z == g.nz) {
     const long j = g.at(x, y, 0);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      st<T>(Ec[k] + j, cmul(a.pzm, ev[k]));
-      st<T>(H[k] + j, cmul(a.pzm, h[k]));
-    }
+    for (int k = 0; k < 3; ++k)
+      if (MASK & (1 << k)) {
+        st<T>(Ec[k] + j, cmul(a.pzm, ev[k]));
+        st<T>(H[k] + j, cmul(a.pzm, h[k]));
+      }
   }
 }
 
@@ -412,49 +426,72 @@ template <> __device__ __forceinline__ void corr<float>(float2* p, cx<double> v,
 
 constexpr int TFSF_YCH = 16;
 
-// Incident field at ix and the corrections of the rows iy in [y0, y1].
-template <typename T>
-__device__ __forceinline__ void tfsf_column(typename V2<T>::t* e, typename V2<T>::t* h, const Geo& g,
-                                            const SrcArgs& s, int it, int ix, int y0, int y1) {
+// The two corrections of one column at one step, as tabulated for the
+// persistent kernel.
+struct __align__(32) TfsfVal {
+  double er, ei, hr, hi;  // vE, vH
+};
+
+// The two corrections of column ix at step it: vE (added to or subtracted
+// from E at iz_min) and vH (at iz_min-1 in variant 1, iz_min in variant 2).
+// They depend on (ix, it) only: the incident field is y-independent.
+__device__ __forceinline__ void tfsf_values(const SrcArgs& s, int it, int ix, cx<double>& vE, cx<double>& vH) {
   const int zm = s.iz_min;
-  cx<double> ta, tb, vE, vH;
-  typename V2<T>::t *pe, *ph;
-  int sE, sH, exE, exH, eyE, eyH;  // ix limit and iy limit per update
   if (s.variant == 1) {
     cx<double> a0, b0, a1, b1;
     incident(s, ix, zm - 1, it, a0, b0);  // tfsf_data(:, ix, iy, iz_min-1)
     incident(s, ix, zm, it, a1, b1);      // tfsf_data(:, ix, iy, iz_min)
     vE = {dm(s.eps_in1, b0.re), dm(s.eps_in1, b0.im)};
     vH = {dm(s.dtcq2, a1.re), dm(s.dtcq2, a1.im)};
-    if (s.i_pol == 2) {
-      // E_x(iz_min) += eps_in(1)*tf5(iz_min-1): ix in [0,nx], iy in [0,ny+1]
-      // H_y(iz_min-1) += dtcq2*tf1(iz_min):      ix in [0,nx], iy in [0,ny+1]
-      pe = e;
-      ph = h + g.comp;
-      sE = +1; sH = +1;
-      exE = s.nx; exH = s.nx; eyE = s.ny + 1; eyH = s.ny + 1;
-    } else {
-      // E_y(iz_min) -= eps_in(1)*tf4(iz_min-1): ix in [0,nx+1], iy in [0,ny]
-      // H_x(iz_min-1) -= dtcq2*tf2(iz_min):      ix in [0,nx+1], iy in [0,ny]
-      pe = e + g.comp;
-      ph = h;
-      sE = -1; sH = -1;
-      exE = s.nx + 1; exH = s.nx + 1; eyE = s.ny; eyH = s.ny;
-    }
-    for (int iy = y0; iy <= y1; ++iy) {
-      if (ix <= exE && iy <= eyE) corr<T>(pe + g.at(ix, iy, zm), vE, sE);
-      if (ix <= exH && iy <= eyH) corr<T>(ph + g.at(ix, iy, zm - 1), vH, sH);
-    }
   } else if (s.variant == 2) {
-    // E_x(iz_min) += tf5(iz_min)/eps ; H_y(iz_min) += dtcq2*tf1(iz_min)
+    cx<double> ta, tb;
     incident(s, ix, zm, it, ta, tb);
     vE = {dq(tb.re, s.eps_src), dq(tb.im, s.eps_src)};
     vH = {dm(s.dtcq2, ta.re), dm(s.dtcq2, ta.im)};
+  } else {
+    vE = {0.0, 0.0};
+    vH = {0.0, 0.0};
+  }
+}
+
+// The corrections of column ix over the rows iy in [y0, y1]
+// (code/tfsf.f90:76-153, :163-227).
+template <typename T>
+__device__ __forceinline__ void tfsf_apply(typename V2<T>::t* e, typename V2<T>::t* h, const Geo& g,
+                                           const SrcArgs& s, int ix, int y0, int y1, cx<double> vE, cx<double> vH) {
+  const int zm = s.iz_min;
+  if (s.variant == 1) {
+    if (s.i_pol == 2) {
+      // E_x(iz_min) += eps_in(1)*tf5(iz_min-1): ix in [0,nx], iy in [0,ny+1]
+      // H_y(iz_min-1) += dtcq2*tf1(iz_min):      ix in [0,nx], iy in [0,ny+1]
+      for (int iy = y0; iy <= y1; ++iy) {
+        if (ix <= s.nx && iy <= s.ny + 1) corr<T>(e + g.at(ix, iy, zm), vE, +1);
+        if (ix <= s.nx && iy <= s.ny + 1) corr<T>(h + g.comp + g.at(ix, iy, zm - 1), vH, +1);
+      }
+    } else {
+      // E_y(iz_min) -= eps_in(1)*tf4(iz_min-1): ix in [0,nx+1], iy in [0,ny]
+      // H_x(iz_min-1) -= dtcq2*tf2(iz_min):      ix in [0,nx+1], iy in [0,ny]
+      for (int iy = y0; iy <= y1; ++iy) {
+        if (ix <= s.nx + 1 && iy <= s.ny) corr<T>(e + g.comp + g.at(ix, iy, zm), vE, -1);
+        if (ix <= s.nx + 1 && iy <= s.ny) corr<T>(h + g.at(ix, iy, zm - 1), vH, -1);
+      }
+    }
+  } else if (s.variant == 2) {
+    // E_x(iz_min) += tf5(iz_min)/eps ; H_y(iz_min) += dtcq2*tf1(iz_min)
     for (int iy = y0; iy <= y1; ++iy) {
       corr<T>(e + g.at(ix, iy, zm), vE, +1);
       corr<T>(h + g.comp + g.at(ix, iy, zm), vH, +1);
     }
   }
+}
+
+// Incident field at ix and the corrections of the rows iy in [y0, y1].
+template <typename T>
+__device__ __forceinline__ void tfsf_column(typename V2<T>::t* e, typename V2<T>::t* h, const Geo& g,
+                                            const SrcArgs& s, int it, int ix, int y0, int y1) {
+  cx<double> vE, vH;
+  tfsf_values(s, it, ix, vE, vH);
+  tfsf_apply<T>(e, h, g, s, ix, y0, y1, vE, vH);
 }
 
 // ---------------------------------------------------------------------------

@@ -490,20 +490,24 @@ __device__ __forceinline__ void acc_add(float4& a, float re, float im) {
   df_add(a.y, a.w, im);
 }
 // v * 2^e2 as a double, formed from the float's bits with integer operations
-// (exact; GB300's FP64 pipe is kept out of the flux epilogue).  A zero stays
-// a signed zero, Inf and NaN stay Inf and NaN; subnormal v goes through the
-// FP64 pipe (rare: v is a sum of values scaled to about 1).
+// only (exact for |e2| well inside the double range; GB300's FP64 pipe is
+// kept out of the flux epilogue).  A zero stays a signed zero, Inf and NaN
+// stay Inf and NaN, a subnormal v is normalised by its leading bit.
 __device__ __forceinline__ double scaled_double(float v, int e2) {
   const unsigned u = __float_as_uint(v);
   const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-  const unsigned ef = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  const unsigned ef = (u >> 23) & 0xffu;
+  unsigned long long m = u & 0x7fffffu;
+  if (ef == 0xffu) return __longlong_as_double((long long)(sign | (0x7ffull << 52) | (m << 29)));
+  int e = (int)ef - 127;
   if (ef == 0u) {
     if (m == 0u) return __longlong_as_double((long long)sign);
-    return (double)v * __longlong_as_double((long long)(1023 + e2) << 52);
+    // subnormal: m * 2^-149, normalised by its leading bit
+    const int top = 31 - __clz((int)m);  // 0 .. 22
+    e = top - 149;
+    m = (m << (23 - top)) & 0x7fffffull;
   }
-  if (ef == 0xffu) return __longlong_as_double((long long)(sign | (0x7ffull << 52) | ((unsigned long long)m << 29)));
-  return __longlong_as_double(
-      (long long)(sign | ((unsigned long long)((int)ef - 127 + 1023 + e2) << 52) | ((unsigned long long)m << 29)));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023 + e2) << 52) | (m << 29)));
 }
 
 // Value of an accumulator in FP64.
@@ -727,7 +731,11 @@ __device__ __forceinline__ long face_comp(const FluxFace& F, int c) {
 //   * producers (warps 0-1, two A rows a thread): the samples of a chunk of
 //     8 samples into the TF32 hi/lo A operands of a stage (plain loads, one
 //     chunk ahead in registers), and one thread bulk-copies the chunk's B
-//     operands into the same stage; WS_STAGES stages in a ring;
+//     operands into the same stage; WS_STAGES stages in a ring.  Shared
+//     memory stays at the three stages: what more it takes comes out of the
+//     L1, which holds the loads in flight (a raw sample ring in shared memory
+//     fed by asynchronous copies left 20 KB of L1 and made both modes 1.3 to
+//     1.8 times slower);
 //   * the MMA thread (warp 18): three tcgen05.mma kind::tf32 per 8 K columns
 //     into one of two TMEM accumulators (256 columns each), each stage freed
 //     by a commit when its MMAs are done, each finished item signalled by a
@@ -738,9 +746,7 @@ __device__ __forceinline__ long face_comp(const FluxFace& F, int c) {
 //     of the next item fill the other, streaming the accumulators one chunk
 //     ahead in registers.  Sixteen warps, because the epilogue's work per
 //     value (the double-float update, the products and their shuffles) needs
-//     more warps in flight than its memory stream alone would.  Registers
-//     are handed out to whole groups of four warps: the 19 warps take 96 a
-//     thread.
+//     more warps in flight than its memory stream alone would.
 // Commit mode: rows are 128 consecutive sample points; the epilogue adds the
 // partial sums into fdata (read once, written once).
 // Flux mode: rows are the four flux components of 32 locations of one face,
@@ -1036,32 +1042,40 @@ template <bool FLUX> __global__ void __launch_bounds__(WS_THREADS, 1) k_dft_ws(W
           for (int q = 0; q < WS_FCH; ++q) acc_add(fa[q], __uint_as_float(t[2 * q]), __uint_as_float(t[2 * q + 1]));
         }
         if (FLUX) {
-          // lane 4 l + c holds component c of location 8 q4 + l: the lane of
-          // component 0 forms Re(a conj b) - Re(c conj d) from the leading
-          // parts of its three neighbours' values, the 8 locations are summed
-          // in a fixed order, and the sum goes out in FP64.  The products are
-          // FP32 on values scaled by a power of two that brings the warp's
-          // largest to [1, 2) (undone exactly when the sum is widened), so
-          // that fields far below 1 (the pulse's leading tail) neither
-          // underflow nor lose precision; values far below the warp's largest
-          // do not count.
-          const bool has = ep >= 0;
+          // lane 4 l + c holds component c of location 8 q4 + l.  Per
+          // frequency the values are scaled by a power of two that brings the
+          // warp's largest to [1, 2) (undone exactly when the sum is widened),
+          // so that fields far below 1 (the pulse's leading tail) neither
+          // underflow nor lose precision in FP32 products; values far below
+          // the warp's largest do not count.  Lanes c = 0 and c = 2 form
+          // Re(a conj b) and -Re(c conj d) with their partner lane (c ^ 1);
+          // the four frequencies' 32 lane values are then summed in one
+          // transposed butterfly (fixed order): lane 8 q + 0 ends with the
+          // sum of frequency q, which goes out in FP64.
+          float v[WS_FCH];
+          int sc[WS_FCH];
 #pragma unroll
           for (int q = 0; q < WS_FCH; ++q) {
-            const unsigned ex = max(__float_as_uint(fa[q].x) >> 23 & 0xffu, __float_as_uint(fa[q].y) >> 23 & 0xffu);
-            const int sc = min(126, max(-126, 127 - (int)__reduce_max_sync(0xffffffffu, ex)));
-            const float f = __uint_as_float((unsigned)(127 + sc) << 23);
+            const unsigned mb = max(__float_as_uint(fa[q].x) & 0x7fffffffu, __float_as_uint(fa[q].y) & 0x7fffffffu);
+            sc[q] = min(126, max(-126, 127 - (int)(__reduce_max_sync(0xffffffffu, mb) >> 23)));
+            const float f = __uint_as_float((unsigned)(127 + sc[q]) << 23);
             const float ax = fa[q].x * f, ay = fa[q].y * f;
-            const float bx = __shfl_down_sync(0xffffffffu, ax, 1), by = __shfl_down_sync(0xffffffffu, ay, 1);
-            const float cx2 = __shfl_down_sync(0xffffffffu, ax, 2), cy = __shfl_down_sync(0xffffffffu, ay, 2);
-            const float dx = __shfl_down_sync(0xffffffffu, ax, 3), dy = __shfl_down_sync(0xffffffffu, ay, 3);
-            float v = ((lane & 3) == 0 && has) ? (ax * bx + ay * by) - (cx2 * dx + cy * dy) : 0.f;
-#pragma unroll
-            for (int o = 16; o >= 4; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0 && WS_FCH * ch + q < nw)
-              A.part[(long)(g * TC_NW + WS_FCH * ch + q) * (4L * A.ft.start[6]) + 4L * r.tile + q4] =
-                  scaled_double(v, -2 * sc);
+            const float bx = __shfl_xor_sync(0xffffffffu, ax, 1), by = __shfl_xor_sync(0xffffffffu, ay, 1);
+            const float pr = __fmaf_rn(ay, by, __fmul_rn(ax, bx));
+            v[q] = (lane & 1) ? 0.f : (lane & 2) ? -pr : pr;
           }
+          const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+          const float w0 = (h16 ? v[2] : v[0]) + __shfl_xor_sync(0xffffffffu, h16 ? v[0] : v[2], 16);
+          const float w1 = (h16 ? v[3] : v[1]) + __shfl_xor_sync(0xffffffffu, h16 ? v[1] : v[3], 16);
+          float t = (h8 ? w1 : w0) + __shfl_xor_sync(0xffffffffu, h8 ? w0 : w1, 8);
+          t += __shfl_xor_sync(0xffffffffu, t, 4);
+          t += __shfl_xor_sync(0xffffffffu, t, 2);
+          t += __shfl_xor_sync(0xffffffffu, t, 1);
+          const int qq = lane >> 3;
+          const int myc = qq == 0 ? sc[0] : qq == 1 ? sc[1] : qq == 2 ? sc[2] : sc[3];
+          if ((lane & 7) == 0 && WS_FCH * ch + qq < nw)
+            A.part[(long)(g * TC_NW + WS_FCH * ch + qq) * (4L * A.ft.start[6]) + 4L * r.tile + q4] =
+                scaled_double(t, -2 * myc);
         } else if (ep >= 0) {
 #pragma unroll
           for (int q = 0; q < WS_FCH; ++q)
@@ -1123,12 +1137,29 @@ FluxTiles flux_tiles(const FluxFace* f6) {
 // few microseconds of launch latency for well under a microsecond of work.
 // k_tiny runs a span of steps in one cooperative launch (every CTA resident
 // at once): per step the E pass, the H pass, the TF/SF corrections and the
-// DFT sample, each a grid-stride loop over its cells with the split passes'
+// DFT sample, each a grid-stride loop over its work with the split passes'
 // per-cell functions, separated by grid-wide barriers.  The arithmetic and
 // every value stored are the split passes', so the results are theirs bit
-// for bit.  The barrier is a counter and a generation word in global
-// memory; every wait is bounded (about a second): a CTA that gives up
-// records it (code 6) and returns, and so do the others at their next wait.
+// for bit.  What shapes it is GB300's FP64 rate (two FP64 instructions a
+// cycle per SM, one warp instruction every 64 cycles on a sub-partition):
+//   * a pass costs its slowest warp's FP64 instruction count, so in FP64 a
+//     UPML cell (about 2.5 times an interior cell's work) is split over three
+//     work items, one per component, and interior cells are one item each
+//     (compiled without the slab code); the UPML items come first,
+//     component-major, so that a warp's items take one path.  FP64 rounds
+//     every operation explicitly, so any split gives the split passes'
+//     values; FP32 arithmetic may be contracted to FMAs differently in a
+//     different instantiation, so FP32 keeps the split passes' own per-cell
+//     function, one item per cell;
+//   * the TF/SF corrections' incident field (exp, sincos and divisions in
+//     FP64, a dependent chain of a few hundred FP64 instructions) is
+//     evaluated for every step of the span up front by k_tfsf_table, in
+//     parallel, and the TF/SF phase only adds the tabulated values;
+//   * the DFT sample shares the TF/SF phase (one barrier less a step) when
+//     no sample point lies on a plane the corrections write.
+// The barrier is a counter and a generation word in global memory; every
+// wait is bounded (about a second): a CTA that gives up records it (code 6)
+// and returns, and so do the others at their next wait.
 
 struct GridBar {
   unsigned count, gen;
@@ -1186,6 +1217,8 @@ __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned& gen, unsigned
 template <typename T> struct TinyArgs {
   FieldArgs<T> a;
   SrcArgs s;
+  const TfsfVal* tfv;    // TF/SF corrections per [step of the span][ix in 0..nx+1]
+  int merged;            // the DFT sample runs in the TF/SF phase
   const Seg* segs;
   int nsegs;
   typename V2<T>::t* S;  // the DFT ring
@@ -1210,36 +1243,98 @@ __global__ void k_barrier_check(GridBar* bar, int* err, int shift) {
   grid_barrier(bar, gen, 2, err, STREAM_WAIT_CYCLES >> shift);
 }
 
+// The TF/SF corrections of steps it0 .. it0+n-1 for every column ix in
+// [0, nx+1] (tfsf_values, the split passes' function).
+__global__ void k_tfsf_table(SrcArgs s, int it0, int n, int ncol, TfsfVal* __restrict__ out) {
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= (long)n * ncol) return;
+  cx<double> vE, vH;
+  tfsf_values(s, it0 + (int)(j / ncol), (int)(j % ncol), vE, vH);
+  out[j] = TfsfVal{vE.re, vE.im, vH.re, vH.im};
+}
+
+// Work items of the E and H passes of k_tiny: the UPML cells three times
+// (component k = item / nu), then the interior cells once.  lo: UPML planes
+// 1..lo; hi0: the first plane of the upper slab (planes hi0..nz).
+struct TinyItems {
+  int lo, hi0;
+  long nxy, nu;  // cells per plane, UPML cells
+  __device__ __forceinline__ void cell(long c, bool upml, int nx, int& x, int& y, int& z) const {
+    const long p = c / nxy, r = c - p * nxy;
+    z = upml ? (p < lo ? (int)p + 1 : hi0 + (int)(p - lo)) : lo + 1 + (int)p;
+    x = (int)(r % nx) + 1;
+    y = (int)(r / nx) + 1;
+  }
+};
+
 template <typename T, bool CEPS> __global__ void __launch_bounds__(TINY_THREADS) k_tiny(TinyArgs<T> A) {
   using V = typename V2<T>::t;
   const Geo g = A.a.g;
-  const long nxy = (long)g.nx * g.ny, ncell = nxy * g.nz;
+  const long nxy = (long)g.nx * g.ny;
   const long gt = (long)blockIdx.x * blockDim.x + threadIdx.x, gs = (long)gridDim.x * blockDim.x;
   const long tf_items = (long)(g.nx + 2) * ((g.ny + 2 + TFSF_YCH - 1) / TFSF_YCH);
+  TinyItems ti;
+  ti.lo = min(max(A.a.pmlzi, 0), g.nz);
+  ti.hi0 = max(A.a.pmlzf, ti.lo + 1);
+  ti.nxy = nxy;
+  ti.nu = nxy * (ti.lo + max(0, g.nz - ti.hi0 + 1));
+  constexpr bool SPLIT = std::is_same<T, double>::value;
+  const long nitems = SPLIT ? 3 * ti.nu + nxy * g.nz - ti.nu : nxy * g.nz;
   unsigned gen = 0;
   if (threadIdx.x == 0) gen = ld_acquire_u32(&A.bar->gen);
   int slot = A.slot0;
   for (int i = 0; i < A.n; ++i) {
     const int it = A.it0 + i;
-    for (long c = gt; c < ncell; c += gs) {
-      const int z = (int)(c / nxy) + 1, r = (int)(c % nxy);
-      e_split_cell<T, CEPS>(A.a, r % g.nx + 1, r / g.nx + 1, z);
+    for (long w = gt; w < nitems; w += gs) {
+      int x, y, z;
+      if (!SPLIT) {
+        z = (int)(w / nxy) + 1;
+        x = (int)(w % nxy % g.nx) + 1;
+        y = (int)(w % nxy / g.nx) + 1;
+        e_split_cell<T, CEPS>(A.a, x, y, z);
+      } else if (w < 3 * ti.nu) {
+        const int k = (int)(w / ti.nu);
+        ti.cell(w - k * ti.nu, true, g.nx, x, y, z);
+        if (k == 0) e_split_cell<T, CEPS, true, 1>(A.a, x, y, z);
+        else if (k == 1) e_split_cell<T, CEPS, true, 2>(A.a, x, y, z);
+        else e_split_cell<T, CEPS, true, 4>(A.a, x, y, z);
+      } else {
+        ti.cell(w - 3 * ti.nu, false, g.nx, x, y, z);
+        e_split_cell<T, CEPS, false>(A.a, x, y, z);
+      }
     }
     if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
-    for (long c = gt; c < ncell; c += gs) {
-      const int z = (int)(c / nxy) + 1, r = (int)(c % nxy);
-      h_split_cell<T>(A.a, r % g.nx + 1, r / g.nx + 1, z);
+    for (long w = gt; w < nitems; w += gs) {
+      int x, y, z;
+      if (!SPLIT) {
+        z = (int)(w / nxy) + 1;
+        x = (int)(w % nxy % g.nx) + 1;
+        y = (int)(w % nxy / g.nx) + 1;
+        h_split_cell<T>(A.a, x, y, z);
+      } else if (w < 3 * ti.nu) {
+        const int k = (int)(w / ti.nu);
+        ti.cell(w - k * ti.nu, true, g.nx, x, y, z);
+        if (k == 0) h_split_cell<T, true, 1>(A.a, x, y, z);
+        else if (k == 1) h_split_cell<T, true, 2>(A.a, x, y, z);
+        else h_split_cell<T, true, 4>(A.a, x, y, z);
+      } else {
+        ti.cell(w - 3 * ti.nu, false, g.nx, x, y, z);
+        h_split_cell<T, false>(A.a, x, y, z);
+      }
     }
     if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
+    const bool sample = A.dft && it >= A.to_fourier && it % A.sample_fourier == 0;
     if (A.s.variant != 0) {
       // the columns k_tfsf covers: ix in [0, nx+1], rows in chunks of TFSF_YCH
       for (long w = gt; w < tf_items; w += gs) {
         const int ix = (int)(w % (g.nx + 2)), y0 = (int)(w / (g.nx + 2)) * TFSF_YCH;
-        tfsf_column<T>(A.a.e, A.a.h, g, A.s, it, ix, y0, min(y0 + TFSF_YCH - 1, g.ny + 1));
+        const TfsfVal v = A.tfv[(long)i * (g.nx + 2) + ix];
+        tfsf_apply<T>(A.a.e, A.a.h, g, A.s, ix, y0, min(y0 + TFSF_YCH - 1, g.ny + 1), cx<double>{v.er, v.ei},
+                      cx<double>{v.hr, v.hi});
       }
-      if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
+      if (!(sample && A.merged) && !grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
     }
-    if (A.dft && it >= A.to_fourier && it % A.sample_fourier == 0) {
+    if (sample) {
       V* dst = A.S + (long)slot * A.P;
       for (int k = 0; k < A.nsegs; ++k) {
         const Seg sg = A.segs[k];
@@ -1787,14 +1882,39 @@ template <typename T> int step_t(iris_engine* E, int it0, int n) {
   return IRIS_OK;
 }
 
+// Whether no DFT sample point lies on a plane the TF/SF corrections write
+// (E at iz_min, H at iz_min-1 in variant 1 and at iz_min in variant 2): then
+// k_tiny samples in the TF/SF phase.
+static bool tiny_sample_merges(const iris_engine* E) {
+  const int zm = E->src.iz_min;
+  const int zh = E->src.variant == 1 ? zm - 1 : zm;
+  for (const Seg& sg : E->segs) {
+    long lo = sg.src, hi = sg.src;
+    for (int cu = 0; cu < 2; ++cu)
+      for (int cv = 0; cv < 2; ++cv) {
+        const long q = sg.src + (cu ? (long)(sg.nu - 1) * sg.su : 0) + (cv ? (long)(sg.nv - 1) * sg.sv : 0);
+        lo = std::min(lo, q);
+        hi = std::max(hi, q);
+      }
+    const long z0 = lo / E->g.plane, z1 = hi / E->g.plane;
+    const int zc = sg.field < 3 ? zm : zh;
+    if (zc >= z0 && zc <= z1) return false;
+  }
+  return true;
+}
+
 // Steps it0 .. it0+n-1 with the persistent kernel: spans that end where the
-// DFT ring fills (its commit runs between launches) or after 1024 steps.
+// DFT ring fills (its commit runs between launches), after 1024 steps or at
+// the TF/SF table's capacity; before each span k_tfsf_table evaluates its
+// TF/SF corrections.
 template <typename T> int step_persist(iris_engine* E, int it0, int n) {
   const iris_params& p = E->p;
+  const int cap = E->src.variant != 0 ? E->tfv_cap : 1024;
+  const bool merged = tiny_sample_merges(E);
   int it = it0;
   while (it < it0 + n) {
     int span = 0, samples = 0;
-    while (it + span < it0 + n && span < 1024) {
+    while (it + span < it0 + n && span < cap) {
       const int t = it + span;
       ++span;
       if (E->P > 0 && t >= p.to_fourier && t % p.sample_fourier == 0 && ++samples + E->nslot == E->K) break;
@@ -1802,6 +1922,8 @@ template <typename T> int step_persist(iris_engine* E, int it0, int n) {
     TinyArgs<T> A{};
     A.a = field_args<T>(E);
     A.s = E->src;
+    A.tfv = E->d_tfv;
+    A.merged = merged ? 1 : 0;
     A.segs = E->d_segs;
     A.nsegs = (int)E->segs.size();
     A.S = (typename V2<T>::t*)E->S;
@@ -1818,6 +1940,10 @@ template <typename T> int step_persist(iris_engine* E, int it0, int n) {
     void* args[] = {&A};
     {
       KTimer tm(E, IRIS_KC_PERSIST);
+      if (E->src.variant != 0) {
+        const long nt = (long)span * (p.nx + 2);
+        k_tfsf_table<<<(unsigned)((nt + 127) / 128), 128, 0, E->st>>>(E->src, it, span, p.nx + 2, E->d_tfv);
+      }
       CK(cudaMemsetAsync(E->d_bar, 0, sizeof(GridBar), E->st));
       const void* k = E->eps_complex ? (const void*)k_tiny<T, true> : (const void*)k_tiny<T, false>;
       CK(cudaLaunchCooperativeKernel(k, dim3(E->persist_blocks), dim3(TINY_THREADS), args, 0, E->st));
@@ -2155,7 +2281,8 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
 void free_engine(iris_engine* E) {
   void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
                   E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J, E->e2, E->h2, E->pml_d2[0],
-                  E->pml_d2[1], E->d_err, E->d_it, E->d_wtc, E->d_wt64, E->d_part, E->d_bar, E->d_stage};
+                  E->pml_d2[1], E->d_err, E->d_it, E->d_wtc, E->d_wt64, E->d_part, E->d_bar, E->d_stage,
+                  E->d_tfv};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (E->h_J) cudaFreeHost(E->h_J);
@@ -2296,8 +2423,11 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k, TINY_THREADS, 0) == cudaSuccess &&
           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, kc, TINY_THREADS, 0) == cudaSuccess)
         occ = std::min(o1, o2);
-      // one CTA per SM at most (the FP64 pipes are per SM), no more than the cells need
-      const long need = (cells + TINY_THREADS - 1) / TINY_THREADS;
+      // one CTA per SM at most (the FP64 pipes are per SM), no more than the
+      // work items need (UPML cells count three times)
+      const int lo = std::min(std::max(p.pmlzi, 0), p.nz), hi0 = std::max(p.pmlzf, lo + 1);
+      const long nu = (long)p.nx * p.ny * (lo + std::max(0, p.nz - hi0 + 1));
+      const long need = (cells + (E->prec == IRIS_FP64 ? 2 * nu : 0) + TINY_THREADS - 1) / TINY_THREADS;
       E->persist_blocks = (int)std::max(1L, std::min<long>(need, (long)nsm * std::min(occ, 1)));
       E->persist = occ >= 1;
     }
@@ -2305,6 +2435,12 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
       return bail(fail(IRIS_EINVAL, "the persistent stencil needs cooperative launches on this device"));
     if (E->persist && cudaMalloc(&E->d_bar, 64) != cudaSuccess)
       return bail(fail(IRIS_ENOMEM, "barrier allocation failed"));
+    if (E->persist && E->src.variant != 0) {
+      // TF/SF table of a span: at most 1024 steps and 8 MB
+      E->tfv_cap = (int)std::max(1L, std::min(1024L, (8L << 20) / (32L * (p.nx + 2))));
+      if (cudaMalloc(&E->d_tfv, sizeof(TfsfVal) * (size_t)E->tfv_cap * (p.nx + 2)) != cudaSuccess)
+        return bail(fail(IRIS_ENOMEM, "TF/SF table allocation failed"));
+    }
   }
   E->fused = !E->persist && E->prec == IRIS_FP32 &&
              (p.stencil == IRIS_STENCIL_FUSED || p.stencil == IRIS_STENCIL_DEFAULT);

@@ -109,6 +109,9 @@ struct iris_engine {
   bool persist = false;
   int persist_blocks = 0;
   void* d_bar = nullptr;
+  // its TF/SF corrections (vE, vH) per [step of a span][ix], up to tfv_cap steps
+  iris::TfsfVal* d_tfv = nullptr;
+  int tfv_cap = 0;
   // staging buffer of the complex(8) field transfers (allocated on first use)
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
