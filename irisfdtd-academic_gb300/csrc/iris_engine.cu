@@ -1142,27 +1142,31 @@ FluxTiles flux_tiles(const FluxFace* f6) {
 // every value stored are the split passes', so the results are theirs bit
 // for bit.  What shapes it is GB300's FP64 rate (two FP64 instructions a
 // cycle per SM, one warp instruction every 64 cycles on a sub-partition):
-//   * a pass costs its slowest warp's FP64 instruction count, so in FP64 a
-//     UPML cell (about 2.5 times an interior cell's work) is split over three
-//     work items, one per component, and interior cells are one item each
-//     (compiled without the slab code); the UPML items come first,
-//     component-major, so that a warp's items take one path.  FP64 rounds
-//     every operation explicitly, so any split gives the split passes'
-//     values; FP32 arithmetic may be contracted to FMAs differently in a
-//     different instantiation, so FP32 keeps the split passes' own per-cell
-//     function, one item per cell;
+//   * a pass costs its busiest sub-partition's FP64 instruction count, so
+//     in FP64 every cell is split over three work items, one per component
+//     (the Bloch ghost products of a cell on the x or y border cost as much
+//     as its update), component-major so that a warp's items take one path,
+//     spread over every SM, the UPML items on threads that do no second
+//     item; cells outside the UPML slabs run code compiled without the slab
+//     branch.  FP64 rounds every operation explicitly, so
+//     any split gives the split passes' values; FP32 arithmetic may be
+//     contracted to FMAs differently in a different instantiation, so FP32
+//     keeps the split passes' own per-cell function, one item per cell;
 //   * the TF/SF corrections' incident field (exp, sincos and divisions in
 //     FP64, a dependent chain of a few hundred FP64 instructions) is
 //     evaluated for every step of the span up front by k_tfsf_table, in
-//     parallel, and the TF/SF phase only adds the tabulated values;
-//   * the DFT sample shares the TF/SF phase (one barrier less a step) when
-//     no sample point lies on a plane the corrections write.
-// The barrier is a counter and a generation word in global memory; every
-// wait is bounded (about a second): a CTA that gives up records it (code 6)
-// and returns, and so do the others at their next wait.
+//     parallel; the TF/SF phase only adds the tabulated values, one thread
+//     per corrected row;
+//   * the DFT sample reads a flat table of its points' field and storage
+//     index (one dependent load, not a walk over the run list), and shares
+//     the TF/SF phase (one barrier less a step) when no sample point lies on
+//     a plane the corrections write.
+// The barrier is an arrival counter in global memory; every wait is bounded
+// (about a second): a CTA that gives up records it (code 6) and returns, and
+// so do the others at their next wait.
 
 struct GridBar {
-  unsigned count, gen;
+  unsigned count;
 };
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
@@ -1170,43 +1174,32 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned x) {
-  unsigned v;
-  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "r"(x) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_relaxed_u32(unsigned* p, unsigned x) {
-  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
-}
 __device__ __forceinline__ void red_add_release(unsigned* p, unsigned x) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
 }
 
 // All CTAs of the launch reach this point before any passes it; false when
-// the wait gave up.  gen: the generation this CTA waits to see advance
-// (thread 0's copy is the one used).
-__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned& gen, unsigned nblk, int* err,
+// the wait gave up.  The count only grows within a launch (it is zeroed
+// before each): every CTA's thread 0 adds its arrival with release semantics
+// and waits, with acquire loads, until the count reaches its target, nblk
+// per barrier passed so far (thread 0's copy of target is the one used).
+// One arrival without a returned value and one load per poll: measured on
+// GB300 at 1.1-1.2 microseconds a barrier for 72 or 152 CTAs, against 1.7
+// for an arrival counter reset by the last arriver plus a generation word.
+__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned& target, unsigned nblk, int* err,
                                              long long limit = STREAM_WAIT_CYCLES) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    // the arrival releases this CTA's writes (ordered before it by the
-    // __syncthreads) and acquires the earlier arrivals'; the last arriver
-    // resets the count and releases the new generation, which the others
-    // acquire
-    if (atom_add_acq_rel(&b->count, 1u) == nblk - 1) {
-      st_relaxed_u32(&b->count, 0u);
-      red_add_release(&b->gen, 1u);
-    } else {
-      const long long t0 = clock64();
-      while (ld_acquire_u32(&b->gen) == gen)
-        if (clock64() - t0 > limit) {
-          ok = 0;
-          break;
-        }
-    }
-    gen += 1;
+    target += nblk;
+    red_add_release(&b->count, 1u);
+    const long long t0 = clock64();
+    while ((int)(ld_acquire_u32(&b->count) - target) < 0)
+      if (clock64() - t0 > limit) {
+        ok = 0;
+        break;
+      }
     if (!ok) atomicExch(err, 6);
     ok_s = ok;
   }
@@ -1219,6 +1212,7 @@ template <typename T> struct TinyArgs {
   SrcArgs s;
   const TfsfVal* tfv;    // TF/SF corrections per [step of the span][ix in 0..nx+1]
   int merged;            // the DFT sample runs in the TF/SF phase
+  const long* sidx;      // per sample point: storage index * 8 + field (0..5)
   const Seg* segs;
   int nsegs;
   typename V2<T>::t* S;  // the DFT ring
@@ -1237,10 +1231,9 @@ constexpr int TINY_THREADS = 128;
 // returns without arriving, so the first waits at the grid barrier with the
 // persistent kernel's limit divided by 2^shift, gives up and records it.
 __global__ void k_barrier_check(GridBar* bar, int* err, int shift) {
-  unsigned gen = 0;
+  unsigned target = 0;
   if (blockIdx.x != 0) return;
-  if (threadIdx.x == 0) gen = ld_acquire_u32(&bar->gen);
-  grid_barrier(bar, gen, 2, err, STREAM_WAIT_CYCLES >> shift);
+  grid_barrier(bar, target, 2, err, STREAM_WAIT_CYCLES >> shift);
 }
 
 // The TF/SF corrections of steps it0 .. it0+n-1 for every column ix in
@@ -1253,102 +1246,126 @@ __global__ void k_tfsf_table(SrcArgs s, int it0, int n, int ncol, TfsfVal* __res
   out[j] = TfsfVal{vE.re, vE.im, vH.re, vH.im};
 }
 
-// Work items of the E and H passes of k_tiny: the UPML cells three times
-// (component k = item / nu), then the interior cells once.  lo: UPML planes
-// 1..lo; hi0: the first plane of the upper slab (planes hi0..nz).
-struct TinyItems {
-  int lo, hi0;
-  long nxy, nu;  // cells per plane, UPML cells
-  __device__ __forceinline__ void cell(long c, bool upml, int nx, int& x, int& y, int& z) const {
-    const long p = c / nxy, r = c - p * nxy;
-    z = upml ? (p < lo ? (int)p + 1 : hi0 + (int)(p - lo)) : lo + 1 + (int)p;
-    x = (int)(r % nx) + 1;
-    y = (int)(r / nx) + 1;
+// FP64 work items of k_tiny: component k of a cell, UPML cells with the slab
+// code, the others without.  The grid-stride loop gives the threads below
+// nitems - stride two items; the UPML items (about 1.5 times an interior
+// item's FP64 work) go to the positions of one-item threads, so that no
+// thread does a UPML item and a second one.  Position w maps to UPML item
+// w - u0 in [u0, u0 + nu3) and to interior item w (w < u0) or w - nu3.
+struct TinyMap {
+  int lo, hi0;         // UPML planes 1..lo and hi0..nz
+  unsigned nxy, nuc, nic;  // cells per plane, UPML cells, interior cells
+  unsigned u0;             // first position of the UPML items
+  __device__ __forceinline__ void item(unsigned w, int nx, int& k, int& x, int& y, int& z, bool& upml) const {
+    unsigned c;
+    upml = w >= u0 && w < u0 + 3 * nuc;
+    if (upml) {
+      const unsigned u = w - u0;
+      k = (int)(u / nuc);
+      c = u - (unsigned)k * nuc;
+      const unsigned pl = c / nxy;
+      z = pl < (unsigned)lo ? (int)pl + 1 : hi0 + (int)(pl - lo);
+    } else {
+      const unsigned v = w < u0 ? w : w - 3 * nuc;
+      k = (int)(v / nic);
+      c = v - (unsigned)k * nic;
+      z = lo + 1 + (int)(c / nxy);
+    }
+    const unsigned r = c % nxy;
+    x = (int)(r % (unsigned)nx) + 1;
+    y = (int)(r / (unsigned)nx) + 1;
   }
 };
+template <bool CEPS, int MASK>
+__device__ __forceinline__ void tiny_e(const FieldArgs<double>& a, int x, int y, int z, bool upml) {
+  if (upml) e_split_cell<double, CEPS, true, MASK>(a, x, y, z);
+  else e_split_cell<double, CEPS, false, MASK>(a, x, y, z);
+}
+template <int MASK> __device__ __forceinline__ void tiny_h(const FieldArgs<double>& a, int x, int y, int z, bool upml) {
+  if (upml) h_split_cell<double, true, MASK>(a, x, y, z);
+  else h_split_cell<double, false, MASK>(a, x, y, z);
+}
 
 template <typename T, bool CEPS> __global__ void __launch_bounds__(TINY_THREADS) k_tiny(TinyArgs<T> A) {
   using V = typename V2<T>::t;
   const Geo g = A.a.g;
-  const long nxy = (long)g.nx * g.ny;
+  const long nxy = (long)g.nx * g.ny, ncell = nxy * g.nz;
   const long gt = (long)blockIdx.x * blockDim.x + threadIdx.x, gs = (long)gridDim.x * blockDim.x;
-  const long tf_items = (long)(g.nx + 2) * ((g.ny + 2 + TFSF_YCH - 1) / TFSF_YCH);
-  TinyItems ti;
-  ti.lo = min(max(A.a.pmlzi, 0), g.nz);
-  ti.hi0 = max(A.a.pmlzf, ti.lo + 1);
-  ti.nxy = nxy;
-  ti.nu = nxy * (ti.lo + max(0, g.nz - ti.hi0 + 1));
+  const long tf_rows = (long)(g.nx + 2) * (g.ny + 2);
   constexpr bool SPLIT = std::is_same<T, double>::value;
-  const long nitems = SPLIT ? 3 * ti.nu + nxy * g.nz - ti.nu : nxy * g.nz;
-  unsigned gen = 0;
-  if (threadIdx.x == 0) gen = ld_acquire_u32(&A.bar->gen);
+  const long nitems = SPLIT ? 3 * ncell : ncell;
+  TinyMap tm;
+  tm.lo = min(max(A.a.pmlzi, 0), g.nz);
+  tm.hi0 = max(A.a.pmlzf, tm.lo + 1);
+  tm.nxy = (unsigned)nxy;
+  tm.nuc = (unsigned)(nxy * (tm.lo + max(0, g.nz - tm.hi0 + 1)));
+  tm.nic = (unsigned)ncell - tm.nuc;
+  tm.u0 = (unsigned)min(max(nitems - gs, 0L), nitems - 3L * tm.nuc);
+  unsigned target = 0;  // grid barrier target
   int slot = A.slot0;
   for (int i = 0; i < A.n; ++i) {
     const int it = A.it0 + i;
     for (long w = gt; w < nitems; w += gs) {
-      int x, y, z;
-      if (!SPLIT) {
-        z = (int)(w / nxy) + 1;
-        x = (int)(w % nxy % g.nx) + 1;
-        y = (int)(w % nxy / g.nx) + 1;
-        e_split_cell<T, CEPS>(A.a, x, y, z);
-      } else if (w < 3 * ti.nu) {
-        const int k = (int)(w / ti.nu);
-        ti.cell(w - k * ti.nu, true, g.nx, x, y, z);
-        if (k == 0) e_split_cell<T, CEPS, true, 1>(A.a, x, y, z);
-        else if (k == 1) e_split_cell<T, CEPS, true, 2>(A.a, x, y, z);
-        else e_split_cell<T, CEPS, true, 4>(A.a, x, y, z);
+      // 32-bit index arithmetic: the host keeps 3 x cells below 2^31
+      if constexpr (SPLIT) {
+        int k, x, y, z;
+        bool upml;
+        tm.item((unsigned)w, g.nx, k, x, y, z, upml);
+        if (k == 0) tiny_e<CEPS, 1>(A.a, x, y, z, upml);
+        else if (k == 1) tiny_e<CEPS, 2>(A.a, x, y, z, upml);
+        else tiny_e<CEPS, 4>(A.a, x, y, z, upml);
       } else {
-        ti.cell(w - 3 * ti.nu, false, g.nx, x, y, z);
-        e_split_cell<T, CEPS, false>(A.a, x, y, z);
+        const unsigned r = (unsigned)w % (unsigned)nxy;
+        e_split_cell<T, CEPS>(A.a, (int)(r % (unsigned)g.nx) + 1, (int)(r / (unsigned)g.nx) + 1,
+                              (int)((unsigned)w / (unsigned)nxy) + 1);
       }
     }
-    if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
+    if (!grid_barrier(A.bar, target, gridDim.x, A.err)) return;
     for (long w = gt; w < nitems; w += gs) {
-      int x, y, z;
-      if (!SPLIT) {
-        z = (int)(w / nxy) + 1;
-        x = (int)(w % nxy % g.nx) + 1;
-        y = (int)(w % nxy / g.nx) + 1;
-        h_split_cell<T>(A.a, x, y, z);
-      } else if (w < 3 * ti.nu) {
-        const int k = (int)(w / ti.nu);
-        ti.cell(w - k * ti.nu, true, g.nx, x, y, z);
-        if (k == 0) h_split_cell<T, true, 1>(A.a, x, y, z);
-        else if (k == 1) h_split_cell<T, true, 2>(A.a, x, y, z);
-        else h_split_cell<T, true, 4>(A.a, x, y, z);
+      // 32-bit index arithmetic: the host keeps 3 x cells below 2^31
+      if constexpr (SPLIT) {
+        int k, x, y, z;
+        bool upml;
+        tm.item((unsigned)w, g.nx, k, x, y, z, upml);
+        if (k == 0) tiny_h<1>(A.a, x, y, z, upml);
+        else if (k == 1) tiny_h<2>(A.a, x, y, z, upml);
+        else tiny_h<4>(A.a, x, y, z, upml);
       } else {
-        ti.cell(w - 3 * ti.nu, false, g.nx, x, y, z);
-        h_split_cell<T, false>(A.a, x, y, z);
+        const unsigned r = (unsigned)w % (unsigned)nxy;
+        h_split_cell<T>(A.a, (int)(r % (unsigned)g.nx) + 1, (int)(r / (unsigned)g.nx) + 1,
+                        (int)((unsigned)w / (unsigned)nxy) + 1);
       }
     }
-    if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
+    if (!grid_barrier(A.bar, target, gridDim.x, A.err)) return;
     const bool sample = A.dft && it >= A.to_fourier && it % A.sample_fourier == 0;
-    if (A.s.variant != 0) {
-      // the columns k_tfsf covers: ix in [0, nx+1], rows in chunks of TFSF_YCH
-      for (long w = gt; w < tf_items; w += gs) {
-        const int ix = (int)(w % (g.nx + 2)), y0 = (int)(w / (g.nx + 2)) * TFSF_YCH;
+    const bool tf = A.s.variant != 0;
+    // TF/SF rows (one thread per (ix, iy) of the ranges k_tfsf covers), then
+    // the sample points; in one phase when merged, else separated by a barrier
+    const long n_tf = tf ? tf_rows : 0, n_s = sample ? A.P : 0;
+    const bool one = sample && A.merged;
+    for (long w = gt; w < (one ? n_tf + n_s : n_tf); w += gs) {
+      if (w < n_tf) {
+        const int ix = (int)(w % (g.nx + 2)), iy = (int)(w / (g.nx + 2));
         const TfsfVal v = A.tfv[(long)i * (g.nx + 2) + ix];
-        tfsf_apply<T>(A.a.e, A.a.h, g, A.s, ix, y0, min(y0 + TFSF_YCH - 1, g.ny + 1), cx<double>{v.er, v.ei},
-                      cx<double>{v.hr, v.hi});
+        tfsf_apply<T>(A.a.e, A.a.h, g, A.s, ix, iy, iy, cx<double>{v.er, v.ei}, cx<double>{v.hr, v.hi});
+      } else {
+        const long q = w - n_tf, code = A.sidx[q];
+        const int f = (int)(code & 7);
+        A.S[(long)slot * A.P + q] = (f < 3 ? A.a.e + f * g.comp : A.a.h + (f - 3) * g.comp)[code >> 3];
       }
-      if (!(sample && A.merged) && !grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
     }
+    if (tf && !one && !grid_barrier(A.bar, target, gridDim.x, A.err)) return;
     if (sample) {
-      V* dst = A.S + (long)slot * A.P;
-      for (int k = 0; k < A.nsegs; ++k) {
-        const Seg sg = A.segs[k];
-        const V* src = sg.field < 3 ? A.a.e + sg.field * g.comp : A.a.h + (sg.field - 3) * g.comp;
-        const long n = (long)sg.nu * sg.nv;
-        for (long L = gt; L < n; L += gs) {
-          const long v = L / sg.nu, u = L - v * sg.nu;
-          dst[sg.p0 + L] = src[sg.src + u * sg.su + v * sg.sv];
+      if (!one)
+        for (long q = gt; q < A.P; q += gs) {
+          const long code = A.sidx[q];
+          const int f = (int)(code & 7);
+          A.S[(long)slot * A.P + q] = (f < 3 ? A.a.e + f * g.comp : A.a.h + (f - 3) * g.comp)[code >> 3];
         }
-      }
       if (gt == 0) A.tk[slot] = it + 1 - A.to_fourier;
       ++slot;
       // the next step's E pass overwrites what was just sampled
-      if (!grid_barrier(A.bar, gen, gridDim.x, A.err)) return;
+      if (!grid_barrier(A.bar, target, gridDim.x, A.err)) return;
     }
   }
 }
@@ -1911,6 +1928,17 @@ template <typename T> int step_persist(iris_engine* E, int it0, int n) {
   const iris_params& p = E->p;
   const int cap = E->src.variant != 0 ? E->tfv_cap : 1024;
   const bool merged = tiny_sample_merges(E);
+  if (E->P > 0 && !E->d_sidx) {
+    // flat table of the sample points: storage index * 8 + field
+    std::vector<long> code((size_t)E->P);
+    for (const Seg& sg : E->segs)
+      for (long L = 0; L < (long)sg.nu * sg.nv; ++L) {
+        const long v = L / sg.nu, u = L - v * sg.nu;
+        code[(size_t)(sg.p0 + L)] = (sg.src + u * sg.su + v * sg.sv) * 8 + sg.field;
+      }
+    CK(cudaMalloc(&E->d_sidx, sizeof(long) * (size_t)E->P));
+    CK(cudaMemcpy(E->d_sidx, code.data(), sizeof(long) * (size_t)E->P, cudaMemcpyHostToDevice));
+  }
   int it = it0;
   while (it < it0 + n) {
     int span = 0, samples = 0;
@@ -1924,6 +1952,7 @@ template <typename T> int step_persist(iris_engine* E, int it0, int n) {
     A.s = E->src;
     A.tfv = E->d_tfv;
     A.merged = merged ? 1 : 0;
+    A.sidx = E->d_sidx;
     A.segs = E->d_segs;
     A.nsegs = (int)E->segs.size();
     A.S = (typename V2<T>::t*)E->S;
@@ -2282,7 +2311,7 @@ void free_engine(iris_engine* E) {
   void* ptrs[] = {E->e, E->h, E->pml_d[0], E->pml_d[1], E->pml_b[0], E->pml_b[1], E->coef, E->eps, E->d_segs,
                   E->S, E->d_tk, E->d_fw, E->fd, E->d_wt, E->d_faces, E->d_J, E->e2, E->h2, E->pml_d2[0],
                   E->pml_d2[1], E->d_err, E->d_it, E->d_wtc, E->d_wt64, E->d_part, E->d_bar, E->d_stage,
-                  E->d_tfv};
+                  E->d_tfv, E->d_sidx};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (E->h_J) cudaFreeHost(E->h_J);
@@ -2414,8 +2443,9 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, E->device);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E->device);
     const long cells = (long)p.nx * p.ny * p.nz;
-    const bool want = !member && (p.stencil == IRIS_STENCIL_PERSISTENT ||
-                                  (p.stencil == IRIS_STENCIL_DEFAULT && cells <= IRIS_PERSISTENT_MAX_CELLS));
+    const bool want = !member && 3 * cells < (1L << 31) &&
+                      (p.stencil == IRIS_STENCIL_PERSISTENT ||
+                       (p.stencil == IRIS_STENCIL_DEFAULT && cells <= IRIS_PERSISTENT_MAX_CELLS));
     if (want && coop) {
       const void* k = E->prec == IRIS_FP64 ? (const void*)k_tiny<double, false> : (const void*)k_tiny<float, false>;
       const void* kc = E->prec == IRIS_FP64 ? (const void*)k_tiny<double, true> : (const void*)k_tiny<float, true>;
@@ -2424,15 +2454,14 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, kc, TINY_THREADS, 0) == cudaSuccess)
         occ = std::min(o1, o2);
       // one CTA per SM at most (the FP64 pipes are per SM), no more than the
-      // work items need (UPML cells count three times)
-      const int lo = std::min(std::max(p.pmlzi, 0), p.nz), hi0 = std::max(p.pmlzf, lo + 1);
-      const long nu = (long)p.nx * p.ny * (lo + std::max(0, p.nz - hi0 + 1));
-      const long need = (cells + (E->prec == IRIS_FP64 ? 2 * nu : 0) + TINY_THREADS - 1) / TINY_THREADS;
+      // work items need (three a cell in FP64)
+      const long need = ((E->prec == IRIS_FP64 ? 3 : 1) * cells + TINY_THREADS - 1) / TINY_THREADS;
       E->persist_blocks = (int)std::max(1L, std::min<long>(need, (long)nsm * std::min(occ, 1)));
       E->persist = occ >= 1;
     }
     if (p.stencil == IRIS_STENCIL_PERSISTENT && !E->persist)
-      return bail(fail(IRIS_EINVAL, "the persistent stencil needs cooperative launches on this device"));
+      return bail(fail(IRIS_EINVAL, "the persistent stencil needs cooperative launches on this device and "
+                                    "fewer than 2^31 / 3 cells"));
     if (E->persist && cudaMalloc(&E->d_bar, 64) != cudaSuccess)
       return bail(fail(IRIS_ENOMEM, "barrier allocation failed"));
     if (E->persist && E->src.variant != 0) {

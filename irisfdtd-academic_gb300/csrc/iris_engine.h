@@ -112,6 +112,7 @@ struct iris_engine {
   // its TF/SF corrections (vE, vH) per [step of a span][ix], up to tfv_cap steps
   iris::TfsfVal* d_tfv = nullptr;
   int tfv_cap = 0;
+  long* d_sidx = nullptr;  // its DFT sample points: storage index * 8 + field
   // staging buffer of the complex(8) field transfers (allocated on first use)
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
