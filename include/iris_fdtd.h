@@ -368,6 +368,16 @@ int iris_timing_read(iris_engine* eng, double* region_ms, double* kernel_ms, lon
  * material flag, [5] number of DFT boxes, [6] DFT samples buffered and not
  * yet accumulated into fdata (info: 7 entries). */
 int iris_info(const iris_engine* eng, long* info);
+/* Bounds-check record of the process's kernels.  Returns 1 when the library
+ * was built with bounds checks (libiris_fdtd_bc.so, -DIRIS_BOUNDS_CHECK), 0
+ * otherwise; *first receives the first out-of-range access any kernel met
+ * since the last call, (site << 48) | index (0: none; sites: 1 E cell, 2 H
+ * cell, 3 and 4 E and H UPML slab rows, 5 material, 6 TF/SF row, 7 and 8 DFT
+ * sample source and slot, 9 and 10 fused-pass chunk and slab row, 11 and 12
+ * DFT block point and sample, 13 flux face), and the record is cleared.  A
+ * checked kernel skips the access it refuses.  No counterpart in the
+ * reference (a Fortran build with -check bounds stops the program). */
+int iris_bounds_check(unsigned long long* first);
 
 /* ---- batched form ------------------------------------------------------ */
 /*

@@ -407,6 +407,19 @@ class Batch:
 from .adjoint import Adjoint, design_objective  # noqa: E402
 
 
+def bounds_check():
+    """(enabled, first) of iris_bounds_check: whether the loaded library is the
+    bounds-checking build (IRIS_BOUNDS_CHECK=1 in the environment before the
+    first call loads it), and the first out-of-range access its kernels met
+    since the last call as (site, index), or None; the record is cleared."""
+    v = ctypes.c_ulonglong(0)
+    enabled = lib().iris_bounds_check(ctypes.byref(v))
+    if enabled < 0:
+        check(enabled, "iris_bounds_check")
+    first = None if v.value == 0 else (int(v.value >> 48), int(v.value & 0xFFFFFFFFFFFF))
+    return bool(enabled), first
+
+
 def run_input(directory: str, precision: int = FP64):
     """The drop-in main program: reads directory/inputFDTD.dat, writes log.dat and
     the <box>_scatt*.dat files there."""

@@ -37,6 +37,9 @@ using namespace iris;
 // E pass output of step n, C_n the forward curl of H that pass used.
 
 namespace iris {
+
+unsigned long long bc_take_adjoint() { return bc_take_module(); }
+
 namespace {
 
 // adjoint UPML rows, 24 per UPML plane (+k: component)
@@ -662,6 +665,7 @@ int iris_adjoint_set_design(iris_adjoint* J, const double* v) {
 }
 
 int iris_adjoint_forward(iris_adjoint* J, int nsteps, double* L, double* Jout) {
+  iris::NvtxRange nvtx_("iris_adjoint_forward");
   clear_error();
   if (!J || nsteps < 1) return fail(IRIS_EINVAL, "bad argument");
   iris_engine* F = J->F;
@@ -681,6 +685,7 @@ int iris_adjoint_forward(iris_adjoint* J, int nsteps, double* L, double* Jout) {
 }
 
 int iris_adjoint_backward(iris_adjoint* J, double* grad) {
+  iris::NvtxRange nvtx_("iris_adjoint_backward");
   clear_error();
   if (!J || !grad) return fail(IRIS_EINVAL, "null argument");
   if (J->nsteps < 1) return fail(IRIS_EINVAL, "no forward solve to differentiate");

@@ -28,6 +28,9 @@ using namespace iris;
 // batch itself.
 
 namespace iris {
+
+unsigned long long bc_take_batch() { return bc_take_module(); }
+
 namespace {
 
 struct BItem {
@@ -186,13 +189,13 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_batch_gather(const FieldArgs<T>* __restrict__ args,
                                                       const BSeg* __restrict__ segs,
                                                       typename V2<T>::t* __restrict__ slot, int* tk, int islot,
-                                                      int t, const int* tp) {
+                                                      int t, const int* tp, long np) {
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = tp ? *tp + t : t;
   const BSeg b = segs[blockIdx.y];
   if (blockIdx.x * (unsigned)GATHER_BLOCK >= (unsigned)b.s.nu * (unsigned)b.s.nv) return;
   const FieldArgs<T>& a = args[b.cell];
   const typename V2<T>::t* src = b.s.field < 3 ? a.e + b.s.field * a.g.comp : a.h + (b.s.field - 3) * a.g.comp;
-  gather_run<T>(b.s, src, slot);
+  gather_run<T>(b.s, src, slot, a.g.comp, np);
 }
 
 }  // namespace
@@ -522,7 +525,7 @@ template <typename T> void batch_one_step(iris_batch* B, int it, const int* itp,
       V* slot = (V*)M->S + (long)M->nslot * M->P;
       dim3 grid((unsigned)((B->max_seg + GATHER_BLOCK - 1) / GATHER_BLOCK), (unsigned)B->nbsegs);
       k_batch_gather<T><<<grid, 256, 0, M->st>>>(args, B->d_bsegs, slot, M->d_tk, M->nslot, it + 1 - p.to_fourier,
-                                                 itp);
+                                                 itp, M->P);
     }
     if (++M->nslot == M->K) dft_flush(M);
   }
@@ -566,6 +569,7 @@ void batch_free(iris_batch* B) {
 extern "C" {
 
 int iris_batch_create(int ncells, const iris_params* params, const double* fw, int dft_faces, iris_batch** out) {
+  iris::NvtxRange nvtx_("iris_batch_create");
   clear_error();
   if (ncells < 1 || !params || !fw || !out) return fail(IRIS_EINVAL, "bad argument");
   *out = nullptr;
@@ -685,6 +689,7 @@ int iris_batch_material_pattern(iris_batch* B, int cell, unsigned long long seed
 }
 
 int iris_batch_step(iris_batch* B, int it0, int nsteps) {
+  iris::NvtxRange nvtx_("iris_batch_step");
   clear_error();
   if (!B || nsteps < 0) return fail(IRIS_EINVAL, "bad argument");
   CK(cudaSetDevice(B->device));
@@ -692,6 +697,7 @@ int iris_batch_step(iris_batch* B, int it0, int nsteps) {
 }
 
 int iris_batch_flux(iris_batch* B, int cell, double* J) {
+  iris::NvtxRange nvtx_("iris_batch_flux");
   clear_error();
   if (!B || !J || cell < 0 || cell >= B->n) return fail(IRIS_EINVAL, "bad argument");
   CK(cudaSetDevice(B->device));

@@ -14,6 +14,35 @@
 
 namespace iris {
 
+// ---------------------------------------------------------------------------
+// Bounds checks (built with -DIRIS_BOUNDS_CHECK: libiris_fdtd_bc.so).  At the
+// points where a kernel maps its thread to a cell, a slab row, a correction
+// row, a DFT point or an accumulator, bc_ok tests the index against its
+// range; the first failure of the process's kernels is recorded as
+// (site << 48) | (index & 0xffffffffffff) in a device word of the module and
+// the access is skipped.  iris_bounds_check reads and clears the words.  In
+// the ordinary build bc_ok is the constant true and costs nothing.
+enum BcSite {
+  BC_E_CELL = 1, BC_H_CELL, BC_E_SLAB, BC_H_SLAB, BC_EPS, BC_TFSF, BC_GATHER_SRC, BC_GATHER_DST,
+  BC_FUSED_CELL, BC_FUSED_SLAB, BC_DFT_POINT, BC_DFT_SAMPLE, BC_FLUX_POINT
+};
+#ifdef IRIS_BOUNDS_CHECK
+static __device__ unsigned long long g_bc_first;
+__device__ __forceinline__ bool bc_ok(bool ok, int site, long v) {
+  if (!ok) atomicCAS(&g_bc_first, 0ull, ((unsigned long long)site << 48) | ((unsigned long long)v & 0xffffffffffffull));
+  return ok;
+}
+// The module's record, cleared (host).
+static inline unsigned long long bc_take_module() {
+  unsigned long long v = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&v, g_bc_first, sizeof v) != cudaSuccess) return ~0ull;
+  cudaMemcpyToSymbol(g_bc_first, &z, sizeof z);
+  return v;
+}
+#else
+__device__ __forceinline__ bool bc_ok(bool, int, long) { return true; }
+static inline unsigned long long bc_take_module() { return 0; }
+#endif
 
 // ---------------------------------------------------------------------------
 // device arithmetic
@@ -109,6 +138,7 @@ __device__ __forceinline__ void e_apply(const FieldArgs<T>& a, typename V2<T>::t
     const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
     const V* D = a.pml_d[slab];
     const long pc = a.pcomp[slab];
+    if (!bc_ok(pi >= 0 && pi < pc, BC_E_SLAB, pi)) return;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       if (!(MASK & (1 << k))) continue;
@@ -120,6 +150,7 @@ __device__ __forceinline__ void e_apply(const FieldArgs<T>& a, typename V2<T>::t
     }
   } else if (z >= a.hi && z <= a.hf) {
     const long ie = (long)(z - a.hi) * g.plane + (long)y * g.pitch + (long)(x + g.xo);
+    if (!bc_ok(x >= 0 && x <= g.nx + 1 && y >= 0 && y <= g.ny + 1, BC_EPS, ie)) return;
     if (CEPS) {
       const cx<T> epc = ld<T>(a.eps_c + ie);
 #pragma unroll
@@ -204,6 +235,7 @@ __device__ __forceinline__ void h_update(const FieldArgs<T>& a, int x, int y, in
     const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
     V* B = a.pml_b[slab];
     const long pc = a.pcomp[slab];
+    if (!bc_ok(pi >= 0 && pi < pc, BC_H_SLAB, pi)) return;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       if (!(MASK & (1 << k))) continue;
@@ -239,6 +271,7 @@ __device__ __forceinline__ void e_split_cell(const FieldArgs<T>& a, int x, int y
   using V = typename V2<T>::t;
   const Geo& g = a.g;
   const long i = g.at(x, y, z);
+  if (!bc_ok(x >= 1 && x <= g.nx && y >= 1 && y <= g.ny && z >= 1 && z <= g.nz, BC_E_CELL, i)) return;
   V* E[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
   cx<T> e[3];
   e_cell<T, CEPS, MASK, UPML>(a, a.pml_d, x, y, z, e);
@@ -274,6 +307,7 @@ __device__ __forceinline__ void h_split_cell(const FieldArgs<T>& a, int x, int y
   using V = typename V2<T>::t;
   const Geo& g = a.g;
   const long i = g.at(x, y, z);
+  if (!bc_ok(x >= 1 && x <= g.nx && y >= 1 && y <= g.ny && z >= 1 && z <= g.nz, BC_H_CELL, i)) return;
   V* Ec[3] = {a.e, a.e + g.comp, a.e + 2 * g.comp};
   V* H[3] = {a.h, a.h + g.comp, a.h + 2 * g.comp};
   cx<T> ev[3], xp[3], yp[3], zp[3], h[3];
@@ -460,6 +494,9 @@ template <typename T>
 __device__ __forceinline__ void tfsf_apply(typename V2<T>::t* e, typename V2<T>::t* h, const Geo& g,
                                            const SrcArgs& s, int ix, int y0, int y1, cx<double> vE, cx<double> vH) {
   const int zm = s.iz_min;
+  if (!bc_ok(ix >= 0 && ix <= s.nx + 1 && y0 >= 0 && y1 <= s.ny + 1 && zm >= 1 && zm <= g.nz, BC_TFSF,
+             ((long)ix << 32) | (unsigned)y1))
+    return;
   if (s.variant == 1) {
     if (s.i_pol == 2) {
       // E_x(iz_min) += eps_in(1)*tf5(iz_min-1): ix in [0,nx], iy in [0,ny+1]
@@ -511,9 +548,11 @@ struct Seg {
 // thread, their loads issued before their stores.  Sample L of the run is
 // location (u, v) = (L mod nu, L div nu); runs hold fewer than 2^31 samples.
 constexpr int GATHER_PER = 4, GATHER_BLOCK = 256 * GATHER_PER;
+// comp: elements of a field component, np: points of a ring slot (checked
+// by the bounds-check build).
 template <typename T>
 __device__ __forceinline__ void gather_run(const Seg& sg, const typename V2<T>::t* __restrict__ src,
-                                           typename V2<T>::t* __restrict__ slot) {
+                                           typename V2<T>::t* __restrict__ slot, long comp, long np) {
   using V = typename V2<T>::t;
   const unsigned n = (unsigned)sg.nu * (unsigned)sg.nv, nu = (unsigned)sg.nu;
   const unsigned L0 = blockIdx.x * (unsigned)GATHER_BLOCK + threadIdx.x;
@@ -523,13 +562,14 @@ __device__ __forceinline__ void gather_run(const Seg& sg, const typename V2<T>::
     const unsigned L = L0 + 256u * j;
     if (L < n) {
       const unsigned v = L / nu, u = L - v * nu;
-      val[j] = src[sg.src + (long)u * sg.su + (long)v * sg.sv];
+      const long q = sg.src + (long)u * sg.su + (long)v * sg.sv;
+      val[j] = bc_ok(q >= 0 && q < comp, BC_GATHER_SRC, q) ? src[q] : V{};
     }
   }
 #pragma unroll
   for (int j = 0; j < GATHER_PER; ++j) {
     const unsigned L = L0 + 256u * j;
-    if (L < n) slot[sg.p0 + L] = val[j];
+    if (L < n && bc_ok(sg.p0 + L < np, BC_GATHER_DST, sg.p0 + L)) slot[sg.p0 + L] = val[j];
   }
 }
 

@@ -405,11 +405,11 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_dft_gather(const typename V2<T>::t* __restrict__ e,
                                                     const typename V2<T>::t* __restrict__ h, long comp,
                                                     const Seg* __restrict__ segs, typename V2<T>::t* __restrict__ slot,
-                                                    int* tk, int islot, int t, const int* tp) {
+                                                    int* tk, int islot, int t, const int* tp, long np) {
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) tk[islot] = tp ? *tp + t : t;
   const Seg sg = segs[blockIdx.y];
   const typename V2<T>::t* src = sg.field < 3 ? e + sg.field * comp : h + (sg.field - 3) * comp;
-  gather_run<T>(sg, src, slot);
+  gather_run<T>(sg, src, slot, comp, np);
 }
 
 // FP64 mode: fdata(p, iw) += (dt*F_k(p))*exp(i*fw(iw)*t_k), k in the
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(DFT_THREADS) k_dft_fp32(const float2* __restri
 // hi/lo (K-major core matrices, no swizzle) in shared memory, the B
 // operands, identical for every item of a group, prepared once per block in
 // global memory in the same layout by k_twiddle_tc and bulk-copied (TMA) per
-// chunk.  The kernel is k_dft_ws below.
+// chunk.  The kernels are k_dft_ws_commit and k_dft_ws_flux below.
 
 constexpr int TC_M = 128, TC_NW = 128, TC_KC = 16;
 constexpr int TC_NMAX = 2 * TC_NW;                       // TMEM columns per CTA
@@ -710,7 +710,7 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
 // operands, so each A_x is the value a commit would store), but nothing is
 // written back: a flux read costs one read of the four flux components'
 // accumulators, and the ring is committed when it is full, as before.  Its
-// work items are tiles of FL_LOC = 32 locations of one face (k_dft_ws in
+// work items are tiles of FL_LOC = 32 locations of one face (k_dft_ws_flux,
 // flux mode); k_flux_sum adds the partials of a face in a fixed order, so
 // the result does not depend on scheduling.
 constexpr int FL_LOC = 32;
@@ -760,10 +760,24 @@ __device__ __forceinline__ long face_comp(const FluxFace& F, int c) {
 // mode, 5 in flux mode) and stops; the others stop at their next wait; the
 // CTA waits (bounded) for its copies and MMAs before it frees its TMEM.
 
-constexpr int WS_STAGES = 3, WS_PROD = 64, WS_EPI = 512, WS_FCH = 4;
-constexpr int WS_THREADS = WS_PROD + WS_EPI + 32;  // + the MMA warp: 19 warps
-constexpr int WS_MMA_WARP = (WS_PROD + WS_EPI) / 32;
+constexpr int WS_STAGES = 3, WS_EPI = 512, WS_FCH = 4;
 constexpr size_t WS_SMEM = WS_STAGES * TC_STAGE;
+// Per-mode layout.  A sub-partition holds a quarter of the register file, and
+// the warps of a CTA are dealt to the four in turn, so W warps of R registers
+// fit when ceil(W / 4) x 32 x R <= 16384.  Commit mode (the A stream is the
+// whole sample ring): four producer warps, one A row a thread, two chunks
+// ahead in registers (one chunk ahead left 8 KB of sample loads in flight per
+// SM and the producers latency-bound); 21 warps, 80 registers.  Flux mode
+// (a few buffered samples, the accumulators dominate): two producer warps,
+// two rows a thread, one chunk ahead; 19 warps, 96 registers for the
+// epilogue's products.
+template <bool FLUX> struct WsCfg {
+  static constexpr int PROD = FLUX ? 64 : 128;  // producer threads
+  static constexpr int RPT = TC_M / PROD;       // A rows per producer thread
+  static constexpr int AHEAD = FLUX ? 1 : 2;    // chunks of samples loaded ahead
+  static constexpr int THREADS = PROD + WS_EPI + 32;
+  static constexpr int MMA_WARP = (PROD + WS_EPI) / 32;
+};
 
 struct WsArgs {
   const float2* S;  // the sample ring [nk][P]
@@ -827,7 +841,8 @@ template <bool FLUX> __device__ __forceinline__ long ws_point(const WsRow<FLUX>&
   return row < r.np ? r.p0 + row : -1;
 }
 
-template <bool FLUX> __global__ void __launch_bounds__(WS_THREADS, 1) k_dft_ws(WsArgs A) {
+template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
+  constexpr int WS_PROD = WsCfg<FLUX>::PROD, RPT = WsCfg<FLUX>::RPT, WS_MMA_WARP = WsCfg<FLUX>::MMA_WARP;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint64_t full[WS_STAGES], empty[WS_STAGES], accf[2], acce[2], fin;
   __shared__ uint32_t taddr_s;
@@ -868,44 +883,62 @@ template <bool FLUX> __global__ void __launch_bounds__(WS_THREADS, 1) k_dft_ws(W
 
   if (tid < WS_PROD) {
     // ---- producers: one flat sequence of (item, chunk) pairs; a thread takes
-    // rows tid and tid + 64, the samples of the next chunk in registers while
-    // a chunk is split into its stage
+    // rows tid + h WS_PROD (h < RPT), the samples of the next AHEAD chunks in
+    // registers while a chunk is split into its stage
     if (mma) {
       int armed[WS_STAGES] = {};  // fills issued per stage (thread 0: the last one is drained at exit)
       struct Cur {
         long j;
         int c, g;
-        long rp0, rp1;
+        long rp[RPT];
         bool ok;
       };
       auto at = [&](long j, int c) {
-        Cur x{j, c, 0, -1, -1, false};
+        Cur x;
+        x.j = j;
+        x.c = c;
+        x.g = 0;
+        x.ok = false;
+#pragma unroll
+        for (int h = 0; h < RPT; ++h) x.rp[h] = -1;
         const long item = blockIdx.x + j * gridDim.x;
         if (item < A.nitems) {
           const WsRow<FLUX> r = ws_item<FLUX>(A, item, x.g);
-          x.rp0 = ws_point<FLUX>(r, tid);
-          x.rp1 = ws_point<FLUX>(r, tid + WS_PROD);
+#pragma unroll
+          for (int h = 0; h < RPT; ++h) {
+            x.rp[h] = ws_point<FLUX>(r, tid + h * WS_PROD);
+            if (!bc_ok(x.rp[h] < A.P, BC_DFT_SAMPLE, x.rp[h])) x.rp[h] = -1;
+          }
           x.ok = true;
         }
         return x;
       };
       auto next = [&](const Cur& x) {
-        return x.c + 1 < nch ? Cur{x.j, x.c + 1, x.g, x.rp0, x.rp1, x.ok} : at(x.j + 1, 0);
+        if (x.c + 1 < nch) {
+          Cur y = x;
+          ++y.c;
+          return y;
+        }
+        return at(x.j + 1, 0);
       };
+      constexpr int NV = 8 * RPT;  // samples a thread holds per chunk
       auto load = [&](const Cur& x, float2* dst) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           const int k = x.c * (TC_KC / 2) + q;
           const bool kk = x.ok && k < A.nk;
-          dst[q] = (kk && x.rp0 >= 0) ? A.S[(long)k * A.P + x.rp0] : make_float2(0.f, 0.f);
-          dst[8 + q] = (kk && x.rp1 >= 0) ? A.S[(long)k * A.P + x.rp1] : make_float2(0.f, 0.f);
+#pragma unroll
+          for (int h = 0; h < RPT; ++h)
+            dst[8 * h + q] = (kk && x.rp[h] >= 0) ? A.S[(long)k * A.P + x.rp[h]] : make_float2(0.f, 0.f);
         }
       };
-      Cur c0 = at(0, 0), c1 = next(c0);
-      float2 v0[16], v1[16];
+      Cur c0 = at(0, 0), c1 = next(c0), c2 = WsCfg<FLUX>::AHEAD > 1 ? next(c1) : c1;
+      float2 v0[NV], v1[NV], v2[WsCfg<FLUX>::AHEAD > 1 ? NV : 1];
       load(c0, v0);
+      if constexpr (WsCfg<FLUX>::AHEAD > 1) load(c1, v1);
       for (long n = 0; c0.ok && !stopped(); ++n) {
-        load(c1, v1);
+        if constexpr (WsCfg<FLUX>::AHEAD > 1) load(c2, v2);
+        else load(c1, v1);
         const int s = (int)(n % WS_STAGES);
         const long u = n / WS_STAGES;
         if (u > 0 && !mbar_wait(&empty[s], (unsigned)((u - 1) & 1), STREAM_WAIT_CYCLES)) {
@@ -926,23 +959,28 @@ template <bool FLUX> __global__ void __launch_bounds__(WS_THREADS, 1) k_dft_ws(W
         float* Ah = (float*)st;
         float* Al = (float*)(st + TC_A_BYTES);
 #pragma unroll
-        for (int h2 = 0; h2 < 2; ++h2) {
-          const int row = tid + h2 * WS_PROD;
+        for (int h = 0; h < RPT; ++h) {
+          const int row = tid + h * WS_PROD;
 #pragma unroll
           for (int m = 0; m < 4; ++m) {
-            const float2 a = v0[8 * h2 + 2 * m], bq = v0[8 * h2 + 2 * m + 1];
+            const float2 a = v0[8 * h + 2 * m], bq = v0[8 * h + 2 * m + 1];
             const float4 x = make_float4(a.x, a.y, bq.x, bq.y);
-            const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
-            *(float4*)(Ah + tc_off(row, 4 * m)) = h;
-            *(float4*)(Al + tc_off(row, 4 * m)) = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+            const float4 hv = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+            *(float4*)(Ah + tc_off(row, 4 * m)) = hv;
+            *(float4*)(Al + tc_off(row, 4 * m)) = make_float4(x.x - hv.x, x.y - hv.y, x.z - hv.z, x.w - hv.w);
           }
         }
         fence_proxy_async();  // the generic-proxy writes of A before the tensor core reads them
         mbar_arrive(&full[s]);
 #pragma unroll
-        for (int q = 0; q < 16; ++q) v0[q] = v1[q];
+        for (int q = 0; q < NV; ++q) v0[q] = v1[q];
+        if constexpr (WsCfg<FLUX>::AHEAD > 1) {
+#pragma unroll
+          for (int q = 0; q < NV; ++q) v1[q] = v2[q];
+        }
         c0 = c1;
-        c1 = next(c1);
+        c1 = WsCfg<FLUX>::AHEAD > 1 ? c2 : next(c1);
+        if constexpr (WsCfg<FLUX>::AHEAD > 1) c2 = next(c2);
       }
       if (tid == 0)
         // copies issued into a stage whose MMAs never ran must land before the CTA exits
@@ -1009,7 +1047,8 @@ template <bool FLUX> __global__ void __launch_bounds__(WS_THREADS, 1) k_dft_ws(W
       const long vv = j >> 1;
       int g;
       const WsRow<FLUX> r = ws_item<FLUX>(A, item, g);
-      const long ep = ws_point<FLUX>(r, 32 * q4 + lane);
+      long ep = ws_point<FLUX>(r, 32 * q4 + lane);
+      if (!bc_ok(ep < A.P, BC_DFT_POINT, ep)) ep = -1;
       const int nw = min(TC_NW, A.nof - g * TC_NW), nchk = (nw + WS_FCH - 1) / WS_FCH;
       float4* fdg = A.fd + (long)g * TC_NW * A.P;
       auto load_fd = [&](int ch, float4* dst) {
@@ -1095,6 +1134,9 @@ template <bool FLUX> __global__ void __launch_bounds__(WS_THREADS, 1) k_dft_ws(W
   if (warp == WS_MMA_WARP && mma)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_NMAX) : "memory");
 }
+
+__global__ void __maxnreg__(80) k_dft_ws_commit(WsArgs A) { dft_ws<false>(A); }
+__global__ void __launch_bounds__(WsCfg<true>::THREADS, 1) k_dft_ws_flux(WsArgs A) { dft_ws<true>(A); }
 
 // J[f][iw] = scale * sign * (sum of face f's partials, four per tile, in
 // order within each thread, then a fixed tree).
@@ -1351,7 +1393,8 @@ template <typename T, bool CEPS> __global__ void __launch_bounds__(TINY_THREADS)
       } else {
         const long q = w - n_tf, code = A.sidx[q];
         const int f = (int)(code & 7);
-        A.S[(long)slot * A.P + q] = (f < 3 ? A.a.e + f * g.comp : A.a.h + (f - 3) * g.comp)[code >> 3];
+        if (bc_ok(f < 6 && (code >> 3) < g.comp, BC_GATHER_SRC, code >> 3))
+          A.S[(long)slot * A.P + q] = (f < 3 ? A.a.e + f * g.comp : A.a.h + (f - 3) * g.comp)[code >> 3];
       }
     }
     if (tf && !one && !grid_barrier(A.bar, target, gridDim.x, A.err)) return;
@@ -1360,7 +1403,8 @@ template <typename T, bool CEPS> __global__ void __launch_bounds__(TINY_THREADS)
         for (long q = gt; q < A.P; q += gs) {
           const long code = A.sidx[q];
           const int f = (int)(code & 7);
-          A.S[(long)slot * A.P + q] = (f < 3 ? A.a.e + f * g.comp : A.a.h + (f - 3) * g.comp)[code >> 3];
+          if (bc_ok(f < 6 && (code >> 3) < g.comp, BC_GATHER_SRC, code >> 3))
+            A.S[(long)slot * A.P + q] = (f < 3 ? A.a.e + f * g.comp : A.a.h + (f - 3) * g.comp)[code >> 3];
         }
       if (gt == 0) A.tk[slot] = it + 1 - A.to_fourier;
       ++slot;
@@ -1396,11 +1440,20 @@ struct SphereBox {
   int zlo, zhi, xlo, lx, ylo, ly;
 };
 
+// Spheres binned per (plane, 32 x 32 tile of x, y): lst[off[b] .. off[b+1])
+// holds, ascending, the spheres whose bounding box touches bin b = ((z - hi)
+// nty + ty) ntx + tx; null when the lists would be too long (the generator
+// then tests every sphere).
+constexpr int GEN_TILE = 32;
+
 struct GenArgs {
   int kind, hi, hf;
   double base;
   const SphereBox* sph;
   int nsph;
+  const int* off;
+  const int* lst;
+  int ntx, nty;
   unsigned long long seed;
   double fill, v_in, v_out;
   int x0, x1, y0, y1;
@@ -1438,14 +1491,30 @@ template <typename T> __global__ void k_material_gen(GenArgs G, Geo g, T* __rest
           ((unsigned long long)zz * g.ny + (unsigned long long)(ys - 1)) * (unsigned long long)g.nx + (xs - 1);
       v = splitmix_u(G.seed, i) < G.fill ? G.v_in : G.v_out;
     } else {
-      for (int k = 0; k < G.nsph; ++k) {
-        const SphereBox b = G.sph[k];
-        if (z < b.zlo || z > b.zhi) continue;
+      // the last sphere that holds the cell wins: search from the last
+      auto inside = [&](const SphereBox& b) {
+        if (z < b.zlo || z > b.zhi) return false;
         const int xu = b.xlo + ((xs - b.xlo) % g.nx + g.nx) % g.nx, yu = b.ylo + ((ys - b.ylo) % g.ny + g.ny) % g.ny;
-        if (xu > b.xlo + b.lx - 1 || yu > b.ylo + b.ly - 1) continue;
+        if (xu > b.xlo + b.lx - 1 || yu > b.ylo + b.ly - 1) return false;
         const double dz = __dsub_rn((double)z, b.cz), dy = __dsub_rn((double)yu, b.cy), dx = __dsub_rn((double)xu, b.cx);
         const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dz, dz), __dmul_rn(dy, dy)), __dmul_rn(dx, dx));
-        if (d2 <= b.r2) v = b.inv;
+        return d2 <= b.r2;
+      };
+      if (G.off) {
+        const long bin = ((long)zz * G.nty + (ys - 1) / GEN_TILE) * G.ntx + (xs - 1) / GEN_TILE;
+        for (int j = G.off[bin + 1] - 1; j >= G.off[bin]; --j) {
+          const SphereBox& b = G.sph[G.lst[j]];
+          if (inside(b)) {
+            v = b.inv;
+            break;
+          }
+        }
+      } else {
+        for (int k = G.nsph - 1; k >= 0; --k)
+          if (inside(G.sph[k])) {
+            v = G.sph[k].inv;
+            break;
+          }
       }
     }
   }
@@ -1570,7 +1639,9 @@ __global__ void __launch_bounds__(256) k_flux(const ACC* __restrict__ fd, long P
   const int iw = blockIdx.x, f = blockIdx.y;
   const FluxFace F = faces[f];
   double s = 0.0;
-  if (F.active) {
+  if (F.active && bc_ok(F.pa >= 0 && F.pb >= 0 && F.pc >= 0 && F.pd >= 0 &&
+                            max(max(F.pa, F.pb), max(F.pc, F.pd)) + F.n <= P,
+                        BC_FLUX_POINT, F.n)) {
     const ACC* row = fd + (long)iw * P;
     for (long L = threadIdx.x; L < F.n; L += blockDim.x) {
       const double2 a = acc_value(row[F.pa + L]), b = acc_value(row[F.pb + L]), c = acc_value(row[F.pc + L]),
@@ -1781,7 +1852,7 @@ template <typename T> void dft_sample(iris_engine* E, int t, const int* tp = nul
   V* slot = (V*)E->S + (long)E->nslot * E->P;
   dim3 grid((unsigned)((E->max_seg + GATHER_BLOCK - 1) / GATHER_BLOCK), (unsigned)E->segs.size());
   k_dft_gather<T><<<grid, 256, 0, E->st>>>((const V*)E->e, (const V*)E->h, E->g.comp, E->d_segs, slot, E->d_tk,
-                                          E->nslot, t, tp);
+                                          E->nslot, t, tp, E->P);
   }
   if (++E->nslot == E->K) dft_flush(E);
 }
@@ -2066,6 +2137,7 @@ int generate_material(iris_engine* E, GenArgs G, const double* host_spheres) {
   CK(cudaMalloc(&E->eps, (size_t)nzs * g.plane * rsz));
   CK(cudaMemsetAsync(E->eps, 0, (size_t)nzs * g.plane * rsz, E->st));
   SphereBox* dsph = nullptr;
+  int *doff = nullptr, *dlst = nullptr;
   std::vector<SphereBox> boxes;
   if (G.kind == 1 && G.nsph > 0) {
     boxes.resize(G.nsph);
@@ -2087,6 +2159,47 @@ int generate_material(iris_engine* E, GenArgs G, const double* host_spheres) {
     }
     CK(cudaMalloc(&dsph, sizeof(SphereBox) * G.nsph));
     CK(cudaMemcpyAsync(dsph, boxes.data(), sizeof(SphereBox) * G.nsph, cudaMemcpyHostToDevice, E->st));
+    // bin the spheres per (plane, tile): the x (y) tiles a box touches are
+    // those of the cells (x - xlo) mod nx < lx, wrapped into 1..nx
+    const int ntx = (p.nx + GEN_TILE - 1) / GEN_TILE, nty = (p.ny + GEN_TILE - 1) / GEN_TILE;
+    const long nbin = (long)nzs * ntx * nty;
+    std::vector<std::vector<int>> tx(G.nsph), ty(G.nsph);
+    long total = 0;
+    for (int k = 0; k < G.nsph; ++k) {
+      const SphereBox& b = boxes[k];
+      auto tiles = [](int lo, int len, int n, std::vector<int>& out) {
+        std::vector<char> hit((n + GEN_TILE - 1) / GEN_TILE, 0);
+        for (int i = 0; i < len; ++i) hit[(((lo + i - 1) % n + n) % n) / GEN_TILE] = 1;
+        for (int t = 0; t < (int)hit.size(); ++t)
+          if (hit[t]) out.push_back(t);
+      };
+      tiles(b.xlo, b.lx, p.nx, tx[k]);
+      tiles(b.ylo, b.ly, p.ny, ty[k]);
+      if (b.zhi >= b.zlo) total += (long)(b.zhi - b.zlo + 1) * tx[k].size() * ty[k].size();
+    }
+    if (total < (1L << 26)) {
+      std::vector<int> off(nbin + 1, 0), lst(std::max(1L, total));
+      for (int k = 0; k < G.nsph; ++k)
+        for (int z = boxes[k].zlo; z <= boxes[k].zhi; ++z)
+          for (int ya : ty[k])
+            for (int xa : tx[k]) ++off[((long)(z - p.hi) * nty + ya) * ntx + xa + 1];
+      for (long b = 0; b < nbin; ++b) off[b + 1] += off[b];
+      std::vector<int> fill(off.begin(), off.end() - 1);
+      for (int k = 0; k < G.nsph; ++k)  // ascending within every bin
+        for (int z = boxes[k].zlo; z <= boxes[k].zhi; ++z)
+          for (int ya : ty[k])
+            for (int xa : tx[k]) lst[fill[((long)(z - p.hi) * nty + ya) * ntx + xa]++] = k;
+      CK(cudaMalloc(&doff, sizeof(int) * off.size()));
+      CK(cudaMalloc(&dlst, sizeof(int) * lst.size()));
+      CK(cudaMemcpyAsync(doff, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, E->st));
+      CK(cudaMemcpyAsync(dlst, lst.data(), sizeof(int) * lst.size(), cudaMemcpyHostToDevice, E->st));
+      // the host vectors must outlive the copies
+      CK(cudaStreamSynchronize(E->st));
+      G.off = doff;
+      G.lst = dlst;
+      G.ntx = ntx;
+      G.nty = nty;
+    }
   }
   G.sph = dsph;
   const long n = (long)(p.nx + 2) * (p.ny + 2) * nzs;
@@ -2096,6 +2209,8 @@ int generate_material(iris_engine* E, GenArgs G, const double* host_spheres) {
   const cudaError_t e1 = cudaGetLastError();
   const cudaError_t e2 = cudaStreamSynchronize(E->st);
   if (dsph) cudaFree(dsph);
+  if (doff) cudaFree(doff);
+  if (dlst) cudaFree(dlst);
   if (e1 != cudaSuccess || e2 != cudaSuccess) return fail(IRIS_ECUDA, "material generation failed");
   E->eps_complex = false;
   return IRIS_OK;
@@ -2197,7 +2312,7 @@ void dft_flush(iris_engine* E) {
     A.ngroups = ng;
     A.nitems = (E->P + TC_M - 1) / TC_M * ng;
     A.err = E->d_err;
-    k_dft_ws<false><<<(unsigned)std::min<long>(A.nitems, E->ws_blocks), WS_THREADS, WS_SMEM, E->st>>>(A);
+    k_dft_ws_commit<<<(unsigned)std::min<long>(A.nitems, E->ws_blocks), WsCfg<false>::THREADS, WS_SMEM, E->st>>>(A);
   } else {
     const int nt = nk * E->p.nof;
     k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
@@ -2287,8 +2402,8 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
   if (E->dft_tc) {
     const int ng = (p.nof + TC_NW - 1) / TC_NW, nch = (2 * E->K + TC_KC - 1) / TC_KC;
     CK(cudaMalloc(&E->d_wtc, sizeof(float) * (size_t)ng * nch * 2 * TC_BROWS * TC_KC));
-    CK(cudaFuncSetAttribute(k_dft_ws<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WS_SMEM));
-    CK(cudaFuncSetAttribute(k_dft_ws<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WS_SMEM));
+    CK(cudaFuncSetAttribute(k_dft_ws_commit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WS_SMEM));
+    CK(cudaFuncSetAttribute(k_dft_ws_flux, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WS_SMEM));
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E->device));
     E->ws_blocks = std::max(1, nsm);  // one persistent CTA per SM (its TMEM takes all 512 columns)
@@ -2556,7 +2671,7 @@ static int stream_status(iris_engine* E) {
 
 // The flux of one face set.  FP32 mode on the tensor cores: over the
 // accumulators plus the samples still in the ring, which stay there
-// (k_twiddle_tc for the pending samples, k_dft_ws in flux mode, k_flux_sum).  Otherwise
+// (k_twiddle_tc for the pending samples, k_dft_ws_flux, k_flux_sum).  Otherwise
 // the ring is committed first and k_flux reads the accumulators.
 int iris::read_flux(iris_engine* E, int set, double* J) {
   const iris_params& p = E->p;
@@ -2587,7 +2702,7 @@ int iris::read_flux(iris_engine* E, int set, double* J) {
       A.ft = ft;
       A.part = E->d_part;
       A.err = E->d_err;
-      k_dft_ws<true><<<(unsigned)std::min<long>(A.nitems, E->ws_blocks), WS_THREADS, WS_SMEM, E->st>>>(A);
+      k_dft_ws_flux<<<(unsigned)std::min<long>(A.nitems, E->ws_blocks), WsCfg<true>::THREADS, WS_SMEM, E->st>>>(A);
     }
     k_flux_sum<<<dim3(p.nof, 6), 256, 0, E->st>>>(E->d_part, ft, E->d_faces + 6 * set, p.nof, scale, E->d_J);
   } else {
@@ -2616,6 +2731,7 @@ int iris::read_flux(iris_engine* E, int set, double* J) {
 extern "C" {
 
 int iris_create(const iris_params* pin, const double* fw, iris_engine** out) {
+  iris::NvtxRange nvtx_("iris_create");
   return create_engine(pin, fw, false, false, out);
 }
 
@@ -2706,6 +2822,7 @@ int iris_get_material(iris_engine* E, double* re, double* im) {
 }
 
 int iris_step(iris_engine* E, int it0, int nsteps) {
+  iris::NvtxRange nvtx_("iris_step");
   clear_error();
   if (!E || nsteps < 0) return fail(IRIS_EINVAL, "bad argument");
   CK(cudaSetDevice(E->device));
@@ -2724,6 +2841,7 @@ int iris_sync(iris_engine* E) {
 }
 
 int iris_flux(iris_engine* E, int box, double* J) {
+  iris::NvtxRange nvtx_("iris_flux");
   clear_error();
   if (!E || !J || box < 0 || box > 1) return fail(IRIS_EINVAL, "bad argument");
   CK(cudaSetDevice(E->device));
@@ -3031,7 +3149,22 @@ int iris_info(const iris_engine* E, long* info) {
   return IRIS_OK;
 }
 
+int iris_bounds_check(unsigned long long* first) {
+  clear_error();
+  if (!first) return fail(IRIS_EINVAL, "bad argument");
+  const unsigned long long r[3] = {bc_take_module(), bc_take_batch(), bc_take_adjoint()};
+  *first = 0;
+  for (unsigned long long v : r)
+    if (v && !*first) *first = v;
+#ifdef IRIS_BOUNDS_CHECK
+  return 1;
+#else
+  return 0;
+#endif
+}
+
 int iris_dft_commit(iris_engine* E) {
+  iris::NvtxRange nvtx_("iris_dft_commit");
   clear_error();
   if (!E) return fail(IRIS_EINVAL, "null engine");
   CK(cudaSetDevice(E->device));

@@ -10,6 +10,8 @@
 #include <utility>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "iris_device.cuh"
 #include "iris_internal.h"
 
@@ -129,6 +131,15 @@ struct iris_engine {
 
 namespace iris {
 
+// An NVTX range over one ABI call (visible in Nsight timelines; NVTX costs a
+// branch when no tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 // Brackets one kernel launch (or the fused pass's two concurrent launches)
 // with a pair of events when timing is on.
 struct KTimer {
@@ -199,6 +210,11 @@ int read_flux(iris_engine* E, int set, double* J);
 // steps, then TF/SF), with the DFT sample of step it when dft is set and the
 // step is sampled.
 void one_step(iris_engine* E, int it, bool dft);
+
+// Bounds-check records of the batch and adjoint modules (read and cleared;
+// 0 in the ordinary build).
+unsigned long long bc_take_batch();
+unsigned long long bc_take_adjoint();
 
 // CUDA graph of one DFT block of steps.
 bool graph_ready(const iris_engine* E, int it, int left);

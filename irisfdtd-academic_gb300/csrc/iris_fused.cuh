@@ -112,6 +112,7 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
   auto& epsh = S.epsh;
   const int lane = threadIdx.x, w = threadIdx.y;
   const int x = 1 + bx * FZ_OX + lane, y = 1 + by * FZ_OY + w;
+  if (!bc_ok(z0 >= 1 && z1 <= g.nz && z0 <= z1 + 1, BC_FUSED_CELL, ((long)z0 << 32) | (unsigned)z1)) return;
   const bool act = x <= g.nx + 1 && y <= g.ny + 1;
   const bool ximg = x == g.nx + 1, yimg = y == g.ny + 1;
   const int cxx = ximg ? 1 : x, cyy = yimg ? 1 : y;  // the cell whose E' this thread computes
@@ -151,14 +152,16 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
         if (act && pe) {
           const int slab = zp <= a.pmlzi ? 0 : 1, zr = slab == 0 ? zp - 1 : zp - a.pmlzf;
           const long pi = ((long)zr * g.ny + (cyy - 1)) * (long)g.nx + (cxx - 1);
+          if (bc_ok(pi >= 0 && pi < a.pcomp[slab], BC_FUSED_SLAB, pi))
 #pragma unroll
-          for (int k = 0; k < 3; ++k) cpa8(&U.d[p & 1][w][lane][k], a.pml_d[slab] + k * a.pcomp[slab] + pi);
+            for (int k = 0; k < 3; ++k) cpa8(&U.d[p & 1][w][lane][k], a.pml_d[slab] + k * a.pcomp[slab] + pi);
         }
         if (own && pb) {
           const int slab = zb <= a.pmlzi ? 0 : 1, zr = slab == 0 ? zb - 1 : zb - a.pmlzf;
           const long pi = ((long)zr * g.ny + (y - 1)) * (long)g.nx + (x - 1);
+          if (bc_ok(pi >= 0 && pi < a.pcomp[slab], BC_FUSED_SLAB, pi))
 #pragma unroll
-          for (int k = 0; k < 3; ++k) cpa8(&U.b[p & 1][w][lane][k], a.pml_b[slab] + k * a.pcomp[slab] + pi);
+            for (int k = 0; k < 3; ++k) cpa8(&U.b[p & 1][w][lane][k], a.pml_b[slab] + k * a.pcomp[slab] + pi);
         }
         if (w < 2 && lane < NCOEF && (w == 0 ? pe : pb)) {
           const int zz = w == 0 ? zp : zb;

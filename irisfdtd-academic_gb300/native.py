@@ -14,7 +14,10 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
-LIB = os.path.join(PKG, "libiris_fdtd.so")
+LIB_PLAIN = os.path.join(PKG, "libiris_fdtd.so")
+# the bounds-checking build (-DIRIS_BOUNDS_CHECK); IRIS_BOUNDS_CHECK=1 loads it
+LIB_BC = os.path.join(PKG, "libiris_fdtd_bc.so")
+LIB = LIB_BC if os.environ.get("IRIS_BOUNDS_CHECK") == "1" else LIB_PLAIN
 SOURCES = ["iris_engine.cu", "iris_batch.cu", "iris_adjoint.cu", "iris_host.cpp"]
 HEADERS = [os.path.join(INCLUDE, "iris_fdtd.h")] + [os.path.join(CSRC, h) for h in
                                                    ("iris_internal.h", "iris_device.cuh", "iris_engine.h",
@@ -29,38 +32,48 @@ def nvcc() -> str:
     return "nvcc"
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB):
-        return True
-    t = os.path.getmtime(LIB)
+def _stale(lib_path: str = None) -> bool:
+    paths = [lib_path] if lib_path else [LIB_PLAIN, LIB_BC]
     deps = [os.path.join(CSRC, s) for s in SOURCES] + HEADERS
-    return any(os.path.getmtime(d) > t for d in deps)
+    for path in paths:
+        if not os.path.exists(path):
+            return True
+        t = os.path.getmtime(path)
+        if any(os.path.getmtime(d) > t for d in deps):
+            return True
+    return False
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile the engine for sm_103a (nvcc cross-compiles without a GPU)."""
+    """Compile the engine for sm_103a (nvcc cross-compiles without a GPU):
+    libiris_fdtd.so and its bounds-checking twin libiris_fdtd_bc.so, all
+    translation units in parallel."""
     if not force and not _stale():
         return LIB
-    objs = []
+    jobs = []  # (library, objects)
     procs = []
-    for s in SOURCES:
-        src = os.path.join(CSRC, s)
-        obj = os.path.join(CSRC, os.path.splitext(s)[0] + ".o")
-        cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
-               "-I", INCLUDE, "-c", src, "-o", obj]
-        if verbose:
-            print(" ".join(cmd))
-        procs.append(subprocess.Popen(cmd))
-        objs.append(obj)
+    for lib_path, defs, tag in ((LIB_PLAIN, [], ""), (LIB_BC, ["-DIRIS_BOUNDS_CHECK"], "_bc")):
+        objs = []
+        for s in SOURCES:
+            src = os.path.join(CSRC, s)
+            obj = os.path.join(CSRC, os.path.splitext(s)[0] + tag + ".o")
+            cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", *defs,
+                   "-I", INCLUDE, "-c", src, "-o", obj]
+            if verbose:
+                print(" ".join(cmd))
+            procs.append(subprocess.Popen(cmd))
+            objs.append(obj)
+        jobs.append((lib_path, objs))
     for pr in procs:
         if pr.wait() != 0:
             raise RuntimeError("nvcc failed building the engine")
-    tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
-    subprocess.run(cmd, check=True)
-    os.replace(tmp, LIB)
-    for o in objs:
-        os.remove(o)
+    for lib_path, objs in jobs:
+        tmp = lib_path + ".tmp"
+        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, lib_path)
+        for o in objs:
+            os.remove(o)
     return LIB
 
 
@@ -104,6 +117,7 @@ EXPORTS = [
     "iris_get_material", "iris_batch_material_pattern", "iris_write_scatt", "iris_get_field", "iris_set_field", "iris_get_pml", "iris_set_pml",
     "iris_get_field_c", "iris_set_field_c", "iris_get_pml_c", "iris_set_pml_c",
     "iris_get_fdata", "iris_get_plane", "iris_apply", "iris_run_input", "iris_timing", "iris_timing_read", "iris_info",
+    "iris_bounds_check",
     "iris_dft_block_noalloc", "iris_batch_create", "iris_batch_destroy", "iris_batch_set_material",
     "iris_batch_step", "iris_batch_flux", "iris_batch_dft_commit", "iris_batch_get_field", "iris_batch_tune", "iris_batch_set_tile",
     "iris_batch_timing", "iris_batch_timing_read", "iris_batch_info",
@@ -120,7 +134,7 @@ def lib():
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB) or _stale():
+    if not os.path.exists(LIB) or _stale(LIB):
         build()
     L = ctypes.CDLL(LIB)
     vp, ip, dp, cp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_char_p
@@ -163,6 +177,7 @@ def lib():
     L.iris_timing.argtypes = [vp, ip]
     L.iris_timing_read.argtypes = [vp, dp, dp, ctypes.POINTER(ctypes.c_long)]
     L.iris_info.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
+    L.iris_bounds_check.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)]
     L.iris_dft_block_noalloc.argtypes = [vp, ip, ctypes.c_long, ip, ip, vp, ip, ctypes.c_double, vp, vp]
     lp = ctypes.POINTER(ctypes.c_long)
     L.iris_batch_create.argtypes = [ip, P, dp, ip, ctypes.POINTER(vp)]

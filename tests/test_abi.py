@@ -25,6 +25,21 @@ def test_exports_match_header(iris):
     assert set(names) == set(iris.native.EXPORTS)
 
 
+def test_bounds_checking_twin_exports_the_same_entry_points(iris):
+    """libiris_fdtd_bc.so (built with -DIRIS_BOUNDS_CHECK beside the ordinary
+    library) loads and exports every header function; the ordinary library
+    reports that it does not check and has nothing recorded (no device
+    call)."""
+    iris.lib()  # builds both when stale
+    bc = ctypes.CDLL(iris.native.LIB_BC)
+    for n in header_functions():
+        assert hasattr(bc, n), n
+    v = ctypes.c_ulonglong(7)
+    plain = ctypes.CDLL(iris.native.LIB_PLAIN)
+    plain.iris_bounds_check.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)]
+    assert plain.iris_bounds_check(ctypes.byref(v)) == 0 and v.value == 0
+
+
 def test_strerror(iris):
     L = iris.lib()
     assert L.iris_strerror(0) == b"success"
