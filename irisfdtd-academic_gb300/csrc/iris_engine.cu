@@ -770,7 +770,9 @@ constexpr size_t WS_SMEM = WS_STAGES * TC_STAGE;
 // SM and the producers latency-bound); 21 warps, 80 registers.  Flux mode
 // (a few buffered samples, the accumulators dominate): two producer warps,
 // two rows a thread, one chunk ahead; 19 warps, 96 registers for the
-// epilogue's products.
+// epilogue's products (twelve epilogue warps streaming two chunks ahead, 15
+// warps at 128 registers, measured 1.13-1.17 times slower: the flux epilogue
+// is bound by instruction issue more than by loads in flight).
 template <bool FLUX> struct WsCfg {
   static constexpr int PROD = FLUX ? 64 : 128;  // producer threads
   static constexpr int RPT = TC_M / PROD;       // A rows per producer thread
