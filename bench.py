@@ -385,7 +385,8 @@ def run_engine(args, rank, world, local):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "c64 fields (fp32), fp64 incident field and DFT accumulation" if prec == iris.FP32 else "c128 (fp64)",
+        "dtype": ("c64 fields (fp32), fp64 incident field, compensated fp32 (double-float) DFT accumulation"
+                  if prec == iris.FP32 else "c128 (fp64)"),
         "data": ("synthetic (seeded spheres, numpy PCG64 seed 0)" if w.structure == "spheres"
                  else f"synthetic ({w.structure} geometry)"),
         "config": {
@@ -530,7 +531,7 @@ def measure_batch(iris, args, rank, world, local, K, W, D, loop_sample=0):
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": round(reg_ms / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64 fields (fp32), fp64 incident field and DFT accumulation",
+        "dtype": "c64 fields (fp32), fp64 incident field, compensated fp32 (double-float) DFT accumulation",
         "data": "synthetic (seeded binary eps patterns, numpy PCG64 seed+i per cell)",
         "config": {"workload": f"batch of {ncells} uneven Bloch cells", "grid_cells": cells,
                    "nof": 128, "dft_points": info["dft_points"], "dft_block": kb,
