@@ -432,9 +432,9 @@ def run_engine(args, rank, world, local):
         out["batch"] = {k: bt[k] for k in keys if k in bt}
     if args.workload == 3 and not args.grid and not args.no_configs and world == 1:
         # the other named workloads, each through the public API on this GPU
-        out["configs0_tiny"] = guarded(measure_tiny, iris, local)
-        out["configs1_slit"] = guarded(measure_slit, iris, local)
-        out["configs4_adjoint"] = guarded(measure_adjoint, iris, local, args.adjoint_fd_voxels)
+        out["slab_4x4x512_fp64"] = guarded(measure_tiny, iris, local)
+        out["slit_256x4x768"] = guarded(measure_slit, iris, local)
+        out["adjoint_160x160x512"] = guarded(measure_adjoint, iris, local, args.adjoint_fd_voxels)
     D.close()
     return out
 
@@ -741,7 +741,7 @@ def guarded(fn, *a, **k):
 
 
 def measure_slit(iris, local):
-    """configs[1]: the 256x4x768 slit array, FP32 against FP64 over its 8000 steps."""
+    """The 256x4x768 slit array, FP32 against FP64 over its 8000 steps."""
     cfg = importlib.import_module(PKG + ".configs")
     w = cfg.workload(2)
     path = cfg.write_input(os.path.join(tempfile.mkdtemp(prefix="iris_slit_"), "inputFDTD.dat"), w)
@@ -751,7 +751,7 @@ def measure_slit(iris, local):
 
 
 def measure_tiny(iris, local):
-    """configs[0]: the 4x4x512 FP64 slab, DFT of the z = 30 and z = 480 planes at
+    """The 4x4x512 FP64 slab, DFT of the z = 30 and z = 480 planes at
     200 frequencies, 4000 steps, stepped by the persistent kernel (one
     cooperative launch per span of steps); the same run through the split
     passes replayed from CUDA graphs, which must give the same spectra bit
@@ -800,7 +800,7 @@ def measure_tiny(iris, local):
 
 
 def measure_adjoint(iris, local, fd_voxels=64):
-    """configs[4]: dL/d eps over the 128x128x32 design region of the 160x160x512
+    """dL/d eps over the 128x128x32 design region of the 160x160x512
     cell, FP32 forward and adjoint over 6000 steps with checkpoints every 256;
     the gradient against the FP64 adjoint, and against central differences
     (h = 1e-3) of the FP64 forward along a seeded +-1 direction over
@@ -1040,7 +1040,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="default workload: skip the batched-form sub-measurement")
     ap.add_argument("--no-configs", action="store_true",
-                    help="default workload: skip the configs[0], [1] and [4] sub-measurements")
+                    help="default workload: skip the 4x4x512 slab, slit-array and adjoint sub-measurements")
     ap.add_argument("--adjoint-fd-voxels", type=int, default=64,
                     help="default line: voxels of the adjoint's directional finite-difference check")
     ap.add_argument("--cpu-sample-steps", type=int, default=192)
