@@ -414,6 +414,14 @@ int iris_batch_get_field(iris_batch* b, int cell, int which, double* re, double*
  */
 #define IRIS_BATCH_NTILES 8
 int iris_batch_tune(iris_batch* b, int reps, int* best, double* ms);
+/* The autotuner with a cache by size class (the device, the precision, a
+ * complex material, and the binary orders of magnitude of the cell count,
+ * the total grid cells and the mean nx, ny, nz): a batch whose class was
+ * tuned before in this process, or is listed in the file named by the
+ * environment variable IRIS_TUNE_CACHE, takes the cached pick without
+ * timing (*cached = 1); otherwise iris_batch_tune runs and its pick is
+ * stored (and appended to that file).  Call before the first step. */
+int iris_batch_autotune(iris_batch* b, int reps, int* best, int* cached);
 /* Force a candidate work list (0..4: x*y*z blocks 32x8x1, 32x4x2, 64x4x1,
  * 16x16x1, 32x2x4 of the split E and H passes; 5, 6: runs of 256
  * consecutive cells of one plane, with registers capped for five resident

@@ -380,6 +380,15 @@ class Batch:
         check(self.L.iris_batch_tune(self.h, reps, ctypes.byref(best), _dp(ms)), "iris_batch_tune")
         return TILES[best.value], dict(zip(TILES, ms.tolist()))
 
+    def autotune(self, reps: int = 3):
+        """iris_batch_autotune: the cached pick for this batch's size class, or
+        tune() and cache its pick.  Returns (the chosen entry of TILES, whether
+        it came from the cache)."""
+        best, cached = ctypes.c_int(0), ctypes.c_int(0)
+        check(self.L.iris_batch_autotune(self.h, reps, ctypes.byref(best), ctypes.byref(cached)),
+              "iris_batch_autotune")
+        return TILES[best.value], bool(cached.value)
+
     def set_tile(self, tile_index: int):
         check(self.L.iris_batch_set_tile(self.h, tile_index), "iris_batch_set_tile")
 

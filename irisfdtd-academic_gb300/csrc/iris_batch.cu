@@ -5,7 +5,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -718,6 +722,99 @@ int iris_batch_set_tile(iris_batch* B, int tile) {
   CK(cudaSetDevice(B->device));
   CK(cudaStreamSynchronize(B->master->st));
   return batch_build_items(B, tile);
+}
+
+namespace {
+
+// The autotuner's picks by size class: in the process, and in the file named
+// by IRIS_TUNE_CACHE when set (lines "<class> <tile>", read once, appended to).
+std::mutex g_tune_mu;
+std::map<std::string, int> g_tune;
+bool g_tune_loaded = false;
+
+// Size class of a batch: the device, the precision, a complex material, and
+// the binary orders of magnitude of the cell count, the total grid cells and
+// the mean nx, ny and nz (the work lists' efficiency follows row lengths and
+// the amount of work).
+std::string size_class(const iris_batch* B) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, B->device);
+  double sx = 0, sy = 0, sz = 0, tot = 0;
+  bool cplx = false;
+  for (const iris_engine* E : B->cells) {
+    sx += E->p.nx;
+    sy += E->p.ny;
+    sz += E->p.nz;
+    tot += (double)E->p.nx * E->p.ny * E->p.nz;
+    cplx |= E->eps_complex;
+  }
+  const double n = std::max(1, B->n);
+  auto lg = [](double v) { return (int)std::floor(std::log2(std::max(1.0, v))); };
+  std::string name(prop.name);
+  for (char& c : name)
+    if (c == ' ') c = '_';
+  return name + "|sm" + std::to_string(prop.multiProcessorCount) + (B->prec == IRIS_FP64 ? "|fp64" : "|fp32") +
+         (cplx ? "|cplx" : "|real") + "|n" + std::to_string(lg(n)) + "|c" + std::to_string(lg(tot)) + "|x" +
+         std::to_string(lg(sx / n)) + "|y" + std::to_string(lg(sy / n)) + "|z" + std::to_string(lg(sz / n));
+}
+
+void tune_cache_load() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* path = std::getenv("IRIS_TUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  char key[256];
+  int t;
+  while (std::fscanf(f, "%255s %d", key, &t) == 2)
+    if (t >= 0 && t < NTILES) g_tune[key] = t;
+  std::fclose(f);
+}
+
+void tune_cache_store(const std::string& key, int t) {
+  g_tune[key] = t;
+  const char* path = std::getenv("IRIS_TUNE_CACHE");
+  if (!path || !*path) return;
+  if (FILE* f = std::fopen(path, "a")) {
+    std::fprintf(f, "%s %d\n", key.c_str(), t);
+    std::fclose(f);
+  }
+}
+
+}  // namespace
+
+int iris_batch_autotune(iris_batch* B, int reps, int* best, int* cached) {
+  clear_error();
+  if (!B || reps < 1) return fail(IRIS_EINVAL, "bad argument");
+  if (B->steps_taken) return fail(IRIS_EINVAL, "tune before the first step (it runs E and H passes on the state)");
+  CK(cudaSetDevice(B->device));
+  const std::string key = size_class(B);
+  int t = -1;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_cache_load();
+    auto it = g_tune.find(key);
+    if (it != g_tune.end() && !(it->second == FUSED && B->prec != IRIS_FP32)) t = it->second;
+  }
+  if (t >= 0) {
+    int rc = iris_batch_set_tile(B, t);
+    if (rc == IRIS_OK) {
+      if (best) *best = t;
+      if (cached) *cached = 1;
+      return IRIS_OK;
+    }
+    clear_error();  // a pick this batch cannot take (memory): time the candidates
+  }
+  int rc = iris_batch_tune(B, reps, &t, nullptr);
+  if (rc) return rc;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_cache_store(key, t);
+  }
+  if (best) *best = t;
+  if (cached) *cached = 0;
+  return IRIS_OK;
 }
 
 int iris_batch_tune(iris_batch* B, int reps, int* best, double* ms) {

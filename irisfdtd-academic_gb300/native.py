@@ -119,7 +119,8 @@ EXPORTS = [
     "iris_get_fdata", "iris_get_plane", "iris_apply", "iris_run_input", "iris_timing", "iris_timing_read", "iris_info",
     "iris_bounds_check",
     "iris_dft_block_noalloc", "iris_batch_create", "iris_batch_destroy", "iris_batch_set_material",
-    "iris_batch_step", "iris_batch_flux", "iris_batch_dft_commit", "iris_batch_get_field", "iris_batch_tune", "iris_batch_set_tile",
+    "iris_batch_step", "iris_batch_flux", "iris_batch_dft_commit", "iris_batch_get_field", "iris_batch_tune",
+    "iris_batch_autotune", "iris_batch_set_tile",
     "iris_batch_timing", "iris_batch_timing_read", "iris_batch_info",
     "iris_adjoint_create", "iris_adjoint_destroy", "iris_adjoint_set_material", "iris_adjoint_set_design",
     "iris_adjoint_forward", "iris_adjoint_backward", "iris_adjoint_engine", "iris_adjoint_apply",
@@ -189,6 +190,7 @@ def lib():
     L.iris_batch_dft_commit.argtypes = [vp]
     L.iris_batch_get_field.argtypes = [vp, ip, ip, dp, dp]
     L.iris_batch_tune.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int), dp]
+    L.iris_batch_autotune.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.iris_batch_set_tile.argtypes = [vp, ip]
     L.iris_batch_timing.argtypes = [vp, ip]
     L.iris_batch_timing_read.argtypes = [vp, dp, dp, lp]

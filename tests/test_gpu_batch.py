@@ -162,3 +162,75 @@ def test_batch_fused_cell_without_interior_range(iris, oracle, tmp_path):
             fb = interior(b.get_field(c, which), cells[c][1])
             fs = interior(e.get_field(which), cells[c][1])
             assert np.array_equal(fb, fs), (c, which)
+
+
+def _batch(iris, cells, precision):
+    params = [engine_params_from_oracle(iris, op, precision=precision, ak=ak) for _, op, ak, _ in cells]
+    b = iris.Batch(params, cells[0][1].fw, dft_faces=iris.DFT_Z)
+    for c, (_, _, _, eps) in enumerate(cells):
+        b.set_material(c, eps)
+    return b
+
+
+def test_autotune_cache_by_size_class(iris, oracle, tmp_path):
+    """iris_batch_autotune times the work lists once per size class: a second
+    batch of the same class takes the cached pick without timing, and steps
+    exactly like a batch set to that pick by hand."""
+    cells = make_cells(oracle, tmp_path)
+    a = _batch(iris, cells, 1)
+    t1, c1 = a.autotune(reps=2)
+    b = _batch(iris, cells, 1)
+    t2, c2 = b.autotune(reps=2)
+    assert (t2, c2) == (t1, True)
+    if not c1:  # this process had not seen the class before
+        assert t1 in iris.TILES
+    ref = _batch(iris, cells, 1)
+    ref.set_tile(iris.TILES.index(t1))
+    for x in (b, ref):
+        x.step(1, 20)
+    for c in range(len(cells)):
+        assert np.array_equal(b.get_field(c, iris.E), ref.get_field(c, iris.E)), c
+    for x in (a, b, ref):
+        x.close()
+
+
+CHILD = """
+import importlib, os, sys
+sys.path.insert(0, sys.argv[1])
+sys.path.insert(0, os.path.join(sys.argv[1], "tests"))
+import numpy as np
+iris = importlib.import_module("irisfdtd-academic_gb300")
+cfg = importlib.import_module("irisfdtd-academic_gb300.configs")
+params, mats = [], []
+for i, (nx, ny, nz) in enumerate([(12, 7, 60), (33, 9, 48), (5, 17, 72)]):
+    w = cfg.Workload("t%d" % i, nx, ny, nz, 8, nz - 7, nz // 2 - 5, 10, 1.0, 0, 14, (1, nx, 1, ny, 10, nz - 10), 9, 40,
+                     structure="pattern", extra=dict(seed=7 + i, fill=0.5))
+    p, fw, _ = iris.setparam(cfg.write_input(os.path.join(sys.argv[2], "t%d.dat" % i), w))
+    p.precision = iris.FP32
+    params.append(p)
+    mats.append(cfg.binary_pattern_material(w))
+b = iris.Batch(params, fw, dft_faces=iris.DFT_Z)
+for c, m in enumerate(mats):
+    b.set_material(c, m)
+tile, cached = b.autotune(reps=1)
+print("PICK", iris.TILES.index(tile), int(cached))
+"""
+
+
+def test_autotune_cache_file_across_processes(tmp_path):
+    """With IRIS_TUNE_CACHE set, the first process times and appends its pick;
+    a second process reads the file and takes the pick without timing."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, IRIS_TUNE_CACHE=str(tmp_path / "tune.txt"))
+    out = []
+    for _ in range(2):
+        r = subprocess.run([sys.executable, "-c", CHILD, root, str(tmp_path)], env=env, capture_output=True, text=True,
+                           timeout=600)
+        assert r.returncode == 0, r.stderr[-3000:]
+        tile, cached = r.stdout.split("PICK")[1].split()
+        out.append((int(tile), int(cached)))
+    assert out[0][1] == 0 and out[1] == (out[0][0], 1)
+    lines = (tmp_path / "tune.txt").read_text().split("\n")
+    assert len([ln for ln in lines if ln.strip()]) == 1 and "|fp32|real|" in lines[0]
