@@ -1664,14 +1664,15 @@ __global__ void __launch_bounds__(256) k_flux(const ACC* __restrict__ fd, long P
 // Fused E+H pass (FP32): one CTA per column tile and z chunk of the launch;
 // the tile column itself is fused_column (iris_fused.cuh).
 
-template <bool CEPS, bool UPML> __global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(FusedArgs A) {
+template <bool CEPS, bool UPML, typename IT>
+__global__ void __launch_bounds__(FZ_X* FZ_Y, 2) k_fused(FusedArgs A) {
   __shared__ FusedSmem S;
   extern __shared__ __align__(16) unsigned char fz_dyn[];
   FusedUpml& U = *reinterpret_cast<FusedUpml*>(fz_dyn);  // UPML = true only
   const bool r0 = (int)blockIdx.z < A.nc0;
   const int z0 = r0 ? A.za0 + A.zc0 * (int)blockIdx.z : A.za1 + A.zc1 * ((int)blockIdx.z - A.nc0);
   const int z1 = min(z0 + (r0 ? A.zc0 : A.zc1) - 1, r0 ? A.zb0 : A.zb1);
-  fused_column<CEPS, UPML>(A, S, U, blockIdx.x, blockIdx.y, z0, z1);
+  fused_column<CEPS, UPML, IT>(A, S, U, blockIdx.x, blockIdx.y, z0, z1);
 }
 
 }  // namespace
@@ -1906,12 +1907,22 @@ void fused_one(iris_engine* E, int it, const int* itp, bool sampled) {
       const FusedArgs a = fused_args(E, part);
       const dim3 grd(E->fgrd.x, E->fgrd.y, (unsigned)(r[3] + (r.size() > 4 ? r[7] : 0)));
       if (part == 0) {
-        if (E->eps_complex) k_fused<true, false><<<grd, E->fblk, 0, E->st>>>(a);
-        else k_fused<false, false><<<grd, E->fblk, 0, E->st>>>(a);
+        if (E->fz_i32) {
+          if (E->eps_complex) k_fused<true, false, int><<<grd, E->fblk, 0, E->st>>>(a);
+          else k_fused<false, false, int><<<grd, E->fblk, 0, E->st>>>(a);
+        } else {
+          if (E->eps_complex) k_fused<true, false, long><<<grd, E->fblk, 0, E->st>>>(a);
+          else k_fused<false, false, long><<<grd, E->fblk, 0, E->st>>>(a);
+        }
       } else {
         cudaStream_t s = both ? E->st2 : E->st;
-        if (E->eps_complex) k_fused<true, true><<<grd, E->fblk, FZ_UPML_SMEM, s>>>(a);
-        else k_fused<false, true><<<grd, E->fblk, FZ_UPML_SMEM, s>>>(a);
+        if (E->fz_i32) {
+          if (E->eps_complex) k_fused<true, true, int><<<grd, E->fblk, FZ_UPML_SMEM, s>>>(a);
+          else k_fused<false, true, int><<<grd, E->fblk, FZ_UPML_SMEM, s>>>(a);
+        } else {
+          if (E->eps_complex) k_fused<true, true, long><<<grd, E->fblk, FZ_UPML_SMEM, s>>>(a);
+          else k_fused<false, true, long><<<grd, E->fblk, FZ_UPML_SMEM, s>>>(a);
+        }
       }
     }
     if (both) {
@@ -2618,10 +2629,12 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
         cudaEventCreateWithFlags(&E->fz_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&E->fz_join, cudaEventDisableTiming) != cudaSuccess)
       return bail(fail(IRIS_ECUDA, "fused pass: stream creation failed"));
-    for (const void* kf : {(const void*)k_fused<false, true>, (const void*)k_fused<true, true>})
+    for (const void* kf : {(const void*)k_fused<false, true, long>, (const void*)k_fused<true, true, long>,
+                           (const void*)k_fused<false, true, int>, (const void*)k_fused<true, true, int>})
       if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FZ_UPML_SMEM) != cudaSuccess)
         return bail(fail(IRIS_ECUDA, "fused pass: shared memory configuration failed"));
     E->fgrd = dim3((p.nx + FZ_OX - 1) / FZ_OX, (p.ny + FZ_OY - 1) / FZ_OY, 1);
+    E->fz_i32 = 3 * E->g.comp < (1L << 31);
   }
   if (cudaMalloc(&E->d_err, sizeof(int)) != cudaSuccess) return bail(fail(IRIS_ENOMEM, "allocation failed"));
   cudaMemsetAsync(E->d_err, 0, sizeof(int), E->st);

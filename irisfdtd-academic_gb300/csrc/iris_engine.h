@@ -97,6 +97,7 @@ struct iris_engine {
   // the UPML slabs, [1] the slabs
   std::vector<int> fzr[2];
   dim3 fblk, fgrd;
+  bool fz_i32 = false;  // the fused pass's offsets fit int (3 x comp < 2^31)
   // the slab launch runs on st2, concurrently with the interior launch (they
   // write disjoint planes and read only the old state): fork / join events
   cudaStream_t st2 = nullptr;

@@ -100,8 +100,11 @@ struct FusedSmem {
 };
 
 // Planes z0..z1 of column tile (bx, by), called by every thread of the CTA;
-// U is used by UPML = true only.
-template <bool CEPS, bool UPML>
+// U is used by UPML = true only.  IT: the integer type of the element offsets
+// of the per-plane loads and stores (int when every offset of the three field
+// components fits, which saves the 64-bit index arithmetic of every access;
+// long otherwise).
+template <bool CEPS, bool UPML, typename IT = long>
 __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, FusedUpml& U, int bx, int by, int z0,
                                              int z1) {
   const FieldArgs<float>& a = A.f;
@@ -122,9 +125,11 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
   if (yimg) ph = cmul(ph, a.pyp);
   const float2* E = a.e;
   const float2* H = a.h;
-  auto ldc = [&](const float2* f, int k, int xx, int yy, int zz) {
-    return ld<float>(f + k * g.comp + g.at(xx, yy, zz));
-  };
+  // element offsets: plane, row, component, and this thread's columns
+  // (cxx, cyy) for what it reads and (x, y) for what it writes
+  const IT pl = (IT)g.plane, pt = (IT)g.pitch, cp = (IT)g.comp;
+  const IT oc = (IT)cyy * pt + (IT)(cxx + g.xo), ow = (IT)y * pt + (IT)(x + g.xo);
+  auto ldc = [&](const float2* f, int k, int zz) { return ld<float>(f + ((IT)k * cp + (IT)zz * pl + oc)); };
   const bool xhalo = act && (lane == 0 || ximg), yhalo = act && (w == 0 || yimg);
   const int xs = lane == 0 ? 0 : 1, ys = w == 0 ? 0 : 1;
   // The copies of plane p in [z0, z1 + 1] (plane nz + 1 is the image of
@@ -133,16 +138,16 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
     if (p <= z1 + 1) {
       const int zp = p == g.nz + 1 ? 1 : p;
       if (!CEPS && act && zp >= a.hi && zp <= a.hf)
-        cpa4(&epsh[p & 1][w][lane], a.eps_r + (long)(zp - a.hi) * g.plane + (long)cyy * g.pitch + (cxx + g.xo));
+        cpa4(&epsh[p & 1][w][lane], a.eps_r + ((IT)(zp - a.hi) * pl + oc));
       if (xhalo) {
-        const long q = g.at(cxx - 1, cyy, zp);
-        cpa8(&xh[p & 1][w][xs][0], H + g.comp + q);
-        cpa8(&xh[p & 1][w][xs][1], H + 2 * g.comp + q);
+        const IT q = (IT)zp * pl + oc - 1;
+        cpa8(&xh[p & 1][w][xs][0], H + (cp + q));
+        cpa8(&xh[p & 1][w][xs][1], H + (2 * cp + q));
       }
       if (yhalo) {
-        const long q = g.at(cxx, cyy - 1, zp);
+        const IT q = (IT)zp * pl + oc - pt;
         cpa8(&yh[p & 1][ys][0][lane], H + q);
-        cpa8(&yh[p & 1][ys][1][lane], H + 2 * g.comp + q);
+        cpa8(&yh[p & 1][ys][1][lane], H + (2 * cp + q));
       }
       if (UPML) {
         // the old D of this thread's E' cell on plane zp, the B of its H'
@@ -178,9 +183,9 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
   // (written there for the neighbours anyway): components 1, 3 of H(z-1) in
   // rows of parity (z-1)&1 and of E'(z-1) in rows of parity z&1 (stored at
   // the end of the previous plane); component 2 of both in registers.
-  cx<float> ep1 = zero, hp1 = act ? ldc(H, 1, cxx, cyy, z0 - 1) : zero;
+  cx<float> ep1 = zero, hp1 = act ? ldc(H, 1, z0 - 1) : zero;
   {
-    const cx<float> h0 = act ? ldc(H, 0, cxx, cyy, z0 - 1) : zero, h2 = act ? ldc(H, 2, cxx, cyy, z0 - 1) : zero;
+    const cx<float> h0 = act ? ldc(H, 0, z0 - 1) : zero, h2 = act ? ldc(H, 2, z0 - 1) : zero;
     xr[(z0 - 1) & 1][w][0][lane] = make_float2(h0.re, h0.im);
     xr[(z0 - 1) & 1][w][1][lane] = make_float2(h2.re, h2.im);
     xr[z0 & 1][w][2][lane] = make_float2(0.f, 0.f);
@@ -189,8 +194,8 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
   cx<float> en[3], hn_[3];  // E and H of the next plane, loaded one plane ahead
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    en[k] = act ? ldc(E, k, cxx, cyy, z0) : zero;
-    hn_[k] = act ? ldc(H, k, cxx, cyy, z0) : zero;
+    en[k] = act ? ldc(E, k, z0) : zero;
+    hn_[k] = act ? ldc(H, k, z0) : zero;
   }
   for (int z = z0; z <= z1 + 1; ++z) {
     const int buf = z & 1;
@@ -216,14 +221,14 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
       const int zn = z + 1 == g.nz + 1 ? 1 : z + 1;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        en[k] = ldc(E, k, cxx, cyy, zn);
-        hn_[k] = ldc(H, k, cxx, cyy, zn);
+        en[k] = ldc(E, k, zn);
+        hn_[k] = ldc(H, k, zn);
       }
     }
     ahead(z + 1);
     if (zimg && act) {
-      hzm0 = ldc(H, 0, cxx, cyy, 0);
-      hzm1 = ldc(H, 1, cxx, cyy, 0);
+      hzm0 = ldc(H, 0, 0);
+      hzm1 = ldc(H, 1, 0);
     } else {
       hzm0 = hp[0];
       hzm1 = hp[1];
@@ -285,9 +290,9 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
         for (int k = 0; k < 3; ++k) hn[k] = hp[k];
         h_update<float, UPML>(a, x, y, z - 1, ep, xp, yp, zp, hn, UPML ? U.b[z & 1][w][lane] : nullptr,
                               UPML ? U.cf[z % 3][1] : nullptr);
-        const long i = g.at(x, y, z - 1);
+        const IT i = (IT)(z - 1) * pl + ow;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) st<float>(A.h_new + k * g.comp + i, hn[k]);
+        for (int k = 0; k < 3; ++k) st<float>(A.h_new + ((IT)k * cp + i), hn[k]);
         if (x == g.nx) {
           const long q = g.at(0, y, z - 1);
 #pragma unroll
@@ -314,9 +319,9 @@ __device__ __forceinline__ void fused_column(const FusedArgs& A, FusedSmem& S, F
         }
       }
       if (own && z <= z1) {
-        const long i = g.at(x, y, z);
+        const IT i = (IT)z * pl + ow;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) st<float>(A.e_new + k * g.comp + i, enew[k]);
+        for (int k = 0; k < 3; ++k) st<float>(A.e_new + ((IT)k * cp + i), enew[k]);
         if (x == 1) {
           const long q = g.at(g.nx + 1, y, z);
 #pragma unroll
