@@ -489,6 +489,14 @@ __device__ __forceinline__ void acc_add(float4& a, float re, float im) {
   df_add(a.x, a.z, re);
   df_add(a.y, a.w, im);
 }
+// The leading part df_add leaves in hi, without the new lo (a flux read uses
+// the leading parts only and stores nothing): the same operations up to hi.
+__device__ __forceinline__ float df_add_hi(float hi, float lo, float p) {
+  const float s = __fadd_rn(hi, p);
+  const float bp = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+  return __fadd_rn(s, __fadd_rn(lo, e));
+}
 // v * 2^e2 as a double, formed from the float's bits with integer operations
 // only (exact for |e2| well inside the double range; GB300's FP64 pipe is
 // kept out of the flux epilogue).  A zero stays a signed zero, Inf and NaN
@@ -1080,7 +1088,14 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
                        : "memory");
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-          for (int q = 0; q < WS_FCH; ++q) acc_add(fa[q], __uint_as_float(t[2 * q]), __uint_as_float(t[2 * q + 1]));
+          for (int q = 0; q < WS_FCH; ++q) {
+            if (FLUX) {
+              fa[q].x = df_add_hi(fa[q].x, fa[q].z, __uint_as_float(t[2 * q]));
+              fa[q].y = df_add_hi(fa[q].y, fa[q].w, __uint_as_float(t[2 * q + 1]));
+            } else {
+              acc_add(fa[q], __uint_as_float(t[2 * q]), __uint_as_float(t[2 * q + 1]));
+            }
+          }
         }
         if (FLUX) {
           // lane 4 l + c holds component c of location 8 q4 + l.  Per
@@ -1097,7 +1112,8 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
           int sc[WS_FCH];
 #pragma unroll
           for (int q = 0; q < WS_FCH; ++q) {
-            const unsigned mb = max(__float_as_uint(fa[q].x) & 0x7fffffffu, __float_as_uint(fa[q].y) & 0x7fffffffu);
+            // the larger magnitude (non-negative floats order as their bits)
+            const unsigned mb = __float_as_uint(fmaxf(fabsf(fa[q].x), fabsf(fa[q].y)));
             sc[q] = min(126, max(-126, 127 - (int)(__reduce_max_sync(0xffffffffu, mb) >> 23)));
             const float f = __uint_as_float((unsigned)(127 + sc[q]) << 23);
             const float ax = fa[q].x * f, ay = fa[q].y * f;
