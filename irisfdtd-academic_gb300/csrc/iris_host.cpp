@@ -2,7 +2,9 @@
 // the physical constants, the output writers and the drop-in main program
 // (program IrisFDTD -> main -> driver) on top of the C ABI.
 #include <cerrno>
+#include <chrono>
 #include <cmath>
+#include <ctime>
 #include <complex>
 #include <cstdint>
 #include <cstdio>
@@ -577,6 +579,29 @@ int run_main(const std::string& dir, int precision, bool loop = false) {
     if (p.box1[i] != p.box2[i]) single = false;
   std::vector<double> J(6 * (size_t)p.nof);
   int nos = 1;
+  // the screen progress of code/driver.f90:339-354 (date, iteration, rate,
+  // time left, share done) every OUTPUT_TIME_STEP steps, printed at the next
+  // point where the host waits for the device anyway (an output step), with
+  // the rate measured over the steps since the last line; IRIS_QUIET=1
+  // silences it
+  const bool quiet = std::getenv("IRIS_QUIET") && std::string(std::getenv("IRIS_QUIET")) == "1";
+  auto last_t = std::chrono::steady_clock::now();
+  int last_it = 0;
+  auto progress = [&](int at) {
+    if (quiet || p.output_time_step <= 0 || at / p.output_time_step == last_it / p.output_time_step) return;
+    const auto now = std::chrono::steady_clock::now();
+    const double sec = std::chrono::duration<double>(now - last_t).count();
+    const double rate = sec > 0 ? (at - last_it) / sec : 0.0;
+    const std::time_t tt = std::time(nullptr);
+    char date[32];
+    std::strftime(date, sizeof date, "%d/%m/%Y-%H:%M:%S", std::localtime(&tt));
+    std::printf("  Date = %s\n  Iteration %d of %d\n  Iteration/second = %.3f\n  Finish in %.6f hours\n"
+                "  Completed %.3f %%\n",
+                date, at, p.texit, rate, rate > 0 ? (p.texit - at) / rate / 3600.0 : 0.0, 100.0 * at / p.texit);
+    std::fflush(stdout);
+    last_t = now;
+    last_it = at;
+  };
   // step in chunks that end at output steps
   int it = 1;
   while (it <= p.texit && rc == IRIS_OK) {
@@ -611,6 +636,7 @@ int run_main(const std::string& dir, int precision, bool loop = false) {
         if (rc == IRIS_OK) rc = iris_write_scatt(dir.c_str(), 1, it, p.nof, J.data());
       }
       ++nos;
+      progress(it);
     }
     ++it;
   }

@@ -77,11 +77,19 @@ def check_scatt(d, op, its, Jo, repeats=1):
     assert not os.path.exists(os.path.join(d, "2_scatt1.dat"))
 
 
-def test_run_input_example1_against_oracle(iris, example1_oracle, tmp_path):
+def test_run_input_example1_against_oracle(iris, example1_oracle, tmp_path, capfd):
     op, its, Jo, (lp, R, T) = example1_oracle
     shutil.copy(golden("example_1.inputFDTD.dat"), tmp_path / "inputFDTD.dat")
     iris.run_input(str(tmp_path), iris.FP64)
     check_scatt(str(tmp_path), op, its, Jo)
+    # the screen progress of code/driver.f90:339-354: one block each time a
+    # multiple of OUTPUT_TIME_STEP (1000 here) was passed, at the output steps
+    out = capfd.readouterr().out.splitlines()
+    steps = [int(ln.split()[1]) for ln in out if ln.strip().startswith("Iteration ") and " of %d" % op.texit in ln]
+    assert len(steps) == op.texit // op.output_time_step
+    assert steps == sorted(steps) and all(s in its for s in steps)
+    assert sum(1 for ln in out if ln.strip().startswith("Iteration/second = ")) == len(steps)
+    assert sum(1 for ln in out if ln.strip().startswith("Completed ")) == len(steps)
     # log.dat: the step size and step count the reference quotes for example_1
     pins = json.load(open(golden("pins.json")))
     log = open(tmp_path / "log.dat").read().splitlines()

@@ -297,12 +297,19 @@ def test_fp32_mode_tr_error(iris, oracle):
     assert err <= 1e-4, err
 
 
-def test_step_is_deterministic(iris, oracle, tmp_path):
-    op = small_case(oracle, tmp_path, nx=8, ny=6, nz=48, nof=6)
+@pytest.mark.parametrize("precision,shape", [(0, (8, 6, 48)), (1, (70, 40, 48))])
+def test_step_is_deterministic(iris, oracle, tmp_path, precision, shape):
+    """Two runs agree bit for bit: FP64 on a small grid (the persistent
+    kernel), and FP32 above the persistent limit (the fused pass, the
+    tensor-core DFT commit and flux read): no atomics and no order-dependent
+    reduction anywhere on the path."""
+    nx, ny, nz = shape
+    op = small_case(oracle, tmp_path, nx=nx, ny=ny, nz=nz, nof=6)
     res = []
     for _ in range(2):
-        eng = iris.Engine(engine_params_from_oracle(iris, op), op.fw)
+        eng = iris.Engine(engine_params_from_oracle(iris, op, precision=precision), op.fw, dft_block=32)
         eng.step(1, 120)
-        res.append((eng.get_field(iris.E), eng.flux(0)))
+        res.append((eng.get_field(iris.E), eng.get_field(iris.H), eng.flux(0), eng.get_fdata(0, 1)))
         eng.close()
-    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+    for a, b in zip(*res):
+        assert np.array_equal(a, b)
