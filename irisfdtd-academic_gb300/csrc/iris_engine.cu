@@ -773,18 +773,21 @@ constexpr size_t WS_SMEM = WS_STAGES * TC_STAGE;
 // Per-mode layout.  A sub-partition holds a quarter of the register file, and
 // the warps of a CTA are dealt to the four in turn, so W warps of R registers
 // fit when ceil(W / 4) x 32 x R <= 16384.  Commit mode (the A stream is the
-// whole sample ring): four producer warps, one A row a thread, two chunks
-// ahead in registers (one chunk ahead left 8 KB of sample loads in flight per
-// SM and the producers latency-bound); 21 warps, 80 registers.  Flux mode
+// whole sample ring): eight producer warps, each thread half a row (4 of a
+// chunk's 8 samples), three chunks ahead in registers (12 KB of sample loads
+// in flight per SM per chunk slot; one chunk ahead on two warps left 8 KB in
+// flight and the producers latency-bound, two ahead on four warps measured
+// 9 % slower than this, four ahead 7 % slower); 25 warps, 72 registers.  Flux mode
 // (a few buffered samples, the accumulators dominate): two producer warps,
 // two rows a thread, one chunk ahead; 19 warps, 96 registers for the
 // epilogue's products (twelve epilogue warps streaming two chunks ahead, 15
 // warps at 128 registers, measured 1.13-1.17 times slower: the flux epilogue
 // is bound by instruction issue more than by loads in flight).
 template <bool FLUX> struct WsCfg {
-  static constexpr int PROD = FLUX ? 64 : 128;  // producer threads
-  static constexpr int RPT = TC_M / PROD;       // A rows per producer thread
-  static constexpr int AHEAD = FLUX ? 1 : 2;    // chunks of samples loaded ahead
+  static constexpr int PROD = FLUX ? 64 : 256;           // producer threads
+  static constexpr int RPT = PROD < TC_M ? TC_M / PROD : 1;  // A rows per producer thread
+  static constexpr int SPT = 8 * TC_M / (PROD * RPT);   // samples of a chunk per thread and row
+  static constexpr int AHEAD = FLUX ? 1 : 3;             // chunks of samples loaded ahead
   static constexpr int THREADS = PROD + WS_EPI + 32;
   static constexpr int MMA_WARP = (PROD + WS_EPI) / 32;
 };
@@ -893,9 +896,12 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
 
   if (tid < WS_PROD) {
     // ---- producers: one flat sequence of (item, chunk) pairs; a thread takes
-    // rows tid + h WS_PROD (h < RPT), the samples of the next AHEAD chunks in
-    // registers while a chunk is split into its stage
+    // RPT rows (row0 + h WS_PROD) and SPT of a chunk's 8 samples from q0, the
+    // samples of the next AHEAD chunks in registers while a chunk is split
+    // into its stage
     if (mma) {
+      constexpr int SPT = WsCfg<FLUX>::SPT, AH = WsCfg<FLUX>::AHEAD;
+      const int row0 = tid % TC_M, q0 = (tid / TC_M) * SPT;
       int armed[WS_STAGES] = {};  // fills issued per stage (thread 0: the last one is drained at exit)
       struct Cur {
         long j;
@@ -916,7 +922,7 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
           const WsRow<FLUX> r = ws_item<FLUX>(A, item, x.g);
 #pragma unroll
           for (int h = 0; h < RPT; ++h) {
-            x.rp[h] = ws_point<FLUX>(r, tid + h * WS_PROD);
+            x.rp[h] = ws_point<FLUX>(r, row0 + h * WS_PROD);
             if (!bc_ok(x.rp[h] < A.P, BC_DFT_SAMPLE, x.rp[h])) x.rp[h] = -1;
           }
           x.ok = true;
@@ -931,24 +937,28 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
         }
         return at(x.j + 1, 0);
       };
-      constexpr int NV = 8 * RPT;  // samples a thread holds per chunk
+      constexpr int NV = SPT * RPT;  // samples a thread holds per chunk
       auto load = [&](const Cur& x, float2* dst) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int k = x.c * (TC_KC / 2) + q;
+        for (int q = 0; q < SPT; ++q) {
+          const int k = x.c * (TC_KC / 2) + q0 + q;
           const bool kk = x.ok && k < A.nk;
 #pragma unroll
           for (int h = 0; h < RPT; ++h)
-            dst[8 * h + q] = (kk && x.rp[h] >= 0) ? A.S[(long)k * A.P + x.rp[h]] : make_float2(0.f, 0.f);
+            dst[SPT * h + q] = (kk && x.rp[h] >= 0) ? A.S[(long)k * A.P + x.rp[h]] : make_float2(0.f, 0.f);
         }
       };
-      Cur c0 = at(0, 0), c1 = next(c0), c2 = WsCfg<FLUX>::AHEAD > 1 ? next(c1) : c1;
-      float2 v0[NV], v1[NV], v2[WsCfg<FLUX>::AHEAD > 1 ? NV : 1];
-      load(c0, v0);
-      if constexpr (WsCfg<FLUX>::AHEAD > 1) load(c1, v1);
-      for (long n = 0; c0.ok && !stopped(); ++n) {
-        if constexpr (WsCfg<FLUX>::AHEAD > 1) load(c2, v2);
-        else load(c1, v1);
+      // a register ring of AHEAD + 1 chunks: v[0] is split while v[1..AHEAD]
+      // are in flight (constant indices after unrolling)
+      Cur cu[AH + 1];
+      float2 v[AH + 1][NV];
+      cu[0] = at(0, 0);
+#pragma unroll
+      for (int d = 1; d <= AH; ++d) cu[d] = next(cu[d - 1]);
+#pragma unroll
+      for (int d = 0; d < AH; ++d) load(cu[d], v[d]);
+      for (long n = 0; cu[0].ok && !stopped(); ++n) {
+        load(cu[AH], v[AH]);
         const int s = (int)(n % WS_STAGES);
         const long u = n / WS_STAGES;
         if (u > 0 && !mbar_wait(&empty[s], (unsigned)((u - 1) & 1), STREAM_WAIT_CYCLES)) {
@@ -957,9 +967,9 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
         }
         unsigned char* st = smem + s * TC_STAGE;
         if (tid == 0) {
-          const int ncol = ((2 * min(TC_NW, A.nof - c0.g * TC_NW) + 15) / 16) * 16;
+          const int ncol = ((2 * min(TC_NW, A.nof - cu[0].g * TC_NW) + 15) / 16) * 16;
           const unsigned nb = (unsigned)(ncol * TC_KC * 4);
-          const float* src = A.Bt + ((long)(c0.g * nch + c0.c) * 2) * per;
+          const float* src = A.Bt + ((long)(cu[0].g * nch + cu[0].c) * 2) * per;
           mbar_expect_tx_only(&full[s], 2 * nb);
           fence_proxy_async();
           bulk_g2s(st + 2 * TC_A_BYTES, src, nb, &full[s]);
@@ -970,27 +980,26 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
         float* Al = (float*)(st + TC_A_BYTES);
 #pragma unroll
         for (int h = 0; h < RPT; ++h) {
-          const int row = tid + h * WS_PROD;
+          const int row = row0 + h * WS_PROD;
 #pragma unroll
-          for (int m = 0; m < 4; ++m) {
-            const float2 a = v0[8 * h + 2 * m], bq = v0[8 * h + 2 * m + 1];
+          for (int m = 0; m < SPT / 2; ++m) {
+            const float2 a = v[0][SPT * h + 2 * m], bq = v[0][SPT * h + 2 * m + 1];
             const float4 x = make_float4(a.x, a.y, bq.x, bq.y);
             const float4 hv = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
-            *(float4*)(Ah + tc_off(row, 4 * m)) = hv;
-            *(float4*)(Al + tc_off(row, 4 * m)) = make_float4(x.x - hv.x, x.y - hv.y, x.z - hv.z, x.w - hv.w);
+            const int col = 2 * q0 + 4 * m;  // K column of sample q0 + 2 m
+            *(float4*)(Ah + tc_off(row, col)) = hv;
+            *(float4*)(Al + tc_off(row, col)) = make_float4(x.x - hv.x, x.y - hv.y, x.z - hv.z, x.w - hv.w);
           }
         }
         fence_proxy_async();  // the generic-proxy writes of A before the tensor core reads them
         mbar_arrive(&full[s]);
 #pragma unroll
-        for (int q = 0; q < NV; ++q) v0[q] = v1[q];
-        if constexpr (WsCfg<FLUX>::AHEAD > 1) {
+        for (int d = 0; d < AH; ++d) {
 #pragma unroll
-          for (int q = 0; q < NV; ++q) v1[q] = v2[q];
+          for (int q = 0; q < NV; ++q) v[d][q] = v[d + 1][q];
+          cu[d] = cu[d + 1];
         }
-        c0 = c1;
-        c1 = WsCfg<FLUX>::AHEAD > 1 ? c2 : next(c1);
-        if constexpr (WsCfg<FLUX>::AHEAD > 1) c2 = next(c2);
+        cu[AH] = next(cu[AH - 1]);
       }
       if (tid == 0)
         // copies issued into a stage whose MMAs never ran must land before the CTA exits
@@ -1153,7 +1162,7 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_NMAX) : "memory");
 }
 
-__global__ void __maxnreg__(80) k_dft_ws_commit(WsArgs A) { dft_ws<false>(A); }
+__global__ void __maxnreg__(72) k_dft_ws_commit(WsArgs A) { dft_ws<false>(A); }
 __global__ void __launch_bounds__(WsCfg<true>::THREADS, 1) k_dft_ws_flux(WsArgs A) { dft_ws<true>(A); }
 
 // J[f][iw] = scale * sign * (sum of face f's partials, four per tile, in
