@@ -768,7 +768,7 @@ __device__ __forceinline__ long face_comp(const FluxFace& F, int c) {
 // mode, 5 in flux mode) and stops; the others stop at their next wait; the
 // CTA waits (bounded) for its copies and MMAs before it frees its TMEM.
 
-constexpr int WS_STAGES = 3, WS_EPI = 512, WS_FCH = 4;
+constexpr int WS_STAGES = 3, WS_FCH = 4;
 constexpr size_t WS_SMEM = WS_STAGES * TC_STAGE;
 // Per-mode layout.  A sub-partition holds a quarter of the register file, and
 // the warps of a CTA are dealt to the four in turn, so W warps of R registers
@@ -788,8 +788,11 @@ template <bool FLUX> struct WsCfg {
   static constexpr int RPT = PROD < TC_M ? TC_M / PROD : 1;  // A rows per producer thread
   static constexpr int SPT = 8 * TC_M / (PROD * RPT);   // samples of a chunk per thread and row
   static constexpr int AHEAD = FLUX ? 1 : 3;             // chunks of samples loaded ahead
-  static constexpr int THREADS = PROD + WS_EPI + 32;
-  static constexpr int MMA_WARP = (PROD + WS_EPI) / 32;
+  static constexpr int EPI = FLUX ? 512 : 384;           // epilogue threads: EPI / 128 groups of four warps
+  static constexpr int NGRP = EPI / 128;
+  static constexpr int EAHEAD = FLUX ? 1 : 2;            // accumulator chunks loaded ahead
+  static constexpr int THREADS = PROD + EPI + 32;
+  static constexpr int MMA_WARP = (PROD + EPI) / 32;
 };
 
 struct WsArgs {
@@ -856,6 +859,7 @@ template <bool FLUX> __device__ __forceinline__ long ws_point(const WsRow<FLUX>&
 
 template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
   constexpr int WS_PROD = WsCfg<FLUX>::PROD, RPT = WsCfg<FLUX>::RPT, WS_MMA_WARP = WsCfg<FLUX>::MMA_WARP;
+  constexpr int WS_EPI = WsCfg<FLUX>::EPI, NG = WsCfg<FLUX>::NGRP, EA = WsCfg<FLUX>::EAHEAD;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint64_t full[WS_STAGES], empty[WS_STAGES], accf[2], acce[2], fin;
   __shared__ uint32_t taddr_s;
@@ -1056,8 +1060,8 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
       mbar_wait(&fin, 0, STREAM_WAIT_CYCLES);
     }
   } else {
-    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4); group (w - 2) / 4
-    // takes the 4-frequency chunks of its index mod 4
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4); group (w - PROD/32) / 4
+    // takes the 4-frequency chunks of its index mod NG
     const int q4 = warp & 3, grp = (warp - WS_PROD / 32) >> 2;
     long j = 0;
     for (long item = blockIdx.x; item < A.nitems; item += gridDim.x, ++j) {
@@ -1076,8 +1080,9 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
           dst[q] = (ep >= 0 && WS_FCH * ch + q < nw) ? fdg[(long)(WS_FCH * ch + q) * A.P + ep]
                                                      : make_float4(0.f, 0.f, 0.f, 0.f);
       };
-      float4 fa[WS_FCH], fb[WS_FCH];
+      float4 fa[WS_FCH], fb[WS_FCH], fc[EA > 1 ? WS_FCH : 1];
       if (grp < nchk) load_fd(grp, fa);
+      if (EA > 1 && grp + NG < nchk) load_fd(grp + NG, fb);
       if (mma) {
         const bool ok = __all_sync(0xffffffffu, mbar_wait(&accf[b], (unsigned)(vv & 1), STREAM_WAIT_CYCLES));
         if (!ok) {
@@ -1086,8 +1091,12 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       }
-      for (int ch = grp; ch < nchk; ch += 4) {
-        if (ch + 4 < nchk) load_fd(ch + 4, fb);
+      for (int ch = grp; ch < nchk; ch += NG) {
+        if constexpr (EA > 1) {
+          if (ch + 2 * NG < nchk) load_fd(ch + 2 * NG, fc);
+        } else {
+          if (ch + NG < nchk) load_fd(ch + NG, fb);
+        }
         if (mma) {
           uint32_t t[2 * WS_FCH];
           const uint32_t ta = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(b * TC_NMAX + 2 * WS_FCH * ch);
@@ -1149,6 +1158,10 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
         }
 #pragma unroll
         for (int q = 0; q < WS_FCH; ++q) fa[q] = fb[q];
+        if constexpr (EA > 1) {
+#pragma unroll
+          for (int q = 0; q < WS_FCH; ++q) fb[q] = fc[q];
+        }
       }
       if (mma) {
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -1162,7 +1175,7 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_NMAX) : "memory");
 }
 
-__global__ void __maxnreg__(72) k_dft_ws_commit(WsArgs A) { dft_ws<false>(A); }
+__global__ void __maxnreg__(80) k_dft_ws_commit(WsArgs A) { dft_ws<false>(A); }
 __global__ void __launch_bounds__(WsCfg<true>::THREADS, 1) k_dft_ws_flux(WsArgs A) { dft_ws<true>(A); }
 
 // J[f][iw] = scale * sign * (sum of face f's partials, four per tile, in
