@@ -774,10 +774,12 @@ constexpr size_t WS_SMEM = WS_STAGES * TC_STAGE;
 // the warps of a CTA are dealt to the four in turn, so W warps of R registers
 // fit when ceil(W / 4) x 32 x R <= 16384.  Commit mode (the A stream is the
 // whole sample ring): eight producer warps, each thread half a row (4 of a
-// chunk's 8 samples), three chunks ahead in registers (12 KB of sample loads
-// in flight per SM per chunk slot; one chunk ahead on two warps left 8 KB in
-// flight and the producers latency-bound, two ahead on four warps measured
-// 9 % slower than this, four ahead 7 % slower); 25 warps, 72 registers.  Flux mode
+// chunk's 8 samples), three chunks ahead in registers (one chunk ahead on two
+// warps left 8 KB of sample loads in flight per SM and the producers
+// latency-bound; two ahead on four warps measured 9 % slower than this, four
+// ahead 3-7 % slower), and twelve epilogue warps streaming the accumulators
+// two chunks ahead (4 % faster than sixteen one chunk ahead); 21 warps, 80
+// registers.  Flux mode
 // (a few buffered samples, the accumulators dominate): two producer warps,
 // two rows a thread, one chunk ahead; 19 warps, 96 registers for the
 // epilogue's products (twelve epilogue warps streaming two chunks ahead, 15
