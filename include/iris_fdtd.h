@@ -164,7 +164,9 @@ typedef struct iris_params {
 /* small grids: one cooperative launch runs a span of whole steps (E, H,
  * TF/SF, DFT sample) with grid-wide barriers between the passes; the split
  * passes' arithmetic, so the same results bit for bit.  The default for
- * grids of at most IRIS_PERSISTENT_MAX_CELLS cells in both precisions     */
+ * grids of at most IRIS_PERSISTENT_MAX_CELLS cells in both precisions;
+ * asked for explicitly, grids of fewer than 2^31 / 3 cells on a device
+ * with cooperative launches (else iris_create returns IRIS_EINVAL)       */
 #define IRIS_STENCIL_PERSISTENT 4
 #define IRIS_PERSISTENT_MAX_CELLS 65536
 
