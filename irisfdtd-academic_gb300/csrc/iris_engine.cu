@@ -735,26 +735,27 @@ __device__ __forceinline__ long face_comp(const FluxFace& F, int c) {
 // Warp-specialised persistent DFT block kernel (FP32 mode, tensor cores).
 //
 // One CTA per SM walks work items (a row tile and a frequency group) with
-// three roles that overlap each other through mbarriers:
-//   * producers (warps 0-1, two A rows a thread): the samples of a chunk of
-//     8 samples into the TF32 hi/lo A operands of a stage (plain loads, one
-//     chunk ahead in registers), and one thread bulk-copies the chunk's B
-//     operands into the same stage; WS_STAGES stages in a ring.  Shared
-//     memory stays at the three stages: what more it takes comes out of the
-//     L1, which holds the loads in flight (a raw sample ring in shared memory
-//     fed by asynchronous copies left 20 KB of L1 and made both modes 1.3 to
-//     1.8 times slower);
-//   * the MMA thread (warp 18): three tcgen05.mma kind::tf32 per 8 K columns
-//     into one of two TMEM accumulators (256 columns each), each stage freed
-//     by a commit when its MMAs are done, each finished item signalled by a
-//     commit on that accumulator;
-//   * epilogue warps (2-17; warp w reads TMEM lanes 32 (w % 4), the four
-//     warps of a group cover the four lane quarters, group k takes the
-//     4-frequency chunks k, k + 4, ...): drain an accumulator while the MMAs
-//     of the next item fill the other, streaming the accumulators one chunk
-//     ahead in registers.  Sixteen warps, because the epilogue's work per
-//     value (the double-float update, the products and their shuffles) needs
-//     more warps in flight than its memory stream alone would.
+// three roles that overlap each other through mbarriers (the per-mode warp
+// counts and prefetch depths are WsCfg's, below):
+//   * producer warps: the samples of a chunk of 8 samples into the TF32
+//     hi/lo A operands of a stage (plain loads, held some chunks ahead in
+//     registers), and one thread bulk-copies the chunk's B operands into the
+//     same stage; WS_STAGES stages in a ring.  Shared memory stays at the
+//     three stages: what more it takes comes out of the L1, which holds the
+//     loads in flight (a raw sample ring in shared memory fed by
+//     asynchronous copies left 20 KB of L1 and made both modes 1.3 to 1.8
+//     times slower);
+//   * the MMA thread (the last warp): three tcgen05.mma kind::tf32 per 8 K
+//     columns into one of two TMEM accumulators (256 columns each), each
+//     stage freed by a commit when its MMAs are done, each finished item
+//     signalled by a commit on that accumulator;
+//   * epilogue warps (warp w reads TMEM lanes 32 (w % 4), the four warps of a
+//     group cover the four lane quarters, group k of NG takes the 4-frequency
+//     chunks k, k + NG, ...): drain an accumulator while the MMAs of the next
+//     item fill the other, streaming the accumulators ahead in registers.
+//     Many warps, because the epilogue's work per value (the double-float
+//     update, the products and their shuffles) needs more warps in flight
+//     than its memory stream alone would.
 // Commit mode: rows are 128 consecutive sample points; the epilogue adds the
 // partial sums into fdata (read once, written once).
 // Flux mode: rows are the four flux components of 32 locations of one face,
