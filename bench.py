@@ -400,7 +400,9 @@ def run_engine(args, rank, world, local):
         "e2e": {"value": round(world * cells * K / t_e2e / 1e9, 3), "unit": "Gcell/s",
                 "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(d2h / K, 1),
                 "what": ("iris_create + %s + %d steps + iris_flux to host, in a process whose CUDA context was "
-                         "started by a small engine before the clock" % (mat_what, K))},
+                         "started by a small engine before the clock; the DFT accumulators are first written "
+                         "by the run's first commit (no zeroing pass), and a flux read before that commit "
+                         "reads only the buffered samples" % (mat_what, K))},
         "gpu_launches": int(launches),
         "kernels_ms_per_step": {k: round(v / K, 4) for k, v in kms.items()},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",

@@ -454,6 +454,7 @@ template <typename T> int adj_forward(iris_adjoint* J, int nsteps) {
   int rc = zero_state(F, J->fbytes, J->sbytes);
   if (rc) return rc;
   CK(cudaMemsetAsync(F->fd, 0, (size_t)F->P * F->p.nof * 16, F->st));
+  F->fd_zero = false;
   F->nslot = 0;
   CK(cudaEventRecord(J->ev[0], F->st));
   for (int it = 1; it <= nsteps; ++it) {

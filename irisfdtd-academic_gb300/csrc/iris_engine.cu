@@ -804,6 +804,7 @@ struct WsArgs {
   int nk;
   const float* Bt;  // B operands of the nk samples (k_twiddle_tc)
   float4* fd;       // double-float accumulators [nof][P]
+  int fd_zero;      // they hold no sum yet: taken as zeros, not read
   int nof, ngroups;
   long nitems;      // row tiles x frequency groups
   // flux mode
@@ -1080,8 +1081,8 @@ template <bool FLUX> __device__ __forceinline__ void dft_ws(const WsArgs& A) {
       auto load_fd = [&](int ch, float4* dst) {
 #pragma unroll
         for (int q = 0; q < WS_FCH; ++q)
-          dst[q] = (ep >= 0 && WS_FCH * ch + q < nw) ? fdg[(long)(WS_FCH * ch + q) * A.P + ep]
-                                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+          dst[q] = (ep >= 0 && !A.fd_zero && WS_FCH * ch + q < nw) ? fdg[(long)(WS_FCH * ch + q) * A.P + ep]
+                                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
       };
       float4 fa[WS_FCH], fb[WS_FCH], fc[EA > 1 ? WS_FCH : 1];
       if (grp < nchk) load_fd(grp, fa);
@@ -2345,6 +2346,8 @@ void dft_flush(iris_engine* E) {
   if (E->nslot == 0) return;
   KTimer tm(E, IRIS_KC_DFT);
   const int nk = E->nslot;
+  // the CUDA-core blocks read what they add to (on a failure the samples stay buffered)
+  if (!E->dft_tc && fd_materialise(E)) return;
   if (E->prec == IRIS_FP64) {
     const int nwc = (E->p.nof + DFT64_WC - 1) / DFT64_WC;
     const long nblk = (E->P + 127) / 128;
@@ -2362,11 +2365,13 @@ void dft_flush(iris_engine* E) {
     A.nk = nk;
     A.Bt = E->d_wtc;
     A.fd = (float4*)E->fd;
+    A.fd_zero = E->fd_zero;
     A.nof = E->p.nof;
     A.ngroups = ng;
     A.nitems = (E->P + TC_M - 1) / TC_M * ng;
     A.err = E->d_err;
     k_dft_ws_commit<<<(unsigned)std::min<long>(A.nitems, E->ws_blocks), WsCfg<false>::THREADS, WS_SMEM, E->st>>>(A);
+    E->fd_zero = false;  // every accumulator of every frequency has been written
   } else {
     const int nt = nk * E->p.nof;
     k_twiddle<<<(nt + 255) / 256, 256, 0, E->st>>>(E->d_tk, 0, 0, nk, E->d_fw, E->p.nof, E->p.dt, E->d_wt);
@@ -2376,6 +2381,13 @@ void dft_flush(iris_engine* E) {
                                                         (float4*)E->fd);
   }
   E->nslot = 0;
+}
+
+int fd_materialise(iris_engine* E) {
+  if (!E->fd_zero) return IRIS_OK;
+  CK(cudaMemsetAsync(E->fd, 0, (size_t)E->P * E->p.nof * 16, E->st));
+  E->fd_zero = false;
+  return IRIS_OK;
 }
 
 // A whole DFT block of steps from it on can be replayed from a graph: every
@@ -2403,6 +2415,8 @@ int graph_block(iris_engine* E, int it, const std::function<void()>& record) {
   }
   if (E->dev_it != it) k_set_int<<<1, 1, 0, E->st>>>(E->d_it, it);
   if (!E->gexec) {
+    // the captured commit is replayed for every block: it must read the sums
+    if (int rc = fd_materialise(E)) return rc;
     cudaGraph_t gr = nullptr;
     CK(cudaStreamBeginCapture(E->st, cudaStreamCaptureModeRelaxed));
     record();
@@ -2444,7 +2458,7 @@ int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces) {
   E->K = std::max(1, K);
   E->nslot = 0;
   CK(cudaMalloc(&E->fd, std::max<size_t>(fd_bytes, 16)));
-  CK(cudaMemsetAsync(E->fd, 0, std::max<size_t>(fd_bytes, 16), E->st));
+  E->fd_zero = true;  // zeroed when first read as it lies, never for the tensor-core path
   CK(cudaMalloc(&E->S, (size_t)E->K * slot_bytes));
   CK(cudaMalloc(&E->d_tk, sizeof(int) * E->K));
   CK(cudaMalloc(&E->d_fw, sizeof(double) * p.nof));
@@ -2751,6 +2765,7 @@ int iris::read_flux(iris_engine* E, int set, double* J) {
       A.nk = nk;
       A.Bt = E->d_wtc;
       A.fd = (float4*)E->fd;
+      A.fd_zero = E->fd_zero;
       A.nof = p.nof;
       A.ngroups = ng;
       A.nitems = (long)ft.start[6] * ng;
@@ -2763,6 +2778,7 @@ int iris::read_flux(iris_engine* E, int set, double* J) {
     k_flux_sum<<<dim3(p.nof, 6), 256, 0, E->st>>>(E->d_part, ft, E->d_faces + 6 * set, p.nof, scale, E->d_J);
   } else {
     dft_flush(E);
+    if (int rc = fd_materialise(E)) return rc;  // no block committed yet
     KTimer tm(E, IRIS_KC_FLUX);
     if (E->prec == IRIS_FP64)
       k_flux<double2><<<dim3(p.nof, 6), 256, 0, E->st>>>((const double2*)E->fd, E->P, E->d_faces + 6 * set, p.nof,
@@ -3128,6 +3144,7 @@ int iris_get_fdata(iris_engine* E, int box, int j, double* re, double* im, long*
   if (!re || n == 0) return IRIS_OK;
   if (!im) return fail(IRIS_EINVAL, "null buffer");
   dft_flush(E);
+  if (int rc = fd_materialise(E)) return rc;
   const int nof = E->p.nof;
   // 16 bytes per value: a double2, or in FP32 mode the double-float pairs
   // (re_hi, im_hi, re_lo, im_lo) whose sums are exact in FP64

@@ -72,6 +72,12 @@ struct iris_engine {
   // accumulators [nof][P], 16 bytes a value: double2 in FP64 mode, the
   // double-float float4 (re_hi, im_hi, re_lo, im_lo) in FP32 mode
   void* fd = nullptr;
+  // the accumulators hold no sum yet (no block committed since they were
+  // allocated): their memory is left unwritten, the tensor-core commit
+  // writes its first block without reading them and the tensor-core flux
+  // read takes them as zeros; every other reader zeroes them first
+  // (fd_materialise)
+  bool fd_zero = false;
   float2* d_wt = nullptr;
   double2* d_wt64 = nullptr;  // FP64 mode twiddles of one block
   bool dft_tc = false;     // FP32 block accumulation on the tensor cores
@@ -205,6 +211,9 @@ void free_engine(iris_engine* E);
 int alloc_dft(iris_engine* E, const FluxFace* faces, int nfaces);
 // Accumulate the sample ring into fdata (one block kernel pass).
 void dft_flush(iris_engine* E);
+// Zero the accumulators in memory if they hold no sum yet (fd_zero), before
+// a kernel or copy that reads them as they lie.
+int fd_materialise(iris_engine* E);
 // Flux of face set `set` (6 FluxFace from d_faces + 6 set) into J[6][nof].
 int read_flux(iris_engine* E, int set, double* J);
 // One step (the fused pass or the split E and H passes, as the engine

@@ -104,3 +104,42 @@ def test_flux_read_leaves_buffer_and_equals_commit(iris, oracle, tmp_path, case,
     e.step(steps + 1, 10)
     c.step(steps + 1, 10)
     assert rel_err(e.flux(0), c.flux(0)) <= 1e-5
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_unwritten_accumulators_equal_zeroed(iris, oracle, tmp_path, case):
+    """Until the first block is committed the accumulators hold no sum: the
+    engine leaves their memory unwritten, the first tensor-core commit writes
+    without reading and a flux read before it takes them as zeros.  An engine
+    whose accumulators were zeroed in memory first (iris_get_fdata reads them
+    as they lie, so it zeroes them) must give the same bits at every stage,
+    and so must one that replays its blocks from a CUDA graph (the capture
+    zeroes them, since the captured commit reads)."""
+    name, spec, nof, _ = case
+    block = 32
+    w, op = make(oracle, tmp_path, spec, nof, 3 * block + 20)
+    eps = cfg.spheres_material(w, seed=2)
+    p = engine_params_from_oracle(iris, op, precision=1, ak=(0.3 + 0j, 0j, 0j))
+    lazy = iris.Engine(p, op.fw, dft_block=block, dft_kernel=iris.DFT_KERNEL_TENSOR)
+    zeroed = iris.Engine(p, op.fw, dft_block=block, dft_kernel=iris.DFT_KERNEL_TENSOR)
+    graphed = iris.Engine(p, op.fw, dft_block=block, dft_kernel=iris.DFT_KERNEL_TENSOR, graph=True)
+    assert not np.any(zeroed.get_fdata(0, 3))
+    engines = (lazy, zeroed, graphed)
+    for e in engines:
+        e.set_material(eps)
+        e.step(1, 13)
+    assert lazy.info()["dft_buffered"] > 0
+    J = [e.flux(0) for e in engines]  # before any commit
+    assert np.all(np.isfinite(J[0])) and np.any(J[0])
+    assert np.array_equal(J[0], J[1]) and np.array_equal(J[0], J[2])
+    for e in engines:
+        e.dft_commit()  # the first commit: written without a read on the lazy engine
+    for j in (1, 2, 3):
+        F = [e.get_fdata(0, j) for e in engines]
+        assert np.array_equal(F[0], F[1]) and np.array_equal(F[0], F[2]), j
+    for e in engines:
+        e.step(14, 2 * block + 6)  # whole blocks on: committed (and replayed from the graph) on top of the first
+    J = [e.flux(0) for e in engines]
+    assert np.array_equal(J[0], J[1]) and np.array_equal(J[0], J[2])
+    for e in engines:
+        e.close()
