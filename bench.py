@@ -729,8 +729,9 @@ def tr_error(iris, p, fw, eps, local):
             "fp32_gcells": round(cells * p.texit / (ms32 * 1e-3) / 1e9, 3),
             "device_ms": {"fp64": round(ms64, 1), "fp32": round(ms32, 1)},
             "wall_s": {"fp64": round(s64, 2), "fp32": round(s32, 2)},
-            "note": ("FP32 (fused pass, tensor-core DFT) against FP64 over the full run, per spectrum; its state "
-                     "(75 MB) lives in the 129 MB L2, so no HBM roofline applies")}
+            "note": ("FP32 (tensor-core DFT) against FP64 over the full run, per spectrum, both on the default "
+                     "stencil (the persistent whole-step kernel on a grid this size; spectra bitwise those of the "
+                     "split passes); its state (75 MB) lives in the 129 MB L2, so no HBM roofline applies")}
 
 
 def guarded(fn, *a, **k):

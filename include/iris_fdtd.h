@@ -149,7 +149,9 @@ typedef struct iris_params {
 
 /* ---- stencil variants (iris_params.stencil) -------------------------- */
 /* default: the persistent kernel on small grids, else the fused pass in
- * IRIS_FP32 (the faster variant on GB300) and the split passes in
+ * IRIS_FP32 (the faster variant on GB300; the split passes instead on
+ * grids whose x-y plane would leave more than half of the fused pass's
+ * 32 x 16 tile threads idle, e.g. 4 cells in y) and the split passes in
  * IRIS_FP64                                                               */
 #define IRIS_STENCIL_DEFAULT 0
 /* separate in-place E and H passes (18 complex values per cell per step)  */
@@ -164,11 +166,15 @@ typedef struct iris_params {
 /* small grids: one cooperative launch runs a span of whole steps (E, H,
  * TF/SF, DFT sample) with grid-wide barriers between the passes; the split
  * passes' arithmetic, so the same results bit for bit.  The default for
- * grids of at most IRIS_PERSISTENT_MAX_CELLS cells in both precisions;
- * asked for explicitly, grids of fewer than 2^31 / 3 cells on a device
- * with cooperative launches (else iris_create returns IRIS_EINVAL)       */
+ * IRIS_FP64 grids of at most IRIS_PERSISTENT_MAX_CELLS cells and IRIS_FP32
+ * grids of at most IRIS_PERSISTENT_MAX_CELLS_FP32 cells (up to those sizes
+ * it steps faster than the split passes, and the split passes than the
+ * fused pass); asked for explicitly, grids of fewer than
+ * 2^31 / 3 cells on a device with cooperative launches (else iris_create
+ * returns IRIS_EINVAL)                                                    */
 #define IRIS_STENCIL_PERSISTENT 4
-#define IRIS_PERSISTENT_MAX_CELLS 65536
+#define IRIS_PERSISTENT_MAX_CELLS 1048576
+#define IRIS_PERSISTENT_MAX_CELLS_FP32 8388608
 
 typedef struct iris_engine iris_engine;
 

@@ -35,7 +35,8 @@ from .native import IrisError, IrisParams, build, check, lib
 
 FP64, FP32 = 0, 1
 STENCIL_DEFAULT, STENCIL_SPLIT, STENCIL_FUSED, STENCIL_STREAM, STENCIL_PERSISTENT = 0, 1, 2, 3, 4
-PERSISTENT_MAX_CELLS = 65536
+PERSISTENT_MAX_CELLS = 1048576  # IRIS_PERSISTENT_MAX_CELLS: the persistent kernel's default limit in FP64
+PERSISTENT_MAX_CELLS_FP32 = 8388608  # IRIS_PERSISTENT_MAX_CELLS_FP32: the same in FP32
 DFT_KERNEL_AUTO, DFT_KERNEL_CUDA, DFT_KERNEL_TENSOR = 0, 1, 2
 E, H = 0, 1
 OP_E, OP_H, OP_TFSF, OP_DFT, OP_WAIT_CHECK, OP_BARRIER_CHECK = 1, 2, 3, 4, 5, 6

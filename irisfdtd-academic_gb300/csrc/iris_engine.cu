@@ -1311,7 +1311,10 @@ template <typename T> struct TinyArgs {
   int* err;
 };
 
-constexpr int TINY_THREADS = 128;
+// Threads per CTA: 128 while the work items (three a cell in FP64, one in
+// FP32) spread that thinly over the SMs, up to 1024 as the grid grows (the
+// kernel is compiled for 1024, so at most 64 registers a thread).
+constexpr int TINY_MIN_THREADS = 128, TINY_MAX_THREADS = 1024;
 
 // IRIS_OP_BARRIER_CHECK: a cooperative launch of two CTAs in which the second
 // returns without arriving, so the first waits at the grid barrier with the
@@ -1372,7 +1375,7 @@ template <int MASK> __device__ __forceinline__ void tiny_h(const FieldArgs<doubl
   else h_split_cell<double, false, MASK>(a, x, y, z);
 }
 
-template <typename T, bool CEPS> __global__ void __launch_bounds__(TINY_THREADS) k_tiny(TinyArgs<T> A) {
+template <typename T, bool CEPS> __global__ void __launch_bounds__(TINY_MAX_THREADS) k_tiny(TinyArgs<T> A) {
   using V = typename V2<T>::t;
   const Geo g = A.a.g;
   const long nxy = (long)g.nx * g.ny, ncell = nxy * g.nz;
@@ -1914,6 +1917,13 @@ FusedArgs fused_args(const iris_engine* E, int part) {
   return a;
 }
 
+// Share of the fused pass's threads that own a cell of an nx x ny plane
+// (each 32 x 16 tile writes 31 x 15 cells).
+double fused_fill(int nx, int ny) {
+  const long tx = (nx + FZ_OX - 1) / FZ_OX, ty = (ny + FZ_OY - 1) / FZ_OY;
+  return (double)nx * ny / ((double)tx * FZ_X * ty * FZ_Y);
+}
+
 // z chunks of planes za..zb for a launch over `tiles` column tiles: about
 // eight waves of two CTAs per SM, at least 16 planes each; appends
 // (za, zb, planes per chunk, chunks) to r.
@@ -2101,7 +2111,7 @@ template <typename T> int step_persist(iris_engine* E, int it0, int n) {
       }
       CK(cudaMemsetAsync(E->d_bar, 0, sizeof(GridBar), E->st));
       const void* k = E->eps_complex ? (const void*)k_tiny<T, true> : (const void*)k_tiny<T, false>;
-      CK(cudaLaunchCooperativeKernel(k, dim3(E->persist_blocks), dim3(TINY_THREADS), args, 0, E->st));
+      CK(cudaLaunchCooperativeKernel(k, dim3(E->persist_blocks), dim3(E->persist_threads), args, 0, E->st));
     }
     E->nslot += samples;
     if (E->nslot == E->K) dft_flush(E);
@@ -2617,28 +2627,38 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
   E->src = make_src(p);
   E->tf_blk = dim3(64);
   E->tf_grd = dim3((p.nx + 2 + 63) / 64, (p.ny + 2 + TFSF_YCH - 1) / TFSF_YCH);
-  // Small grids step with the persistent kernel (asked for, or by default up
-  // to IRIS_PERSISTENT_MAX_CELLS cells when the device runs cooperative
-  // launches); otherwise FP32 steps with the fused E+H pass unless the split
-  // or streamed passes are asked for (FP64 with the split passes).
+  // Small grids step with the persistent kernel (asked for, or by default
+  // when the device runs cooperative launches: FP64 grids of at most
+  // IRIS_PERSISTENT_MAX_CELLS cells, FP32 grids of at most
+  // IRIS_PERSISTENT_MAX_CELLS_FP32: up to those sizes it steps faster than
+  // the split passes); otherwise FP32 steps with the fused E+H pass unless the split or
+  // streamed passes are asked for, or unless the fused pass's 32 x 16 tiles
+  // would leave more than half of their threads idle on the grid's x-y
+  // plane (rows or columns short of a tile: the split passes then); FP64
+  // steps with the split passes.
   {
     int coop = 0, nsm = 0, occ = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, E->device);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E->device);
     const long cells = (long)p.nx * p.ny * p.nz;
+    const long dflt = E->prec == IRIS_FP64 ? IRIS_PERSISTENT_MAX_CELLS : IRIS_PERSISTENT_MAX_CELLS_FP32;
     const bool want = !member && 3 * cells < (1L << 31) &&
-                      (p.stencil == IRIS_STENCIL_PERSISTENT ||
-                       (p.stencil == IRIS_STENCIL_DEFAULT && cells <= IRIS_PERSISTENT_MAX_CELLS));
-    if (want && coop) {
+                      (p.stencil == IRIS_STENCIL_PERSISTENT || (p.stencil == IRIS_STENCIL_DEFAULT && cells <= dflt));
+    if (want && coop && nsm > 0) {
+      // the widest CTA that still gives every SM at least one work item a
+      // thread (three a cell in FP64); one CTA per SM at most (the FP64
+      // pipes are per SM), no more than the work items need
+      const long items = (E->prec == IRIS_FP64 ? 3 : 1) * cells;
+      int thr = TINY_MIN_THREADS;
+      while (thr < TINY_MAX_THREADS && items >= 2L * thr * nsm) thr *= 2;
       const void* k = E->prec == IRIS_FP64 ? (const void*)k_tiny<double, false> : (const void*)k_tiny<float, false>;
       const void* kc = E->prec == IRIS_FP64 ? (const void*)k_tiny<double, true> : (const void*)k_tiny<float, true>;
       int o1 = 0, o2 = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k, TINY_THREADS, 0) == cudaSuccess &&
-          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, kc, TINY_THREADS, 0) == cudaSuccess)
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k, thr, 0) == cudaSuccess &&
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, kc, thr, 0) == cudaSuccess)
         occ = std::min(o1, o2);
-      // one CTA per SM at most (the FP64 pipes are per SM), no more than the
-      // work items need (three a cell in FP64)
-      const long need = ((E->prec == IRIS_FP64 ? 3 : 1) * cells + TINY_THREADS - 1) / TINY_THREADS;
+      const long need = (items + thr - 1) / thr;
+      E->persist_threads = thr;
       E->persist_blocks = (int)std::max(1L, std::min<long>(need, (long)nsm * std::min(occ, 1)));
       E->persist = occ >= 1;
     }
@@ -2655,7 +2675,7 @@ int create_engine(const iris_params* pin, const double* fw, bool member, bool z_
     }
   }
   E->fused = !E->persist && E->prec == IRIS_FP32 &&
-             (p.stencil == IRIS_STENCIL_FUSED || p.stencil == IRIS_STENCIL_DEFAULT);
+             (p.stencil == IRIS_STENCIL_FUSED || (p.stencil == IRIS_STENCIL_DEFAULT && fused_fill(p.nx, p.ny) >= 0.5));
   if (E->fused) {
     if (cudaMalloc(&E->e2, fbytes) != cudaSuccess || cudaMalloc(&E->h2, fbytes) != cudaSuccess)
       return bail(fail(IRIS_ENOMEM, "second field buffers: allocation failed"));

@@ -113,10 +113,10 @@ struct iris_engine {
   cudaGraphExec_t gexec = nullptr;
   int* d_it = nullptr;
   int dev_it = -1;
-  // persistent whole-step kernel (small grids): CTAs of its cooperative
-  // launch and its grid-barrier words
+  // persistent whole-step kernel (small grids): CTAs and threads per CTA of
+  // its cooperative launch and its grid-barrier words
   bool persist = false;
-  int persist_blocks = 0;
+  int persist_blocks = 0, persist_threads = 0;
   void* d_bar = nullptr;
   // its TF/SF corrections (vE, vH) per [step of a span][ix], up to tfv_cap steps
   iris::TfsfVal* d_tfv = nullptr;

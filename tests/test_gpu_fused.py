@@ -132,17 +132,28 @@ def test_fused_rejected_in_fp64(iris, oracle, tmp_path):
 
 
 def test_stencil_selection(iris, oracle, tmp_path):
-    """The per-kernel timers show which pass ran: fused by default in FP32
-    above PERSISTENT_MAX_CELLS cells (one timer a step over its two
-    concurrent launches: the planes outside the UPML slabs and the slabs),
-    the persistent kernel by default at or below it (one launch for the five
-    steps), split, fused or persistent on request."""
+    """The per-kernel timers show which pass ran.  By default the persistent
+    kernel up to PERSISTENT_MAX_CELLS cells in FP64 and
+    PERSISTENT_MAX_CELLS_FP32 in FP32 (one launch for the five steps);
+    above them FP64 steps with the split passes and FP32 with the fused pass
+    (one timer a step over its two concurrent launches: the planes outside
+    the UPML slabs and the slabs), or with the split passes on a grid whose
+    x-y plane would leave most of the fused tiles' threads idle (4 cells in
+    y); split, fused or persistent on request."""
     small = make_case(oracle, tmp_path, (16, 8, 40, 6, 35, 15, 10, 4.0, 10, (1, 16, 1, 8, 8, 32)), 2)[1]
-    large = make_case(oracle, tmp_path, (48, 40, 40, 6, 35, 15, 10, 4.0, 10, (1, 48, 1, 40, 8, 32)), 2)[1]
-    assert 48 * 40 * 40 > iris.PERSISTENT_MAX_CELLS
-    for op, stencil, kind in ((large, 0, "fused"), (small, 0, "persistent"), (small, 1, "split"),
-                              (small, 2, "fused"), (small, 4, "persistent")):
-        eng = iris.Engine(engine_params_from_oracle(iris, op, precision=1), op.fw, stencil=stencil)
+    mid = make_case(oracle, tmp_path, (48, 40, 40, 6, 35, 15, 10, 4.0, 10, (1, 48, 1, 40, 8, 32)), 2)[1]
+    big64 = make_case(oracle, tmp_path, (128, 96, 88, 6, 83, 30, 10, 4.0, 10, (1, 128, 1, 96, 8, 80)), 2)[1]
+    big32 = make_case(oracle, tmp_path, (256, 256, 136, 6, 131, 60, 10, 4.0, 10, (1, 256, 1, 256, 8, 128)), 2)[1]
+    thin = make_case(oracle, tmp_path, (2048, 4, 1100, 6, 1095, 500, 10, 4.0, 10, (1, 2048, 1, 4, 8, 1090)), 2)[1]
+    assert 48 * 40 * 40 <= iris.PERSISTENT_MAX_CELLS < 128 * 96 * 88
+    assert 256 * 256 * 136 > iris.PERSISTENT_MAX_CELLS_FP32 and 2048 * 4 * 1100 > iris.PERSISTENT_MAX_CELLS_FP32
+    for op, prec, stencil, kind in ((big32, 1, 0, "fused"), (thin, 1, 0, "split"), (mid, 1, 0, "persistent"),
+                                    (small, 1, 0, "persistent"), (mid, 0, 0, "persistent"), (big64, 0, 0, "split"),
+                                    (small, 1, 1, "split"), (small, 1, 2, "fused"), (small, 1, 4, "persistent"),
+                                    (big64, 0, 4, "persistent")):
+        q = engine_params_from_oracle(iris, op, precision=prec)
+        q.dft_faces = iris.DFT_Z  # the large grids' x and y faces would hold tens of millions of points
+        eng = iris.Engine(q, op.fw, stencil=stencil)
         eng.timing_start()
         eng.step(1, 5)
         _, ms, n = eng.timing_read()

@@ -1,5 +1,6 @@
 """The persistent whole-step kernel for small grids (IRIS_STENCIL_PERSISTENT,
-the default up to PERSISTENT_MAX_CELLS cells): one cooperative launch runs a
+the default up to PERSISTENT_MAX_CELLS cells in FP64 and
+PERSISTENT_MAX_CELLS_FP32 in FP32): one cooperative launch runs a
 span of steps (E pass, H pass, TF/SF, DFT sample) with grid-wide barriers
 between the passes, using the split passes' per-cell functions.  Every
 stored value (fields with their ghosts, UPML auxiliaries, DFT accumulators
