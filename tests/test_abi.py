@@ -25,6 +25,33 @@ def test_exports_match_header(iris):
     assert set(names) == set(iris.native.EXPORTS)
 
 
+def header_constants():
+    """Integer macros of the header: IRIS_NAME -> value (status codes in
+    parentheses included)."""
+    src = open(os.path.join(ROOT, "include", "iris_fdtd.h")).read()
+    return {m.group(1): int(m.group(2)) for m in re.finditer(r"^#define IRIS_([A-Z0-9_]+)\s+\(?(-?\d+)\)?", src, re.M)}
+
+
+def test_python_constants_match_header(iris):
+    """The Python mirror's constants carry the header's values: every
+    IRIS_<NAME> the module also defines as <NAME>, the kernel classes'
+    order (IRIS_KC_*) and the batch's work lists (IRIS_BATCH_NTILES)."""
+    c = header_constants()
+    matched = [n for n in c if hasattr(iris, n)]
+    for n in matched:
+        assert getattr(iris, n) == c[n], n
+    for n in ("FP64", "FP32", "STENCIL_DEFAULT", "STENCIL_PERSISTENT", "PERSISTENT_MAX_CELLS",
+              "PERSISTENT_MAX_CELLS_FP32", "DFT_KERNEL_TENSOR", "DFT_Z", "OP_BARRIER_CHECK", "E", "H"):
+        assert n in matched, n
+    assert c["EINVAL"] == -1 and c["ETIMEOUT"] == -7
+    kc = {"update_e": "KC_E", "update_h": "KC_H", "tfsf": "KC_TFSF", "dft_gather": "KC_GATHER",
+          "dft_block": "KC_DFT", "flux": "KC_FLUX", "fused_eh": "KC_FUSED", "persistent": "KC_PERSIST"}
+    assert len(iris.Engine.KERNELS) == c["NKC"]
+    for i, k in enumerate(iris.Engine.KERNELS):
+        assert c[kc[k]] == i, k
+    assert len(iris.TILES) == c["BATCH_NTILES"]
+
+
 def test_bounds_checking_twin_exports_the_same_entry_points(iris):
     """libiris_fdtd_bc.so (built with -DIRIS_BOUNDS_CHECK beside the ordinary
     library) loads and exports every header function; the ordinary library
