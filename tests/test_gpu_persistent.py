@@ -7,7 +7,8 @@ stored value (fields with their ghosts, UPML auxiliaries, DFT accumulators
 and spectra) equals the split passes' bit for bit, in both precisions, for
 both TF/SF variants, the CW source, complex materials and Bloch phases, DFT
 sampling that starts late and skips steps, and DFT blocks that fill inside
-a span.  Against the FP64 oracle it inherits the split passes' 1e-12
+a span, on grids small enough for 128-thread CTAs and on one that takes
+1024.  Against the FP64 oracle it inherits the split passes' 1e-12
 (the parity tests' small grids step with it by default).  The grid
 barrier's bounded wait gives up cleanly (IRIS_OP_BARRIER_CHECK).
 """
@@ -38,6 +39,10 @@ CASES = [
     ("cw_late_sparse_sampling", cfg.Workload("cw", 12, 7, 60, 8, 53, 24, 10, 4.0, 0, 14, (2, 11, 1, 7, 10, 50), 7, 200,
                                              structure="slit"), (0.3 + 0j, 0j, 0j), None,
      {"plane_wave": 0, "to_fourier": 17, "sample_fourier": 3}, 0),
+    # 294,912 cells: CTAs of 1024 threads in both precisions (the width grows with the grid)
+    ("3d_wide_ctas", cfg.Workload("wide", 96, 64, 48, 8, 41, 18, 10, 2.25, 0, 12, (1, 96, 1, 64, 9, 38), 9, 120,
+                                  structure="spheres", extra=dict(nspheres=8, rmin=2, rmax=6, emin=1.5, emax=6.0)),
+     (0.3 + 0j, 0.1 + 0j, 0j), None, {}, 0),
 ]
 CALLS = [(1, 1), (2, 37), (39, 64), (103, 5)]
 
