@@ -124,8 +124,9 @@ def test_run_input_loop_two_indices(iris, example1_oracle, tmp_path):
 
 
 def test_run_input_example2_fp32_tr(iris, oracle, tmp_path):
-    """The slit-array example in FP32 through the drop-in program (the fused
-    pass, the tensor-core DFT and its flux read): T/R of every output block
+    """The slit-array example in FP32 through the drop-in program (the default
+    stepping, the persistent kernel on this grid; the tensor-core DFT and its
+    flux read): T/R of every output block
     within 1e-4 of the FP64 oracle, steps trimmed to 6000."""
     src = open(golden("example_2.inputFDTD.dat")).read()
     d = tmp_path / "ex2"

@@ -300,14 +300,16 @@ def test_fp32_mode_tr_error(iris, oracle):
 @pytest.mark.parametrize("precision,shape", [(0, (8, 6, 48)), (1, (70, 40, 48))])
 def test_step_is_deterministic(iris, oracle, tmp_path, precision, shape):
     """Two runs agree bit for bit: FP64 on a small grid (the persistent
-    kernel), and FP32 above the persistent limit (the fused pass, the
-    tensor-core DFT commit and flux read): no atomics and no order-dependent
-    reduction anywhere on the path."""
+    kernel, the default there), and FP32 with the fused pass, the tensor-core
+    DFT commit and flux read: no atomics and no order-dependent reduction
+    anywhere on the path."""
     nx, ny, nz = shape
     op = small_case(oracle, tmp_path, nx=nx, ny=ny, nz=nz, nof=6)
+    stencil = iris.STENCIL_FUSED if precision == iris.FP32 else iris.STENCIL_DEFAULT
     res = []
     for _ in range(2):
-        eng = iris.Engine(engine_params_from_oracle(iris, op, precision=precision), op.fw, dft_block=32)
+        eng = iris.Engine(engine_params_from_oracle(iris, op, precision=precision), op.fw, dft_block=32,
+                          stencil=stencil)
         eng.step(1, 120)
         res.append((eng.get_field(iris.E), eng.get_field(iris.H), eng.flux(0), eng.get_fdata(0, 1)))
         eng.close()

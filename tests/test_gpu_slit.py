@@ -6,7 +6,8 @@ tests/golden/make_slit_fixture.py; 24 of the 300 frequencies, every output
 block).
 
 FP64 mode: every flux spectrum within 1e-12 norm-wise of the oracle's.
-FP32 mode (fused pass, tensor-core DFT): R = J5/(J5+J6) and T = J6/(J5+J6)
+FP32 mode (the default stepping, the persistent kernel on a grid this size;
+tensor-core DFT): R = J5/(J5+J6) and T = J6/(J5+J6)
 of the final block within 1e-4 of the oracle's, per spectrum; the errors
 are printed.
 """
